@@ -1,0 +1,166 @@
+/*
+ * aln_corr.h -- C ABI of the GB300 tile-matching library (libaln_corr.so).
+ *
+ * This is the drop-in boundary for Aligner's FFT normalised
+ * cross-correlation (0_GEN/Correlation.h) and the CThmScan angle sweep
+ * (0_GEN/CThmScan.h).  Every entry point below names the reference
+ * interface it replaces.  Plain C types only: pointers, sizes, status codes.
+ *
+ * Conventions shared with the reference:
+ *   - rasters are row-major, element (x, y) at data[x + stride*y];
+ *   - a raster is the bounding box of a point cloud (0_GEN/Geometry.cpp:78-106):
+ *     (x0, y0) are the box's integer left/bottom (B.L, B.B), w/h its size;
+ *     pixels without a point hold 0;
+ *   - a lag (dx, dy) shifts image 1 into image 2's frame
+ *     (0_GEN/Geometry.cpp:142-176);
+ *   - FFT sizes are CeilPow2(n1 + n2 - 1) per axis
+ *     (0_GEN/Correlation.cpp:344-347).
+ *
+ * Errors: the library never exits the process.  Hard errors are negative
+ * status codes with a message from aln_last_error(); a search that finds no
+ * legal lag returns ALN_NO_PEAK with r = dx = dy = 0, which is what the
+ * reference returns in that case (0_GEN/Correlation.cpp:1074-1087,3098-3119).
+ *
+ * Threading: each aln_ctx owns a CUDA stream and its workspaces; use one
+ * context per host thread.  Contexts are independent.
+ */
+#pragma once
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------- */
+
+enum aln_status {
+    ALN_OK = 0,
+    ALN_NO_PEAK = 1,            /* soft result: no legal lag / too small */
+    ALN_ERR_ARG = -1,           /* bad argument (size, dtype, pointer) */
+    ALN_ERR_CUDA = -2,          /* CUDA runtime error (message has details) */
+    ALN_ERR_NOMEM = -3,         /* device allocation failed */
+    ALN_ERR_UNSUPPORTED = -4,   /* size outside the compiled FFT plans */
+    ALN_ERR_TIMEOUT = -5,       /* deadline passed / bounded wait gave up */
+    ALN_ERR_REFUSED = -6,       /* admission refused (server full) */
+    ALN_ERR_CANCELLED = -7      /* request cancelled */
+};
+
+enum aln_dtype { ALN_U8 = 0, ALN_U16 = 1, ALN_F32 = 2, ALN_F64 = 3 };
+
+/* ---- inputs --------------------------------------------------------- */
+
+typedef struct aln_image {
+    const void *data;   /* host pointer, or device pointer if on_device */
+    int dtype;          /* enum aln_dtype */
+    int w, h;           /* bounding-box size in pixels */
+    int stride;         /* elements between rows (>= w) */
+    int x0, y0;         /* bounding-box origin B.L, B.B (integer) */
+    int on_device;      /* 1 if data lives on the context's device */
+} aln_image;
+
+/*
+ * Legality tests applied to every lag, the typed form of the reference's
+ * EvalType callbacks (0_GEN/Correlation.h:91):
+ *   LegalRgn(olw, olh): the overlap box size;
+ *   LegalCnt(c1, c2):   non-zero pixel counts of image 1 / image 2 inside it.
+ *
+ * rgn_kind:
+ *   ALN_RGN_NONE     always legal (LegalRgn == NULL)
+ *   ALN_RGN_MIN      olw >= a && olh >= b && olw*olh > area
+ *                    (CThmScan BigEnough, 0_GEN/CThmScan.cpp:28-33;
+ *                     testnormcorr SomeArea with a=b=2, area=0)
+ *   ALN_RGN_SECTION  olw*olh > area && (olw >= a || olh > b)
+ *                    (1_DMesh/InSectionOverlap.cpp:41-47)
+ *   ALN_RGN_EXACT    olw == a && olh == b (1_Mosaic_current/mos.cpp:1270-1274)
+ *   ALN_RGN_TABLE    table[(olh-1)*table_w + (olw-1)] != 0, for any other
+ *                    callback tabulated by the caller over
+ *                    olw in [1, table_w], olh in [1, table_h]
+ * cnt_kind:
+ *   ALN_CNT_NONE     no count test (LegalCnt == NULL, or always true)
+ *   ALN_CNT_GT       c1 > n && c2 > n (CThmScan EnoughPoints, 0_GEN/CThmScan.cpp:39-42)
+ */
+enum { ALN_RGN_NONE = 0, ALN_RGN_MIN = 1, ALN_RGN_SECTION = 2,
+       ALN_RGN_EXACT = 3, ALN_RGN_TABLE = 4 };
+enum { ALN_CNT_NONE = 0, ALN_CNT_GT = 1 };
+
+typedef struct aln_legal {
+    int rgn_kind;
+    int rgn_a, rgn_b;
+    long long rgn_area;
+    const unsigned char *table;   /* host pointer (ALN_RGN_TABLE only) */
+    int table_w, table_h;
+    int cnt_kind;
+    long long cnt_n;
+} aln_legal;
+
+/* ---- outputs -------------------------------------------------------- */
+
+typedef struct aln_result {
+    double r;           /* correlation (CorrPatches/R/F) or S score (S) */
+    double dx, dy;      /* sub-pixel displacement placing image 1 into image 2 */
+    int status;         /* ALN_OK or ALN_NO_PEAK */
+    int peak_x, peak_y; /* integer lag of the peak (before bbox offsets) */
+    int nx, ny;         /* FFT size used */
+} aln_result;
+
+typedef struct aln_ctx aln_ctx;
+
+/* ---- context -------------------------------------------------------- */
+
+/* Create a context on CUDA device `device`.  No reference counterpart
+ * (the reference's state is the static mutex_fft, 0_GEN/Correlation.cpp:26-27). */
+int aln_ctx_create(int device, aln_ctx **out);
+void aln_ctx_destroy(aln_ctx *ctx);
+/* Message of the last hard error on this context (or of the last failed
+ * aln_ctx_create when ctx is NULL). */
+const char *aln_last_error(const aln_ctx *ctx);
+
+/* ---- FFT support: 0_GEN/Correlation.h:14-31 ------------------------- */
+
+/* FFTSize, 0_GEN/Correlation.cpp:344-347 */
+int aln_fft_size(int n1, int n2);
+/* FFTSizeSQR, 0_GEN/Correlation.cpp:355-359 */
+int aln_fft_size_sqr(int w1, int h1, int w2, int h2);
+
+/* FFT_2D, 0_GEN/Correlation_fft_fftw.cpp:36-56: unnormalised forward r2c of
+ * in[Nslow][Nfast] (host, FP64) into out[Nslow][Nfast/2+1] complex
+ * interleaved (host, FP64), computed on the GPU in FP32.  Returns
+ * M = Nslow*(Nfast/2+1) or a negative status. */
+int aln_fft_2d(aln_ctx *ctx, const double *in, int nfast, int nslow, double *out);
+
+/* IFT_2D, 0_GEN/Correlation_fft_fftw.cpp:65-92: unnormalised c2r inverse.
+ * Returns 0 or a negative status. */
+int aln_ift_2d(aln_ctx *ctx, const double *in, int nfast, int nslow, double *out);
+
+/* ParabPeakFFT, 0_GEN/Correlation.cpp:482-517 (host arithmetic, O(1)). */
+void aln_parab_peak_fft(double *xpk, double *ypk, int d, const double *I,
+                        int nx, int ny);
+
+/* ---- correlation ---------------------------------------------------- */
+
+/* CorrPatches, 0_GEN/Correlation.cpp:901-1170: Pearson-r correlation over
+ * all lags inside the disc (Ox, Oy, radius), legal per `legal`, peak with
+ * parabolic refinement; out->r, dx, dy as the reference returns them.
+ * One pair per call (the plain per-pair path). */
+int aln_corr_patches(aln_ctx *ctx, const aln_image *a, const aln_image *b,
+                     int ox, int oy, int radius, const aln_legal *legal,
+                     aln_result *out);
+
+/* One CorrPatches job of a batch. */
+typedef struct aln_pair {
+    aln_image a, b;
+    int ox, oy, radius;
+    aln_legal legal;
+} aln_pair;
+
+/* Many CorrPatches calls in one submission (pairs of any mix of sizes).
+ * Pairs are grouped by FFT size and run by batched kernels; results are
+ * identical to calling aln_corr_patches on each pair. */
+int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *pairs,
+                           aln_result *out);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,107 @@
+"""The C restatement (oracle/aln_oracle.c) against the reference's own outputs.
+
+tests/golden/*.npz were produced by tests/golden/make_golden.py, which runs the
+reference's unmodified correlation sources.  The restatement must reproduce
+them to the last bits (FP64 with the same operation order); a tolerance of
+1e-12 covers libm differences between hosts.
+"""
+import numpy as np
+import pytest
+
+from conftest import legal_from, load_golden
+
+TOL = 1e-12
+
+
+def close(a, b, tol=TOL):
+    return abs(float(a) - float(b)) <= tol * max(1.0, abs(float(b)))
+
+
+@pytest.mark.parametrize("case", sorted(load_golden("corr_patches")))
+def test_corr_patches_golden(orc, case):
+    d = load_golden("corr_patches")[case]
+    lg = legal_from(d["legal"])
+    o = orc.corr_patches(d["pa"], d["va"], d["pb"], d["vb"], int(d["ox"]), int(d["oy"]),
+                         int(d["radius"]), lg)
+    assert close(o["r"], d["r"]), (o["r"], float(d["r"]))
+    if o["status"] == 1:
+        # no legal lag: the reference returns 0.0 and leaves dx, dy untouched
+        assert float(d["r"]) == 0.0
+    else:
+        assert close(o["dx"], d["dx"]) and close(o["dy"], d["dy"]), (o, d["dx"], d["dy"])
+
+
+def test_kat_testnormcorr_values():
+    """Retired_Proj/4_TestNormCorr: exact copy at lag (-4, +2) gives r = 1."""
+    d = load_golden("corr_patches")["kat_testnormcorr"]
+    assert float(d["r"]) == 1.0
+    assert round(float(d["dx"])) == -4 and float(d["dy"]) == 2.0
+
+
+@pytest.mark.parametrize("case", sorted(load_golden("corr_images")))
+def test_corr_images_golden(orc, case):
+    d = load_golden("corr_images")[case]
+    lg = legal_from(d["legal"])
+    disc = [int(v) for v in d["disc"]]
+    o = orc.corr_images(int(d["kind"]), d["pa"], d["va"], d["pb"], d["vb"], lg,
+                        float(d["mincor"]), float(d["nbmaxht"]), *disc)
+    assert close(o["r"], d["r"]), (o["r"], float(d["r"]))
+    assert close(o["dx"], d["dx"]) and close(o["dy"], d["dy"])
+
+
+@pytest.mark.parametrize("case", ["fft_8x16", "fft_64x32", "fft_32x128"])
+def test_fft_golden(orc, case):
+    d = load_golden("fft")[case]
+    F = orc.fft_2d(d["x"])
+    assert np.abs(F - d["F"]).max() <= 1e-12 * np.abs(d["F"]).max()
+    x = d["x"]
+    G = orc.ift_2d(F * np.conj(orc.fft_2d(np.roll(x, (2, 3), (0, 1)))), x.shape[1])
+    assert np.abs(G - d["G"]).max() <= 1e-12 * np.abs(d["G"]).max()
+
+
+def test_kat_time_fft(orc):
+    """Retired_Proj/4_Time_FFT: a copy shifted by index 2N+3 is recovered."""
+    d = load_golden("fft")["kat_time_fft"]
+    N = d["in1"].shape[0]
+    G = orc.ift_2d(orc.fft_2d(d["in1"]) * np.conj(orc.fft_2d(d["in2"])), N)
+    assert int(np.argmax(G)) == int(d["argmax"])
+    x, y = divmod(int(d["argmax"]), N)
+    x = x - N if x > N // 2 else x
+    y = y - N if y > N // 2 else y
+    assert (x, y) == (-2, -3)
+
+
+@pytest.mark.parametrize("case", ["conv_37x50", "conv_64x64"])
+def test_convolve_golden(orc, case):
+    d = load_golden("convolve")[case]
+    out = orc.convolve(d["src"], d["K"])
+    assert np.abs(out - d["dst"]).max() <= 1e-12
+
+
+@pytest.mark.parametrize("case", ["p2i_f0", "p2i_f1"])
+def test_patch_to_image_golden(orc, case):
+    d = load_golden("patch_to_image")[case]
+    o = orc.corr_patch_to_image(d["pa"], d["va"], d["img2"], 0, 0, 4096,
+                                bool(int(d["bfilter"])))
+    assert close(o["r"], d["r"]) and close(o["dx"], d["dx"]) and close(o["dy"], d["dy"])
+
+
+@pytest.mark.parametrize("case", sorted(load_golden("thm_scan")))
+def test_thm_scan_golden(orc, case):
+    d = load_golden("thm_scan")[case]
+    disc = tuple(int(v) for v in d["disc"])
+    o = orc.thm_search(d["pa"], d["va"], d["pb"], d["vb"], int(d["req"]),
+                       rthresh=float(d["rthresh"]), pretweak=int(d["pretweak"]),
+                       disc=disc, mode=int(d["mode"]), ang0=float(d["ang0"]),
+                       hfang=float(d["hfang"]), step=float(d["step"]))
+    for k in ("A", "X", "Y", "R"):
+        assert close(o[k], d[k]), (k, o[k], float(d[k]))
+    assert o["err"] == int(d["err"])
+
+
+def test_decimate_golden(orc):
+    d = load_golden("decimate")["dec8"]
+    xy, v = orc.decimate_normalize(d["pa"], d["va"], int(d["w"]), int(d["h"]),
+                                   int(d["lbin"]))
+    assert np.array_equal(xy, d["xy"])
+    assert np.abs(v - d["v"]).max() <= 1e-12
