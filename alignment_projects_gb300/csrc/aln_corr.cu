@@ -1,0 +1,1405 @@
+// aln_corr.cu -- GB300 (sm_103a) FFT normalised cross-correlation:
+// the CorrPatches pipeline (0_GEN/Correlation.cpp:901-1170) as batched
+// kernels, plus the FFT_2D / IFT_2D drop-ins.
+//
+// Pipeline for a group of pairs sharing one FFT size (Nx, Ny):
+//   k_colsum    column prefix sums of v, v^2, (v != 0) -> summed-area-table
+//               rows the lag window needs; column totals
+//   k_mean      mean of each image -> shift mu (integer for integer pixels)
+//   k_rowscan   x-prefix of the needed rows -> summed-area-table rows
+//   k_rowfft    per image row: (v - mu) zero-padded to Nx, real FFT,
+//               written transposed T[kx][y]
+//   k_colfft    image b: column FFTs -> spectrum X2[kx][ky]
+//   k_corrcol   image a: column FFTs, X2 * conj(X1), inverse column FFTs,
+//               only the lag rows of the window -> Q[kx][j]
+//   k_lagrow    per lag row: inverse real FFT, Pearson r per lag from the
+//               FP64 summed-area tables, legality, disc, row argmax
+//   k_final     argmax over rows (ties: smallest storage index, as the
+//               reference's row-major scan with strict '>'), ParabPeakFFT
+//
+// Pearson r is shift-invariant: with C' the cross sum of the mean-shifted
+// images, num = n*C' - (S1 - n mu1)(S2 - n mu2) equals the reference's
+// n*C - S1*S2, and d1, d2 use the unshifted sums exactly as the reference
+// (CLinCorr::GetCorr, 0_GEN/Correlation.cpp:705-757).  The shift keeps the
+// FP32 FFT error proportional to the signal, not to the mean.
+#include "aln_fft.cuh"
+#include "aln_corr_kernels.cuh"
+#include "../../include/aln_corr.h"
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <vector>
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ double load_px(const void *p, int dt, long long idx)
+{
+    switch (dt) {
+    case ALN_U8: return (double)((const uint8_t *)p)[idx];
+    case ALN_U16: return (double)((const uint16_t *)p)[idx];
+    case ALN_F32: return (double)((const float *)p)[idx];
+    default: return ((const double *)p)[idx];
+    }
+}
+
+__device__ __forceinline__ int sat_slot(const PairDev &p, int i, int y)
+{
+    const int len0 = p.need_hi[i][0] - p.need_lo[i][0] + 1;
+    return (y <= p.need_hi[i][0]) ? y - p.need_lo[i][0] : len0 + y - p.need_lo[i][1];
+}
+
+__device__ __forceinline__ bool row_needed(const PairDev &p, int i, int y)
+{
+    return (y >= p.need_lo[i][0] && y <= p.need_hi[i][0]) ||
+           (y >= p.need_lo[i][1] && y <= p.need_hi[i][1]);
+}
+
+__device__ __forceinline__ int nslots(const PairDev &p, int i)
+{
+    int n = 0;
+    for (int k = 0; k < 2; ++k)
+        if (p.need_hi[i][k] >= p.need_lo[i][k])
+            n += p.need_hi[i][k] - p.need_lo[i][k] + 1;
+    return n;
+}
+
+// IntegralTable, 0_GEN/Correlation.cpp:112-150, on slot-indexed SAT rows
+__device__ __forceinline__ double sat_box(const double *t, const PairDev &p, int i,
+                                          int L, int R, int B, int T)
+{
+    const int w = p.w[i];
+    double r = t[(long long)sat_slot(p, i, T) * w + R];
+    if (L > 0)
+        r -= t[(long long)sat_slot(p, i, T) * w + L - 1];
+    if (B > 0)
+        r -= t[(long long)sat_slot(p, i, B - 1) * w + R];
+    if (L > 0 && B > 0)
+        r += t[(long long)sat_slot(p, i, B - 1) * w + L - 1];
+    return r;
+}
+
+__device__ __forceinline__ int sat_box_n(const int *t, const PairDev &p, int i, int L,
+                                         int R, int B, int T)
+{
+    const int w = p.w[i];
+    int r = t[(long long)sat_slot(p, i, T) * w + R];
+    if (L > 0)
+        r -= t[(long long)sat_slot(p, i, T) * w + L - 1];
+    if (B > 0)
+        r -= t[(long long)sat_slot(p, i, B - 1) * w + R];
+    if (L > 0 && B > 0)
+        r += t[(long long)sat_slot(p, i, B - 1) * w + L - 1];
+    return r;
+}
+
+__device__ __forceinline__ bool rgn_ok(const PairDev &p, int sx, int sy)
+{
+    switch (p.rgn_kind) {
+    case ALN_RGN_MIN:
+        return sx >= p.rgn_a && sy >= p.rgn_b && (long long)sx * sy > p.rgn_area;
+    case ALN_RGN_SECTION:
+        return (long long)sx * sy > p.rgn_area && (sx >= p.rgn_a || sy > p.rgn_b);
+    case ALN_RGN_EXACT:
+        return sx == p.rgn_a && sy == p.rgn_b;
+    case ALN_RGN_TABLE:
+        if (sx < 1 || sy < 1 || sx > p.table_w || sy > p.table_h)
+            return false;
+        return p.table[(long long)(sy - 1) * p.table_w + (sx - 1)] != 0;
+    default:
+        return true;
+    }
+}
+
+// Pearson r of lag (x, y) given the shifted cross sum cs = C'/(Nx*Ny).
+// Returns false (and r = 0) for an illegal lag, as CLinCorr::CheckSize /
+// CheckDensity / GetCorr do (0_GEN/Correlation.cpp:658-757).
+__device__ __forceinline__ bool lag_r(const PairDev &p, int x, int y, double cs, double &r)
+{
+    const int w1 = p.w[0], h1 = p.h[0], w2 = p.w[1], h2 = p.h[1];
+    // BoxesFromShifts, 0_GEN/Geometry.cpp:150-176
+    int L2 = max(0, x), R2 = min(w2 - 1, x + w1 - 1);
+    int B2 = max(0, y), T2 = min(h2 - 1, y + h1 - 1);
+    R2 = max(R2, L2);
+    T2 = max(T2, B2);
+    const int L1 = L2 - x, R1 = R2 - x, B1 = B2 - y, T1 = T2 - y;
+    const int olw = R1 - L1 + 1, olh = T1 - B1 + 1;
+    r = 0.0;
+    if (p.rgn_kind != ALN_RGN_NONE && !rgn_ok(p, olw, olh))
+        return false;
+    if (p.cnt_kind == ALN_CNT_GT) {
+        const int c1 = sat_box_n(p.satN[0], p, 0, L1, R1, B1, T1);
+        const int c2 = sat_box_n(p.satN[1], p, 1, L2, R2, B2, T2);
+        if (!(c1 > p.cnt_n && c2 > p.cnt_n))
+            return false;
+    }
+    const double n = (double)(olw * olh);
+    const double s1 = sat_box(p.satS[0], p, 0, L1, R1, B1, T1);
+    const double q1 = sat_box(p.satQ[0], p, 0, L1, R1, B1, T1);
+    const double s2 = sat_box(p.satS[1], p, 1, L2, R2, B2, T2);
+    const double q2 = sat_box(p.satQ[1], p, 1, L2, R2, B2, T2);
+    const double num = n * cs - (s1 - n * p.mu[0]) * (s2 - n * p.mu[1]);
+    const double d1 = n * q1 - s1 * s1;
+    const double d2 = n * q2 - s2 * s2;
+    const double d = d1 * d2;
+    r = (d < n * n * 1.0E-9) ? 0.0 : num / sqrt(d);
+    return true;
+}
+
+__device__ __forceinline__ int isqrt_ll(long long v)
+{
+    if (v < 0)
+        return -1;
+    long long s = (long long)sqrt((double)v);
+    while (s * s > v)
+        --s;
+    while ((s + 1) * (s + 1) <= v)
+        ++s;
+    return (int)s;
+}
+
+// ---------------------------------------------------------------------------
+// summed-area tables and mean shift
+// ---------------------------------------------------------------------------
+
+// grid (ceil(maxw/128), 2, npairs), block 128: one thread per column walks
+// down the rows (IntegrateImage's sums, 0_GEN/Correlation.cpp:49-105).
+__global__ void k_colsum(PairDev *pairs)
+{
+    PairDev &p = pairs[blockIdx.z];
+    const int i = blockIdx.y;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int w = p.w[i], h = p.h[i], dt = p.dt[i];
+    if (c >= w || p.status != 0)
+        return;
+    const void *img = p.img[i];
+    const long long st = p.stride[i];
+    double *S = p.satS[i], *Q = p.satQ[i];
+    int *N = p.satN[i];
+    if (dt == ALN_U8 || dt == ALN_U16) {
+        long long s = 0, q = 0;
+        int nz = 0;
+        for (int y = 0; y < h; ++y) {
+            const long long v = dt == ALN_U8 ? ((const uint8_t *)img)[y * st + c]
+                                             : ((const uint16_t *)img)[y * st + c];
+            s += v;
+            q += v * v;
+            nz += (v != 0);
+            if (row_needed(p, i, y)) {
+                const long long o = (long long)sat_slot(p, i, y) * w + c;
+                S[o] = (double)s;
+                Q[o] = (double)q;
+                N[o] = nz;
+            }
+        }
+        p.colsum[i][c] = (double)s;
+    } else {
+        double s = 0.0, q = 0.0;
+        int nz = 0;
+        for (int y = 0; y < h; ++y) {
+            const double v = load_px(img, dt, y * st + c);
+            s += v;
+            q += v * v;
+            nz += (v != 0.0);
+            if (row_needed(p, i, y)) {
+                const long long o = (long long)sat_slot(p, i, y) * w + c;
+                S[o] = s;
+                Q[o] = q;
+                N[o] = nz;
+            }
+        }
+        p.colsum[i][c] = s;
+    }
+}
+
+// grid (2, npairs), block 256: deterministic total -> mean shift
+__global__ void k_mean(PairDev *pairs)
+{
+    PairDev &p = pairs[blockIdx.y];
+    const int i = blockIdx.x;
+    if (p.status != 0)
+        return;
+    __shared__ double part[256];
+    double s = 0.0;
+    for (int c = threadIdx.x; c < p.w[i]; c += blockDim.x)
+        s += p.colsum[i][c];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if (threadIdx.x < k)
+            part[threadIdx.x] += part[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double mean = part[0] / ((double)p.w[i] * p.h[i]);
+        p.mu[i] = (p.dt[i] == ALN_U8 || p.dt[i] == ALN_U16) ? floor(mean + 0.5) : mean;
+    }
+}
+
+// grid (maxslots, 2, npairs), block 256: inclusive x-prefix of one needed row
+__global__ void k_rowscan(PairDev *pairs)
+{
+    PairDev &p = pairs[blockIdx.z];
+    const int i = blockIdx.y;
+    const int slot = blockIdx.x;
+    if (p.status != 0 || slot >= nslots(p, i))
+        return;
+    const int w = p.w[i];
+    double *S = p.satS[i] + (long long)slot * w;
+    double *Q = p.satQ[i] + (long long)slot * w;
+    int *N = p.satN[i] + (long long)slot * w;
+    const int per = (w + blockDim.x - 1) / blockDim.x;
+    const int c0 = threadIdx.x * per, c1 = min(w, c0 + per);
+    double s = 0.0, q = 0.0;
+    int n = 0;
+    for (int c = c0; c < c1; ++c) {
+        s += S[c];
+        q += Q[c];
+        n += N[c];
+    }
+    __shared__ double ss[256], sq[256];
+    __shared__ int sn[256];
+    ss[threadIdx.x] = s;
+    sq[threadIdx.x] = q;
+    sn[threadIdx.x] = n;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double as = 0.0, aq = 0.0;
+        int an = 0;
+        for (int t = 0; t < (int)blockDim.x; ++t) {
+            const double ts = ss[t], tq = sq[t];
+            const int tn = sn[t];
+            ss[t] = as;
+            sq[t] = aq;
+            sn[t] = an;
+            as += ts;
+            aq += tq;
+            an += tn;
+        }
+    }
+    __syncthreads();
+    s = ss[threadIdx.x];
+    q = sq[threadIdx.x];
+    n = sn[threadIdx.x];
+    for (int c = c0; c < c1; ++c) {
+        s += S[c];
+        q += Q[c];
+        n += N[c];
+        S[c] = s;
+        Q[c] = q;
+        N[c] = n;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// forward row pass: (v - mu), zero pad, real FFT, transposed store
+// ---------------------------------------------------------------------------
+
+// grid (ceil(maxh/RB), 2, npairs), block 256, smem 2*RB*(L+1) float2
+__global__ void k_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int RB, int only_img)
+{
+    extern __shared__ float2 smem[];
+    PairDev &p = pairs[blockIdx.z];
+    const int i = only_img >= 0 ? only_img : blockIdx.y;
+    if (p.status != 0)
+        return;
+    const int h = p.h[i], w = p.w[i], dt = p.dt[i];
+    const int y0 = blockIdx.x * RB;
+    if (y0 >= h)
+        return;
+    const int logL = p.logNx - 1, L = 1 << logL, pitch = L + 1;
+    float2 *b0 = smem, *b1 = smem + RB * pitch;
+    const void *img = p.img[i];
+    const long long st = p.stride[i];
+    const double mu = p.mu[i];
+    for (int e = threadIdx.x; e < RB * L; e += blockDim.x) {
+        const int r = e >> logL, n = e & (L - 1);
+        const int y = y0 + r;
+        float2 z = make_float2(0.f, 0.f);
+        if (y < h) {
+            const int xa = 2 * n, xb = 2 * n + 1;
+            if (xa < w)
+                z.x = (float)(load_px(img, dt, y * st + xa) - mu);
+            if (xb < w)
+                z.y = (float)(load_px(img, dt, y * st + xb) - mu);
+        }
+        b0[r * pitch + n] = z;
+    }
+    __syncthreads();
+    // G transforms with row pitch L+1: run the passes on a padded layout by
+    // viewing each row as its own transform (pitch folded into the index).
+    float2 *src = b0, *dst = b1;
+    int logNs = 0;
+    for (; logNs + 2 <= logL; logNs += 2) {
+        const int nb = L >> 2, Ns = 1 << logNs;
+        for (int b = threadIdx.x; b < RB * nb; b += blockDim.x) {
+            const int g = b / nb, j = b - g * nb, k = j & (Ns - 1);
+            const float2 *s = src + g * pitch;
+            float2 *d = dst + g * pitch;
+            float2 a0 = s[j], a1 = s[j + nb], a2 = s[j + 2 * nb], a3 = s[j + 3 * nb];
+            if (Ns > 1) {
+                const int step = k << (logL - logNs - 2);
+                a1 = cmul(a1, twiddle<-1>(tw, L, step));
+                a2 = cmul(a2, twiddle<-1>(tw, L, 2 * step));
+                a3 = cmul(a3, twiddle<-1>(tw, L, 3 * step));
+            }
+            const float2 t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), t3 = csub(a1, a3);
+            const float2 it3 = make_float2(t3.y, -t3.x);
+            const int base = ((j - k) << 2) + k;
+            d[base] = cadd(t0, t2);
+            d[base + Ns] = cadd(t1, it3);
+            d[base + 2 * Ns] = csub(t0, t2);
+            d[base + 3 * Ns] = csub(t1, it3);
+        }
+        __syncthreads();
+        float2 *t = src;
+        src = dst;
+        dst = t;
+    }
+    if (logNs < logL) {
+        const int nb = L >> 1, Ns = 1 << logNs;
+        for (int b = threadIdx.x; b < RB * nb; b += blockDim.x) {
+            const int g = b / nb, j = b - g * nb, k = j & (Ns - 1);
+            const float2 *s = src + g * pitch;
+            float2 *d = dst + g * pitch;
+            float2 a0 = s[j], a1 = s[j + nb];
+            if (Ns > 1)
+                a1 = cmul(a1, twiddle<-1>(tw, L, k << (logL - logNs - 1)));
+            const int base = ((j - k) << 1) + k;
+            d[base] = cadd(a0, a1);
+            d[base + Ns] = csub(a0, a1);
+        }
+        __syncthreads();
+        float2 *t = src;
+        src = dst;
+        dst = t;
+    }
+    // post-process and store transposed: T[kx][y]
+    float2 *T = p.T[i];
+    const int Ts = p.Ts[i];
+    const int rows = min(RB, h - y0);
+    for (int e = threadIdx.x; e < (L + 1) * RB; e += blockDim.x) {
+        const int kx = e / RB, r = e - kx * RB;
+        if (r < rows)
+            T[(long long)kx * Ts + y0 + r] = r2c_bin(src + r * pitch, L, logL, kx, tw);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// column passes
+// ---------------------------------------------------------------------------
+
+template <int DIR>
+__device__ float2 *fft_cols(float2 *b0, float2 *b1, int G, int logL, int pitch,
+                            const float2 *__restrict__ tw)
+{
+    const int L = 1 << logL;
+    float2 *src = b0, *dst = b1;
+    int logNs = 0;
+    for (; logNs + 2 <= logL; logNs += 2) {
+        const int nb = L >> 2, Ns = 1 << logNs;
+        for (int b = threadIdx.x; b < G * nb; b += blockDim.x) {
+            const int g = b / nb, j = b - g * nb, k = j & (Ns - 1);
+            const float2 *s = src + g * pitch;
+            float2 *d = dst + g * pitch;
+            float2 a0 = s[j], a1 = s[j + nb], a2 = s[j + 2 * nb], a3 = s[j + 3 * nb];
+            if (Ns > 1) {
+                const int step = k << (logL - logNs - 2);
+                a1 = cmul(a1, twiddle<DIR>(tw, L, step));
+                a2 = cmul(a2, twiddle<DIR>(tw, L, 2 * step));
+                a3 = cmul(a3, twiddle<DIR>(tw, L, 3 * step));
+            }
+            const float2 t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), t3 = csub(a1, a3);
+            const float2 it3 = DIR < 0 ? make_float2(t3.y, -t3.x) : make_float2(-t3.y, t3.x);
+            const int base = ((j - k) << 2) + k;
+            d[base] = cadd(t0, t2);
+            d[base + Ns] = cadd(t1, it3);
+            d[base + 2 * Ns] = csub(t0, t2);
+            d[base + 3 * Ns] = csub(t1, it3);
+        }
+        __syncthreads();
+        float2 *t = src;
+        src = dst;
+        dst = t;
+    }
+    if (logNs < logL) {
+        const int nb = L >> 1, Ns = 1 << logNs;
+        for (int b = threadIdx.x; b < G * nb; b += blockDim.x) {
+            const int g = b / nb, j = b - g * nb, k = j & (Ns - 1);
+            const float2 *s = src + g * pitch;
+            float2 *d = dst + g * pitch;
+            float2 a0 = s[j], a1 = s[j + nb];
+            if (Ns > 1)
+                a1 = cmul(a1, twiddle<DIR>(tw, L, k << (logL - logNs - 1)));
+            const int base = ((j - k) << 1) + k;
+            d[base] = cadd(a0, a1);
+            d[base + Ns] = csub(a0, a1);
+        }
+        __syncthreads();
+        float2 *t = src;
+        src = dst;
+        dst = t;
+    }
+    return src;
+}
+
+// grid (ceil((Nx/2+1)/CG), npairs), block 256, smem 2*CG*(Ny+1) float2
+// Forward column FFTs of image 1 (b): X2[kx][ky].
+__global__ void k_colfft(PairDev *pairs, const float2 *__restrict__ tw, int CG)
+{
+    extern __shared__ float2 smem[];
+    PairDev &p = pairs[blockIdx.y];
+    if (p.status != 0)
+        return;
+    const int L = 1 << (p.logNx - 1);
+    const int Ny = p.Ny, logNy = p.logNy, pitch = Ny + 1;
+    const int kx0 = blockIdx.x * CG;
+    if (kx0 > L)
+        return;
+    const int G = min(CG, L + 1 - kx0);
+    float2 *b0 = smem, *b1 = smem + CG * pitch;
+    const float2 *T = p.T[1];
+    const int Ts = p.Ts[1], h = p.h[1];
+    for (int e = threadIdx.x; e < G * Ny; e += blockDim.x) {
+        const int g = e >> logNy, y = e & (Ny - 1);
+        b0[g * pitch + y] = (y < h) ? T[(long long)(kx0 + g) * Ts + y] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    float2 *res = fft_cols<-1>(b0, b1, G, logNy, pitch, tw);
+    for (int e = threadIdx.x; e < G * Ny; e += blockDim.x) {
+        const int g = e >> logNy, y = e & (Ny - 1);
+        p.X2[(long long)(kx0 + g) * Ny + y] = res[g * pitch + y];
+    }
+}
+
+// grid (ceil((Nx/2+1)/CG), npairs): image 0 (a) column FFTs, cross spectrum
+// X2 * conj(X1) (0_GEN/Correlation.cpp:977-985), inverse column FFTs, store
+// the window's lag rows Q[kx][j].
+__global__ void k_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int CG)
+{
+    extern __shared__ float2 smem[];
+    PairDev &p = pairs[blockIdx.y];
+    if (p.status != 0)
+        return;
+    const int L = 1 << (p.logNx - 1);
+    const int Ny = p.Ny, logNy = p.logNy, pitch = Ny + 1;
+    const int kx0 = blockIdx.x * CG;
+    if (kx0 > L)
+        return;
+    const int G = min(CG, L + 1 - kx0);
+    float2 *b0 = smem, *b1 = smem + CG * pitch;
+    const float2 *T = p.T[0];
+    const int Ts = p.Ts[0], h = p.h[0];
+    for (int e = threadIdx.x; e < G * Ny; e += blockDim.x) {
+        const int g = e >> logNy, y = e & (Ny - 1);
+        b0[g * pitch + y] = (y < h) ? T[(long long)(kx0 + g) * Ts + y] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    float2 *res = fft_cols<-1>(b0, b1, G, logNy, pitch, tw);
+    float2 *oth = (res == b0) ? b1 : b0;
+    for (int e = threadIdx.x; e < G * Ny; e += blockDim.x) {
+        const int g = e >> logNy, y = e & (Ny - 1);
+        const float2 x2 = p.X2[(long long)(kx0 + g) * Ny + y];
+        res[g * pitch + y] = cmulc(x2, res[g * pitch + y]);
+    }
+    __syncthreads();
+    float2 *fin = fft_cols<+1>(res, oth, G, logNy, pitch, tw);
+    const int Wy = p.yhi - p.ylo + 1;
+    for (int e = threadIdx.x; e < G * Wy; e += blockDim.x) {
+        const int g = e / Wy, j = e - g * Wy;
+        const int y = p.ylo + j;
+        const int ys = y < 0 ? y + Ny : y;
+        p.Q[(long long)(kx0 + g) * Wy + j] = fin[g * pitch + ys];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// lag rows: inverse real FFT, normalisation, legality, disc, row argmax
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void best_merge(double &r, long long &k, double r2, long long k2)
+{
+    if (r2 > r || (r2 == r && k2 < k)) {
+        r = r2;
+        k = k2;
+    }
+}
+
+// grid (ceil(maxWy/RBL), npairs), block 256, smem 2*RBL*(L+1) float2
+__global__ void k_lagrow(PairDev *pairs, const float2 *__restrict__ tw, int RBL)
+{
+    extern __shared__ float2 smem[];
+    __shared__ double red_r[32];
+    __shared__ long long red_k[32];
+    PairDev &p = pairs[blockIdx.y];
+    if (p.status != 0)
+        return;
+    const int Wy = p.yhi - p.ylo + 1, Wx = p.xhi - p.xlo + 1;
+    const int j0 = blockIdx.x * RBL;
+    if (j0 >= Wy)
+        return;
+    const int logL = p.logNx - 1, L = 1 << logL, pitch = L + 1;
+    const int Nx = p.Nx, Ny = p.Ny;
+    float2 *bX = smem + RBL * pitch;   // spectrum rows (L+1 bins)
+    float2 *bZ = smem;                 // pre-processed rows
+    const int rows = min(RBL, Wy - j0);
+    for (int e = threadIdx.x; e < (L + 1) * RBL; e += blockDim.x) {
+        const int kx = e / RBL, r = e - kx * RBL;
+        bX[r * pitch + kx] = (r < rows) ? p.Q[(long long)kx * Wy + j0 + r] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < RBL * L; e += blockDim.x) {
+        const int r = e >> logL, k = e & (L - 1);
+        bZ[r * pitch + k] = c2r_pre(bX + r * pitch, L, k, tw);
+    }
+    __syncthreads();
+    float2 *res = fft_cols<+1>(bZ, bX, RBL, logL, pitch, tw);
+    const double inv = 1.0 / ((double)Nx * (double)Ny);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int r = 0; r < rows; ++r) {
+        const int j = j0 + r, y = p.ylo + j;
+        const long long dy = y - p.oy;
+        const int xr = isqrt_ll(p.rsqr - dy * dy);
+        const int xa = xr < 0 ? 1 : max(p.xlo, p.ox - xr);
+        const int xb = xr < 0 ? 0 : min(p.xhi, p.ox + xr);
+        const int ys = y < 0 ? y + Ny : y;
+        double br = -1.0e30;
+        long long bk = 0x7fffffffffffffffLL;
+        const float *row = (const float *)(res + r * pitch);
+        for (int x = p.xlo + threadIdx.x; x <= p.xhi; x += blockDim.x) {
+            double rv = 0.0;
+            if (x >= xa && x <= xb) {
+                const int xs = x < 0 ? x + Nx : x;
+                const double cs = (double)row[xs] * inv;
+                if (lag_r(p, x, y, cs, rv))
+                    best_merge(br, bk, rv, (long long)ys * Nx + xs);
+            }
+            p.rr[(long long)j * Wx + (x - p.xlo)] = rv;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double r2 = __shfl_down_sync(0xffffffff, br, o);
+            const long long k2 = __shfl_down_sync(0xffffffff, bk, o);
+            best_merge(br, bk, r2, k2);
+        }
+        if (lane == 0) {
+            red_r[wid] = br;
+            red_k[wid] = bk;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int q = 1; q < nw; ++q)
+                best_merge(br, bk, red_r[q], red_k[q]);
+            p.rb[j].r = br;
+            p.rb[j].key = bk;
+        }
+        __syncthreads();
+    }
+}
+
+// value at FFT storage index (xs, ys) after the reference's lag loop:
+// r for a legal lag in the disc, 0 otherwise (dead zone, outside the disc,
+// illegal) -- the rslt array ParabPeakFFT reads.
+__device__ double stored_value(const PairDev &p, int xs, int ys)
+{
+    const int nnegx = p.w[0] - 1, nposx = p.w[1];
+    const int nnegy = p.h[0] - 1, nposy = p.h[1];
+    int x, y;
+    if (xs >= p.Nx - nnegx)
+        x = xs - p.Nx;
+    else if (xs < nposx)
+        x = xs;
+    else
+        return 0.0;
+    if (ys >= p.Ny - nnegy)
+        y = ys - p.Ny;
+    else if (ys < nposy)
+        y = ys;
+    else
+        return 0.0;
+    if (x < p.xlo || x > p.xhi || y < p.ylo || y > p.yhi)
+        return 0.0;
+    const int Wx = p.xhi - p.xlo + 1;
+    return p.rr[(long long)(y - p.ylo) * Wx + (x - p.xlo)];
+}
+
+// grid (npairs), block 256
+__global__ void k_final(PairDev *pairs, int nreal_x_is_one, int nreal_y_is_one)
+{
+    __shared__ double red_r[32];
+    __shared__ long long red_k[32];
+    PairDev &p = pairs[blockIdx.x];
+    if (p.status != 0)
+        return;
+    const int Wy = p.yhi - p.ylo + 1;
+    double br = -1.0e30;
+    long long bk = 0x7fffffffffffffffLL;
+    for (int j = threadIdx.x; j < Wy; j += blockDim.x)
+        best_merge(br, bk, p.rb[j].r, p.rb[j].key);
+    for (int o = 16; o > 0; o >>= 1) {
+        const double r2 = __shfl_down_sync(0xffffffff, br, o);
+        const long long k2 = __shfl_down_sync(0xffffffff, bk, o);
+        best_merge(br, bk, r2, k2);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        red_r[wid] = br;
+        red_k[wid] = bk;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0)
+        return;
+    for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
+        best_merge(br, bk, red_r[q], red_k[q]);
+    if (br < -2.0) {
+        p.status = ALN_NO_PEAK;
+        p.r = p.dx = p.dy = 0.0;
+        p.px = p.py = 0;
+        return;
+    }
+    const int Nx = p.Nx, Ny = p.Ny;
+    const int ys = (int)(bk / Nx), xs = (int)(bk - (long long)ys * Nx);
+    const int bigx = xs >= Nx - (p.w[0] - 1) ? xs - Nx : xs;
+    const int bigy = ys >= Ny - (p.h[0] - 1) ? ys - Ny : ys;
+    // ParabPeakFFT, 0_GEN/Correlation.cpp:482-517, d = 1, on the reference's
+    // FFT-sized raster (nx, ny are the reference's sizes).
+    const int nx = nreal_x_is_one ? 1 : Nx, ny = nreal_y_is_one ? 1 : Ny;
+    double xpk = bigx, ypk = bigy;
+    const int ix = bigx, iy = bigy;
+    const double z1 = br;
+    double z0, z2;
+    if (ix - 1 >= 0 && ix + 1 < nx && (z0 = stored_value(p, ix - 1, ys)) != 0.0 &&
+        (z2 = stored_value(p, ix + 1, ys)) != 0.0) {
+        z0 = 1 * (z0 - z2) / (2 * (z0 + z2 - z1 - z1));
+        if (fabs(z0) <= 8 * 1)
+            xpk += z0;
+    }
+    if (iy - 1 >= 0 && iy + 1 < ny && (z0 = stored_value(p, xs, iy - 1)) != 0.0 &&
+        (z2 = stored_value(p, xs, iy + 1)) != 0.0) {
+        z0 = 1 * (z0 - z2) / (2 * (z0 + z2 - z1 - z1));
+        if (fabs(z0) <= 8 * 1)
+            ypk += z0;
+    }
+    p.r = br;
+    p.dx = xpk + (p.x0[1] - p.x0[0]);
+    p.dy = ypk + (p.y0[1] - p.y0[0]);
+    p.px = bigx;
+    p.py = bigy;
+    p.status = ALN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FFT_2D / IFT_2D drop-ins (FFTW layout, FP64 on the host side)
+// ---------------------------------------------------------------------------
+
+// X2[kx][ky] (float2) -> out[ky][kx] (double complex), FFTW r2c layout
+__global__ void k_spec_to_fftw(const float2 *X, int L1, int Ny, double *out)
+{
+    const long long n = (long long)L1 * Ny;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int ky = (int)(e / L1), kx = (int)(e - (long long)ky * L1);
+        const float2 v = X[(long long)kx * Ny + ky];
+        out[2 * e] = v.x;
+        out[2 * e + 1] = v.y;
+    }
+}
+
+// in[ky][kx] (double complex) -> S[kx][ky] (float2)
+__global__ void k_fftw_to_spec(const double *in, int L1, int Ny, float2 *S)
+{
+    const long long n = (long long)L1 * Ny;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int kx = (int)(e / Ny), ky = (int)(e - (long long)kx * Ny);
+        S[e] = make_float2((float)in[2 * ((long long)ky * L1 + kx)],
+                           (float)in[2 * ((long long)ky * L1 + kx) + 1]);
+    }
+}
+
+// inverse column FFTs of S[kx][ky] (all rows) -> Q[kx][y] (in place allowed)
+__global__ void k_icolfft(const float2 *S, float2 *Qo, int L1, int logNy,
+                          const float2 *__restrict__ tw, int CG)
+{
+    extern __shared__ float2 smem[];
+    const int Ny = 1 << logNy, pitch = Ny + 1;
+    const int kx0 = blockIdx.x * CG;
+    if (kx0 >= L1)
+        return;
+    const int G = min(CG, L1 - kx0);
+    float2 *b0 = smem, *b1 = smem + CG * pitch;
+    for (int e = threadIdx.x; e < G * Ny; e += blockDim.x) {
+        const int g = e >> logNy, y = e & (Ny - 1);
+        b0[g * pitch + y] = S[(long long)(kx0 + g) * Ny + y];
+    }
+    __syncthreads();
+    float2 *res = fft_cols<+1>(b0, b1, G, logNy, pitch, tw);
+    for (int e = threadIdx.x; e < G * Ny; e += blockDim.x) {
+        const int g = e >> logNy, y = e & (Ny - 1);
+        Qo[(long long)(kx0 + g) * Ny + y] = res[g * pitch + y];
+    }
+}
+
+// inverse real rows of Q[kx][y] -> out[y][x] (double, unnormalised)
+__global__ void k_irowfft(const float2 *Q, int logNx, int Ny, double *out,
+                          const float2 *__restrict__ tw, int RBL)
+{
+    extern __shared__ float2 smem[];
+    const int logL = logNx - 1, L = 1 << logL, pitch = L + 1;
+    const int y0 = blockIdx.x * RBL;
+    if (y0 >= Ny)
+        return;
+    const int rows = min(RBL, Ny - y0);
+    float2 *bX = smem + RBL * pitch, *bZ = smem;
+    for (int e = threadIdx.x; e < (L + 1) * RBL; e += blockDim.x) {
+        const int kx = e / RBL, r = e - kx * RBL;
+        bX[r * pitch + kx] = (r < rows) ? Q[(long long)kx * Ny + y0 + r] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < RBL * L; e += blockDim.x) {
+        const int r = e >> logL, k = e & (L - 1);
+        bZ[r * pitch + k] = c2r_pre(bX + r * pitch, L, k, tw);
+    }
+    __syncthreads();
+    float2 *res = fft_cols<+1>(bZ, bX, RBL, logL, pitch, tw);
+    const int Nx = 2 * L;
+    for (int e = threadIdx.x; e < rows * Nx; e += blockDim.x) {
+        const int r = e / Nx, x = e - r * Nx;
+        const float *row = (const float *)(res + r * pitch);
+        out[(long long)(y0 + r) * Nx + x] = (double)row[x];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+struct aln_ctx {
+    int device;
+    cudaStream_t stream;
+    float2 *tw;
+    char *ws;
+    size_t ws_cap;
+    PairDev *dpairs;
+    size_t dpairs_cap;
+    size_t ws_budget;
+    char err[512];
+};
+
+static char g_create_err[512];
+
+static int set_err(aln_ctx *c, int code, const char *fmt, ...)
+{
+    char *buf = c ? c->err : g_create_err;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, 512, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CK(call)                                                                     \
+    do {                                                                             \
+        cudaError_t e_ = (call);                                                     \
+        if (e_ != cudaSuccess)                                                       \
+            return set_err(ctx, ALN_ERR_CUDA, "%s: %s (%s:%d)", #call,               \
+                           cudaGetErrorString(e_), __FILE__, __LINE__);              \
+    } while (0)
+
+static const int kSmemMax = 200 * 1024;
+
+static int configure_kernels()
+{
+    const void *ks[] = {(const void *)k_rowfft, (const void *)k_colfft,
+                        (const void *)k_corrcol, (const void *)k_lagrow,
+                        (const void *)k_icolfft, (const void *)k_irowfft};
+    for (const void *k : ks) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kSmemMax);
+        if (e != cudaSuccess)
+            return (int)e;
+    }
+    return 0;
+}
+
+extern "C" int aln_ctx_create(int device, aln_ctx **out)
+{
+    *out = nullptr;
+    aln_ctx *ctx = nullptr;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess)
+        return set_err(nullptr, ALN_ERR_CUDA, "cudaSetDevice(%d): %s", device,
+                       cudaGetErrorString(e));
+    ctx = new aln_ctx();
+    memset(ctx, 0, sizeof *ctx);
+    ctx->device = device;
+    ctx->ws_budget = (size_t)4 << 30;
+    if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        set_err(nullptr, ALN_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
+        delete ctx;
+        return ALN_ERR_CUDA;
+    }
+    if (int ke = configure_kernels()) {
+        set_err(nullptr, ALN_ERR_CUDA, "kernel attributes: %s",
+                cudaGetErrorString((cudaError_t)ke));
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return ALN_ERR_CUDA;
+    }
+    // twiddle table tw[N + m] = exp(-2 pi i m / N), N = 1..ALN_MAX_N
+    std::vector<float2> h(2 * ALN_MAX_N);
+    h[0] = make_float2(1.f, 0.f);
+    for (int N = 1; N <= ALN_MAX_N; N <<= 1)
+        for (int m = 0; m < N; ++m) {
+            const double a = -2.0 * M_PI * (double)m / (double)N;
+            h[N + m] = make_float2((float)cos(a), (float)sin(a));
+        }
+    if ((e = cudaMalloc(&ctx->tw, sizeof(float2) * h.size())) != cudaSuccess ||
+        (e = cudaMemcpy(ctx->tw, h.data(), sizeof(float2) * h.size(),
+                        cudaMemcpyHostToDevice)) != cudaSuccess) {
+        set_err(nullptr, ALN_ERR_CUDA, "twiddles: %s", cudaGetErrorString(e));
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return ALN_ERR_CUDA;
+    }
+    *out = ctx;
+    return ALN_OK;
+}
+
+extern "C" void aln_ctx_destroy(aln_ctx *ctx)
+{
+    if (!ctx)
+        return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->tw);
+    cudaFree(ctx->ws);
+    cudaFree(ctx->dpairs);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" const char *aln_last_error(const aln_ctx *ctx)
+{
+    return ctx ? ctx->err : g_create_err;
+}
+
+static int ceil_pow2(int n)
+{
+    int p = 1;
+    while (p < n)
+        p *= 2;
+    return p;
+}
+
+extern "C" int aln_fft_size(int n1, int n2) { return ceil_pow2(n1 + n2 - 1); }
+
+extern "C" int aln_fft_size_sqr(int w1, int h1, int w2, int h2)
+{
+    return ceil_pow2(std::max(w1 + w2, h1 + h2) - 1);
+}
+
+static int ilog2(int n)
+{
+    int k = 0;
+    while ((1 << k) < n)
+        ++k;
+    return k;
+}
+
+static size_t dtype_size(int dt)
+{
+    switch (dt) {
+    case ALN_U8: return 1;
+    case ALN_U16: return 2;
+    case ALN_F32: return 4;
+    case ALN_F64: return 8;
+    default: return 0;
+    }
+}
+
+static int ensure_ws(aln_ctx *ctx, size_t bytes)
+{
+    if (bytes <= ctx->ws_cap)
+        return ALN_OK;
+    if (ctx->ws) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        cudaFree(ctx->ws);
+        ctx->ws = nullptr;
+        ctx->ws_cap = 0;
+    }
+    size_t cap = bytes + bytes / 4;
+    cudaError_t e = cudaMalloc(&ctx->ws, cap);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(ctx, ALN_ERR_NOMEM, "workspace of %zu bytes: %s", cap,
+                       cudaGetErrorString(e));
+    }
+    ctx->ws_cap = cap;
+    return ALN_OK;
+}
+
+static int ensure_pairs(aln_ctx *ctx, size_t n)
+{
+    if (n <= ctx->dpairs_cap)
+        return ALN_OK;
+    if (ctx->dpairs) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        cudaFree(ctx->dpairs);
+    }
+    size_t cap = std::max<size_t>(n, 64);
+    CK(cudaMalloc(&ctx->dpairs, cap * sizeof(PairDev)));
+    ctx->dpairs_cap = cap;
+    return ALN_OK;
+}
+
+static inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Host-side plan of one pair: sizes, window, needed SAT rows, workspace.
+struct PairPlan {
+    PairDev d;
+    int orig_nx, orig_ny;
+    size_t ws_bytes;
+    size_t in_bytes[2];
+    const aln_pair *src;
+    int index;
+};
+
+static void need_rows(const PairDev &d, int img, int lo[2], int hi[2])
+{
+    // rows T and B-1 (when B > 0) of the overlap box for every lag row
+    int tmin = 1 << 30, tmax = -1, bmin = 1 << 30, bmax = -1;
+    const int h1 = d.h[0], h2 = d.h[1];
+    for (int y = d.ylo; y <= d.yhi; ++y) {
+        int B2 = std::max(0, y), T2 = std::min(h2 - 1, y + h1 - 1);
+        T2 = std::max(T2, B2);
+        const int B = img == 0 ? B2 - y : B2;
+        const int T = img == 0 ? T2 - y : T2;
+        tmin = std::min(tmin, T);
+        tmax = std::max(tmax, T);
+        if (B > 0) {
+            bmin = std::min(bmin, B - 1);
+            bmax = std::max(bmax, B - 1);
+        }
+    }
+    int a0 = tmin, a1 = tmax, c0 = bmin, c1 = bmax;
+    if (c1 < c0) {
+        lo[0] = a0;
+        hi[0] = a1;
+        lo[1] = 1;
+        hi[1] = 0;
+        return;
+    }
+    if (c0 < a0) {
+        std::swap(a0, c0);
+        std::swap(a1, c1);
+    }
+    if (c0 <= a1 + 1) {
+        lo[0] = a0;
+        hi[0] = std::max(a1, c1);
+        lo[1] = 1;
+        hi[1] = 0;
+    } else {
+        lo[0] = a0;
+        hi[0] = a1;
+        lo[1] = c0;
+        hi[1] = c1;
+    }
+}
+
+static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl)
+{
+    PairDev &d = pl.d;
+    memset(&d, 0, sizeof d);
+    const aln_image *im[2] = {&P.a, &P.b};
+    for (int i = 0; i < 2; ++i) {
+        if (!im[i]->data || im[i]->w < 1 || im[i]->h < 1 || im[i]->stride < im[i]->w ||
+            !dtype_size(im[i]->dtype))
+            return set_err(ctx, ALN_ERR_ARG, "image %d: bad data/size/stride/dtype", i);
+        d.img[i] = im[i]->data;
+        d.dt[i] = im[i]->dtype;
+        d.stride[i] = im[i]->stride;
+        d.w[i] = im[i]->w;
+        d.h[i] = im[i]->h;
+        d.x0[i] = im[i]->x0;
+        d.y0[i] = im[i]->y0;
+    }
+    pl.orig_nx = ceil_pow2(d.w[0] + d.w[1] - 1);
+    pl.orig_ny = ceil_pow2(d.h[0] + d.h[1] - 1);
+    d.Nx = std::max(2, pl.orig_nx);
+    d.Ny = std::max(2, pl.orig_ny);
+    if (d.Nx > ALN_MAX_N || d.Ny > ALN_MAX_N)
+        return set_err(ctx, ALN_ERR_UNSUPPORTED, "FFT size %dx%d exceeds %d", d.Nx, d.Ny,
+                       ALN_MAX_N);
+    d.logNx = ilog2(d.Nx);
+    d.logNy = ilog2(d.Ny);
+    d.ox = P.ox;
+    d.oy = P.oy;
+    const long long rad = P.radius < 0 ? -(long long)P.radius : P.radius;
+    d.rsqr = rad * rad;
+    const int R = (int)std::min<long long>(rad, 1 << 20);
+    d.xlo = std::max(-(d.w[0] - 1), P.ox - R);
+    d.xhi = std::min(d.w[1] - 1, P.ox + R);
+    d.ylo = std::max(-(d.h[0] - 1), P.oy - R);
+    d.yhi = std::min(d.h[1] - 1, P.oy + R);
+    d.rgn_kind = P.legal.rgn_kind;
+    d.rgn_a = P.legal.rgn_a;
+    d.rgn_b = P.legal.rgn_b;
+    d.rgn_area = P.legal.rgn_area;
+    d.table_w = P.legal.table_w;
+    d.table_h = P.legal.table_h;
+    d.cnt_kind = P.legal.cnt_kind;
+    d.cnt_n = P.legal.cnt_n;
+    if (d.rgn_kind == ALN_RGN_TABLE &&
+        (!P.legal.table || d.table_w < 1 || d.table_h < 1))
+        return set_err(ctx, ALN_ERR_ARG, "legality table missing");
+    if (d.rgn_kind < 0 || d.rgn_kind > ALN_RGN_TABLE)
+        return set_err(ctx, ALN_ERR_ARG, "bad rgn_kind %d", d.rgn_kind);
+    if (d.xlo > d.xhi || d.ylo > d.yhi) {
+        d.status = ALN_NO_PEAK;   // empty search region
+        pl.ws_bytes = 0;
+        pl.in_bytes[0] = pl.in_bytes[1] = 0;
+        return ALN_OK;
+    }
+    for (int i = 0; i < 2; ++i)
+        need_rows(d, i, d.need_lo[i], d.need_hi[i]);
+    const int L1 = d.Nx / 2 + 1;
+    const int Wy = d.yhi - d.ylo + 1, Wx = d.xhi - d.xlo + 1;
+    size_t b = 0;
+    for (int i = 0; i < 2; ++i) {
+        pl.in_bytes[i] = im[i]->on_device ? 0 : al256((size_t)d.w[i] * d.h[i] * dtype_size(d.dt[i]));
+        b += pl.in_bytes[i];
+        d.Ts[i] = (d.h[i] + 3) & ~3;
+        b += al256((size_t)L1 * d.Ts[i] * sizeof(float2));
+        int ns = 0;
+        for (int k = 0; k < 2; ++k)
+            if (d.need_hi[i][k] >= d.need_lo[i][k])
+                ns += d.need_hi[i][k] - d.need_lo[i][k] + 1;
+        b += 2 * al256((size_t)ns * d.w[i] * sizeof(double)) + al256((size_t)ns * d.w[i] * sizeof(int));
+        b += al256((size_t)d.w[i] * sizeof(double));
+    }
+    b += al256((size_t)L1 * d.Ny * sizeof(float2));
+    b += al256((size_t)L1 * Wy * sizeof(float2));
+    b += al256((size_t)Wx * Wy * sizeof(double));
+    b += al256((size_t)Wy * sizeof(RowBest));
+    if (d.rgn_kind == ALN_RGN_TABLE)
+        b += al256((size_t)d.table_w * d.table_h);
+    pl.ws_bytes = b;
+    return ALN_OK;
+}
+
+// carve a pair's workspace starting at base; returns bytes used
+static size_t carve(PairPlan &pl, char *base, const aln_pair &P)
+{
+    PairDev &d = pl.d;
+    char *p = base;
+    const int L1 = d.Nx / 2 + 1;
+    const int Wy = d.yhi - d.ylo + 1, Wx = d.xhi - d.xlo + 1;
+    for (int i = 0; i < 2; ++i) {
+        if (pl.in_bytes[i]) {
+            d.img[i] = p;
+            d.stride[i] = d.w[i];
+            p += pl.in_bytes[i];
+        }
+        d.T[i] = (float2 *)p;
+        p += al256((size_t)L1 * d.Ts[i] * sizeof(float2));
+        int ns = 0;
+        for (int k = 0; k < 2; ++k)
+            if (d.need_hi[i][k] >= d.need_lo[i][k])
+                ns += d.need_hi[i][k] - d.need_lo[i][k] + 1;
+        d.satS[i] = (double *)p;
+        p += al256((size_t)ns * d.w[i] * sizeof(double));
+        d.satQ[i] = (double *)p;
+        p += al256((size_t)ns * d.w[i] * sizeof(double));
+        d.satN[i] = (int *)p;
+        p += al256((size_t)ns * d.w[i] * sizeof(int));
+        d.colsum[i] = (double *)p;
+        p += al256((size_t)d.w[i] * sizeof(double));
+    }
+    d.X2 = (float2 *)p;
+    p += al256((size_t)L1 * d.Ny * sizeof(float2));
+    d.Q = (float2 *)p;
+    p += al256((size_t)L1 * Wy * sizeof(float2));
+    d.rr = (double *)p;
+    p += al256((size_t)Wx * Wy * sizeof(double));
+    d.rb = (RowBest *)p;
+    p += al256((size_t)Wy * sizeof(RowBest));
+    if (d.rgn_kind == ALN_RGN_TABLE) {
+        d.table = (const unsigned char *)p;
+        p += al256((size_t)d.table_w * d.table_h);
+    }
+    (void)P;
+    return (size_t)(p - base);
+}
+
+static int rows_per_cta(int L) { return std::max(1, std::min(16, 4096 / L)); }
+static int cols_per_cta(int Ny) { return std::max(1, std::min(16, 4096 / Ny)); }
+
+// Runs one chunk of pairs that share (Nx, Ny).
+static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk)
+{
+    const int n = (int)chunk.size();
+    size_t total = 0;
+    for (auto *pl : chunk)
+        total += pl->ws_bytes;
+    if (int rc = ensure_ws(ctx, total))
+        return rc;
+    if (int rc = ensure_pairs(ctx, n))
+        return rc;
+    char *base = ctx->ws;
+    std::vector<PairDev> hd(n);
+    int maxw = 1, maxh = 1, maxslots = 1, maxWy = 1;
+    const int Nx = chunk[0]->d.Nx, Ny = chunk[0]->d.Ny;
+    for (int k = 0; k < n; ++k) {
+        PairPlan &pl = *chunk[k];
+        const aln_pair &P = *pl.src;
+        base += carve(pl, base, P);
+        const aln_image *im[2] = {&P.a, &P.b};
+        for (int i = 0; i < 2; ++i) {
+            if (pl.in_bytes[i]) {
+                const size_t es = dtype_size(im[i]->dtype);
+                CK(cudaMemcpy2DAsync((void *)pl.d.img[i], (size_t)im[i]->w * es, im[i]->data,
+                                     (size_t)im[i]->stride * es, (size_t)im[i]->w * es,
+                                     im[i]->h, cudaMemcpyHostToDevice, ctx->stream));
+            }
+            maxw = std::max(maxw, pl.d.w[i]);
+            maxh = std::max(maxh, pl.d.h[i]);
+            int ns = 0;
+            for (int q = 0; q < 2; ++q)
+                if (pl.d.need_hi[i][q] >= pl.d.need_lo[i][q])
+                    ns += pl.d.need_hi[i][q] - pl.d.need_lo[i][q] + 1;
+            maxslots = std::max(maxslots, ns);
+        }
+        maxWy = std::max(maxWy, pl.d.yhi - pl.d.ylo + 1);
+        hd[k] = pl.d;
+    }
+    // legality tables (host) -> device
+    for (int k = 0; k < n; ++k)
+        if (hd[k].rgn_kind == ALN_RGN_TABLE)
+            CK(cudaMemcpyAsync((void *)hd[k].table, chunk[k]->src->legal.table,
+                               (size_t)hd[k].table_w * hd[k].table_h, cudaMemcpyHostToDevice,
+                               ctx->stream));
+    CK(cudaMemcpyAsync(ctx->dpairs, hd.data(), n * sizeof(PairDev), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    cudaStream_t st = ctx->stream;
+    const int L = Nx / 2;
+    {
+        dim3 g((maxw + 127) / 128, 2, n);
+        k_colsum<<<g, 128, 0, st>>>(ctx->dpairs);
+        k_mean<<<dim3(2, n), 256, 0, st>>>(ctx->dpairs);
+        k_rowscan<<<dim3(maxslots, 2, n), 256, 0, st>>>(ctx->dpairs);
+    }
+    {
+        const int RB = rows_per_cta(L);
+        const size_t sm = 2 * (size_t)RB * (L + 1) * sizeof(float2);
+        k_rowfft<<<dim3((maxh + RB - 1) / RB, 2, n), 256, sm, st>>>(ctx->dpairs, ctx->tw, RB, -1);
+    }
+    {
+        const int CG = cols_per_cta(Ny);
+        const size_t sm = 2 * (size_t)CG * (Ny + 1) * sizeof(float2);
+        const int gx = (L + 1 + CG - 1) / CG;
+        k_colfft<<<dim3(gx, n), 256, sm, st>>>(ctx->dpairs, ctx->tw, CG);
+        k_corrcol<<<dim3(gx, n), 256, sm, st>>>(ctx->dpairs, ctx->tw, CG);
+    }
+    {
+        const int RBL = std::max(1, std::min(8, 4096 / std::max(1, L)));
+        const size_t sm = 2 * (size_t)RBL * (L + 1) * sizeof(float2);
+        k_lagrow<<<dim3((maxWy + RBL - 1) / RBL, n), 256, sm, st>>>(ctx->dpairs, ctx->tw, RBL);
+    }
+    k_final<<<n, 256, 0, st>>>(ctx->dpairs, chunk[0]->orig_nx == 1, chunk[0]->orig_ny == 1);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(hd.data(), ctx->dpairs, n * sizeof(PairDev), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int k = 0; k < n; ++k)
+        chunk[k]->d = hd[k];
+    return ALN_OK;
+}
+
+static void fill_result(const PairPlan &pl, aln_result *o)
+{
+    o->status = pl.d.status == ALN_OK ? ALN_OK : ALN_NO_PEAK;
+    o->r = o->status == ALN_OK ? pl.d.r : 0.0;
+    o->dx = o->status == ALN_OK ? pl.d.dx : 0.0;
+    o->dy = o->status == ALN_OK ? pl.d.dy : 0.0;
+    o->peak_x = pl.d.px;
+    o->peak_y = pl.d.py;
+    o->nx = pl.orig_nx;
+    o->ny = pl.orig_ny;
+}
+
+extern "C" int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *pairs,
+                                      aln_result *out)
+{
+    if (!ctx || npairs < 0 || (npairs && (!pairs || !out)))
+        return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    std::vector<PairPlan> plans(npairs);
+    for (int k = 0; k < npairs; ++k) {
+        plans[k].src = &pairs[k];
+        plans[k].index = k;
+        if (int rc = plan_pair(ctx, pairs[k], plans[k]))
+            return rc;
+    }
+    // group by FFT size, keep submission order inside a group
+    std::map<std::pair<int, int>, std::vector<PairPlan *>> groups;
+    for (auto &pl : plans)
+        if (pl.d.status == 0)
+            groups[{pl.d.Nx, pl.d.Ny}].push_back(&pl);
+    for (auto &g : groups) {
+        std::vector<PairPlan *> chunk;
+        size_t bytes = 0;
+        for (PairPlan *pl : g.second) {
+            if (!chunk.empty() && (bytes + pl->ws_bytes > ctx->ws_budget || chunk.size() >= 4096)) {
+                if (int rc = run_chunk(ctx, chunk))
+                    return rc;
+                chunk.clear();
+                bytes = 0;
+            }
+            chunk.push_back(pl);
+            bytes += pl->ws_bytes;
+        }
+        if (!chunk.empty())
+            if (int rc = run_chunk(ctx, chunk))
+                return rc;
+    }
+    for (int k = 0; k < npairs; ++k)
+        fill_result(plans[k], &out[k]);
+    return ALN_OK;
+}
+
+extern "C" int aln_corr_patches(aln_ctx *ctx, const aln_image *a, const aln_image *b, int ox,
+                                int oy, int radius, const aln_legal *legal, aln_result *out)
+{
+    if (!ctx || !a || !b || !out)
+        return ctx ? set_err(ctx, ALN_ERR_ARG, "null argument") : ALN_ERR_ARG;
+    aln_pair P;
+    memset(&P, 0, sizeof P);
+    P.a = *a;
+    P.b = *b;
+    P.ox = ox;
+    P.oy = oy;
+    P.radius = radius;
+    if (legal)
+        P.legal = *legal;
+    return aln_corr_patches_batch(ctx, 1, &P, out);
+}
+
+extern "C" void aln_parab_peak_fft(double *xpk, double *ypk, int d, const double *I, int nx,
+                                   int ny)
+{
+    // ParabPeakFFT, 0_GEN/Correlation.cpp:482-517 (host arithmetic, O(1))
+    auto lk = [&](int x, int y) {
+        if (x < 0)
+            x += nx;
+        if (y < 0)
+            y += ny;
+        return I[x + (long long)nx * y];
+    };
+    const int ix = (int)*xpk, iy = (int)*ypk;
+    const double z1 = lk(ix, iy);
+    double z0, z2;
+    if (ix - d >= 0 && ix + d < nx && (z0 = lk(ix - d, iy)) != 0.0 &&
+        (z2 = lk(ix + d, iy)) != 0.0) {
+        z0 = d * (z0 - z2) / (2 * (z0 + z2 - z1 - z1));
+        if (fabs(z0) <= 8 * d)
+            *xpk += z0;
+    }
+    if (iy - d >= 0 && iy + d < ny && (z0 = lk(ix, iy - d)) != 0.0 &&
+        (z2 = lk(ix, iy + d)) != 0.0) {
+        z0 = d * (z0 - z2) / (2 * (z0 + z2 - z1 - z1));
+        if (fabs(z0) <= 8 * d)
+            *ypk += z0;
+    }
+}
+
+extern "C" int aln_fft_2d(aln_ctx *ctx, const double *in, int nfast, int nslow, double *out)
+{
+    if (!ctx || !in || !out || nfast < 2 || nslow < 1 || (nfast & (nfast - 1)) ||
+        (nslow & (nslow - 1)))
+        return ctx ? set_err(ctx, ALN_ERR_ARG, "fft_2d: sizes must be powers of two, nfast >= 2")
+                   : ALN_ERR_ARG;
+    if (nfast > ALN_MAX_N || nslow > ALN_MAX_N)
+        return set_err(ctx, ALN_ERR_UNSUPPORTED, "fft_2d: size above %d", ALN_MAX_N);
+    CK(cudaSetDevice(ctx->device));
+    const int L1 = nfast / 2 + 1;
+    const size_t M = (size_t)L1 * nslow;
+    const size_t inb = al256((size_t)nfast * nslow * 8), Tb = al256(M * 8), Xb = al256(M * 8),
+                 ob = al256(M * 16);
+    if (int rc = ensure_ws(ctx, inb + Tb + Xb + ob))
+        return rc;
+    if (int rc = ensure_pairs(ctx, 1))
+        return rc;
+    char *p = ctx->ws;
+    PairDev d;
+    memset(&d, 0, sizeof d);
+    d.img[1] = p;
+    d.dt[1] = ALN_F64;
+    d.stride[1] = nfast;
+    d.w[1] = nfast;
+    d.h[1] = nslow;
+    d.Nx = nfast;
+    d.Ny = std::max(1, nslow);
+    d.logNx = ilog2(nfast);
+    d.logNy = ilog2(nslow);
+    d.T[1] = (float2 *)(p + inb);
+    d.Ts[1] = nslow;
+    d.X2 = (float2 *)(p + inb + Tb);
+    d.mu[1] = 0.0;
+    double *dout = (double *)(p + inb + Tb + Xb);
+    CK(cudaMemcpyAsync(p, in, (size_t)nfast * nslow * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->dpairs, &d, sizeof d, cudaMemcpyHostToDevice, ctx->stream));
+    const int L = nfast / 2;
+    const int RB = rows_per_cta(L);
+    k_rowfft<<<dim3((nslow + RB - 1) / RB, 1, 1), 256, 2 * (size_t)RB * (L + 1) * sizeof(float2),
+               ctx->stream>>>(ctx->dpairs, ctx->tw, RB, 1);
+    const int CG = cols_per_cta(nslow);
+    k_colfft<<<dim3((L1 + CG - 1) / CG, 1), 256, 2 * (size_t)CG * (nslow + 1) * sizeof(float2),
+               ctx->stream>>>(ctx->dpairs, ctx->tw, CG);
+    k_spec_to_fftw<<<std::min<size_t>(4096, (M + 255) / 256), 256, 0, ctx->stream>>>(d.X2, L1, nslow, dout);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, dout, M * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return (int)M;
+}
+
+extern "C" int aln_ift_2d(aln_ctx *ctx, const double *in, int nfast, int nslow, double *out)
+{
+    if (!ctx || !in || !out || nfast < 2 || nslow < 1 || (nfast & (nfast - 1)) ||
+        (nslow & (nslow - 1)))
+        return ctx ? set_err(ctx, ALN_ERR_ARG, "ift_2d: sizes must be powers of two, nfast >= 2")
+                   : ALN_ERR_ARG;
+    if (nfast > ALN_MAX_N || nslow > ALN_MAX_N)
+        return set_err(ctx, ALN_ERR_UNSUPPORTED, "ift_2d: size above %d", ALN_MAX_N);
+    CK(cudaSetDevice(ctx->device));
+    const int L1 = nfast / 2 + 1;
+    const size_t M = (size_t)L1 * nslow;
+    const size_t inb = al256(M * 16), Sb = al256(M * 8), Qb = al256(M * 8),
+                 ob = al256((size_t)nfast * nslow * 8);
+    if (int rc = ensure_ws(ctx, inb + Sb + Qb + ob))
+        return rc;
+    char *p = ctx->ws;
+    double *din = (double *)p;
+    float2 *S = (float2 *)(p + inb);
+    float2 *Q = (float2 *)(p + inb + Sb);
+    double *dout = (double *)(p + inb + Sb + Qb);
+    CK(cudaMemcpyAsync(din, in, M * 16, cudaMemcpyHostToDevice, ctx->stream));
+    k_fftw_to_spec<<<std::min<size_t>(4096, (M + 255) / 256), 256, 0, ctx->stream>>>(din, L1, nslow, S);
+    const int CG = cols_per_cta(nslow);
+    k_icolfft<<<(L1 + CG - 1) / CG, 256, 2 * (size_t)CG * (nslow + 1) * sizeof(float2),
+                ctx->stream>>>(S, Q, L1, ilog2(nslow), ctx->tw, CG);
+    const int L = nfast / 2;
+    const int RBL = std::max(1, std::min(8, 4096 / L));
+    k_irowfft<<<(nslow + RBL - 1) / RBL, 256, 2 * (size_t)RBL * (L + 1) * sizeof(float2),
+                ctx->stream>>>(Q, ilog2(nfast), nslow, dout, ctx->tw, RBL);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, dout, (size_t)nfast * nslow * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ALN_OK;
+}

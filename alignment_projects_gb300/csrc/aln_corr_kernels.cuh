@@ -1,0 +1,52 @@
+// aln_corr_kernels.cuh -- device-side data layout shared by the correlation
+// kernels (aln_corr.cu) and the host orchestration.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+// Best legal lag of one lag row (written by the lag kernel).
+struct RowBest {
+    double r;        // best r in the row, -1e30 if no legal lag
+    long long key;   // storage index iy*Nx + ix of that lag (tie-break: smallest)
+};
+
+// One correlation job as the kernels see it.  Lives in device memory; the
+// kernels write the mean shifts and the result back into it.
+struct PairDev {
+    // inputs: image 0 = patch 1 (a), image 1 = patch 2 (b)
+    const void *img[2];
+    int dt[2];          // enum aln_dtype
+    int stride[2];      // elements per row
+    int w[2], h[2];     // bounding boxes
+    int x0[2], y0[2];   // bounding-box origins B.L, B.B
+    int Nx, Ny, logNx, logNy;
+    // search region: lag window (inclusive) and disc
+    int ox, oy;
+    long long rsqr;
+    int xlo, xhi, ylo, yhi;
+    // legality (typed EvalType)
+    int rgn_kind, rgn_a, rgn_b;
+    long long rgn_area;
+    const unsigned char *table;
+    int table_w, table_h;
+    int cnt_kind;
+    long long cnt_n;
+    // summed-area-table rows needed by the lag window, per image: [lo, hi] x 2
+    int need_lo[2][2], need_hi[2][2];
+    int sat_rows[2];    // last row the column walk must reach (max needed / h-1)
+    // workspace
+    float2 *T[2];       // row-pass output [kx][y], stride Ts[i]
+    int Ts[2];
+    float2 *X2;         // spectrum of image 1 (b): [kx][ky], stride Ny
+    float2 *Q;          // column-inverse output [kx][j], j = y - ylo, stride Wy
+    double *satS[2], *satQ[2];   // summed-area tables of v and v^2, [y][x] stride w
+    int *satN[2];                // summed-area table of (v != 0)
+    double *colsum[2];           // per-column totals (mean shift)
+    double *rr;                  // r over the lag window [j][x - xlo]
+    RowBest *rb;                 // per lag row
+    double mu[2];                // mean shift applied before the FFT
+    // result
+    double r, dx, dy;
+    int status, px, py;
+};

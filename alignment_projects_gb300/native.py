@@ -1,0 +1,203 @@
+"""ctypes bindings of the C ABI (include/aln_corr.h) of libaln_corr.so.
+
+The library is the product: every call here goes to the CUDA kernels.  There
+is no CPU fallback -- if the shared library is missing or no GPU is present,
+loading or creating a context raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+ALN_OK, ALN_NO_PEAK = 0, 1
+ALN_ERR_ARG, ALN_ERR_CUDA, ALN_ERR_NOMEM, ALN_ERR_UNSUPPORTED = -1, -2, -3, -4
+ALN_ERR_TIMEOUT, ALN_ERR_REFUSED, ALN_ERR_CANCELLED = -5, -6, -7
+U8, U16, F32, F64 = 0, 1, 2, 3
+RGN_NONE, RGN_MIN, RGN_SECTION, RGN_EXACT, RGN_TABLE = 0, 1, 2, 3, 4
+CNT_NONE, CNT_GT = 0, 1
+
+_DTYPES = {np.dtype(np.uint8): U8, np.dtype(np.uint16): U16,
+           np.dtype(np.float32): F32, np.dtype(np.float64): F64}
+_TORCH_DTYPES = {"torch.uint8": U8, "torch.uint16": U16, "torch.float32": F32,
+                 "torch.float64": F64}
+
+
+class AlnImage(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("dtype", C.c_int), ("w", C.c_int), ("h", C.c_int),
+                ("stride", C.c_int), ("x0", C.c_int), ("y0", C.c_int),
+                ("on_device", C.c_int)]
+
+
+class AlnLegal(C.Structure):
+    _fields_ = [("rgn_kind", C.c_int), ("rgn_a", C.c_int), ("rgn_b", C.c_int),
+                ("rgn_area", C.c_longlong), ("table", C.c_void_p), ("table_w", C.c_int),
+                ("table_h", C.c_int), ("cnt_kind", C.c_int), ("cnt_n", C.c_longlong)]
+
+
+class AlnResult(C.Structure):
+    _fields_ = [("r", C.c_double), ("dx", C.c_double), ("dy", C.c_double),
+                ("status", C.c_int), ("peak_x", C.c_int), ("peak_y", C.c_int),
+                ("nx", C.c_int), ("ny", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class AlnPair(C.Structure):
+    _fields_ = [("a", AlnImage), ("b", AlnImage), ("ox", C.c_int), ("oy", C.c_int),
+                ("radius", C.c_int), ("legal", AlnLegal)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libaln_corr.so (building it first when sources are newer)."""
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        L.aln_ctx_create.argtypes = [C.c_int, C.POINTER(C.c_void_p)]
+        L.aln_ctx_destroy.argtypes = [C.c_void_p]
+        L.aln_last_error.restype = C.c_char_p
+        L.aln_last_error.argtypes = [C.c_void_p]
+        L.aln_corr_patches.argtypes = [C.c_void_p, C.POINTER(AlnImage), C.POINTER(AlnImage),
+                                       C.c_int, C.c_int, C.c_int, C.POINTER(AlnLegal),
+                                       C.POINTER(AlnResult)]
+        L.aln_corr_patches_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnPair),
+                                             C.POINTER(AlnResult)]
+        L.aln_fft_2d.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        L.aln_ift_2d.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        L.aln_parab_peak_fft.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
+                                         C.c_void_p, C.c_int, C.c_int]
+        _lib = L
+    return _lib
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+class AlnError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"aln error {code}: {msg}")
+        self.code = code
+
+
+def legal(rgn=RGN_NONE, a=0, b=0, area=0, cnt=CNT_NONE, n=0, table=None) -> AlnLegal:
+    """Typed LegalRgn / LegalCnt (see aln_legal in include/aln_corr.h)."""
+    L = AlnLegal(rgn, a, b, area, None, 0, 0, cnt, n)
+    if table is not None:
+        t = np.ascontiguousarray(table, dtype=np.uint8)
+        L.rgn_kind = RGN_TABLE
+        L.table = t.ctypes.data
+        L.table_h, L.table_w = t.shape
+        L._keep = t  # keep the buffer alive with the struct
+    return L
+
+
+def image(arr, x0: int = 0, y0: int = 0) -> AlnImage:
+    """Describe a 2D raster (numpy array on the host, or a CUDA torch tensor)."""
+    if hasattr(arr, "data_ptr"):  # torch tensor
+        assert arr.dim() == 2 and arr.stride(1) == 1
+        dt = _TORCH_DTYPES[str(arr.dtype)]
+        im = AlnImage(arr.data_ptr(), dt, arr.shape[1], arr.shape[0], arr.stride(0), x0, y0,
+                      1 if arr.is_cuda else 0)
+        im._keep = arr
+        return im
+    a = np.asarray(arr)
+    if a.dtype not in _DTYPES:
+        a = a.astype(np.float64)
+    if a.strides[1] != a.itemsize:
+        a = np.ascontiguousarray(a)
+    im = AlnImage(a.ctypes.data, _DTYPES[a.dtype], a.shape[1], a.shape[0],
+                  a.strides[0] // a.itemsize, x0, y0, 0)
+    im._keep = a
+    return im
+
+
+class Context:
+    """One aln_ctx: a CUDA stream plus workspaces on one device."""
+
+    def __init__(self, device: int = 0):
+        self._L = lib()
+        h = C.c_void_p()
+        rc = self._L.aln_ctx_create(device, C.byref(h))
+        if rc != ALN_OK:
+            raise AlnError(rc, self._L.aln_last_error(None).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.aln_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc < 0:
+            raise AlnError(rc, self._L.aln_last_error(self.h).decode())
+        return rc
+
+    # -- FFT support (Correlation.h FFT_2D / IFT_2D) -----------------------
+    def fft_2d(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        ny, nx = x.shape
+        out = np.zeros((ny, nx // 2 + 1), np.complex128)
+        self._check(self._L.aln_fft_2d(self.h, x.ctypes.data, nx, ny, out.ctypes.data))
+        return out
+
+    def ift_2d(self, spec, nfast):
+        spec = np.ascontiguousarray(spec, np.complex128)
+        ny = spec.shape[0]
+        out = np.zeros((ny, nfast), np.float64)
+        self._check(self._L.aln_ift_2d(self.h, spec.ctypes.data, nfast, ny, out.ctypes.data))
+        return out
+
+    # -- CorrPatches ----------------------------------------------------------
+    def corr_patches(self, a, b, ox=0, oy=0, radius=4096, lg=None, a_origin=(0, 0),
+                     b_origin=(0, 0)) -> dict:
+        ia = image(a, *a_origin)
+        ib = image(b, *b_origin)
+        res = AlnResult()
+        self._check(self._L.aln_corr_patches(self.h, C.byref(ia), C.byref(ib), ox, oy, radius,
+                                             C.byref(lg) if lg is not None else None,
+                                             C.byref(res)))
+        return res.as_dict()
+
+    def corr_patches_batch(self, pairs) -> list:
+        """pairs: iterable of dicts with a, b, [ox, oy, radius, legal, a_origin, b_origin]."""
+        pairs = list(pairs)
+        arr = (AlnPair * len(pairs))()
+        keep = []
+        for k, p in enumerate(pairs):
+            ia = image(p["a"], *p.get("a_origin", (0, 0)))
+            ib = image(p["b"], *p.get("b_origin", (0, 0)))
+            keep += [ia, ib]
+            arr[k].a = ia
+            arr[k].b = ib
+            arr[k].ox = p.get("ox", 0)
+            arr[k].oy = p.get("oy", 0)
+            arr[k].radius = p.get("radius", 4096)
+            lg = p.get("legal")
+            if lg is not None:
+                keep.append(lg)
+                arr[k].legal = lg
+        out = (AlnResult * len(pairs))()
+        self._check(self._L.aln_corr_patches_batch(self.h, len(pairs), arr, out))
+        return [o.as_dict() for o in out]
+
+
+def parab_peak_fft(xpk, ypk, d, I):
+    I = np.ascontiguousarray(I, np.float64)
+    x, y = C.c_double(xpk), C.c_double(ypk)
+    lib().aln_parab_peak_fft(C.byref(x), C.byref(y), d, I.ctypes.data, I.shape[1], I.shape[0])
+    return x.value, y.value

@@ -1,0 +1,241 @@
+"""GPU parity: the CUDA CorrPatches / FFT path against the oracle and the
+reference's golden outputs, through the C ABI.
+
+Tolerances (FP32 FFTs, FP64 normalisation): the integer peak equals the
+oracle's wherever the oracle's top-two margin exceeds 1e-3; r within 1e-4;
+sub-pixel dx, dy within 0.01 px.
+"""
+import numpy as np
+import pytest
+
+from conftest import legal_from, load_golden
+
+pytestmark = pytest.mark.gpu
+
+R_TOL = 1e-4
+PX_TOL = 0.01
+MARGIN = 1e-3
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import alignment_projects_gb300 as aln
+    c = aln.Context(0)
+    yield c
+    c.close()
+
+
+def aln_legal(o_legal):
+    import alignment_projects_gb300 as aln
+    return aln.legal(o_legal.rgn_kind, o_legal.rgn_a, o_legal.rgn_b, o_legal.rgn_area,
+                     o_legal.cnt_kind, o_legal.cnt_n)
+
+
+def points_to_raster(pts, vals):
+    """Integer point cloud -> (raster, origin): ImageFromValuesAndPoints for
+    integer coordinates (duplicates add)."""
+    pts = np.asarray(pts)
+    assert np.all(pts == np.round(pts))
+    x = pts[:, 0].astype(np.int64)
+    y = pts[:, 1].astype(np.int64)
+    x0, y0 = x.min(), y.min()
+    w, h = x.max() - x0 + 1, y.max() - y0 + 1
+    img = np.zeros((h, w), np.float64)
+    np.add.at(img, (y - y0, x - x0), vals)
+    return img, (int(x0), int(y0))
+
+
+def assert_parity(g, o, ctxmsg=""):
+    import alignment_projects_gb300 as aln
+    if o["status"] == 1:
+        assert g["status"] == aln.ALN_NO_PEAK, (ctxmsg, g, o)
+        return
+    assert g["status"] == aln.ALN_OK, (ctxmsg, g)
+    assert abs(g["r"] - o["r"]) <= R_TOL, (ctxmsg, g["r"], o["r"])
+    if o["r"] - o["second"] > MARGIN:
+        assert (g["peak_x"], g["peak_y"]) == (o["bigx"], o["bigy"]), (ctxmsg, g, o)
+        assert abs(g["dx"] - o["dx"]) <= PX_TOL and abs(g["dy"] - o["dy"]) <= PX_TOL, (ctxmsg, g, o)
+
+
+# ---------------------------------------------------------------- FFT_2D / IFT_2D
+
+@pytest.mark.parametrize("shape", [(1, 2), (4, 8), (8, 16), (64, 32), (32, 128), (256, 512),
+                                   (1024, 1024), (4096, 512), (512, 4096), (8192, 64)])
+def test_fft_2d_matches_numpy(ctx, shape):
+    rng = np.random.default_rng(shape[0] * 7 + shape[1])
+    x = rng.standard_normal(shape)
+    F = ctx.fft_2d(x)
+    ref = np.fft.rfft2(x)
+    err = np.abs(F - ref).max() / np.abs(ref).max()
+    assert err < 2e-6, err
+    back = ctx.ift_2d(ref, shape[1])
+    err2 = np.abs(back / x.size - x).max() / np.abs(x).max()
+    assert err2 < 2e-6, err2
+
+
+def test_fft_golden(ctx):
+    for case, d in load_golden("fft").items():
+        if "x" not in d:
+            continue
+        F = ctx.fft_2d(d["x"])
+        assert np.abs(F - d["F"]).max() <= 2e-6 * np.abs(d["F"]).max(), case
+
+
+def test_kat_time_fft(ctx):
+    """Retired_Proj/4_Time_FFT: a copy shifted by index 2N+3 is recovered."""
+    d = load_golden("fft")["kat_time_fft"]
+    N = d["in1"].shape[0]
+    G = ctx.ift_2d(ctx.fft_2d(d["in1"]) * np.conj(ctx.fft_2d(d["in2"])), N)
+    assert int(np.argmax(G)) == int(d["argmax"])
+
+
+# ---------------------------------------------------------------- CorrPatches golden
+
+@pytest.mark.parametrize("case", sorted(load_golden("corr_patches")))
+def test_corr_patches_golden(ctx, orc, case):
+    d = load_golden("corr_patches")[case]
+    a, ao = points_to_raster(d["pa"], d["va"])
+    b, bo = points_to_raster(d["pb"], d["vb"])
+    lg = legal_from(d["legal"])
+    g = ctx.corr_patches(a, b, int(d["ox"]), int(d["oy"]), int(d["radius"]), aln_legal(lg),
+                         ao, bo)
+    o = orc.corr_patches(d["pa"], d["va"], d["pb"], d["vb"], int(d["ox"]), int(d["oy"]),
+                         int(d["radius"]), lg)
+    # the oracle reproduces the reference bit-exactly (tests/test_oracle_golden.py)
+    assert abs(o["r"] - float(d["r"])) < 1e-12
+    assert_parity(g, o, case)
+    if o["status"] == 0 and o["r"] - o["second"] > MARGIN:
+        assert abs(g["dx"] - float(d["dx"])) <= PX_TOL and abs(g["dy"] - float(d["dy"])) <= PX_TOL
+
+
+def test_kat_testnormcorr(ctx):
+    """Retired_Proj/4_TestNormCorr: the exact copy is found with r = 1 at lag (-4, +2)."""
+    import alignment_projects_gb300 as aln
+    d = load_golden("corr_patches")["kat_testnormcorr"]
+    a, ao = points_to_raster(d["pa"], d["va"])
+    b, bo = points_to_raster(d["pb"], d["vb"])
+    g = ctx.corr_patches(a, b, 0, 0, 4096, aln.legal(aln.RGN_MIN, 2, 2, 0), ao, bo)
+    assert abs(g["r"] - 1.0) < 1e-5
+    assert abs(g["dx"] - float(d["dx"])) < PX_TOL and g["dy"] == pytest.approx(2.0, abs=PX_TOL)
+
+
+# ---------------------------------------------------------------- synthetic workloads
+
+def _oracle_pair(orc, p, lg_o):
+    import oracle
+    A, VA = oracle.image_to_points(p.a)
+    B, VB = oracle.image_to_points(p.b)
+    return orc.corr_patches(A, VA, B, VB, p.ox, p.oy, p.radius, lg_o)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_plain_512_pair(ctx, orc, seed):
+    """The 512^2 uint8 single-pair workload (FFT 1024^2), full lag window."""
+    import oracle
+    from alignment_projects_gb300 import synth
+    p = synth.plain_pair(seed, n=512, margin=64)
+    lg_o = oracle.legal(oracle.RGN_MIN, 32, 32, 0)
+    g = ctx.corr_patches(p.a, p.b, 0, 0, 4096, aln_legal(lg_o))
+    o = _oracle_pair(orc, p, lg_o)
+    assert_parity(g, o, f"plain seed {seed}")
+    assert (g["peak_x"], g["peak_y"]) == p.truth
+
+
+@pytest.mark.parametrize("seed", [11, 12, 13, 14])
+def test_montage_strips(ctx, orc, seed):
+    """Montage overlap strips (W x 2048 / 2048 x W uint8), disc radius 64."""
+    import oracle
+    from alignment_projects_gb300 import synth
+    p = synth.montage_pair(seed)
+    lg_o = oracle.legal(oracle.RGN_SECTION, 1500, 1500, 30000)
+    g = ctx.corr_patches(p.a, p.b, p.ox, p.oy, p.radius, aln_legal(lg_o))
+    o = _oracle_pair(orc, p, lg_o)
+    assert_parity(g, o, f"montage seed {seed}")
+    if not p.decoy:
+        assert (g["peak_x"], g["peak_y"]) == p.truth
+
+
+@pytest.mark.parametrize("seed", range(20, 32))
+def test_uneven_u16(ctx, orc, seed):
+    """uint16 patches of uneven, non-square sizes with a disc."""
+    import oracle
+    from alignment_projects_gb300 import synth
+    p = synth.uneven_pair(seed, smax=512)
+    lg_o = oracle.legal(oracle.RGN_MIN, 8, 8, 0)
+    g = ctx.corr_patches(p.a, p.b, p.ox, p.oy, p.radius, aln_legal(lg_o))
+    o = _oracle_pair(orc, p, lg_o)
+    assert_parity(g, o, f"uneven seed {seed}")
+
+
+def test_batch_equals_single(ctx):
+    """A mixed-size batch gives exactly the per-pair results."""
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300 import synth
+    pairs = []
+    for s in range(6):
+        p = synth.uneven_pair(100 + s, smax=300)
+        pairs.append(dict(a=p.a, b=p.b, ox=p.ox, oy=p.oy, radius=p.radius,
+                          legal=aln.legal(aln.RGN_MIN, 8, 8, 0)))
+    for s in range(3):
+        p = synth.plain_pair(200 + s, n=100, margin=10)
+        pairs.append(dict(a=p.a, b=p.b, legal=aln.legal(aln.RGN_MIN, 16, 16, 0)))
+    batch = ctx.corr_patches_batch(pairs)
+    for p, bres in zip(pairs, batch):
+        single = ctx.corr_patches(p["a"], p["b"], p.get("ox", 0), p.get("oy", 0),
+                                  p.get("radius", 4096), p["legal"])
+        assert bres == single
+
+
+def test_device_resident_inputs(ctx):
+    import torch
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300 import synth
+    p = synth.plain_pair(5, n=200, margin=20)
+    lg = aln.legal(aln.RGN_MIN, 32, 32, 0)
+    host = ctx.corr_patches(p.a, p.b, 0, 0, 4096, lg)
+    da = torch.from_numpy(p.a).cuda()
+    db = torch.from_numpy(p.b).cuda()
+    dev = ctx.corr_patches(da, db, 0, 0, 4096, lg)
+    assert host == dev
+
+
+def test_strided_and_table_legality(ctx, orc):
+    """Row stride > width, and a tabulated LegalRgn callback."""
+    import oracle
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300 import synth
+    p = synth.plain_pair(9, n=120, margin=12)
+    big = np.zeros((120, 160), np.uint8)
+    big[:, :120] = p.a
+    a_view = big[:, :120]  # stride 160
+    tw, th = 120, 120
+    t = np.zeros((th, tw), np.uint8)
+    ys, xs = np.mgrid[1:th + 1, 1:tw + 1]
+    t[(xs * ys > 4000) & ((xs + ys) % 3 != 0)] = 1
+    g = ctx.corr_patches(a_view, p.b, 0, 0, 4096, aln.legal(table=t))
+    lo = oracle.Legal(oracle.RGN_TABLE, 0, 0, 0, t.ctypes.data, tw, th, 0, 0)
+    A, VA = oracle.image_to_points(p.a)
+    B, VB = oracle.image_to_points(p.b)
+    o = orc.corr_patches(A, VA, B, VB, 0, 0, 4096, lo)
+    assert_parity(g, o, "table")
+
+
+def test_no_legal_lag(ctx):
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300 import synth
+    p = synth.plain_pair(4, n=64, margin=8)
+    g = ctx.corr_patches(p.a, p.b, 0, 0, 4096, aln.legal(aln.RGN_EXACT, 999, 999, 0))
+    assert g["status"] == aln.ALN_NO_PEAK and g["r"] == 0.0
+    # disc entirely outside the lag window
+    g = ctx.corr_patches(p.a, p.b, 5000, 5000, 3)
+    assert g["status"] == aln.ALN_NO_PEAK
+
+
+def test_bad_arguments_raise(ctx):
+    import alignment_projects_gb300 as aln
+    a = np.zeros((0, 5), np.uint8)
+    with pytest.raises(aln.AlnError):
+        ctx.corr_patches(a, a)
+    big = np.zeros((5000, 8), np.uint8)
+    with pytest.raises(aln.AlnError):
+        ctx.corr_patches(big, big)   # FFT size 16384 > 8192
