@@ -35,6 +35,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <string>
 #include <vector>
 
 // ---------------------------------------------------------------------------
@@ -631,7 +632,7 @@ __device__ double stored_value(const PairDev &p, int xs, int ys)
 }
 
 // grid (npairs), block 256
-__global__ void k_final(PairDev *pairs, int nreal_x_is_one, int nreal_y_is_one)
+__global__ void k_final(PairDev *pairs, ResultDev *res, int nreal_x_is_one, int nreal_y_is_one)
 {
     __shared__ double red_r[32];
     __shared__ long long red_k[32];
@@ -658,10 +659,14 @@ __global__ void k_final(PairDev *pairs, int nreal_x_is_one, int nreal_y_is_one)
         return;
     for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
         best_merge(br, bk, red_r[q], red_k[q]);
+    ResultDev &o = res[blockIdx.x];
     if (br < -2.0) {
         p.status = ALN_NO_PEAK;
         p.r = p.dx = p.dy = 0.0;
         p.px = p.py = 0;
+        o.r = o.dx = o.dy = 0.0;
+        o.status = ALN_NO_PEAK;
+        o.px = o.py = 0;
         return;
     }
     const int Nx = p.Nx, Ny = p.Ny;
@@ -693,6 +698,12 @@ __global__ void k_final(PairDev *pairs, int nreal_x_is_one, int nreal_y_is_one)
     p.px = bigx;
     p.py = bigy;
     p.status = ALN_OK;
+    o.r = p.r;
+    o.dx = p.dx;
+    o.dy = p.dy;
+    o.status = ALN_OK;
+    o.px = bigx;
+    o.py = bigy;
 }
 
 // ---------------------------------------------------------------------------
@@ -781,6 +792,11 @@ __global__ void k_irowfft(const float2 *Q, int logNx, int Ny, double *out,
 // host side
 // ---------------------------------------------------------------------------
 
+struct ProfRec {
+    const char *name;
+    cudaEvent_t a, b;
+};
+
 struct aln_ctx {
     int device;
     cudaStream_t stream;
@@ -788,10 +804,72 @@ struct aln_ctx {
     char *ws;
     size_t ws_cap;
     PairDev *dpairs;
+    ResultDev *dres;
     size_t dpairs_cap;
     size_t ws_budget;
+    long long h2d_bytes, d2h_bytes;
     char err[512];
+    // tracing: launch count always; CUDA-event times per launch when on
+    long long launches;
+    int prof_on;
+    std::vector<ProfRec> prof;            // pending records
+    std::vector<cudaEvent_t> ev_pool;
+    std::map<std::string, std::pair<long long, double>> prof_acc;  // name -> (launches, ms)
+    std::vector<std::string> prof_names;  // stable storage for returned names
 };
+
+static cudaEvent_t ev_get(aln_ctx *c)
+{
+    if (!c->ev_pool.empty()) {
+        cudaEvent_t e = c->ev_pool.back();
+        c->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+static void prof_begin(aln_ctx *c, const char *name)
+{
+    c->launches++;
+    if (!c->prof_on)
+        return;
+    ProfRec r;
+    r.name = name;
+    r.a = ev_get(c);
+    r.b = ev_get(c);
+    cudaEventRecord(r.a, c->stream);
+    c->prof.push_back(r);
+}
+
+static void prof_end(aln_ctx *c)
+{
+    if (c->prof_on && !c->prof.empty())
+        cudaEventRecord(c->prof.back().b, c->stream);
+}
+
+// fold finished records into the per-kernel totals (stream must be idle)
+static void prof_collect(aln_ctx *c)
+{
+    for (auto &r : c->prof) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, r.a, r.b);
+        auto &acc = c->prof_acc[r.name];
+        acc.first += 1;
+        acc.second += ms;
+        c->ev_pool.push_back(r.a);
+        c->ev_pool.push_back(r.b);
+    }
+    c->prof.clear();
+}
+
+#define LAUNCH(c, name, kern, grid, block, smem, ...)                               \
+    do {                                                                             \
+        prof_begin(c, name);                                                         \
+        kern<<<grid, block, smem, (c)->stream>>>(__VA_ARGS__);                       \
+        prof_end(c);                                                                 \
+    } while (0)
 
 static char g_create_err[512];
 
@@ -838,8 +916,18 @@ extern "C" int aln_ctx_create(int device, aln_ctx **out)
         return set_err(nullptr, ALN_ERR_CUDA, "cudaSetDevice(%d): %s", device,
                        cudaGetErrorString(e));
     ctx = new aln_ctx();
-    memset(ctx, 0, sizeof *ctx);
     ctx->device = device;
+    ctx->stream = nullptr;
+    ctx->tw = nullptr;
+    ctx->ws = nullptr;
+    ctx->ws_cap = 0;
+    ctx->dpairs = nullptr;
+    ctx->dres = nullptr;
+    ctx->dpairs_cap = 0;
+    ctx->h2d_bytes = ctx->d2h_bytes = 0;
+    ctx->err[0] = 0;
+    ctx->launches = 0;
+    ctx->prof_on = 0;
     ctx->ws_budget = (size_t)4 << 30;
     if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) {
         set_err(nullptr, ALN_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
@@ -882,6 +970,10 @@ extern "C" void aln_ctx_destroy(aln_ctx *ctx)
     cudaFree(ctx->tw);
     cudaFree(ctx->ws);
     cudaFree(ctx->dpairs);
+    cudaFree(ctx->dres);
+    prof_collect(ctx);
+    for (cudaEvent_t e : ctx->ev_pool)
+        cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -953,9 +1045,14 @@ static int ensure_pairs(aln_ctx *ctx, size_t n)
     if (ctx->dpairs) {
         CK(cudaStreamSynchronize(ctx->stream));
         cudaFree(ctx->dpairs);
+        cudaFree(ctx->dres);
+        ctx->dpairs = nullptr;
+        ctx->dres = nullptr;
+        ctx->dpairs_cap = 0;
     }
     size_t cap = std::max<size_t>(n, 64);
     CK(cudaMalloc(&ctx->dpairs, cap * sizeof(PairDev)));
+    CK(cudaMalloc(&ctx->dres, cap * sizeof(ResultDev)));
     ctx->dpairs_cap = cap;
     return ALN_OK;
 }
@@ -1168,6 +1265,7 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk)
                 CK(cudaMemcpy2DAsync((void *)pl.d.img[i], (size_t)im[i]->w * es, im[i]->data,
                                      (size_t)im[i]->stride * es, (size_t)im[i]->w * es,
                                      im[i]->h, cudaMemcpyHostToDevice, ctx->stream));
+                ctx->h2d_bytes += (long long)im[i]->w * im[i]->h * es;
             }
             maxw = std::max(maxw, pl.d.w[i]);
             maxh = std::max(maxh, pl.d.h[i]);
@@ -1192,33 +1290,46 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk)
     const int L = Nx / 2;
     {
         dim3 g((maxw + 127) / 128, 2, n);
-        k_colsum<<<g, 128, 0, st>>>(ctx->dpairs);
-        k_mean<<<dim3(2, n), 256, 0, st>>>(ctx->dpairs);
-        k_rowscan<<<dim3(maxslots, 2, n), 256, 0, st>>>(ctx->dpairs);
+        LAUNCH(ctx, "k_colsum", k_colsum, g, 128, 0, ctx->dpairs);
+        LAUNCH(ctx, "k_mean", k_mean, dim3(2, n), 256, 0, ctx->dpairs);
+        LAUNCH(ctx, "k_rowscan", k_rowscan, dim3(maxslots, 2, n), 256, 0, ctx->dpairs);
     }
     {
         const int RB = rows_per_cta(L);
         const size_t sm = 2 * (size_t)RB * (L + 1) * sizeof(float2);
-        k_rowfft<<<dim3((maxh + RB - 1) / RB, 2, n), 256, sm, st>>>(ctx->dpairs, ctx->tw, RB, -1);
+        LAUNCH(ctx, "k_rowfft", k_rowfft, dim3((maxh + RB - 1) / RB, 2, n), 256, sm, ctx->dpairs,
+               ctx->tw, RB, -1);
     }
     {
         const int CG = cols_per_cta(Ny);
         const size_t sm = 2 * (size_t)CG * (Ny + 1) * sizeof(float2);
         const int gx = (L + 1 + CG - 1) / CG;
-        k_colfft<<<dim3(gx, n), 256, sm, st>>>(ctx->dpairs, ctx->tw, CG);
-        k_corrcol<<<dim3(gx, n), 256, sm, st>>>(ctx->dpairs, ctx->tw, CG);
+        LAUNCH(ctx, "k_colfft", k_colfft, dim3(gx, n), 256, sm, ctx->dpairs, ctx->tw, CG);
+        LAUNCH(ctx, "k_corrcol", k_corrcol, dim3(gx, n), 256, sm, ctx->dpairs, ctx->tw, CG);
     }
     {
         const int RBL = std::max(1, std::min(8, 4096 / std::max(1, L)));
         const size_t sm = 2 * (size_t)RBL * (L + 1) * sizeof(float2);
-        k_lagrow<<<dim3((maxWy + RBL - 1) / RBL, n), 256, sm, st>>>(ctx->dpairs, ctx->tw, RBL);
+        LAUNCH(ctx, "k_lagrow", k_lagrow, dim3((maxWy + RBL - 1) / RBL, n), 256, sm, ctx->dpairs,
+               ctx->tw, RBL);
     }
-    k_final<<<n, 256, 0, st>>>(ctx->dpairs, chunk[0]->orig_nx == 1, chunk[0]->orig_ny == 1);
+    LAUNCH(ctx, "k_final", k_final, n, 256, 0, ctx->dpairs, ctx->dres,
+           chunk[0]->orig_nx == 1, chunk[0]->orig_ny == 1);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(hd.data(), ctx->dpairs, n * sizeof(PairDev), cudaMemcpyDeviceToHost, st));
+    std::vector<ResultDev> hr(n);
+    CK(cudaMemcpyAsync(hr.data(), ctx->dres, n * sizeof(ResultDev), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    for (int k = 0; k < n; ++k)
-        chunk[k]->d = hd[k];
+    ctx->d2h_bytes += n * sizeof(ResultDev);
+    prof_collect(ctx);
+    for (int k = 0; k < n; ++k) {
+        PairDev &d = chunk[k]->d;
+        d.r = hr[k].r;
+        d.dx = hr[k].dx;
+        d.dy = hr[k].dy;
+        d.status = hr[k].status;
+        d.px = hr[k].px;
+        d.py = hr[k].py;
+    }
     return ALN_OK;
 }
 
@@ -1357,15 +1468,17 @@ extern "C" int aln_fft_2d(aln_ctx *ctx, const double *in, int nfast, int nslow, 
     CK(cudaMemcpyAsync(ctx->dpairs, &d, sizeof d, cudaMemcpyHostToDevice, ctx->stream));
     const int L = nfast / 2;
     const int RB = rows_per_cta(L);
-    k_rowfft<<<dim3((nslow + RB - 1) / RB, 1, 1), 256, 2 * (size_t)RB * (L + 1) * sizeof(float2),
-               ctx->stream>>>(ctx->dpairs, ctx->tw, RB, 1);
+    LAUNCH(ctx, "k_rowfft", k_rowfft, dim3((nslow + RB - 1) / RB, 1, 1), 256,
+           2 * (size_t)RB * (L + 1) * sizeof(float2), ctx->dpairs, ctx->tw, RB, 1);
     const int CG = cols_per_cta(nslow);
-    k_colfft<<<dim3((L1 + CG - 1) / CG, 1), 256, 2 * (size_t)CG * (nslow + 1) * sizeof(float2),
-               ctx->stream>>>(ctx->dpairs, ctx->tw, CG);
-    k_spec_to_fftw<<<std::min<size_t>(4096, (M + 255) / 256), 256, 0, ctx->stream>>>(d.X2, L1, nslow, dout);
+    LAUNCH(ctx, "k_colfft", k_colfft, dim3((L1 + CG - 1) / CG, 1), 256,
+           2 * (size_t)CG * (nslow + 1) * sizeof(float2), ctx->dpairs, ctx->tw, CG);
+    LAUNCH(ctx, "k_spec_to_fftw", k_spec_to_fftw, (unsigned)std::min<size_t>(4096, (M + 255) / 256),
+           256, 0, d.X2, L1, nslow, dout);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, dout, M * 16, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    prof_collect(ctx);
     return (int)M;
 }
 
@@ -1390,16 +1503,87 @@ extern "C" int aln_ift_2d(aln_ctx *ctx, const double *in, int nfast, int nslow, 
     float2 *Q = (float2 *)(p + inb + Sb);
     double *dout = (double *)(p + inb + Sb + Qb);
     CK(cudaMemcpyAsync(din, in, M * 16, cudaMemcpyHostToDevice, ctx->stream));
-    k_fftw_to_spec<<<std::min<size_t>(4096, (M + 255) / 256), 256, 0, ctx->stream>>>(din, L1, nslow, S);
+    LAUNCH(ctx, "k_fftw_to_spec", k_fftw_to_spec, (unsigned)std::min<size_t>(4096, (M + 255) / 256),
+           256, 0, din, L1, nslow, S);
     const int CG = cols_per_cta(nslow);
-    k_icolfft<<<(L1 + CG - 1) / CG, 256, 2 * (size_t)CG * (nslow + 1) * sizeof(float2),
-                ctx->stream>>>(S, Q, L1, ilog2(nslow), ctx->tw, CG);
+    LAUNCH(ctx, "k_icolfft", k_icolfft, (L1 + CG - 1) / CG, 256,
+           2 * (size_t)CG * (nslow + 1) * sizeof(float2), S, Q, L1, ilog2(nslow), ctx->tw, CG);
     const int L = nfast / 2;
     const int RBL = std::max(1, std::min(8, 4096 / L));
-    k_irowfft<<<(nslow + RBL - 1) / RBL, 256, 2 * (size_t)RBL * (L + 1) * sizeof(float2),
-                ctx->stream>>>(Q, ilog2(nfast), nslow, dout, ctx->tw, RBL);
+    LAUNCH(ctx, "k_irowfft", k_irowfft, (nslow + RBL - 1) / RBL, 256,
+           2 * (size_t)RBL * (L + 1) * sizeof(float2), Q, ilog2(nfast), nslow, dout, ctx->tw, RBL);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, dout, (size_t)nfast * nslow * 8, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    prof_collect(ctx);
+    return ALN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// tracing (no reference counterpart: the reference logs wall-clock Timer
+// lines, 0_GEN/Timer.cpp:25-52)
+// ---------------------------------------------------------------------------
+
+extern "C" int aln_ctx_set_profiling(aln_ctx *ctx, int on)
+{
+    if (!ctx)
+        return ALN_ERR_ARG;
+    ctx->prof_on = on ? 1 : 0;
+    return ALN_OK;
+}
+
+extern "C" void aln_ctx_profile_reset(aln_ctx *ctx)
+{
+    if (!ctx)
+        return;
+    cudaStreamSynchronize(ctx->stream);
+    prof_collect(ctx);
+    ctx->prof_acc.clear();
+    ctx->launches = 0;
+    ctx->h2d_bytes = ctx->d2h_bytes = 0;
+}
+
+extern "C" int aln_ctx_profile(aln_ctx *ctx, int cap, const char **names,
+                               long long *launches, double *ms)
+{
+    if (!ctx)
+        return ALN_ERR_ARG;
+    cudaStreamSynchronize(ctx->stream);
+    prof_collect(ctx);
+    ctx->prof_names.clear();
+    for (auto &kv : ctx->prof_acc)
+        ctx->prof_names.push_back(kv.first);
+    int k = 0;
+    for (auto &kv : ctx->prof_acc) {
+        if (k >= cap)
+            break;
+        if (names)
+            names[k] = ctx->prof_names[k].c_str();
+        if (launches)
+            launches[k] = kv.second.first;
+        if (ms)
+            ms[k] = kv.second.second;
+        ++k;
+    }
+    return (int)ctx->prof_acc.size();
+}
+
+extern "C" long long aln_ctx_counter(aln_ctx *ctx, int which)
+{
+    if (!ctx)
+        return -1;
+    switch (which) {
+    case 0: return ctx->launches;
+    case 1: return ctx->h2d_bytes;
+    case 2: return ctx->d2h_bytes;
+    default: return -1;
+    }
+}
+
+extern "C" int aln_ctx_set_workspace_limit(aln_ctx *ctx, size_t bytes)
+{
+    if (!ctx || bytes < ((size_t)16 << 20))
+        return ALN_ERR_ARG;
+    ctx->ws_budget = bytes;
     return ALN_OK;
 }

@@ -11,6 +11,12 @@ struct RowBest {
     long long key;   // storage index iy*Nx + ix of that lag (tie-break: smallest)
 };
 
+// Compact per-pair result copied back to the host.
+struct ResultDev {
+    double r, dx, dy;
+    int status, px, py, pad;
+};
+
 // One correlation job as the kernels see it.  Lives in device memory; the
 // kernels write the mean shifts and the result back into it.
 struct PairDev {

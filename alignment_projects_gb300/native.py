@@ -72,6 +72,13 @@ def lib():
                                              C.POINTER(AlnResult)]
         L.aln_fft_2d.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         L.aln_ift_2d.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        L.aln_ctx_set_profiling.argtypes = [C.c_void_p, C.c_int]
+        L.aln_ctx_profile_reset.argtypes = [C.c_void_p]
+        L.aln_ctx_profile.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_char_p),
+                                      C.POINTER(C.c_longlong), C.POINTER(C.c_double)]
+        L.aln_ctx_counter.argtypes = [C.c_void_p, C.c_int]
+        L.aln_ctx_counter.restype = C.c_longlong
+        L.aln_ctx_set_workspace_limit.argtypes = [C.c_void_p, C.c_size_t]
         L.aln_parab_peak_fft.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
                                          C.c_void_p, C.c_int, C.c_int]
         _lib = L
@@ -146,6 +153,30 @@ class Context:
         if rc < 0:
             raise AlnError(rc, self._L.aln_last_error(self.h).decode())
         return rc
+
+    # -- tracing ----------------------------------------------------------
+    def set_profiling(self, on: bool):
+        self._L.aln_ctx_set_profiling(self.h, int(on))
+
+    def profile_reset(self):
+        self._L.aln_ctx_profile_reset(self.h)
+
+    def profile(self) -> dict:
+        """{kernel: (launches, total_ms)} since the last reset."""
+        cap = 64
+        names = (C.c_char_p * cap)()
+        launches = (C.c_longlong * cap)()
+        ms = (C.c_double * cap)()
+        n = self._L.aln_ctx_profile(self.h, cap, names, launches, ms)
+        return {names[i].decode(): (launches[i], ms[i]) for i in range(min(n, cap))}
+
+    def counters(self) -> dict:
+        return {"launches": self._L.aln_ctx_counter(self.h, 0),
+                "h2d_bytes": self._L.aln_ctx_counter(self.h, 1),
+                "d2h_bytes": self._L.aln_ctx_counter(self.h, 2)}
+
+    def set_workspace_limit(self, nbytes: int):
+        self._check(self._L.aln_ctx_set_workspace_limit(self.h, nbytes))
 
     # -- FFT support (Correlation.h FFT_2D / IFT_2D) -----------------------
     def fft_2d(self, x):

@@ -219,3 +219,40 @@ def field_torch(gen, h: int, w: int, device, mean=128.0, std=30.0, ellipses=True
                 m = (uu * uu + vv * vv <= 1.0) & (X >= 0) & (X < w) & (Y >= 0) & (Y < h)
                 img[Y[m].long(), X[m].long()] = 40.0
     return img
+
+
+def montage_batch_torch(seed: int, n: int, device, long_side: int = 2048, wmin: int = 164,
+                        wmax: int = 307, jitter: int = 40, decoy_frac: float = 0.02,
+                        noise: float = 8.0):
+    """n montage overlap pairs (as montage_pair) generated with torch on
+    `device`.  Pair i depends only on (seed, i).  Returns a list of dicts with
+    uint8 tensors a, b, the expected lag `truth`, `decoy`, disc (0, 0, 64)."""
+    import torch
+
+    out = []
+    m = 2 * jitter
+    for i in range(n):
+        s = seed * 1000003 + i
+        rng = np.random.default_rng(s)
+        W = int(rng.integers(wmin, wmax + 1))
+        lr = bool(rng.integers(0, 2))
+        tx, ty = (int(v) for v in rng.integers(-jitter, jitter + 1, 2))
+        decoy = bool(rng.random() < decoy_frac)
+        sw, sh = (W, long_side) if lr else (long_side, W)
+        gen = torch.Generator(device=device)
+        gen.manual_seed(s)
+        f = field_torch(gen, sh + 2 * m, sw + 2 * m, device)
+        na = torch.randn((sh, sw), generator=gen, device=device, dtype=torch.float64)
+        nb = torch.randn((sh, sw), generator=gen, device=device, dtype=torch.float64)
+        a = f[m:m + sh, m:m + sw] + noise * na
+        if decoy:
+            g = field_torch(gen, sh + 2 * m, sw + 2 * m, device)
+            bf = g[m:m + sh, m:m + sw]
+        else:
+            bf = f[m + ty:m + ty + sh, m + tx:m + tx + sw]
+        b = bf + noise * nb
+        a8 = torch.clamp(torch.round(a), 0, 255).to(torch.uint8).contiguous()
+        b8 = torch.clamp(torch.round(b), 0, 255).to(torch.uint8).contiguous()
+        out.append(dict(a=a8, b=b8, truth=(-tx, -ty), decoy=decoy, ox=0, oy=0, radius=64,
+                        lr=lr, W=W))
+    return out

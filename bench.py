@@ -1,0 +1,497 @@
+"""Throughput benchmark of the tile-matching hot path on GB300.
+
+Workload (one "step"): the same-layer montage batch -- 4096 neighbour pairs
+of uint8 overlap strips (W x 2048 or 2048 x W, W ~ U[164, 307]) cut from
+2048^2 tiles of the seeded synthetic EM-like generator, +-40 px jitter, 2 %
+decoy pairs, CorrPatches with a disc of radius 64 around the nominal offset
+and the in-section legality rule.  One step runs the whole batch through
+aln_corr_patches_batch.
+
+  value   pairs/s with the strips already resident in HBM (device pointers)
+  e2e     pairs/s through the same C-ABI call with pinned HOST buffers:
+          host-to-device copies and the result read-back inside the timed region
+  plain   the one-pair-per-call path (aln_corr_patches, host buffers) on a
+          sample of the same pairs: pairs/s and p50/p99 latency
+  roofline  dominant kernel: algorithmic bytes / CUDA-event duration against
+          the measured HBM copy bandwidth
+  cpu_baseline  the oracle (FP64 C restatement of the reference) on the host
+          cores, on a bounded sample of the same pairs
+
+--impl reference times the reference algorithm's CPU implementation (the
+oracle port; the reference's own compiled code exists only where its source
+tree is mounted) on the host cores.
+
+Multi-GPU (torchrun): pairs are independent, so every rank runs its own batch
+of 4096 pairs (weak scaling, no collective on the data path); the step time
+is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "matched tile pairs/sec batched vs plain per-pair, 1 GB300, peak-exact; p50/p99 ms"
+WORKLOAD = ("montage strips: 4096 pairs of W x 2048 / 2048 x W uint8 overlap strips "
+            "(W ~ U[164,307]) of 2048^2 synthetic EM tiles, +-40 px jitter, 2% decoys; "
+            "CorrPatches, disc radius 64, in-section legality")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--pairs", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--plain-sample", type=int, default=64)
+    ap.add_argument("--cpu-sample", type=int, default=48)
+    ap.add_argument("--parity-sample", type=int, default=16)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing
+# ---------------------------------------------------------------------------
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws, backend):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def max_over_ranks(dist, value, device=None):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes (canonical two-pass FFT accounting, one read + one write
+# of the array per 1D pass; H = Ny*(Nx/2+1) complex FP32 = 8H bytes)
+# ---------------------------------------------------------------------------
+
+def fft_shape(w1, h1, w2, h2):
+    def cp2(n):
+        p = 1
+        while p < n:
+            p *= 2
+        return p
+    return cp2(w1 + w2 - 1), cp2(h1 + h2 - 1)
+
+
+def alg_bytes_per_pair(w, h, e=1):
+    """Per kernel, for one pair of w x h strips (both the same size here)."""
+    Nx, Ny = fft_shape(w, h, w, h)
+    H = Ny * (Nx // 2 + 1)
+    return {
+        "k_rowfft": 2 * (w * h * e + 8 * H),          # r2c row passes, both images
+        "k_colfft": 16 * H,                            # r2c column pass, image b
+        "k_corrcol": 16 * H + 24 * H + 16 * H,         # column pass a + product + c2r column pass
+        "k_lagrow": 8 * H + 4 * Nx * Ny,               # c2r row pass
+    }
+
+
+def read_traffic(kernel):
+    """DRAM bytes per pair for `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "montage_strips_kernels.md")
+    if not os.path.exists(path):
+        return None
+    for ln in open(path):
+        if ln.startswith("traffic_per_pair ") and kernel in ln:
+            try:
+                return float(ln.split()[-1])
+            except ValueError:
+                return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (oracle port, all host threads)
+# ---------------------------------------------------------------------------
+
+def cpu_pairs_per_s(pairs_host, threads):
+    """Run the oracle's CorrPatches on every pair with `threads` host threads
+    (ctypes releases the GIL); returns (pairs/s, per-pair seconds)."""
+    import concurrent.futures as cf
+    import oracle as O
+    orc = O.Oracle()
+    lg = O.legal(O.RGN_SECTION, 1500, 1500, 30000)
+    prepared = []
+    for a, b in pairs_host:
+        A, VA = O.image_to_points(a)
+        B, VB = O.image_to_points(b)
+        prepared.append((A, VA, B, VB))
+
+    def one(t):
+        A, VA, B, VB = t
+        t0 = time.perf_counter()
+        o = orc.corr_patches(A, VA, B, VB, 0, 0, 64, lg)
+        return time.perf_counter() - t0, o
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        res = list(ex.map(one, prepared))
+    wall = time.perf_counter() - t0
+    return len(prepared) / wall, [r[0] for r in res], [r[1] for r in res], wall
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------
+# reference arm
+# ---------------------------------------------------------------------------
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    import torch
+    from alignment_projects_gb300 import synth
+    import oracle as O
+    O.build()
+    dev = "cuda:%d" % local if torch.cuda.is_available() else "cpu"
+    threads = host_threads()
+    sample = max(threads, args.cpu_sample)
+    batch = synth.montage_batch_torch(args.seed, sample, dev)
+    host = [(p["a"].cpu().numpy(), p["b"].cpu().numpy()) for p in batch]
+    for _ in range(args.warmup):
+        cpu_pairs_per_s(host[:threads], threads)
+    times = []
+    for _ in range(args.steps):
+        pps, per, _, wall = cpu_pairs_per_s(host, threads)
+        times.append(wall)
+    tot = sum(times)
+    value = args.steps * len(host) / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * tot / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "pairs_per_step": len(host),
+                   "note": "bounded sample of the 4096-pair batch per step"},
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
+                         "sample": "%d montage strip pairs per step (first pairs of the batch),"
+                                   " FP64 C restatement of CorrPatches" % len(host)},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def build_pair_array(batch, on_device, host_bufs=None):
+    import ctypes as C
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300.native import AlnPair, AlnResult, AlnImage
+    n = len(batch)
+    arr = (AlnPair * n)()
+    lg = aln.legal(aln.RGN_SECTION, 1500, 1500, 30000)
+    for k, p in enumerate(batch):
+        for slot, key in ((0, "a"), (1, "b")):
+            if on_device:
+                t = p[key]
+                ptr = t.data_ptr()
+            else:
+                t = host_bufs[k][slot]
+                ptr = t.data_ptr()
+            im = AlnImage(ptr, aln.U8, t.shape[1], t.shape[0], t.shape[1], 0, 0,
+                          1 if on_device else 0)
+            if slot == 0:
+                arr[k].a = im
+            else:
+                arr[k].b = im
+        arr[k].ox, arr[k].oy, arr[k].radius = p["ox"], p["oy"], p["radius"]
+        arr[k].legal = lg
+    out = (AlnResult * n)()
+    return arr, out
+
+
+def run_gpu(args):
+    import ctypes as C
+    import torch
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300 import synth
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = dist_init(ws, "nccl")
+    dev = torch.device("cuda", local)
+    L = aln.lib()
+    ctx = aln.Context(local)
+
+    batch = synth.montage_batch_torch(args.seed + 7919 * rank, args.pairs, dev)
+    torch.cuda.synchronize()
+    n = len(batch)
+    strip_bytes = sum(p["a"].numel() + p["b"].numel() for p in batch)
+
+    # ---- device-resident inputs --------------------------------------------
+    arr_d, out_d = build_pair_array(batch, True)
+
+    def step_dev():
+        rc = L.aln_corr_patches_batch(ctx.h, n, arr_d, out_d)
+        if rc < 0:
+            raise RuntimeError(L.aln_last_error(ctx.h).decode())
+
+    for _ in range(args.warmup):
+        step_dev()
+    ctx.set_profiling(True)
+    ctx.profile_reset()
+    clk = ClockSampler(local)
+    clk.start()
+    barrier(dist)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step_dev()
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(dist)
+    ms_dev = e0.elapsed_time(e1)
+    clocks = clk.stop()
+    prof = ctx.profile()
+    launches = ctx.counters()["launches"]
+    ctx.set_profiling(False)
+    ms_dev = max_over_ranks(dist, ms_dev, dev)
+    value = ws * n * args.steps / (ms_dev / 1000.0)
+
+    # ---- roofline of the dominant kernel ------------------------------------
+    ours = {k: v for k, v in prof.items()}
+    dom = max(ours, key=lambda k: ours[k][1])
+    dom_launches, dom_ms = ours[dom]
+    alg_total = 0
+    for p in batch:
+        h, w = p["a"].shape
+        alg_total += alg_bytes_per_pair(w, h).get(dom, 0)
+    alg_per_launch = alg_total * args.steps / max(1, dom_launches)
+    achieved = alg_per_launch / (dom_ms / dom_launches / 1000.0) / 1e9
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak = json.load(open(peaks_path))["hbm_gbs"]
+        peak_src = "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    tr = read_traffic(dom)
+    traffic = None
+    if tr is not None:
+        traffic = tr * n * args.steps / max(1, dom_launches)
+
+    # ---- end to end through the C ABI with pinned host buffers -------------
+    host_bufs = []
+    for p in batch:
+        ha = torch.empty(p["a"].shape, dtype=torch.uint8, pin_memory=True)
+        hb = torch.empty(p["b"].shape, dtype=torch.uint8, pin_memory=True)
+        ha.copy_(p["a"])
+        hb.copy_(p["b"])
+        host_bufs.append((ha, hb))
+    arr_h, out_h = build_pair_array(batch, False, host_bufs)
+
+    def step_host():
+        rc = L.aln_corr_patches_batch(ctx.h, n, arr_h, out_h)
+        if rc < 0:
+            raise RuntimeError(L.aln_last_error(ctx.h).decode())
+
+    step_host()
+    ctx.profile_reset()
+    barrier(dist)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        step_host()
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(dist)
+    ms_e2e = max_over_ranks(dist, e0.elapsed_time(e1), dev)
+    cnt = ctx.counters()
+    e2e_value = ws * n * args.steps / (ms_e2e / 1000.0)
+
+    # results agree between the two input paths
+    same = all((out_d[k].status, out_d[k].peak_x, out_d[k].peak_y, out_d[k].r) ==
+               (out_h[k].status, out_h[k].peak_x, out_h[k].peak_y, out_h[k].r)
+               for k in range(n))
+
+    line = None
+    if rank == 0:
+        # ---- plain one-pair-per-call path ------------------------------------
+        lat = []
+        lg = aln.legal(aln.RGN_SECTION, 1500, 1500, 30000)
+        from alignment_projects_gb300.native import AlnResult, AlnImage
+        r = AlnResult()
+        for k in range(min(args.plain_sample, n)):
+            ha, hb = host_bufs[k]
+            ia = AlnImage(ha.data_ptr(), aln.U8, ha.shape[1], ha.shape[0], ha.shape[1], 0, 0, 0)
+            ib = AlnImage(hb.data_ptr(), aln.U8, hb.shape[1], hb.shape[0], hb.shape[1], 0, 0, 0)
+            t0 = time.perf_counter()
+            rc = L.aln_corr_patches(ctx.h, C.byref(ia), C.byref(ib), 0, 0, 64, C.byref(lg),
+                                    C.byref(r))
+            lat.append(time.perf_counter() - t0)
+            assert rc >= 0
+        lat_ms = sorted(1000.0 * x for x in lat[1:])
+        plain_pps = len(lat_ms) / (sum(lat_ms) / 1000.0)
+
+        # ---- parity on a sample: batch result vs the oracle ------------------
+        parity = None
+        cpu = None
+        threads = host_threads()
+        if not args.no_cpu:
+            samp = [(host_bufs[k][0].numpy(), host_bufs[k][1].numpy())
+                    for k in range(min(n, max(args.cpu_sample, args.parity_sample)))]
+            cpu_pps, per, outs, wall = cpu_pairs_per_s(samp, threads)
+            cpu = {"value": cpu_pps, "unit": "pairs/s", "cores": threads, "kind": "port",
+                   "sample": "%d of the batch's pairs, FP64 C restatement of CorrPatches, "
+                             "%.1f s wall on %d threads" % (len(samp), wall, threads)}
+            ok = tot = 0
+            max_dr = max_dp = 0.0
+            for k, o in enumerate(outs):
+                g = out_d[k]
+                if o["status"] == 0 and o["r"] - o["second"] > 1e-3:
+                    tot += 1
+                    ok += (g.peak_x, g.peak_y) == (o["bigx"], o["bigy"])
+                    max_dp = max(max_dp, abs(g.dx - o["dx"]), abs(g.dy - o["dy"]))
+                max_dr = max(max_dr, abs(g.r - o["r"]))
+            parity = {"pairs": len(outs), "peak_exact": ok, "peak_checked": tot,
+                      "max_abs_dr": max_dr, "max_abs_dsubpix": max_dp}
+        truth_ok = sum(1 for k, p in enumerate(batch)
+                       if not p["decoy"] and (out_d[k].peak_x, out_d[k].peak_y) == p["truth"])
+        decoys = [k for k, p in enumerate(batch) if p["decoy"]]
+        rejected = sum(1 for k in decoys if out_d[k].r < 0.3)
+        line = {
+            "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_dev / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "pairs_per_step": n, "fft": "512|1024 x 4096",
+                       "l2": "inputs %.2f GB per step > 129 MB L2" % (strip_bytes / 1e9),
+                       "parallelism": "replicas x%d" % ws},
+            "e2e": {"value": e2e_value, "unit": "pairs/s",
+                    "h2d_bytes_per_step": cnt["h2d_bytes"] // args.steps,
+                    "d2h_bytes_per_step": cnt["d2h_bytes"] // args.steps},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                         "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "alg_bytes_per_launch": alg_per_launch,
+                         "avg_launch_ms": dom_ms / dom_launches},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": launches,
+            "kernels_ms": {k: round(v[1], 3) for k, v in sorted(ours.items())},
+            "plain": {"pairs_per_s": plain_pps, "p50_ms": lat_ms[len(lat_ms) // 2],
+                      "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))],
+                      "sample": len(lat_ms)},
+            "batched_over_plain": value / plain_pps,
+            "batch_latency_ms": ms_dev / args.steps,
+            "parity": parity,
+            "truth": {"found": truth_ok, "of": n - len(decoys), "decoys_rejected": rejected,
+                      "decoys": len(decoys)},
+            "host_vs_device_inputs_identical": same,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

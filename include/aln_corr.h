@@ -117,6 +117,26 @@ void aln_ctx_destroy(aln_ctx *ctx);
  * aln_ctx_create when ctx is NULL). */
 const char *aln_last_error(const aln_ctx *ctx);
 
+/* Upper bound on the device workspace one batch chunk may use (default
+ * 4 GiB); larger batches are split into chunks.  No reference counterpart. */
+int aln_ctx_set_workspace_limit(aln_ctx *ctx, size_t bytes);
+
+/* ---- tracing: no reference counterpart (the reference logs wall-clock
+ * "Timer:" lines, 0_GEN/Timer.cpp:25-52) ------------------------------ */
+
+/* When on, every kernel launch is bracketed by CUDA events on the context's
+ * stream; aln_ctx_profile() reports launches and summed device time per
+ * kernel name since the last reset. */
+int aln_ctx_set_profiling(aln_ctx *ctx, int on);
+void aln_ctx_profile_reset(aln_ctx *ctx);
+/* Fills up to cap entries; returns the number of kernel names recorded.
+ * Name pointers stay valid until the next call on this context. */
+int aln_ctx_profile(aln_ctx *ctx, int cap, const char **names, long long *launches,
+                    double *ms);
+/* which: 0 = kernel launches, 1 = host-to-device bytes, 2 = device-to-host
+ * bytes, counted since the last aln_ctx_profile_reset. */
+long long aln_ctx_counter(aln_ctx *ctx, int which);
+
 /* ---- FFT support: 0_GEN/Correlation.h:14-31 ------------------------- */
 
 /* FFTSize, 0_GEN/Correlation.cpp:344-347 */
