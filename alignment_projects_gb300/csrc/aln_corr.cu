@@ -1587,3 +1587,166 @@ extern "C" int aln_ctx_set_workspace_limit(aln_ctx *ctx, size_t bytes)
     ctx->ws_budget = bytes;
     return ALN_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free CorrPatches.  No reference counterpart.
+//
+// For callers that must not allocate device memory: code running inside a
+// memory pool or arena they do not control, plugins of hosts that forbid
+// cudaMalloc after start-up, or code whose allocations would stall a busy
+// device.  The work space lives in one file-scope device array of
+// ALN_NOALLOC_SCRATCH_BYTES, which every GPU that loads this library holds
+// until the process exits.  Nothing here calls cudaMalloc, cudaFree or any
+// allocating routine, and no host heap memory is used either.
+// ---------------------------------------------------------------------------
+
+#define ALN_NOALLOC_SCRATCH_BYTES ((size_t)ALN_NOALLOC_SCRATCH_MIB << 20)
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[ALN_NOALLOC_SCRATCH_BYTES];
+
+// the twiddle table sits at the start of the scratch and survives calls
+static const size_t kNoAllocTwBytes = (2 * ALN_MAX_N * sizeof(float2) + 255) & ~(size_t)255;
+
+__global__ void k_fill_twiddles(float2 *tw)
+{
+    const int total = 2 * ALN_MAX_N;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        if (e == 0) {
+            tw[0] = make_float2(1.f, 0.f);
+            continue;
+        }
+        int N = 1;
+        while (2 * N <= e)
+            N <<= 1;
+        const int m = e - N;
+        double s, c;
+        sincospi(-2.0 * (double)m / (double)N, &s, &c);
+        tw[e] = make_float2((float)c, (float)s);
+    }
+}
+
+static std::mutex g_noalloc_lock;
+static char *g_noalloc_base[64];   // scratch device address per device, set once
+
+// One-time set-up on the current device: look up the scratch address, allow
+// the large shared-memory configurations, fill the twiddle table.
+static int noalloc_setup(int dev, cudaStream_t st, char **base)
+{
+    std::lock_guard<std::mutex> g(g_noalloc_lock);
+    if (g_noalloc_base[dev]) {
+        *base = g_noalloc_base[dev];
+        return ALN_OK;
+    }
+    char *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+        return set_err(nullptr, ALN_ERR_CUDA, "scratch address: %s", cudaGetErrorString(e));
+    if (int ke = configure_kernels())
+        return set_err(nullptr, ALN_ERR_CUDA, "kernel attributes: %s",
+                       cudaGetErrorString((cudaError_t)ke));
+    k_fill_twiddles<<<64, 256, 0, st>>>((float2 *)p);
+    if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return set_err(nullptr, ALN_ERR_CUDA, "twiddle set-up: %s", cudaGetErrorString(e));
+    g_noalloc_base[dev] = p;
+    *base = p;
+    return ALN_OK;
+}
+
+extern "C" int aln_corr_patches_noalloc(const aln_image *a, const aln_image *b, int ox, int oy,
+                                        int radius, const aln_legal *legal, void *stream,
+                                        aln_result *out)
+{
+    aln_ctx *ctx = nullptr;   // errors go to aln_last_error(NULL)
+    if (!a || !b || !out)
+        return set_err(nullptr, ALN_ERR_ARG, "noalloc: null argument");
+    if (!a->on_device || !b->on_device)
+        return set_err(nullptr, ALN_ERR_ARG, "noalloc: images must be device pointers");
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64)
+        return set_err(nullptr, ALN_ERR_ARG, "noalloc: device %d out of range", dev);
+    cudaStream_t st = (cudaStream_t)stream;
+    char *base = nullptr;
+    if (int rc = noalloc_setup(dev, st, &base))
+        return rc;
+
+    aln_pair P;
+    memset(&P, 0, sizeof P);
+    P.a = *a;
+    P.b = *b;
+    P.ox = ox;
+    P.oy = oy;
+    P.radius = radius;
+    if (legal)
+        P.legal = *legal;
+    PairPlan pl;
+    memset(&pl, 0, sizeof pl);
+    pl.src = &P;
+    if (int rc = plan_pair(nullptr, P, pl))
+        return rc;
+    memset(out, 0, sizeof *out);
+    out->nx = pl.orig_nx;
+    out->ny = pl.orig_ny;
+    if (pl.d.status != 0) {   // empty search region
+        out->status = ALN_NO_PEAK;
+        return ALN_OK;
+    }
+    const size_t head = kNoAllocTwBytes + al256(sizeof(PairDev)) + al256(sizeof(ResultDev));
+    if (head + pl.ws_bytes > ALN_NOALLOC_SCRATCH_BYTES)
+        return set_err(nullptr, ALN_ERR_UNSUPPORTED,
+                       "noalloc: this pair needs %zu bytes of scratch; the allocation-free entry "
+                       "point has %zu (use aln_corr_patches)",
+                       head + pl.ws_bytes, (size_t)ALN_NOALLOC_SCRATCH_BYTES);
+    float2 *tw = (float2 *)base;
+    PairDev *dpair = (PairDev *)(base + kNoAllocTwBytes);
+    ResultDev *dres = (ResultDev *)(base + kNoAllocTwBytes + al256(sizeof(PairDev)));
+    carve(pl, base + head, P);
+    PairDev &d = pl.d;
+    if (d.rgn_kind == ALN_RGN_TABLE)
+        CK(cudaMemcpyAsync((void *)d.table, P.legal.table, (size_t)d.table_w * d.table_h,
+                           cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dpair, &d, sizeof(PairDev), cudaMemcpyHostToDevice, st));
+    const int Nx = d.Nx, Ny = d.Ny, L = Nx / 2;
+    int maxslots = 1;
+    for (int i = 0; i < 2; ++i) {
+        int ns = 0;
+        for (int q = 0; q < 2; ++q)
+            if (d.need_hi[i][q] >= d.need_lo[i][q])
+                ns += d.need_hi[i][q] - d.need_lo[i][q] + 1;
+        maxslots = std::max(maxslots, ns);
+    }
+    const int maxw = std::max(d.w[0], d.w[1]), maxh = std::max(d.h[0], d.h[1]);
+    const int Wy = d.yhi - d.ylo + 1;
+    k_colsum<<<dim3((maxw + 127) / 128, 2, 1), 128, 0, st>>>(dpair);
+    k_mean<<<dim3(2, 1), 256, 0, st>>>(dpair);
+    k_rowscan<<<dim3(maxslots, 2, 1), 256, 0, st>>>(dpair);
+    {
+        const int RB = rows_per_cta(L);
+        const size_t sm = 2 * (size_t)RB * (L + 1) * sizeof(float2);
+        k_rowfft<<<dim3((maxh + RB - 1) / RB, 2, 1), 256, sm, st>>>(dpair, tw, RB, -1);
+    }
+    {
+        const int CG = cols_per_cta(Ny);
+        const size_t sm = 2 * (size_t)CG * (Ny + 1) * sizeof(float2);
+        const int gx = (L + 1 + CG - 1) / CG;
+        k_colfft<<<dim3(gx, 1), 256, sm, st>>>(dpair, tw, CG);
+        k_corrcol<<<dim3(gx, 1), 256, sm, st>>>(dpair, tw, CG);
+    }
+    {
+        const int RBL = std::max(1, std::min(8, 4096 / std::max(1, L)));
+        const size_t sm = 2 * (size_t)RBL * (L + 1) * sizeof(float2);
+        k_lagrow<<<dim3((Wy + RBL - 1) / RBL, 1), 256, sm, st>>>(dpair, tw, RBL);
+    }
+    k_final<<<1, 256, 0, st>>>(dpair, dres, pl.orig_nx == 1, pl.orig_ny == 1);
+    CK(cudaGetLastError());
+    ResultDev hr;
+    CK(cudaMemcpyAsync(&hr, dres, sizeof hr, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    out->status = hr.status == ALN_OK ? ALN_OK : ALN_NO_PEAK;
+    out->r = out->status == ALN_OK ? hr.r : 0.0;
+    out->dx = out->status == ALN_OK ? hr.dx : 0.0;
+    out->dy = out->status == ALN_OK ? hr.dy : 0.0;
+    out->peak_x = hr.px;
+    out->peak_y = hr.py;
+    return ALN_OK;
+}

@@ -181,6 +181,44 @@ typedef struct aln_pair {
 int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *pairs,
                            aln_result *out);
 
+/* ---- allocation-free CorrPatches: no counterpart in the reference ---- */
+
+/* Size of the device scratch array behind aln_corr_patches_noalloc. */
+#define ALN_NOALLOC_SCRATCH_MIB 32
+
+/*
+ * CorrPatches for callers that cannot allocate device memory -- e.g. code
+ * running inside a caller-managed memory pool or arena, or a plugin whose
+ * host forbids cudaMalloc/cudaFree once it is running (allocation there would
+ * synchronise the device or fragment the pool).  It computes what
+ * aln_corr_patches computes, but allocates nothing: no cudaMalloc, no
+ * cudaFree, no allocating library routine, no host heap.
+ *
+ * Work space comes from one file-scope device array of
+ * ALN_NOALLOC_SCRATCH_MIB MiB that every GPU loading this library keeps until
+ * the process exits.  A pair whose FFT work space does not fit is rejected
+ * with ALN_ERR_UNSUPPORTED (message from aln_last_error(NULL)); 32 MiB holds,
+ * for example, one 512 x 512 pair searched over its whole lag window, or a
+ * montage strip pair up to 256 x 2048 with a disc.
+ *
+ * Inputs: a and b must be device pointers on the calling thread's current
+ * device (on_device = 1).  Output: *out in host memory.  The call runs on
+ * `stream` (a cudaStream_t, NULL for the default stream) and returns after
+ * the result is copied back.
+ *
+ * The first call on each device performs a one-time set-up there (looks up
+ * the scratch array's device address, fills the FFT twiddle table in it,
+ * enables the large shared-memory kernel configurations); make that first
+ * call before any stream capture.  All calls on a device share the one
+ * scratch array and leave their data in it: calls that overlap on the GPU
+ * (several host threads, or several streams) race and must be serialised by
+ * the caller.  Every buffer is fully written before it is read, so no
+ * clearing between calls is needed.
+ */
+int aln_corr_patches_noalloc(const aln_image *a, const aln_image *b, int ox, int oy,
+                             int radius, const aln_legal *legal, void *stream,
+                             aln_result *out);
+
 #ifdef __cplusplus
 }
 #endif
