@@ -36,6 +36,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 // ---------------------------------------------------------------------------
@@ -79,6 +80,22 @@ __device__ __forceinline__ double sat_box(const double *t, const PairDev &p, int
 {
     const int w = p.w[i];
     double r = t[(long long)sat_slot(p, i, T) * w + R];
+    if (L > 0)
+        r -= t[(long long)sat_slot(p, i, T) * w + L - 1];
+    if (B > 0)
+        r -= t[(long long)sat_slot(p, i, B - 1) * w + R];
+    if (L > 0 && B > 0)
+        r += t[(long long)sat_slot(p, i, B - 1) * w + L - 1];
+    return r;
+}
+
+// exact integer box sum; equals the reference's FP64 IntegralTable result
+// whenever the sums are below 2^53 (always, for 8/16-bit pixels)
+__device__ __forceinline__ long long sat_box_i64(const long long *t, const PairDev &p, int i,
+                                                 int L, int R, int B, int T)
+{
+    const int w = p.w[i];
+    long long r = t[(long long)sat_slot(p, i, T) * w + R];
     if (L > 0)
         r -= t[(long long)sat_slot(p, i, T) * w + L - 1];
     if (B > 0)
@@ -134,7 +151,9 @@ __device__ __forceinline__ bool lag_r(const PairDev &p, int x, int y, double cs,
     const int L1 = L2 - x, R1 = R2 - x, B1 = B2 - y, T1 = T2 - y;
     const int olw = R1 - L1 + 1, olh = T1 - B1 + 1;
     r = 0.0;
-    if (p.rgn_kind != ALN_RGN_NONE && !rgn_ok(p, olw, olh))
+    // a transposed job evaluates LegalRgn on the caller's (untransposed) box
+    if (p.rgn_kind != ALN_RGN_NONE &&
+        !(p.transposed ? rgn_ok(p, olh, olw) : rgn_ok(p, olw, olh)))
         return false;
     if (p.cnt_kind == ALN_CNT_GT) {
         const int c1 = sat_box_n(p.satN[0], p, 0, L1, R1, B1, T1);
@@ -143,10 +162,21 @@ __device__ __forceinline__ bool lag_r(const PairDev &p, int x, int y, double cs,
             return false;
     }
     const double n = (double)(olw * olh);
-    const double s1 = sat_box(p.satS[0], p, 0, L1, R1, B1, T1);
-    const double q1 = sat_box(p.satQ[0], p, 0, L1, R1, B1, T1);
-    const double s2 = sat_box(p.satS[1], p, 1, L2, R2, B2, T2);
-    const double q2 = sat_box(p.satQ[1], p, 1, L2, R2, B2, T2);
+    double s1, q1, s2, q2;
+    if (p.sat_int & 1) {
+        s1 = (double)sat_box_i64((const long long *)p.satS[0], p, 0, L1, R1, B1, T1);
+        q1 = (double)sat_box_i64((const long long *)p.satQ[0], p, 0, L1, R1, B1, T1);
+    } else {
+        s1 = sat_box(p.satS[0], p, 0, L1, R1, B1, T1);
+        q1 = sat_box(p.satQ[0], p, 0, L1, R1, B1, T1);
+    }
+    if (p.sat_int & 2) {
+        s2 = (double)sat_box_i64((const long long *)p.satS[1], p, 1, L2, R2, B2, T2);
+        q2 = (double)sat_box_i64((const long long *)p.satQ[1], p, 1, L2, R2, B2, T2);
+    } else {
+        s2 = sat_box(p.satS[1], p, 1, L2, R2, B2, T2);
+        q2 = sat_box(p.satQ[1], p, 1, L2, R2, B2, T2);
+    }
     const double num = n * cs - (s1 - n * p.mu[0]) * (s2 - n * p.mu[1]);
     const double d1 = n * q1 - s1 * s1;
     const double d2 = n * q2 - s2 * s2;
@@ -698,12 +728,19 @@ __global__ void k_final(PairDev *pairs, ResultDev *res, int nreal_x_is_one, int 
     p.px = bigx;
     p.py = bigy;
     p.status = ALN_OK;
+    if (p.transposed) {   // back to the caller's frame
+        const double t = p.dx;
+        p.dx = p.dy;
+        p.dy = t;
+        p.px = bigy;
+        p.py = bigx;
+    }
     o.r = p.r;
     o.dx = p.dx;
     o.dy = p.dy;
     o.status = ALN_OK;
-    o.px = bigx;
-    o.py = bigy;
+    o.px = p.px;
+    o.py = p.py;
 }
 
 // ---------------------------------------------------------------------------
@@ -785,6 +822,52 @@ __global__ void k_irowfft(const float2 *Q, int logNx, int Ny, double *out,
         const int r = e / Nx, x = e - r * Nx;
         const float *row = (const float *)(res + r * pitch);
         out[(long long)(y0 + r) * Nx + x] = (double)row[x];
+    }
+}
+
+#include "aln_pipeline.cuh"
+
+// grid (ceil(w/256), 2, npairs): segment totals -> exclusive prefixes per
+// column; column totals for the mean
+__global__ void k2_segscan(PairDev *pairs)
+{
+    PairDev &p = pairs[blockIdx.z];
+    const int i = blockIdx.y;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int w = p.w[i];
+    if (p.status != 0 || c >= w)
+        return;
+    const int nseg = (p.h[i] + SAT_SEG - 1) / SAT_SEG;
+    int an = 0;
+    if ((p.sat_int >> i) & 1) {
+        long long *S = (long long *)p.segS[i], *Q = (long long *)p.segQ[i];
+        long long as = 0, aq = 0;
+        for (int g = 0; g < nseg; ++g) {
+            const long long o = (long long)g * w + c;
+            const long long ts = S[o], tq = Q[o];
+            const int tn = p.segN[i][o];
+            S[o] = as;
+            Q[o] = aq;
+            p.segN[i][o] = an;
+            as += ts;
+            aq += tq;
+            an += tn;
+        }
+        p.colsum[i][c] = (double)as;
+    } else {
+        double as = 0.0, aq = 0.0;
+        for (int g = 0; g < nseg; ++g) {
+            const long long o = (long long)g * w + c;
+            const double ts = p.segS[i][o], tq = p.segQ[i][o];
+            const int tn = p.segN[i][o];
+            p.segS[i][o] = as;
+            p.segQ[i][o] = aq;
+            p.segN[i][o] = an;
+            as += ts;
+            aq += tq;
+            an += tn;
+        }
+        p.colsum[i][c] = as;
     }
 }
 
@@ -1062,9 +1145,12 @@ static inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 // Host-side plan of one pair: sizes, window, needed SAT rows, workspace.
 struct PairPlan {
     PairDev d;
-    int orig_nx, orig_ny;
+    int orig_nx, orig_ny;        // the reference's FFT size (caller's frame)
+    int frame_nx1, frame_ny1;    // the solving frame's FFT size is 1 on that axis
+    int transposed;
     size_t ws_bytes;
-    size_t in_bytes[2];
+    size_t in_bytes[2];          // staging of host inputs (caller's layout)
+    size_t tr_bytes[2];          // transposed copies
     const aln_pair *src;
     int index;
 };
@@ -1111,7 +1197,7 @@ static void need_rows(const PairDev &d, int img, int lo[2], int hi[2])
     }
 }
 
-static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl)
+static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_transpose = false)
 {
     PairDev &d = pl.d;
     memset(&d, 0, sizeof d);
@@ -1130,22 +1216,41 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl)
     }
     pl.orig_nx = ceil_pow2(d.w[0] + d.w[1] - 1);
     pl.orig_ny = ceil_pow2(d.h[0] + d.h[1] - 1);
-    d.Nx = std::max(2, pl.orig_nx);
-    d.Ny = std::max(2, pl.orig_ny);
+    d.ox = P.ox;
+    d.oy = P.oy;
+    // Wide pairs are solved transposed: their summed-area rows are then short
+    // (and the FFT shapes match the tall pairs').  r, the disc and the
+    // sub-pixel rules are symmetric in x and y; legality is evaluated on the
+    // caller's box orientation.
+    pl.transposed = allow_transpose && (d.w[0] + d.w[1]) > (d.h[0] + d.h[1]);
+    if (pl.transposed) {
+        d.transposed = 1;
+        for (int i = 0; i < 2; ++i) {
+            d.src_img[i] = d.img[i];
+            d.src_stride[i] = d.stride[i];
+            std::swap(d.w[i], d.h[i]);
+            std::swap(d.x0[i], d.y0[i]);
+        }
+        std::swap(d.ox, d.oy);
+    }
+    const int fnx = ceil_pow2(d.w[0] + d.w[1] - 1), fny = ceil_pow2(d.h[0] + d.h[1] - 1);
+    pl.frame_nx1 = fnx == 1;
+    pl.frame_ny1 = fny == 1;
+    d.Nx = std::max(2, fnx);
+    d.Ny = std::max(2, fny);
     if (d.Nx > ALN_MAX_N || d.Ny > ALN_MAX_N)
         return set_err(ctx, ALN_ERR_UNSUPPORTED, "FFT size %dx%d exceeds %d", d.Nx, d.Ny,
                        ALN_MAX_N);
     d.logNx = ilog2(d.Nx);
     d.logNy = ilog2(d.Ny);
-    d.ox = P.ox;
-    d.oy = P.oy;
+    const int P_ox = d.ox, P_oy = d.oy;
     const long long rad = P.radius < 0 ? -(long long)P.radius : P.radius;
     d.rsqr = rad * rad;
     const int R = (int)std::min<long long>(rad, 1 << 20);
-    d.xlo = std::max(-(d.w[0] - 1), P.ox - R);
-    d.xhi = std::min(d.w[1] - 1, P.ox + R);
-    d.ylo = std::max(-(d.h[0] - 1), P.oy - R);
-    d.yhi = std::min(d.h[1] - 1, P.oy + R);
+    d.xlo = std::max(-(d.w[0] - 1), P_ox - R);
+    d.xhi = std::min(d.w[1] - 1, P_ox + R);
+    d.ylo = std::max(-(d.h[0] - 1), P_oy - R);
+    d.yhi = std::min(d.h[1] - 1, P_oy + R);
     d.rgn_kind = P.legal.rgn_kind;
     d.rgn_a = P.legal.rgn_a;
     d.rgn_b = P.legal.rgn_b;
@@ -1173,6 +1278,8 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl)
     for (int i = 0; i < 2; ++i) {
         pl.in_bytes[i] = im[i]->on_device ? 0 : al256((size_t)d.w[i] * d.h[i] * dtype_size(d.dt[i]));
         b += pl.in_bytes[i];
+        pl.tr_bytes[i] = pl.transposed ? al256((size_t)d.w[i] * d.h[i] * dtype_size(d.dt[i])) : 0;
+        b += pl.tr_bytes[i];
         d.Ts[i] = (d.h[i] + 3) & ~3;
         b += al256((size_t)L1 * d.Ts[i] * sizeof(float2));
         int ns = 0;
@@ -1181,6 +1288,8 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl)
                 ns += d.need_hi[i][k] - d.need_lo[i][k] + 1;
         b += 2 * al256((size_t)ns * d.w[i] * sizeof(double)) + al256((size_t)ns * d.w[i] * sizeof(int));
         b += al256((size_t)d.w[i] * sizeof(double));
+        const size_t nseg = (size_t)(d.h[i] + 63) / 64;
+        b += 2 * al256(nseg * d.w[i] * sizeof(double)) + al256(nseg * d.w[i] * sizeof(int));
     }
     b += al256((size_t)L1 * d.Ny * sizeof(float2));
     b += al256((size_t)L1 * Wy * sizeof(float2));
@@ -1201,9 +1310,20 @@ static size_t carve(PairPlan &pl, char *base, const aln_pair &P)
     const int Wy = d.yhi - d.ylo + 1, Wx = d.xhi - d.xlo + 1;
     for (int i = 0; i < 2; ++i) {
         if (pl.in_bytes[i]) {
+            // staging of a host input, in the caller's layout (packed)
+            if (pl.transposed) {
+                d.src_img[i] = p;
+                d.src_stride[i] = d.h[i];   // caller's width
+            } else {
+                d.img[i] = p;
+                d.stride[i] = d.w[i];
+            }
+            p += pl.in_bytes[i];
+        }
+        if (pl.tr_bytes[i]) {
             d.img[i] = p;
             d.stride[i] = d.w[i];
-            p += pl.in_bytes[i];
+            p += pl.tr_bytes[i];
         }
         d.T[i] = (float2 *)p;
         p += al256((size_t)L1 * d.Ts[i] * sizeof(float2));
@@ -1219,6 +1339,13 @@ static size_t carve(PairPlan &pl, char *base, const aln_pair &P)
         p += al256((size_t)ns * d.w[i] * sizeof(int));
         d.colsum[i] = (double *)p;
         p += al256((size_t)d.w[i] * sizeof(double));
+        const size_t nseg = (size_t)(d.h[i] + 63) / 64;
+        d.segS[i] = (double *)p;
+        p += al256(nseg * d.w[i] * sizeof(double));
+        d.segQ[i] = (double *)p;
+        p += al256(nseg * d.w[i] * sizeof(double));
+        d.segN[i] = (int *)p;
+        p += al256(nseg * d.w[i] * sizeof(int));
     }
     d.X2 = (float2 *)p;
     p += al256((size_t)L1 * d.Ny * sizeof(float2));
@@ -1238,6 +1365,67 @@ static size_t carve(PairPlan &pl, char *base, const aln_pair &P)
 
 static int rows_per_cta(int L) { return std::max(1, std::min(16, 4096 / L)); }
 static int cols_per_cta(int Ny) { return std::max(1, std::min(16, 4096 / Ny)); }
+
+template <int LL>
+static void launch_rowfft2(aln_ctx *ctx, int n, int maxh)
+{
+    constexpr int T = RegFFT<LL, -1>::T;
+    const int thr = rowfft_threads(T), G = thr / T;
+    const size_t sm = (size_t)G * (padded(LL) + 1) * sizeof(float2);
+    cudaFuncSetAttribute(k2_rowfft<LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    LAUNCH(ctx, "k2_rowfft", k2_rowfft<LL>, dim3((maxh + G - 1) / G, 2, n), thr, sm,
+           ctx->dpairs, ctx->tw, -1);
+}
+
+template <int NY>
+static void launch_corrcol2(aln_ctx *ctx, int n, int L, int cached)
+{
+    constexpr int T = RegFFT<NY, -1>::T;
+    const int thr = std::max(256, T), G = thr / T;
+    const size_t sm = (size_t)G * (padded(NY) + NY) * sizeof(float2);
+    cudaFuncSetAttribute(k2_corrcol<NY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    LAUNCH(ctx, "k2_corrcol", k2_corrcol<NY>, dim3((L + 1 + G - 1) / G, n), thr, sm,
+           ctx->dpairs, ctx->tw, cached);
+}
+
+template <int LL>
+static void launch_lagrow2(aln_ctx *ctx, int n, int maxWy)
+{
+    constexpr int T = RegFFT<LL, +1>::T;
+    const int thr = std::max(256, T), G = thr / T;
+    const size_t sm = (size_t)G * (padded(LL) + 2) * sizeof(float2);
+    cudaFuncSetAttribute(k2_lagrow<LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    LAUNCH(ctx, "k2_lagrow", k2_lagrow<LL>, dim3((maxWy + G - 1) / G, n), thr, sm,
+           ctx->dpairs, ctx->tw);
+}
+
+#define ALN_CASES_L(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
+#define ALN_CASES_NY(X) ALN_CASES_L(X) X(8192)
+
+// register-FFT pipeline for one chunk: rows (both images), fused columns,
+// lag rows.  L = Nx/2 in [16, 4096], Ny in [16, 8192].
+static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int maxWy)
+{
+    switch (L) {
+#define X(v) case v: launch_rowfft2<v>(ctx, n, maxh); break;
+        ALN_CASES_L(X)
+#undef X
+    default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
+    }
+    switch (Ny) {
+#define X(v) case v: launch_corrcol2<v>(ctx, n, L, 0); break;
+        ALN_CASES_NY(X)
+#undef X
+    default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "column length %d", Ny);
+    }
+    switch (L) {
+#define X(v) case v: launch_lagrow2<v>(ctx, n, maxWy); break;
+        ALN_CASES_L(X)
+#undef X
+    default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
+    }
+    return ALN_OK;
+}
 
 // Runs one chunk of pairs that share (Nx, Ny).
 static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk)
@@ -1262,9 +1450,14 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk)
         for (int i = 0; i < 2; ++i) {
             if (pl.in_bytes[i]) {
                 const size_t es = dtype_size(im[i]->dtype);
-                CK(cudaMemcpy2DAsync((void *)pl.d.img[i], (size_t)im[i]->w * es, im[i]->data,
-                                     (size_t)im[i]->stride * es, (size_t)im[i]->w * es,
-                                     im[i]->h, cudaMemcpyHostToDevice, ctx->stream));
+                void *dst = pl.transposed ? (void *)pl.d.src_img[i] : (void *)pl.d.img[i];
+                if (im[i]->stride == im[i]->w)
+                    CK(cudaMemcpyAsync(dst, im[i]->data, (size_t)im[i]->w * im[i]->h * es,
+                                       cudaMemcpyHostToDevice, ctx->stream));
+                else
+                    CK(cudaMemcpy2DAsync(dst, (size_t)im[i]->w * es, im[i]->data,
+                                         (size_t)im[i]->stride * es, (size_t)im[i]->w * es,
+                                         im[i]->h, cudaMemcpyHostToDevice, ctx->stream));
                 ctx->h2d_bytes += (long long)im[i]->w * im[i]->h * es;
             }
             maxw = std::max(maxw, pl.d.w[i]);
@@ -1276,6 +1469,8 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk)
             maxslots = std::max(maxslots, ns);
         }
         maxWy = std::max(maxWy, pl.d.yhi - pl.d.ylo + 1);
+        pl.d.sat_int = (pl.d.dt[0] == ALN_U8 || pl.d.dt[0] == ALN_U16 ? 1 : 0) |
+                       (pl.d.dt[1] == ALN_U8 || pl.d.dt[1] == ALN_U16 ? 2 : 0);
         hd[k] = pl.d;
     }
     // legality tables (host) -> device
@@ -1289,32 +1484,53 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk)
     cudaStream_t st = ctx->stream;
     const int L = Nx / 2;
     {
-        dim3 g((maxw + 127) / 128, 2, n);
-        LAUNCH(ctx, "k_colsum", k_colsum, g, 128, 0, ctx->dpairs);
+        int sw = 0, sh = 0;   // largest caller-frame image among transposed jobs
+        for (int k = 0; k < n; ++k)
+            if (hd[k].transposed)
+                for (int i = 0; i < 2; ++i) {
+                    sw = std::max(sw, hd[k].h[i]);
+                    sh = std::max(sh, hd[k].w[i]);
+                }
+        if (sw > 0)
+            LAUNCH(ctx, "k_transpose", k_transpose, dim3((sw + 31) / 32, (sh + 31) / 32, 2 * n),
+                   dim3(32, 8), 0, ctx->dpairs);
+    }
+    {
+        int maxseg = 1;
+        for (int k = 0; k < n; ++k)
+            maxseg = std::max(maxseg, (std::max(hd[k].h[0], hd[k].h[1]) + 63) / 64);
+        LAUNCH(ctx, "k2_sat1", k2_sat1, dim3((maxw + 31) / 32, (maxseg + 7) / 8, 2 * n),
+               dim3(32, 8), 0, ctx->dpairs);
+        LAUNCH(ctx, "k2_segscan", k2_segscan, dim3((maxw + 255) / 256, 2, n), 256, 0, ctx->dpairs);
         LAUNCH(ctx, "k_mean", k_mean, dim3(2, n), 256, 0, ctx->dpairs);
-        LAUNCH(ctx, "k_rowscan", k_rowscan, dim3(maxslots, 2, n), 256, 0, ctx->dpairs);
+        LAUNCH(ctx, "k2_sat2", k2_sat2, dim3(maxslots, 2, n), 256, 0, ctx->dpairs);
     }
-    {
-        const int RB = rows_per_cta(L);
-        const size_t sm = 2 * (size_t)RB * (L + 1) * sizeof(float2);
-        LAUNCH(ctx, "k_rowfft", k_rowfft, dim3((maxh + RB - 1) / RB, 2, n), 256, sm, ctx->dpairs,
-               ctx->tw, RB, -1);
-    }
-    {
-        const int CG = cols_per_cta(Ny);
-        const size_t sm = 2 * (size_t)CG * (Ny + 1) * sizeof(float2);
-        const int gx = (L + 1 + CG - 1) / CG;
-        LAUNCH(ctx, "k_colfft", k_colfft, dim3(gx, n), 256, sm, ctx->dpairs, ctx->tw, CG);
-        LAUNCH(ctx, "k_corrcol", k_corrcol, dim3(gx, n), 256, sm, ctx->dpairs, ctx->tw, CG);
-    }
-    {
-        const int RBL = std::max(1, std::min(8, 4096 / std::max(1, L)));
-        const size_t sm = 2 * (size_t)RBL * (L + 1) * sizeof(float2);
-        LAUNCH(ctx, "k_lagrow", k_lagrow, dim3((maxWy + RBL - 1) / RBL, n), 256, sm, ctx->dpairs,
-               ctx->tw, RBL);
+    if (L >= 16 && L <= 4096 && Ny >= 16 && Ny <= 8192) {
+        if (int rc = launch_fft_pipeline(ctx, L, Ny, n, maxh, maxWy))
+            return rc;
+    } else {
+        {
+            const int RB = rows_per_cta(L);
+            const size_t sm = 2 * (size_t)RB * (L + 1) * sizeof(float2);
+            LAUNCH(ctx, "k_rowfft", k_rowfft, dim3((maxh + RB - 1) / RB, 2, n), 256, sm,
+                   ctx->dpairs, ctx->tw, RB, -1);
+        }
+        {
+            const int CG = cols_per_cta(Ny);
+            const size_t sm = 2 * (size_t)CG * (Ny + 1) * sizeof(float2);
+            const int gx = (L + 1 + CG - 1) / CG;
+            LAUNCH(ctx, "k_colfft", k_colfft, dim3(gx, n), 256, sm, ctx->dpairs, ctx->tw, CG);
+            LAUNCH(ctx, "k_corrcol", k_corrcol, dim3(gx, n), 256, sm, ctx->dpairs, ctx->tw, CG);
+        }
+        {
+            const int RBL = std::max(1, std::min(8, 4096 / std::max(1, L)));
+            const size_t sm = 2 * (size_t)RBL * (L + 1) * sizeof(float2);
+            LAUNCH(ctx, "k_lagrow", k_lagrow, dim3((maxWy + RBL - 1) / RBL, n), 256, sm,
+                   ctx->dpairs, ctx->tw, RBL);
+        }
     }
     LAUNCH(ctx, "k_final", k_final, n, 256, 0, ctx->dpairs, ctx->dres,
-           chunk[0]->orig_nx == 1, chunk[0]->orig_ny == 1);
+           chunk[0]->frame_nx1, chunk[0]->frame_ny1);
     CK(cudaGetLastError());
     std::vector<ResultDev> hr(n);
     CK(cudaMemcpyAsync(hr.data(), ctx->dres, n * sizeof(ResultDev), cudaMemcpyDeviceToHost, st));
@@ -1355,14 +1571,14 @@ extern "C" int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *
     for (int k = 0; k < npairs; ++k) {
         plans[k].src = &pairs[k];
         plans[k].index = k;
-        if (int rc = plan_pair(ctx, pairs[k], plans[k]))
+        if (int rc = plan_pair(ctx, pairs[k], plans[k], true))
             return rc;
     }
     // group by FFT size, keep submission order inside a group
-    std::map<std::pair<int, int>, std::vector<PairPlan *>> groups;
+    std::map<std::tuple<int, int, int, int>, std::vector<PairPlan *>> groups;
     for (auto &pl : plans)
         if (pl.d.status == 0)
-            groups[{pl.d.Nx, pl.d.Ny}].push_back(&pl);
+            groups[std::make_tuple(pl.d.Nx, pl.d.Ny, pl.frame_nx1, pl.frame_ny1)].push_back(&pl);
     for (auto &g : groups) {
         std::vector<PairPlan *> chunk;
         size_t bytes = 0;

@@ -27,6 +27,12 @@ struct PairDev {
     int w[2], h[2];     // bounding boxes
     int x0[2], y0[2];   // bounding-box origins B.L, B.B
     int Nx, Ny, logNx, logNy;
+    // 1: the job is solved on transposed images (x <-> y); img/w/h/x0/y0,
+    // the window and the disc are in the transposed frame, src_* describe
+    // the caller's untransposed rasters for k_transpose
+    int transposed;
+    const void *src_img[2];
+    int src_stride[2];
     // search region: lag window (inclusive) and disc
     int ox, oy;
     long long rsqr;
@@ -48,6 +54,9 @@ struct PairDev {
     float2 *Q;          // column-inverse output [kx][j], j = y - ylo, stride Wy
     double *satS[2], *satQ[2];   // summed-area tables of v and v^2, [y][x] stride w
     int *satN[2];                // summed-area table of (v != 0)
+    int sat_int;                 // bit i: image i's sat/seg S, Q tables hold int64
+    double *segS[2], *segQ[2];   // per 64-row segment column totals -> prefixes
+    int *segN[2];
     double *colsum[2];           // per-column totals (mean shift)
     double *rr;                  // r over the lag window [j][x - xlo]
     RowBest *rb;                 // per lag row

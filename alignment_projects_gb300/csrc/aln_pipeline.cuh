@@ -1,0 +1,513 @@
+// aln_pipeline.cuh -- the batched CorrPatches kernels built on the
+// register-resident FFT (aln_fft_reg.cuh).  Included by aln_corr.cu, after
+// the device helpers (load_px, sat slots, lag_r, best_merge).
+//
+//   k2_sat1   per (column, 64-row segment): local column prefix of v, v^2,
+//             (v != 0) at the needed rows; segment totals
+//   k2_segscan (aln_corr.cu) exclusive prefix over segments per column,
+//             column totals; k_mean turns them into the shift mu
+//   k2_sat2   per needed row: add the segments above, x-prefix scan -> SAT row
+//   k2_rowfft<L>   rows: (v - mu), zero pad, real FFT of length 2L, [kx][y]
+//   k2_corrcol<Ny> per column kx: FFT of b's column (or the cached spectrum),
+//             FFT of a's column, X2 * conj(X1), inverse FFT, the window's
+//             lag rows -> Q[kx][j].  Nothing else leaves the SM.
+//   k2_lagrow<L>   per lag row: inverse real FFT, r per lag, row argmax
+#pragma once
+
+#include "aln_fft_reg.cuh"
+
+#define SAT_SEG 64
+
+__device__ __forceinline__ bool int_pixels(int dt) { return dt == ALN_U8 || dt == ALN_U16; }
+
+// grid (ceil(w/32), ceil(nseg/8), 2*npairs), block (32, 8)
+__global__ void k2_sat1(PairDev *pairs)
+{
+    PairDev &p = pairs[blockIdx.z >> 1];
+    const int i = blockIdx.z & 1;
+    const int w = p.w[i], h = p.h[i], dt = p.dt[i];
+    const int c = blockIdx.x * 32 + threadIdx.x;
+    const int seg = blockIdx.y * 8 + threadIdx.y;
+    const int y0 = seg * SAT_SEG;
+    if (p.status != 0 || c >= w || y0 >= h)
+        return;
+    const int y1 = min(h, y0 + SAT_SEG);
+    const void *img = p.img[i];
+    const long long st = p.stride[i];
+    const int nseg = (h + SAT_SEG - 1) / SAT_SEG;
+    int *N = p.satN[i];
+    int nz = 0;
+    if (int_pixels(dt)) {
+        long long *S = (long long *)p.satS[i], *Q = (long long *)p.satQ[i];
+        long long s = 0, q = 0;
+        for (int y = y0; y < y1; ++y) {
+            const long long v = dt == ALN_U8 ? ((const uint8_t *)img)[y * st + c]
+                                             : ((const uint16_t *)img)[y * st + c];
+            s += v;
+            q += v * v;
+            nz += (v != 0);
+            if (row_needed(p, i, y)) {
+                const long long o = (long long)sat_slot(p, i, y) * w + c;
+                S[o] = s;
+                Q[o] = q;
+                N[o] = nz;
+            }
+        }
+        ((long long *)p.segS[i])[(long long)seg * w + c] = s;
+        ((long long *)p.segQ[i])[(long long)seg * w + c] = q;
+    } else {
+        double s = 0.0, q = 0.0;
+        for (int y = y0; y < y1; ++y) {
+            const double v = load_px(img, dt, y * st + c);
+            s += v;
+            q += v * v;
+            nz += (v != 0.0);
+            if (row_needed(p, i, y)) {
+                const long long o = (long long)sat_slot(p, i, y) * w + c;
+                p.satS[i][o] = s;
+                p.satQ[i][o] = q;
+                N[o] = nz;
+            }
+        }
+        p.segS[i][(long long)seg * w + c] = s;
+        p.segQ[i][(long long)seg * w + c] = q;
+    }
+    p.segN[i][(long long)seg * w + c] = nz;
+    (void)nseg;
+}
+
+// ---------------------------------------------------------------------------
+// transposed copies of wide images (jobs solved in the transposed frame)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned long long load_bits(const char *p, int es, long long idx)
+{
+    switch (es) {
+    case 1: return ((const uint8_t *)p)[idx];
+    case 2: return ((const uint16_t *)p)[idx];
+    case 4: return ((const uint32_t *)p)[idx];
+    default: return ((const unsigned long long *)p)[idx];
+    }
+}
+
+__device__ __forceinline__ void store_bits(char *p, int es, long long idx, unsigned long long v)
+{
+    switch (es) {
+    case 1: ((uint8_t *)p)[idx] = (uint8_t)v; break;
+    case 2: ((uint16_t *)p)[idx] = (uint16_t)v; break;
+    case 4: ((uint32_t *)p)[idx] = (uint32_t)v; break;
+    default: ((unsigned long long *)p)[idx] = v; break;
+    }
+}
+
+// grid (ceil(max caller w / 32), ceil(max caller h / 32), 2*npairs), block (32, 8):
+// frame pixel (xf, yf) = caller pixel (yf, xf)
+__global__ void k_transpose(PairDev *pairs)
+{
+    __shared__ unsigned long long tile[32][33];
+    PairDev &p = pairs[blockIdx.z >> 1];
+    const int i = blockIdx.z & 1;
+    if (p.status != 0 || !p.transposed)
+        return;
+    const int sw = p.h[i], sh = p.w[i];   // caller's width and height
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    if (x0 >= sw || y0 >= sh)
+        return;
+    const int es = p.dt[i] == ALN_U8 ? 1 : p.dt[i] == ALN_U16 ? 2 : p.dt[i] == ALN_F32 ? 4 : 8;
+    const char *src = (const char *)p.src_img[i];
+    const long long sst = p.src_stride[i];
+    for (int yy = threadIdx.y; yy < 32; yy += 8) {
+        const int y = y0 + yy, x = x0 + threadIdx.x;
+        if (y < sh && x < sw)
+            tile[yy][threadIdx.x] = load_bits(src, es, y * sst + x);
+    }
+    __syncthreads();
+    char *dst = (char *)p.img[i];
+    const long long dstr = p.stride[i];
+    for (int xx = threadIdx.y; xx < 32; xx += 8) {
+        const int x = x0 + xx, y = y0 + threadIdx.x;
+        if (x < sw && y < sh)
+            store_bits(dst, es, x * dstr + y, tile[threadIdx.x][xx]);
+    }
+}
+
+// inclusive block scan of (a, b, c) over 256 threads (warp shuffles)
+template <typename TA>
+__device__ __forceinline__ void block_scan3(TA &a, TA &b, int &c, TA *sa, TA *sb, int *sc)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const TA a2 = __shfl_up_sync(0xffffffff, a, o);
+        const TA b2 = __shfl_up_sync(0xffffffff, b, o);
+        const int c2 = __shfl_up_sync(0xffffffff, c, o);
+        if (lane >= o) {
+            a += a2;
+            b += b2;
+            c += c2;
+        }
+    }
+    if (lane == 31) {
+        sa[wid] = a;
+        sb[wid] = b;
+        sc[wid] = c;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        TA x = lane < 8 ? sa[lane] : TA(0), y = lane < 8 ? sb[lane] : TA(0);
+        int z = lane < 8 ? sc[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            const TA x2 = __shfl_up_sync(0xffffffff, x, o);
+            const TA y2 = __shfl_up_sync(0xffffffff, y, o);
+            const int z2 = __shfl_up_sync(0xffffffff, z, o);
+            if (lane >= o) {
+                x += x2;
+                y += y2;
+                z += z2;
+            }
+        }
+        if (lane < 8) {
+            sa[lane] = x;
+            sb[lane] = y;
+            sc[lane] = z;
+        }
+    }
+    __syncthreads();
+    if (wid > 0) {
+        a += sa[wid - 1];
+        b += sb[wid - 1];
+        c += sc[wid - 1];
+    }
+    __syncthreads();
+}
+
+template <typename TA>
+__device__ void sat2_row(PairDev &p, int i, int slot, int y, TA *S, TA *Q, const TA *segS,
+                         const TA *segQ)
+{
+    __shared__ TA sa[8], sb[8];
+    __shared__ int sc[8];
+    const int w = p.w[i];
+    const int seg = y / SAT_SEG;
+    TA *rS = S + (long long)slot * w;
+    TA *rQ = Q + (long long)slot * w;
+    int *rN = p.satN[i] + (long long)slot * w;
+    const int *segN = p.segN[i];
+    const int per = (w + 255) / 256;
+    const int c0 = threadIdx.x * per, c1 = min(w, c0 + per);
+    // full column prefix = exclusive segment prefix + local prefix; then the
+    // x-prefix of this thread's columns
+    TA s = 0, q = 0;
+    int n = 0;
+    const long long so = (long long)seg * w;
+    for (int c = c0; c < c1; ++c) {
+        const TA cs = rS[c] + segS[so + c], cq = rQ[c] + segQ[so + c];
+        const int cn = rN[c] + segN[so + c];
+        s += cs;
+        q += cq;
+        n += cn;
+        rS[c] = s;
+        rQ[c] = q;
+        rN[c] = n;
+    }
+    TA ts = s, tq = q;
+    int tn = n;
+    block_scan3<TA>(ts, tq, tn, sa, sb, sc);
+    const TA os = ts - s, oq = tq - q;   // exclusive offsets
+    const int on = tn - n;
+    for (int c = c0; c < c1; ++c) {
+        rS[c] += os;
+        rQ[c] += oq;
+        rN[c] += on;
+    }
+}
+
+// grid (maxslots, 2, npairs), block 256
+__global__ void k2_sat2(PairDev *pairs)
+{
+    PairDev &p = pairs[blockIdx.z];
+    const int i = blockIdx.y;
+    const int slot = blockIdx.x;
+    if (p.status != 0 || slot >= nslots(p, i))
+        return;
+    const int len0 = p.need_hi[i][0] - p.need_lo[i][0] + 1;
+    const int y = slot < len0 ? p.need_lo[i][0] + slot : p.need_lo[i][1] + slot - len0;
+    if (int_pixels(p.dt[i]))
+        sat2_row<long long>(p, i, slot, y, (long long *)p.satS[i], (long long *)p.satQ[i],
+                            (const long long *)p.segS[i], (const long long *)p.segQ[i]);
+    else
+        sat2_row<double>(p, i, slot, y, p.satS[i], p.satQ[i], p.segS[i], p.segQ[i]);
+}
+
+// ---------------------------------------------------------------------------
+// forward rows
+// ---------------------------------------------------------------------------
+
+// threads per CTA of the row kernels: >= 256, four teams when teams are large
+__host__ __device__ constexpr int rowfft_threads(int T) { return T * 4 > 512 ? 512 : (T * 4 < 256 ? 256 : T * 4); }
+
+// Each team of RegFFT<L>::T threads transforms one row.  G = blockDim.x / T
+// rows per CTA; smem: G * (padded(L) + 1) float2 (+1 for bin L).
+template <int L>
+__global__ void k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img)
+{
+    using F = RegFFT<L, -1>;
+    constexpr int R = F::R, T = F::T;
+    constexpr int G = rowfft_threads(T) / T;
+    extern __shared__ float2 smem[];
+    PairDev &p = pairs[blockIdx.z];
+    const int i = only_img >= 0 ? only_img : blockIdx.y;
+    if (p.status != 0)
+        return;
+    const int team = threadIdx.x / T, t = threadIdx.x - team * T;
+    const int h = p.h[i], w = p.w[i], dt = p.dt[i];
+    const int y0 = blockIdx.x * G;
+    if (y0 >= h)
+        return;
+    const int y = y0 + team;
+    constexpr int PITCH = padded(L) + 1;
+    float2 *sm = smem + team * PITCH;
+    const void *img = p.img[i];
+    const long long st = p.stride[i];
+    float2 v[R];
+    if (dt == ALN_U8 || dt == ALN_U16) {
+        // integer pixels, integer shift: exact before the conversion
+        const int mu = (int)p.mu[i];
+        const uint8_t *p8 = (const uint8_t *)img + (dt == ALN_U8 ? y * st : 0);
+        const uint16_t *p16 = (const uint16_t *)img + (dt == ALN_U16 ? y * st : 0);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int n = t + r * T;
+            float2 z = make_float2(0.f, 0.f);
+            if (y < h) {
+                const int xa = 2 * n, xb = 2 * n + 1;
+                if (xa < w)
+                    z.x = (float)((dt == ALN_U8 ? (int)p8[xa] : (int)p16[xa]) - mu);
+                if (xb < w)
+                    z.y = (float)((dt == ALN_U8 ? (int)p8[xb] : (int)p16[xb]) - mu);
+            }
+            v[r] = z;
+        }
+    } else {
+        const double mu = p.mu[i];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int n = t + r * T;
+            float2 z = make_float2(0.f, 0.f);
+            if (y < h) {
+                const int xa = 2 * n, xb = 2 * n + 1;
+                if (xa < w)
+                    z.x = (float)(load_px(img, dt, y * st + xa) - mu);
+                if (xb < w)
+                    z.y = (float)(load_px(img, dt, y * st + xb) - mu);
+            }
+            v[r] = z;
+        }
+    }
+    F::run(v, sm, t, tw);
+    // split the half-length transform into the N/2+1 bins of the real row
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+        sm[padi(t + r * T)] = v[r];
+    __syncthreads();
+    float2 *T_ = p.T[i];
+    const int Ts = p.Ts[i];
+    const int rows = min(G, h - y0);
+    // bins for (kx, row) with row fastest: coalesced [kx][y] stores
+    for (int e = threadIdx.x; e < (L + 1) * G; e += blockDim.x) {
+        const int kx = e / G, rr = e - kx * G;
+        if (rr >= rows)
+            continue;
+        const float2 *Z = smem + rr * PITCH;
+        const float2 a = Z[padi(kx & (L - 1))];
+        const float2 b = cconj(Z[padi((L - kx) & (L - 1))]);
+        const float2 ev = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
+        const float2 dd = make_float2(0.5f * (a.x - b.x), 0.5f * (a.y - b.y));
+        const float2 o = make_float2(dd.y, -dd.x);
+        const float2 wv = __ldg(&tw[2 * L + kx]);
+        T_[(long long)kx * Ts + y0 + rr] = cadd(ev, cmul(o, wv));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// columns: forward b and a, product, inverse, window rows
+// ---------------------------------------------------------------------------
+
+template <int NY>
+__global__ void __launch_bounds__(NY >= 8192 ? 512 : 256, NY >= 8192 ? 1 : 2)
+k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
+{
+    using FF = RegFFT<NY, -1>;
+    using FI = RegFFT<NY, +1>;
+    constexpr int R = FF::R, T = FF::T;
+    extern __shared__ float2 smem[];
+    PairDev &p = pairs[blockIdx.y];
+    if (p.status != 0)
+        return;
+    const int L1 = (p.Nx >> 1) + 1;
+    const int G = blockDim.x / T;
+    const int team = threadIdx.x / T, t = threadIdx.x - team * T;
+    const int kx = blockIdx.x * G + team;
+    const bool live = kx < L1;
+    if (blockIdx.x * G >= L1)
+        return;
+    float2 *sm = smem + team * FF::SMEM;
+    float2 *sb = smem + G * FF::SMEM + team * NY;   // b's spectrum, this team's own slots
+    const int kxc = live ? kx : L1 - 1;   // idle teams compute a copy, store nothing
+    float2 va[R];
+    {
+        float2 vb[R];
+        if (use_cached_b) {
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                vb[r] = p.X2[(long long)kxc * NY + t + r * T];
+        } else {
+            const float2 *Tb = p.T[1] + (long long)kxc * p.Ts[1];
+            const int hb = p.h[1];
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int y = t + r * T;
+                vb[r] = y < hb ? Tb[y] : make_float2(0.f, 0.f);
+            }
+            FF::run(vb, sm, t, tw);
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            sb[r * T + t] = vb[r];
+    }
+    {
+        const float2 *Ta = p.T[0] + (long long)kxc * p.Ts[0];
+        const int ha = p.h[0];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int y = t + r * T;
+            va[r] = y < ha ? Ta[y] : make_float2(0.f, 0.f);
+        }
+    }
+    FF::run(va, sm, t, tw);
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+        va[r] = cmulc(sb[r * T + t], va[r]);   // X2 * conj(X1)
+    FI::run(va, sm, t, tw);
+    if (!live)
+        return;
+    const int Wy = p.yhi - p.ylo + 1;
+    const int nnegy = p.h[0] - 1;
+    float2 *Q = p.Q + (long long)kx * Wy;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int ys = t + r * T;
+        const int y = ys >= NY - nnegy ? ys - NY : ys;
+        if (y >= p.ylo && y <= p.yhi)
+            Q[y - p.ylo] = va[r];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// lag rows
+// ---------------------------------------------------------------------------
+
+template <int L>
+__global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
+{
+    using F = RegFFT<L, +1>;
+    constexpr int R = F::R, T = F::T;
+    constexpr int PITCH = padded(L) + 2;   // holds L+1 bins, then 2L reals
+    extern __shared__ float2 smem[];
+    __shared__ double red_r[32];
+    __shared__ long long red_k[32];
+    PairDev &p = pairs[blockIdx.y];
+    if (p.status != 0)
+        return;
+    const int Wy = p.yhi - p.ylo + 1, Wx = p.xhi - p.xlo + 1;
+    const int G = blockDim.x / T;
+    const int team = threadIdx.x / T, t = threadIdx.x - team * T;
+    const int j0 = blockIdx.x * G;
+    if (j0 >= Wy)
+        return;
+    const int j = j0 + team;
+    const bool live = j < Wy;
+    const int jc = live ? j : Wy - 1;
+    float2 *sm = smem + team * PITCH;
+    const int Nx = p.Nx, Ny = p.Ny;
+    // spectrum bins of this lag row (strided over kx)
+    for (int k = t; k <= L; k += T)
+        sm[padi(k)] = p.Q[(long long)k * Wy + jc];
+    __syncthreads();
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int k = t + r * T;
+        float2 a = sm[padi(k)];
+        float2 b = cconj(sm[padi(L - k)]);
+        if (k == 0) {
+            a.y = 0.f;
+            b.y = 0.f;
+        }
+        const float2 e = cadd(a, b);
+        const float2 dd = csub(a, b);
+        float2 wv = __ldg(&tw[2 * L + k]);
+        wv.y = -wv.y;   // W^{-k}
+        const float2 o = cmul(dd, wv);
+        v[r] = make_float2(e.x - o.y, e.y + o.x);
+    }
+    F::run(v, sm, t, tw);
+    __syncthreads();
+    float *C = (float *)sm;   // 2L reals, unpadded
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int n = t + r * T;
+        C[2 * n] = v[r].x;
+        C[2 * n + 1] = v[r].y;
+    }
+    __syncthreads();
+    const double inv = 1.0 / ((double)Nx * (double)Ny);
+    double br = -1.0e30;
+    long long bk = 0x7fffffffffffffffLL;
+    if (live) {
+        const int y = p.ylo + j;
+        const long long dy = y - p.oy;
+        const int xr = isqrt_ll(p.rsqr - dy * dy);
+        const int xa = xr < 0 ? 1 : max(p.xlo, p.ox - xr);
+        const int xb = xr < 0 ? 0 : min(p.xhi, p.ox + xr);
+        const int ys = y < 0 ? y + Ny : y;
+        for (int x = p.xlo + t; x <= p.xhi; x += T) {
+            double rv = 0.0;
+            if (x >= xa && x <= xb) {
+                const int xs = x < 0 ? x + Nx : x;
+                if (lag_r(p, x, y, (double)C[xs] * inv, rv))
+                    best_merge(br, bk, rv, (long long)ys * Nx + xs);
+            }
+            p.rr[(long long)j * Wx + (x - p.xlo)] = rv;
+        }
+    }
+    // team reduction
+    for (int o = 16; o > 0; o >>= 1) {
+        const double r2 = __shfl_down_sync(0xffffffff, br, o);
+        const long long k2 = __shfl_down_sync(0xffffffff, bk, o);
+        if ((threadIdx.x & 31) + o < 32 && ((threadIdx.x & 31) + o) / T == (threadIdx.x & 31) / T)
+            best_merge(br, bk, r2, k2);
+    }
+    if (T <= 32) {
+        if (live && t == 0) {
+            p.rb[j].r = br;
+            p.rb[j].key = bk;
+        }
+        return;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        red_r[wid] = br;
+        red_k[wid] = bk;
+    }
+    __syncthreads();
+    if (live && t == 0) {
+        const int w0 = team * (T / 32);
+        for (int q = 1; q < T / 32; ++q)
+            best_merge(br, bk, red_r[w0 + q], red_k[w0 + q]);
+        p.rb[j].r = br;
+        p.rb[j].key = bk;
+    }
+}
