@@ -827,50 +827,6 @@ __global__ void k_irowfft(const float2 *Q, int logNx, int Ny, double *out,
 
 #include "aln_pipeline.cuh"
 
-// grid (ceil(w/256), 2, npairs): segment totals -> exclusive prefixes per
-// column; column totals for the mean
-__global__ void k2_segscan(PairDev *pairs)
-{
-    PairDev &p = pairs[blockIdx.z];
-    const int i = blockIdx.y;
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    const int w = p.w[i];
-    if (p.status != 0 || c >= w)
-        return;
-    const int nseg = (p.h[i] + SAT_SEG - 1) / SAT_SEG;
-    int an = 0;
-    if ((p.sat_int >> i) & 1) {
-        long long *S = (long long *)p.segS[i], *Q = (long long *)p.segQ[i];
-        long long as = 0, aq = 0;
-        for (int g = 0; g < nseg; ++g) {
-            const long long o = (long long)g * w + c;
-            const long long ts = S[o], tq = Q[o];
-            const int tn = p.segN[i][o];
-            S[o] = as;
-            Q[o] = aq;
-            p.segN[i][o] = an;
-            as += ts;
-            aq += tq;
-            an += tn;
-        }
-        p.colsum[i][c] = (double)as;
-    } else {
-        double as = 0.0, aq = 0.0;
-        for (int g = 0; g < nseg; ++g) {
-            const long long o = (long long)g * w + c;
-            const double ts = p.segS[i][o], tq = p.segQ[i][o];
-            const int tn = p.segN[i][o];
-            p.segS[i][o] = as;
-            p.segQ[i][o] = aq;
-            p.segN[i][o] = an;
-            as += ts;
-            aq += tq;
-            an += tn;
-        }
-        p.colsum[i][c] = as;
-    }
-}
-
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -886,9 +842,15 @@ struct aln_ctx {
     float2 *tw;
     char *ws;
     size_t ws_cap;
-    PairDev *dpairs;
+    PairDev *dpairs;          // the current chunk's job table (one of two parities)
     ResultDev *dres;
-    size_t dpairs_cap;
+    PairDev *dpairs_base;
+    ResultDev *dres_base;
+    size_t dpairs_cap;        // jobs per parity
+    cudaStream_t cstream;     // host-to-device staging copies
+    cudaEvent_t ev_copy[2], ev_done[2];
+    ResultDev *hres;          // pinned result buffer
+    size_t hres_cap;
     size_t ws_budget;
     long long h2d_bytes, d2h_bytes;
     char err[512];
@@ -1006,17 +968,32 @@ extern "C" int aln_ctx_create(int device, aln_ctx **out)
     ctx->ws_cap = 0;
     ctx->dpairs = nullptr;
     ctx->dres = nullptr;
+    ctx->dpairs_base = nullptr;
+    ctx->dres_base = nullptr;
     ctx->dpairs_cap = 0;
+    ctx->cstream = nullptr;
+    ctx->hres = nullptr;
+    ctx->hres_cap = 0;
     ctx->h2d_bytes = ctx->d2h_bytes = 0;
     ctx->err[0] = 0;
     ctx->launches = 0;
     ctx->prof_on = 0;
     ctx->ws_budget = (size_t)4 << 30;
-    if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&ctx->cstream, cudaStreamNonBlocking)) != cudaSuccess) {
         set_err(nullptr, ALN_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
         delete ctx;
         return ALN_ERR_CUDA;
     }
+    for (int q = 0; q < 2; ++q)
+        if ((e = cudaEventCreateWithFlags(&ctx->ev_copy[q], cudaEventDisableTiming)) !=
+                cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&ctx->ev_done[q], cudaEventDisableTiming)) !=
+                cudaSuccess) {
+            set_err(nullptr, ALN_ERR_CUDA, "events: %s", cudaGetErrorString(e));
+            delete ctx;
+            return ALN_ERR_CUDA;
+        }
     if (int ke = configure_kernels()) {
         set_err(nullptr, ALN_ERR_CUDA, "kernel attributes: %s",
                 cudaGetErrorString((cudaError_t)ke));
@@ -1052,8 +1029,16 @@ extern "C" void aln_ctx_destroy(aln_ctx *ctx)
     cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->tw);
     cudaFree(ctx->ws);
-    cudaFree(ctx->dpairs);
-    cudaFree(ctx->dres);
+    cudaStreamSynchronize(ctx->cstream);
+    cudaFree(ctx->dpairs_base);
+    cudaFree(ctx->dres_base);
+    if (ctx->hres)
+        cudaFreeHost(ctx->hres);
+    for (int q = 0; q < 2; ++q) {
+        cudaEventDestroy(ctx->ev_copy[q]);
+        cudaEventDestroy(ctx->ev_done[q]);
+    }
+    cudaStreamDestroy(ctx->cstream);
     prof_collect(ctx);
     for (cudaEvent_t e : ctx->ev_pool)
         cudaEventDestroy(e);
@@ -1105,6 +1090,7 @@ static int ensure_ws(aln_ctx *ctx, size_t bytes)
     if (bytes <= ctx->ws_cap)
         return ALN_OK;
     if (ctx->ws) {
+        CK(cudaStreamSynchronize(ctx->cstream));
         CK(cudaStreamSynchronize(ctx->stream));
         cudaFree(ctx->ws);
         ctx->ws = nullptr;
@@ -1125,17 +1111,19 @@ static int ensure_pairs(aln_ctx *ctx, size_t n)
 {
     if (n <= ctx->dpairs_cap)
         return ALN_OK;
-    if (ctx->dpairs) {
+    if (ctx->dpairs_base) {
         CK(cudaStreamSynchronize(ctx->stream));
-        cudaFree(ctx->dpairs);
-        cudaFree(ctx->dres);
-        ctx->dpairs = nullptr;
-        ctx->dres = nullptr;
+        cudaFree(ctx->dpairs_base);
+        cudaFree(ctx->dres_base);
+        ctx->dpairs = ctx->dpairs_base = nullptr;
+        ctx->dres = ctx->dres_base = nullptr;
         ctx->dpairs_cap = 0;
     }
     size_t cap = std::max<size_t>(n, 64);
-    CK(cudaMalloc(&ctx->dpairs, cap * sizeof(PairDev)));
-    CK(cudaMalloc(&ctx->dres, cap * sizeof(ResultDev)));
+    CK(cudaMalloc(&ctx->dpairs_base, 2 * cap * sizeof(PairDev)));
+    CK(cudaMalloc(&ctx->dres_base, 2 * cap * sizeof(ResultDev)));
+    ctx->dpairs = ctx->dpairs_base;
+    ctx->dres = ctx->dres_base;
     ctx->dpairs_cap = cap;
     return ALN_OK;
 }
@@ -1278,7 +1266,9 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
     for (int i = 0; i < 2; ++i) {
         pl.in_bytes[i] = im[i]->on_device ? 0 : al256((size_t)d.w[i] * d.h[i] * dtype_size(d.dt[i]));
         b += pl.in_bytes[i];
-        pl.tr_bytes[i] = pl.transposed ? al256((size_t)d.w[i] * d.h[i] * dtype_size(d.dt[i])) : 0;
+        pl.tr_bytes[i] = pl.transposed
+                             ? al256((size_t)((d.w[i] + 15) & ~15) * d.h[i] * dtype_size(d.dt[i]))
+                             : 0;
         b += pl.tr_bytes[i];
         d.Ts[i] = (d.h[i] + 3) & ~3;
         b += al256((size_t)L1 * d.Ts[i] * sizeof(float2));
@@ -1288,8 +1278,8 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
                 ns += d.need_hi[i][k] - d.need_lo[i][k] + 1;
         b += 2 * al256((size_t)ns * d.w[i] * sizeof(double)) + al256((size_t)ns * d.w[i] * sizeof(int));
         b += al256((size_t)d.w[i] * sizeof(double));
-        const size_t nseg = (size_t)(d.h[i] + 63) / 64;
-        b += 2 * al256(nseg * d.w[i] * sizeof(double)) + al256(nseg * d.w[i] * sizeof(int));
+        b += 2 * al256((size_t)SAT_WARPS * d.w[i] * sizeof(double)) +
+             al256((size_t)SAT_WARPS * d.w[i] * sizeof(int));
     }
     b += al256((size_t)L1 * d.Ny * sizeof(float2));
     b += al256((size_t)L1 * Wy * sizeof(float2));
@@ -1302,7 +1292,11 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
 }
 
 // carve a pair's workspace starting at base; returns bytes used
-static size_t carve(PairPlan &pl, char *base, const aln_pair &P)
+// carve a pair's workspace starting at base; returns bytes used.  With a
+// staging cursor, host-input staging goes there instead, packed back to back
+// (aligned to the element size only) so that adjacent host images can be
+// copied with one transfer.
+static size_t carve(PairPlan &pl, char *base, const aln_pair &P, char **stage = nullptr)
 {
     PairDev &d = pl.d;
     char *p = base;
@@ -1311,18 +1305,26 @@ static size_t carve(PairPlan &pl, char *base, const aln_pair &P)
     for (int i = 0; i < 2; ++i) {
         if (pl.in_bytes[i]) {
             // staging of a host input, in the caller's layout (packed)
+            char *q = p;
+            if (stage) {
+                const size_t es = dtype_size(d.dt[i]);
+                *stage = (char *)(((uintptr_t)*stage + es - 1) & ~(uintptr_t)(es - 1));
+                q = *stage;
+                *stage += (size_t)d.w[i] * d.h[i] * es;
+            } else {
+                p += pl.in_bytes[i];
+            }
             if (pl.transposed) {
-                d.src_img[i] = p;
+                d.src_img[i] = q;
                 d.src_stride[i] = d.h[i];   // caller's width
             } else {
-                d.img[i] = p;
+                d.img[i] = q;
                 d.stride[i] = d.w[i];
             }
-            p += pl.in_bytes[i];
         }
         if (pl.tr_bytes[i]) {
             d.img[i] = p;
-            d.stride[i] = d.w[i];
+            d.stride[i] = (d.w[i] + 15) & ~15;
             p += pl.tr_bytes[i];
         }
         d.T[i] = (float2 *)p;
@@ -1339,13 +1341,12 @@ static size_t carve(PairPlan &pl, char *base, const aln_pair &P)
         p += al256((size_t)ns * d.w[i] * sizeof(int));
         d.colsum[i] = (double *)p;
         p += al256((size_t)d.w[i] * sizeof(double));
-        const size_t nseg = (size_t)(d.h[i] + 63) / 64;
         d.segS[i] = (double *)p;
-        p += al256(nseg * d.w[i] * sizeof(double));
+        p += al256((size_t)SAT_WARPS * d.w[i] * sizeof(double));
         d.segQ[i] = (double *)p;
-        p += al256(nseg * d.w[i] * sizeof(double));
+        p += al256((size_t)SAT_WARPS * d.w[i] * sizeof(double));
         d.segN[i] = (int *)p;
-        p += al256(nseg * d.w[i] * sizeof(int));
+        p += al256((size_t)SAT_WARPS * d.w[i] * sizeof(int));
     }
     d.X2 = (float2 *)p;
     p += al256((size_t)L1 * d.Ny * sizeof(float2));
@@ -1371,7 +1372,7 @@ static void launch_rowfft2(aln_ctx *ctx, int n, int maxh)
 {
     constexpr int T = RegFFT<LL, -1>::T;
     const int thr = rowfft_threads(T), G = thr / T;
-    const size_t sm = (size_t)G * (padded(LL) + 1) * sizeof(float2);
+    const size_t sm = (size_t)G * (padded(LL) + 2) * sizeof(float2);
     cudaFuncSetAttribute(k2_rowfft<LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     LAUNCH(ctx, "k2_rowfft", k2_rowfft<LL>, dim3((maxh + G - 1) / G, 2, n), thr, sm,
            ctx->dpairs, ctx->tw, -1);
@@ -1427,38 +1428,64 @@ static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int
     return ALN_OK;
 }
 
-// Runs one chunk of pairs that share (Nx, Ny).
-static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk)
+// One chunk of pairs sharing (Nx, Ny), run as a two-stage pipeline step:
+// host inputs are copied on the copy stream into staging buffer `par`
+// (adjacent host images in one transfer), the kernels run on the compute
+// stream once that copy is done, and the results go to pinned host memory.
+// Nothing here waits for the GPU; the caller synchronises once per batch.
+static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int par, char *stage_base,
+                     char *work_base, ResultDev *hres_out)
 {
     const int n = (int)chunk.size();
-    size_t total = 0;
-    for (auto *pl : chunk)
-        total += pl->ws_bytes;
-    if (int rc = ensure_ws(ctx, total))
-        return rc;
-    if (int rc = ensure_pairs(ctx, n))
-        return rc;
-    char *base = ctx->ws;
+    ctx->dpairs = ctx->dpairs_base + (size_t)par * ctx->dpairs_cap;
+    ctx->dres = ctx->dres_base + (size_t)par * ctx->dpairs_cap;
     std::vector<PairDev> hd(n);
     int maxw = 1, maxh = 1, maxslots = 1, maxWy = 1;
     const int Nx = chunk[0]->d.Nx, Ny = chunk[0]->d.Ny;
+    char *stage = stage_base, *work = work_base;
+    // staging copies, coalesced over host images adjacent in memory
+    CK(cudaStreamWaitEvent(ctx->cstream, ctx->ev_done[par], 0));
+    const char *run_src = nullptr, *run_end = nullptr;
+    char *run_dst = nullptr;
+    auto flush = [&]() -> int {
+        if (run_src && run_end > run_src) {
+            CK(cudaMemcpyAsync(run_dst, run_src, (size_t)(run_end - run_src),
+                               cudaMemcpyHostToDevice, ctx->cstream));
+            ctx->h2d_bytes += (long long)(run_end - run_src);
+        }
+        run_src = run_end = nullptr;
+        run_dst = nullptr;
+        return ALN_OK;
+    };
     for (int k = 0; k < n; ++k) {
         PairPlan &pl = *chunk[k];
         const aln_pair &P = *pl.src;
-        base += carve(pl, base, P);
+        work += carve(pl, work, P, &stage);
         const aln_image *im[2] = {&P.a, &P.b};
         for (int i = 0; i < 2; ++i) {
             if (pl.in_bytes[i]) {
                 const size_t es = dtype_size(im[i]->dtype);
-                void *dst = pl.transposed ? (void *)pl.d.src_img[i] : (void *)pl.d.img[i];
-                if (im[i]->stride == im[i]->w)
-                    CK(cudaMemcpyAsync(dst, im[i]->data, (size_t)im[i]->w * im[i]->h * es,
-                                       cudaMemcpyHostToDevice, ctx->stream));
-                else
+                char *dst = pl.transposed ? (char *)pl.d.src_img[i] : (char *)pl.d.img[i];
+                const size_t bytes = (size_t)im[i]->w * im[i]->h * es;
+                const char *src = (const char *)im[i]->data;
+                if (im[i]->stride == im[i]->w) {
+                    if (run_src && src == run_end && dst == run_dst + (run_end - run_src)) {
+                        run_end += bytes;
+                    } else {
+                        if (int rc = flush())
+                            return rc;
+                        run_src = src;
+                        run_end = src + bytes;
+                        run_dst = dst;
+                    }
+                } else {
+                    if (int rc = flush())
+                        return rc;
                     CK(cudaMemcpy2DAsync(dst, (size_t)im[i]->w * es, im[i]->data,
                                          (size_t)im[i]->stride * es, (size_t)im[i]->w * es,
-                                         im[i]->h, cudaMemcpyHostToDevice, ctx->stream));
-                ctx->h2d_bytes += (long long)im[i]->w * im[i]->h * es;
+                                         im[i]->h, cudaMemcpyHostToDevice, ctx->cstream));
+                    ctx->h2d_bytes += (long long)bytes;
+                }
             }
             maxw = std::max(maxw, pl.d.w[i]);
             maxh = std::max(maxh, pl.d.h[i]);
@@ -1473,15 +1500,17 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk)
                        (pl.d.dt[1] == ALN_U8 || pl.d.dt[1] == ALN_U16 ? 2 : 0);
         hd[k] = pl.d;
     }
-    // legality tables (host) -> device
+    if (int rc = flush())
+        return rc;
+    CK(cudaEventRecord(ctx->ev_copy[par], ctx->cstream));
+    // job table and legality tables (pageable sources: staged before return)
+    cudaStream_t st = ctx->stream;
     for (int k = 0; k < n; ++k)
         if (hd[k].rgn_kind == ALN_RGN_TABLE)
             CK(cudaMemcpyAsync((void *)hd[k].table, chunk[k]->src->legal.table,
-                               (size_t)hd[k].table_w * hd[k].table_h, cudaMemcpyHostToDevice,
-                               ctx->stream));
-    CK(cudaMemcpyAsync(ctx->dpairs, hd.data(), n * sizeof(PairDev), cudaMemcpyHostToDevice,
-                       ctx->stream));
-    cudaStream_t st = ctx->stream;
+                               (size_t)hd[k].table_w * hd[k].table_h, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->dpairs, hd.data(), n * sizeof(PairDev), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamWaitEvent(st, ctx->ev_copy[par], 0));
     const int L = Nx / 2;
     {
         int sw = 0, sh = 0;   // largest caller-frame image among transposed jobs
@@ -1495,16 +1524,10 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk)
             LAUNCH(ctx, "k_transpose", k_transpose, dim3((sw + 31) / 32, (sh + 31) / 32, 2 * n),
                    dim3(32, 8), 0, ctx->dpairs);
     }
-    {
-        int maxseg = 1;
-        for (int k = 0; k < n; ++k)
-            maxseg = std::max(maxseg, (std::max(hd[k].h[0], hd[k].h[1]) + 63) / 64);
-        LAUNCH(ctx, "k2_sat1", k2_sat1, dim3((maxw + 31) / 32, (maxseg + 7) / 8, 2 * n),
-               dim3(32, 8), 0, ctx->dpairs);
-        LAUNCH(ctx, "k2_segscan", k2_segscan, dim3((maxw + 255) / 256, 2, n), 256, 0, ctx->dpairs);
-        LAUNCH(ctx, "k_mean", k_mean, dim3(2, n), 256, 0, ctx->dpairs);
-        LAUNCH(ctx, "k2_sat2", k2_sat2, dim3(maxslots, 2, n), 256, 0, ctx->dpairs);
-    }
+    LAUNCH(ctx, "k3_sat", k3_sat, dim3((maxw + 31) / 32, 2 * n), dim3(32, SAT_WARPS), 0,
+           ctx->dpairs);
+    LAUNCH(ctx, "k_mean", k_mean, dim3(2, n), 256, 0, ctx->dpairs);
+    LAUNCH(ctx, "k2_sat2", k2_sat2, dim3(maxslots, 2, n), 256, 0, ctx->dpairs);
     if (L >= 16 && L <= 4096 && Ny >= 16 && Ny <= 8192) {
         if (int rc = launch_fft_pipeline(ctx, L, Ny, n, maxh, maxWy))
             return rc;
@@ -1529,23 +1552,12 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk)
                    ctx->dpairs, ctx->tw, RBL);
         }
     }
-    LAUNCH(ctx, "k_final", k_final, n, 256, 0, ctx->dpairs, ctx->dres,
-           chunk[0]->frame_nx1, chunk[0]->frame_ny1);
+    LAUNCH(ctx, "k_final", k_final, n, 256, 0, ctx->dpairs, ctx->dres, chunk[0]->frame_nx1,
+           chunk[0]->frame_ny1);
     CK(cudaGetLastError());
-    std::vector<ResultDev> hr(n);
-    CK(cudaMemcpyAsync(hr.data(), ctx->dres, n * sizeof(ResultDev), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpyAsync(hres_out, ctx->dres, n * sizeof(ResultDev), cudaMemcpyDeviceToHost, st));
     ctx->d2h_bytes += n * sizeof(ResultDev);
-    prof_collect(ctx);
-    for (int k = 0; k < n; ++k) {
-        PairDev &d = chunk[k]->d;
-        d.r = hr[k].r;
-        d.dx = hr[k].dx;
-        d.dy = hr[k].dy;
-        d.status = hr[k].status;
-        d.px = hr[k].px;
-        d.py = hr[k].py;
-    }
+    CK(cudaEventRecord(ctx->ev_done[par], st));
     return ALN_OK;
 }
 
@@ -1561,6 +1573,20 @@ static void fill_result(const PairPlan &pl, aln_result *o)
     o->ny = pl.orig_ny;
 }
 
+static int ensure_hres(aln_ctx *ctx, size_t n)
+{
+    if (n <= ctx->hres_cap)
+        return ALN_OK;
+    if (ctx->hres)
+        cudaFreeHost(ctx->hres);
+    ctx->hres = nullptr;
+    ctx->hres_cap = 0;
+    const size_t cap = std::max<size_t>(n, 4096);
+    CK(cudaHostAlloc((void **)&ctx->hres, cap * sizeof(ResultDev), cudaHostAllocDefault));
+    ctx->hres_cap = cap;
+    return ALN_OK;
+}
+
 extern "C" int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *pairs,
                                       aln_result *out)
 {
@@ -1574,28 +1600,72 @@ extern "C" int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *
         if (int rc = plan_pair(ctx, pairs[k], plans[k], true))
             return rc;
     }
-    // group by FFT size, keep submission order inside a group
+    // group by FFT size, keep submission order inside a group, split into
+    // chunks bounded by the workspace budget
     std::map<std::tuple<int, int, int, int>, std::vector<PairPlan *>> groups;
     for (auto &pl : plans)
         if (pl.d.status == 0)
             groups[std::make_tuple(pl.d.Nx, pl.d.Ny, pl.frame_nx1, pl.frame_ny1)].push_back(&pl);
+    std::vector<std::vector<PairPlan *>> chunks;
+    size_t max_stage = 0, max_work = 0, max_n = 1;
     for (auto &g : groups) {
         std::vector<PairPlan *> chunk;
-        size_t bytes = 0;
+        size_t sb = 0, wb = 0;
+        auto close = [&]() {
+            max_stage = std::max(max_stage, sb);
+            max_work = std::max(max_work, wb);
+            max_n = std::max(max_n, chunk.size());
+            chunks.push_back(chunk);
+            chunk.clear();
+            sb = wb = 0;
+        };
         for (PairPlan *pl : g.second) {
-            if (!chunk.empty() && (bytes + pl->ws_bytes > ctx->ws_budget || chunk.size() >= 4096)) {
-                if (int rc = run_chunk(ctx, chunk))
-                    return rc;
-                chunk.clear();
-                bytes = 0;
-            }
+            const size_t st = pl->in_bytes[0] + pl->in_bytes[1];
+            const size_t wk = pl->ws_bytes - st;
+            if (!chunk.empty() && (sb + st + wb + wk > ctx->ws_budget || chunk.size() >= 4096))
+                close();
             chunk.push_back(pl);
-            bytes += pl->ws_bytes;
+            sb += st + 16;
+            wb += wk;
         }
         if (!chunk.empty())
-            if (int rc = run_chunk(ctx, chunk))
-                return rc;
+            close();
     }
+    max_stage = al256(max_stage);
+    max_work = al256(max_work);
+    if (int rc = ensure_ws(ctx, 2 * max_stage + max_work))
+        return rc;
+    if (int rc = ensure_pairs(ctx, max_n))
+        return rc;
+    if (int rc = ensure_hres(ctx, (size_t)npairs))
+        return rc;
+    // two-stage pipeline over the chunks
+    size_t done = 0;
+    std::vector<size_t> first(chunks.size());
+    for (size_t c = 0; c < chunks.size(); ++c) {
+        const int par = (int)(c & 1);
+        first[c] = done;
+        if (int rc = run_chunk(ctx, chunks[c], par, ctx->ws + par * max_stage,
+                               ctx->ws + 2 * max_stage, ctx->hres + done)) {
+            cudaStreamSynchronize(ctx->cstream);
+            cudaStreamSynchronize(ctx->stream);
+            return rc;
+        }
+        done += chunks[c].size();
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    prof_collect(ctx);
+    for (size_t c = 0; c < chunks.size(); ++c)
+        for (size_t k = 0; k < chunks[c].size(); ++k) {
+            const ResultDev &r = ctx->hres[first[c] + k];
+            PairDev &d = chunks[c][k]->d;
+            d.r = r.r;
+            d.dx = r.dx;
+            d.dy = r.dy;
+            d.status = r.status;
+            d.px = r.px;
+            d.py = r.py;
+        }
     for (int k = 0; k < npairs; ++k)
         fill_result(plans[k], &out[k]);
     return ALN_OK;

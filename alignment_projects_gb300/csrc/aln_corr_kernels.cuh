@@ -54,8 +54,8 @@ struct PairDev {
     float2 *Q;          // column-inverse output [kx][j], j = y - ylo, stride Wy
     double *satS[2], *satQ[2];   // summed-area tables of v and v^2, [y][x] stride w
     int *satN[2];                // summed-area table of (v != 0)
-    int sat_int;                 // bit i: image i's sat/seg S, Q tables hold int64
-    double *segS[2], *segQ[2];   // per 64-row segment column totals -> prefixes
+    int sat_int;                 // bit i: image i's S, Q tables hold int64
+    double *segS[2], *segQ[2];   // per column-walk segment: exclusive column offsets
     int *segN[2];
     double *colsum[2];           // per-column totals (mean shift)
     double *rr;                  // r over the lag window [j][x - xlo]

@@ -2,11 +2,10 @@
 // register-resident FFT (aln_fft_reg.cuh).  Included by aln_corr.cu, after
 // the device helpers (load_px, sat slots, lag_r, best_merge).
 //
-//   k2_sat1   per (column, 64-row segment): local column prefix of v, v^2,
-//             (v != 0) at the needed rows; segment totals
-//   k2_segscan (aln_corr.cu) exclusive prefix over segments per column,
-//             column totals; k_mean turns them into the shift mu
-//   k2_sat2   per needed row: add the segments above, x-prefix scan -> SAT row
+//   k3_sat    per 32-column band: warp-local column prefix sums of v, v^2,
+//             (v != 0) at the needed rows, per-warp offsets; column totals
+//             (k_mean turns them into mu)
+//   k2_sat2   per needed row: add the warp offset, x-prefix -> SAT row
 //   k2_rowfft<L>   rows: (v - mu), zero pad, real FFT of length 2L, [kx][y]
 //   k2_corrcol<Ny> per column kx: FFT of b's column (or the cached spectrum),
 //             FFT of a's column, X2 * conj(X1), inverse FFT, the window's
@@ -16,64 +15,117 @@
 
 #include "aln_fft_reg.cuh"
 
-#define SAT_SEG 64
-
 __device__ __forceinline__ bool int_pixels(int dt) { return dt == ALN_U8 || dt == ALN_U16; }
 
-// grid (ceil(w/32), ceil(nseg/8), 2*npairs), block (32, 8)
-__global__ void k2_sat1(PairDev *pairs)
+// Column prefix sums of v, v^2 and (v != 0) at the rows the lag window needs
+// (IntegrateImage's sums, 0_GEN/Correlation.cpp:49-105, restricted to the
+// rows IntegralTable will read).  grid (ceil(w/32), 2*npairs), block
+// (32, SAT_WARPS): each CTA owns 32 columns of one image; warp ty owns rows
+// [ty*segh, (ty+1)*segh) and walks them once, storing its local column
+// prefix at the needed rows.  The warps' exclusive offsets per column go to
+// segoff[ty][c]; k2_sat2 adds them.  Exact int64 for 8/16-bit pixels, FP64
+// otherwise.  Also writes the column totals (mean shift).
+#define SAT_WARPS 16
+
+template <typename TA, typename PIX>
+__device__ __forceinline__ void sat_cols(const PairDev &p, int i, TA *shS, TA *shQ, int *shN)
 {
-    PairDev &p = pairs[blockIdx.z >> 1];
-    const int i = blockIdx.z & 1;
-    const int w = p.w[i], h = p.h[i], dt = p.dt[i];
-    const int c = blockIdx.x * 32 + threadIdx.x;
-    const int seg = blockIdx.y * 8 + threadIdx.y;
-    const int y0 = seg * SAT_SEG;
-    if (p.status != 0 || c >= w || y0 >= h)
-        return;
-    const int y1 = min(h, y0 + SAT_SEG);
-    const void *img = p.img[i];
+    const int w = p.w[i], h = p.h[i];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int c = blockIdx.x * 32 + tx;
+    const bool cok = c < w;
+    const int segh = (h + SAT_WARPS - 1) / SAT_WARPS;
+    const int y0 = min(h, ty * segh), y1 = min(h, y0 + segh);
+    const PIX *img = (const PIX *)p.img[i];
     const long long st = p.stride[i];
-    const int nseg = (h + SAT_SEG - 1) / SAT_SEG;
-    int *N = p.satN[i];
-    int nz = 0;
-    if (int_pixels(dt)) {
-        long long *S = (long long *)p.satS[i], *Q = (long long *)p.satQ[i];
-        long long s = 0, q = 0;
-        for (int y = y0; y < y1; ++y) {
-            const long long v = dt == ALN_U8 ? ((const uint8_t *)img)[y * st + c]
-                                             : ((const uint16_t *)img)[y * st + c];
-            s += v;
-            q += v * v;
-            nz += (v != 0);
-            if (row_needed(p, i, y)) {
-                const long long o = (long long)sat_slot(p, i, y) * w + c;
+    const int lo0 = p.need_lo[i][0], hi0 = p.need_hi[i][0];
+    const int lo1 = p.need_lo[i][1], hi1 = p.need_hi[i][1];
+    const int len0 = hi0 - lo0 + 1;
+    const bool want_n = p.cnt_kind == ALN_CNT_GT;
+    TA *__restrict__ S = (TA *)p.satS[i];
+    TA *__restrict__ Q = (TA *)p.satQ[i];
+    int *__restrict__ N = p.satN[i];
+    TA s = 0, q = 0;
+    int n = 0;
+    if (cok) {
+        const PIX *__restrict__ col = img + c;
+        // walk [y0, y1) as store-free runs (loads batch freely) separated by
+        // the needed rows, where the running prefix is stored
+        int y = y0;
+        while (y < y1) {
+            int stop = y1;   // next needed row at or after y
+            if (hi0 >= lo0 && hi0 >= y)
+                stop = min(stop, max(lo0, y));
+            if (hi1 >= lo1 && hi1 >= y)
+                stop = min(stop, max(lo1, y));
+#pragma unroll 8
+            for (; y < stop; ++y) {
+                const TA v = (TA)__ldg(&col[y * st]);
+                s += v;
+                q += v * v;
+                if (want_n)
+                    n += (v != 0);
+            }
+            if (y >= y1)
+                break;
+            // needed run: rows y .. end of its interval (within the warp's rows)
+            const bool first = y >= lo0 && y <= hi0;
+            const int rend = min(y1 - 1, first ? hi0 : hi1);
+            const long long base = first ? (long long)(y - lo0) : (long long)(len0 + y - lo1);
+            for (long long o = base * w + c; y <= rend; ++y, o += w) {
+                const TA v = (TA)__ldg(&col[y * st]);
+                s += v;
+                q += v * v;
+                if (want_n)
+                    n += (v != 0);
                 S[o] = s;
                 Q[o] = q;
-                N[o] = nz;
+                N[o] = n;
             }
         }
-        ((long long *)p.segS[i])[(long long)seg * w + c] = s;
-        ((long long *)p.segQ[i])[(long long)seg * w + c] = q;
-    } else {
-        double s = 0.0, q = 0.0;
-        for (int y = y0; y < y1; ++y) {
-            const double v = load_px(img, dt, y * st + c);
-            s += v;
-            q += v * v;
-            nz += (v != 0.0);
-            if (row_needed(p, i, y)) {
-                const long long o = (long long)sat_slot(p, i, y) * w + c;
-                p.satS[i][o] = s;
-                p.satQ[i][o] = q;
-                N[o] = nz;
-            }
-        }
-        p.segS[i][(long long)seg * w + c] = s;
-        p.segQ[i][(long long)seg * w + c] = q;
     }
-    p.segN[i][(long long)seg * w + c] = nz;
-    (void)nseg;
+    shS[ty * 32 + tx] = s;
+    shQ[ty * 32 + tx] = q;
+    shN[ty * 32 + tx] = n;
+    __syncthreads();
+    if (!cok)
+        return;
+    TA os = 0, oq = 0;
+    int on = 0;
+    for (int g = 0; g < ty; ++g) {
+        os += shS[g * 32 + tx];
+        oq += shQ[g * 32 + tx];
+        on += shN[g * 32 + tx];
+    }
+    ((TA *)p.segS[i])[ty * w + c] = os;
+    ((TA *)p.segQ[i])[ty * w + c] = oq;
+    p.segN[i][ty * w + c] = on;
+    if (ty == SAT_WARPS - 1)
+        p.colsum[i][c] = (double)(os + s);
+}
+
+__global__ void k3_sat(PairDev *pairs)
+{
+    __shared__ long long shS[32 * SAT_WARPS], shQ[32 * SAT_WARPS];
+    __shared__ int shN[32 * SAT_WARPS];
+    const PairDev &p = pairs[blockIdx.y >> 1];
+    const int i = blockIdx.y & 1;
+    if (p.status != 0 || blockIdx.x * 32 >= p.w[i])
+        return;
+    switch (p.dt[i]) {
+    case ALN_U8:
+        sat_cols<long long, uint8_t>(p, i, shS, shQ, shN);
+        break;
+    case ALN_U16:
+        sat_cols<long long, uint16_t>(p, i, shS, shQ, shN);
+        break;
+    case ALN_F32:
+        sat_cols<double, float>(p, i, (double *)shS, (double *)shQ, shN);
+        break;
+    default:
+        sat_cols<double, double>(p, i, (double *)shS, (double *)shQ, shN);
+        break;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -111,11 +163,49 @@ __global__ void k_transpose(PairDev *pairs)
         return;
     const int sw = p.h[i], sh = p.w[i];   // caller's width and height
     const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
-    if (x0 >= sw || y0 >= sh)
+    if (y0 >= sh)
         return;
     const int es = p.dt[i] == ALN_U8 ? 1 : p.dt[i] == ALN_U16 ? 2 : p.dt[i] == ALN_F32 ? 4 : 8;
     const char *src = (const char *)p.src_img[i];
     const long long sst = p.src_stride[i];
+    if (es == 1) {
+        // uint8: a 32 x 128 tile per CTA (blockIdx.x counts 128-column tiles)
+        unsigned char(*t8)[132] = (unsigned char(*)[132])tile;
+        const int xb0 = blockIdx.x * 128;
+        if (xb0 >= sw)
+            return;
+        for (int rr = threadIdx.y; rr < 32; rr += 8) {
+            const int yy = y0 + rr;
+            for (int m = 0; m < 4; ++m) {
+                const int x = xb0 + 4 * threadIdx.x + m;
+                t8[rr][4 * threadIdx.x + m] =
+                    (yy < sh && x < sw) ? (unsigned char)src[yy * sst + x] : 0;
+            }
+        }
+        __syncthreads();
+        unsigned char *dst = (unsigned char *)p.img[i];
+        const long long dstr = p.stride[i];
+        const int tid = threadIdx.y * 32 + threadIdx.x;
+        for (int e = tid; e < 128 * 8; e += 256) {
+            const int j = e >> 3, wq = e & 7;
+            const int xs = xb0 + j, ys = y0 + 4 * wq;
+            if (xs >= sw || ys >= sh)
+                continue;
+            if (ys + 3 < sh && (dstr & 3) == 0) {
+                const unsigned int word = (unsigned int)t8[4 * wq][j] |
+                                          ((unsigned int)t8[4 * wq + 1][j] << 8) |
+                                          ((unsigned int)t8[4 * wq + 2][j] << 16) |
+                                          ((unsigned int)t8[4 * wq + 3][j] << 24);
+                *(unsigned int *)(dst + xs * dstr + ys) = word;
+            } else {
+                for (int m = 0; m < 4 && ys + m < sh; ++m)
+                    dst[xs * dstr + ys + m] = t8[4 * wq + m][j];
+            }
+        }
+        return;
+    }
+    if (x0 >= sw)
+        return;
     for (int yy = threadIdx.y; yy < 32; yy += 8) {
         const int y = y0 + yy, x = x0 + threadIdx.x;
         if (y < sh && x < sw)
@@ -183,27 +273,27 @@ __device__ __forceinline__ void block_scan3(TA &a, TA &b, int &c, TA *sa, TA *sb
 }
 
 template <typename TA>
-__device__ void sat2_row(PairDev &p, int i, int slot, int y, TA *S, TA *Q, const TA *segS,
-                         const TA *segQ)
+__device__ void sat2_row(PairDev &p, int i, int slot, int y, TA *S, TA *Q)
 {
     __shared__ TA sa[8], sb[8];
     __shared__ int sc[8];
     const int w = p.w[i];
-    const int seg = y / SAT_SEG;
+    const int seg = y / ((p.h[i] + SAT_WARPS - 1) / SAT_WARPS);
+    const TA *oS = (const TA *)p.segS[i] + (long long)seg * w;
+    const TA *oQ = (const TA *)p.segQ[i] + (long long)seg * w;
+    const int *oN = p.segN[i] + (long long)seg * w;
     TA *rS = S + (long long)slot * w;
     TA *rQ = Q + (long long)slot * w;
     int *rN = p.satN[i] + (long long)slot * w;
-    const int *segN = p.segN[i];
     const int per = (w + 255) / 256;
     const int c0 = threadIdx.x * per, c1 = min(w, c0 + per);
-    // full column prefix = exclusive segment prefix + local prefix; then the
-    // x-prefix of this thread's columns
+    // full column prefix (warp segment offset + local), x-prefix of this
+    // thread's columns, then the block-wide offsets
     TA s = 0, q = 0;
     int n = 0;
-    const long long so = (long long)seg * w;
     for (int c = c0; c < c1; ++c) {
-        const TA cs = rS[c] + segS[so + c], cq = rQ[c] + segQ[so + c];
-        const int cn = rN[c] + segN[so + c];
+        const TA cs = rS[c] + oS[c], cq = rQ[c] + oQ[c];
+        const int cn = rN[c] + oN[c];
         s += cs;
         q += cq;
         n += cn;
@@ -234,10 +324,9 @@ __global__ void k2_sat2(PairDev *pairs)
     const int len0 = p.need_hi[i][0] - p.need_lo[i][0] + 1;
     const int y = slot < len0 ? p.need_lo[i][0] + slot : p.need_lo[i][1] + slot - len0;
     if (int_pixels(p.dt[i]))
-        sat2_row<long long>(p, i, slot, y, (long long *)p.satS[i], (long long *)p.satQ[i],
-                            (const long long *)p.segS[i], (const long long *)p.segQ[i]);
+        sat2_row<long long>(p, i, slot, y, (long long *)p.satS[i], (long long *)p.satQ[i]);
     else
-        sat2_row<double>(p, i, slot, y, p.satS[i], p.satQ[i], p.segS[i], p.segQ[i]);
+        sat2_row<double>(p, i, slot, y, p.satS[i], p.satQ[i]);
 }
 
 // ---------------------------------------------------------------------------
@@ -248,7 +337,7 @@ __global__ void k2_sat2(PairDev *pairs)
 __host__ __device__ constexpr int rowfft_threads(int T) { return T * 4 > 512 ? 512 : (T * 4 < 256 ? 256 : T * 4); }
 
 // Each team of RegFFT<L>::T threads transforms one row.  G = blockDim.x / T
-// rows per CTA; smem: G * (padded(L) + 1) float2 (+1 for bin L).
+// rows per CTA; smem: G * (padded(L) + 2) float2 per CTA.
 template <int L>
 __global__ void k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img)
 {
@@ -266,16 +355,31 @@ __global__ void k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int onl
     if (y0 >= h)
         return;
     const int y = y0 + team;
-    constexpr int PITCH = padded(L) + 1;
+    constexpr int PITCH = padded(L) + 2;   // even: 16-byte aligned team regions
     float2 *sm = smem + team * PITCH;
     const void *img = p.img[i];
     const long long st = p.stride[i];
     float2 v[R];
     if (dt == ALN_U8 || dt == ALN_U16) {
-        // integer pixels, integer shift: exact before the conversion
+        // integer pixels, integer shift: exact before the conversion.  The
+        // row is staged in shared memory with 16-byte loads from its
+        // 16-byte-aligned start (an aligned 16-byte block that holds a byte
+        // of the row never leaves the row's allocation page).
+        const int es = dt == ALN_U8 ? 1 : 2;
         const int mu = (int)p.mu[i];
-        const uint8_t *p8 = (const uint8_t *)img + (dt == ALN_U8 ? y * st : 0);
-        const uint16_t *p16 = (const uint16_t *)img + (dt == ALN_U16 ? y * st : 0);
+        unsigned char *sb = (unsigned char *)sm;
+        int off = 0;
+        if (y < h) {
+            const unsigned char *base = (const unsigned char *)img + (long long)y * st * es;
+            const uintptr_t a0 = (uintptr_t)base & ~(uintptr_t)15;
+            off = (int)((uintptr_t)base - a0);
+            const int nvec = (off + w * es + 15) >> 4;
+            const uint4 *src = (const uint4 *)a0;
+            for (int k = t; k < nvec; k += T)
+                ((uint4 *)sb)[k] = src[k];
+        }
+        __syncthreads();
+        const unsigned char *rb8 = sb + off;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const int n = t + r * T;
@@ -283,9 +387,9 @@ __global__ void k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int onl
             if (y < h) {
                 const int xa = 2 * n, xb = 2 * n + 1;
                 if (xa < w)
-                    z.x = (float)((dt == ALN_U8 ? (int)p8[xa] : (int)p16[xa]) - mu);
+                    z.x = (float)((es == 1 ? (int)rb8[xa] : (int)((const uint16_t *)rb8)[xa]) - mu);
                 if (xb < w)
-                    z.y = (float)((dt == ALN_U8 ? (int)p8[xb] : (int)p16[xb]) - mu);
+                    z.y = (float)((es == 1 ? (int)rb8[xb] : (int)((const uint16_t *)rb8)[xb]) - mu);
             }
             v[r] = z;
         }

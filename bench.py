@@ -376,13 +376,20 @@ def run_gpu(args):
         traffic = tr * n * args.steps / max(1, dom_launches)
 
     # ---- end to end through the C ABI with pinned host buffers -------------
+    # host strips in one pinned buffer, pair after pair (a, b), as a tile
+    # loader would stage them; the library copies adjacent images at once
+    pinned = torch.empty(strip_bytes, dtype=torch.uint8, pin_memory=True)
     host_bufs = []
+    off = 0
     for p in batch:
-        ha = torch.empty(p["a"].shape, dtype=torch.uint8, pin_memory=True)
-        hb = torch.empty(p["b"].shape, dtype=torch.uint8, pin_memory=True)
-        ha.copy_(p["a"])
-        hb.copy_(p["b"])
-        host_bufs.append((ha, hb))
+        views = []
+        for key in ("a", "b"):
+            t = p[key]
+            v = pinned[off:off + t.numel()].view(t.shape)
+            v.copy_(t)
+            off += t.numel()
+            views.append(v)
+        host_bufs.append(tuple(views))
     arr_h, out_h = build_pair_array(batch, False, host_bufs)
 
     def step_host():
