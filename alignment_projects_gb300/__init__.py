@@ -26,4 +26,7 @@ from .native import (  # noqa: F401
     RGN_TABLE,
     CNT_NONE,
     CNT_GT,
+    CORR_F,
+    CORR_R,
+    CORR_S,
 )

@@ -185,6 +185,68 @@ __device__ __forceinline__ bool lag_r(const PairDev &p, int x, int y, double cs,
     return true;
 }
 
+// RCalc::Valid + RCalc::CalcR (0_GEN/Correlation.cpp:1790-1845): legality
+// of lag (x, y) and, when want_r, its Pearson r clamped to (-1, 1) (0 outside).
+__device__ __forceinline__ bool lag_eval(const PairDev &p, int x, int y, double cs, bool want_r,
+                                         double &r)
+{
+    const int w1 = p.w[0], h1 = p.h[0], w2 = p.w[1], h2 = p.h[1];
+    int L2 = max(0, x), R2 = min(w2 - 1, x + w1 - 1);
+    int B2 = max(0, y), T2 = min(h2 - 1, y + h1 - 1);
+    R2 = max(R2, L2);
+    T2 = max(T2, B2);
+    const int L1 = L2 - x, R1 = R2 - x, B1 = B2 - y, T1 = T2 - y;
+    const int olw = R1 - L1 + 1, olh = T1 - B1 + 1;
+    bool ok = true;
+    if (p.rgn_kind != ALN_RGN_NONE && !rgn_ok(p, olw, olh))
+        ok = false;
+    if (p.cnt_kind == ALN_CNT_GT) {
+        const int c1 = sat_box_n(p.satN[0], p, 0, L1, R1, B1, T1);
+        const int c2 = sat_box_n(p.satN[1], p, 1, L2, R2, B2, T2);
+        if (!(c1 > p.cnt_n && c2 > p.cnt_n))
+            ok = false;
+    }
+    r = 0.0;
+    if (want_r) {
+        const double n = (double)(olw * olh);
+        double s1, q1, s2, q2;
+        if (p.sat_int & 1) {
+            s1 = (double)sat_box_i64((const long long *)p.satS[0], p, 0, L1, R1, B1, T1);
+            q1 = (double)sat_box_i64((const long long *)p.satQ[0], p, 0, L1, R1, B1, T1);
+        } else {
+            s1 = sat_box(p.satS[0], p, 0, L1, R1, B1, T1);
+            q1 = sat_box(p.satQ[0], p, 0, L1, R1, B1, T1);
+        }
+        if (p.sat_int & 2) {
+            s2 = (double)sat_box_i64((const long long *)p.satS[1], p, 1, L2, R2, B2, T2);
+            q2 = (double)sat_box_i64((const long long *)p.satQ[1], p, 1, L2, R2, B2, T2);
+        } else {
+            s2 = sat_box(p.satS[1], p, 1, L2, R2, B2, T2);
+            q2 = sat_box(p.satQ[1], p, 1, L2, R2, B2, T2);
+        }
+        const double num = n * cs - (s1 - n * p.mu[0]) * (s2 - n * p.mu[1]);
+        const double d1 = n * q1 - s1 * s1;
+        const double d2 = n * q2 - s2 * s2;
+        const double d = d1 * d2;
+        const double v = (d < n * n * 1.0E-9) ? 0.0 : num / sqrt(d);
+        r = (v > -1.0 && v < 1.0) ? v : 0.0;
+    }
+    return ok;
+}
+
+// CCorImg::MaskA, 0_GEN/Correlation.cpp:2011-2054, on R-image indices
+__device__ __forceinline__ bool oval_ok(const PairDev &p, int ix, int iy)
+{
+    if (!p.oval_on)
+        return true;
+    if (iy < p.ocy - p.ory || iy > p.ocy + p.ory)
+        return false;
+    if (ix < p.ocx - p.orx || ix > p.ocx + p.orx)
+        return false;
+    const int x = ix - p.ocx, y = iy - p.ocy;
+    return !((double)(x * x) + p.oasq * y * y > p.orx2);
+}
+
 __device__ __forceinline__ int isqrt_ll(long long v)
 {
     if (v < 0)
@@ -271,7 +333,10 @@ __global__ void k_mean(PairDev *pairs)
     }
     if (threadIdx.x == 0) {
         const double mean = part[0] / ((double)p.w[i] * p.h[i]);
-        p.mu[i] = (p.dt[i] == ALN_U8 || p.dt[i] == ALN_U16) ? floor(mean + 0.5) : mean;
+        double mu = (p.dt[i] == ALN_U8 || p.dt[i] == ALN_U16) ? floor(mean + 0.5) : mean;
+        if (p.dt[i] == ALN_F32)
+            mu = (double)(float)mu;   // exactly representable in the FP32 row pass
+        p.mu[i] = p.no_shift ? 0.0 : mu;
     }
 }
 
@@ -1130,6 +1195,13 @@ static int ensure_pairs(aln_ctx *ctx, size_t n)
 
 static inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// CorrImagesF/R/S parameters of a job (0_GEN/Correlation.h:159-220).
+struct ImgSpec {
+    int kind;   // 1 R, 2 S
+    double mincor;
+    int ox, oy, rx, ry;
+};
+
 // Host-side plan of one pair: sizes, window, needed SAT rows, workspace.
 struct PairPlan {
     PairDev d;
@@ -1185,8 +1257,11 @@ static void need_rows(const PairDev &d, int img, int lo[2], int hi[2])
     }
 }
 
-static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_transpose = false)
+static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_transpose = false,
+                     const ImgSpec *spec = nullptr)
 {
+    if (spec)
+        allow_transpose = false;   // the R image keeps the caller's orientation
     PairDev &d = pl.d;
     memset(&d, 0, sizeof d);
     const aln_image *im[2] = {&P.a, &P.b};
@@ -1252,6 +1327,35 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
         return set_err(ctx, ALN_ERR_ARG, "legality table missing");
     if (d.rgn_kind < 0 || d.rgn_kind > ALN_RGN_TABLE)
         return set_err(ctx, ALN_ERR_ARG, "bad rgn_kind %d", d.rgn_kind);
+    if (spec) {
+        // CCorImg::SetDims "too small" rule, 0_GEN/Correlation.cpp:1991-2000
+        const int mindelta = 11 / 2 + 1;
+        if (d.w[0] - 1 < mindelta || d.w[1] < mindelta || d.h[0] - 1 < mindelta ||
+            d.h[1] < mindelta) {
+            d.status = ALN_NO_PEAK;
+            pl.ws_bytes = 0;
+            pl.in_bytes[0] = pl.in_bytes[1] = 0;
+            return ALN_OK;
+        }
+        d.mode = spec->kind == 2 ? JOB_IMAGES_S : JOB_IMAGES_R;
+        d.want_s = spec->kind == 2;
+        d.want_r = spec->kind == 1 || (spec->kind == 2 && spec->mincor > 0.0);
+        d.no_shift = d.want_s;
+        d.mincor = spec->mincor;
+        d.cx = d.w[0] - 1;
+        d.cy = d.h[0] - 1;
+        d.wR = d.w[0] + d.w[1] - 1;
+        d.hR = d.h[0] + d.h[1] - 1;
+        if (spec->rx > 0 && spec->ry > 0) {
+            d.oval_on = 1;
+            d.ocx = spec->ox + d.x0[0] - d.x0[1] + d.cx;
+            d.ocy = spec->oy + d.y0[0] - d.y0[1] + d.cy;
+            d.orx = spec->rx;
+            d.ory = spec->ry;
+            d.orx2 = (double)(spec->rx * spec->rx);
+            d.oasq = d.orx2 / ((double)spec->ry * spec->ry);
+        }
+    }
     if (d.xlo > d.xhi || d.ylo > d.yhi) {
         d.status = ALN_NO_PEAK;   // empty search region
         pl.ws_bytes = 0;
@@ -1287,6 +1391,10 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
     b += al256((size_t)Wy * sizeof(RowBest));
     if (d.rgn_kind == ALN_RGN_TABLE)
         b += al256((size_t)d.table_w * d.table_h);
+    if (d.want_r && d.want_s)
+        b += al256((size_t)L1 * Wy * sizeof(float2));
+    if (d.mode == JOB_IMAGES_S && d.want_r)
+        b += al256((size_t)Wx * Wy * sizeof(double));
     pl.ws_bytes = b;
     return ALN_OK;
 }
@@ -1360,6 +1468,14 @@ static size_t carve(PairPlan &pl, char *base, const aln_pair &P, char **stage = 
         d.table = (const unsigned char *)p;
         p += al256((size_t)d.table_w * d.table_h);
     }
+    if (d.want_r && d.want_s) {
+        d.Q2 = (float2 *)p;
+        p += al256((size_t)L1 * Wy * sizeof(float2));
+    }
+    if (d.mode == JOB_IMAGES_S && d.want_r) {
+        d.rr2 = (double *)p;
+        p += al256((size_t)Wx * Wy * sizeof(double));
+    }
     (void)P;
     return (size_t)(p - base);
 }
@@ -1400,12 +1516,24 @@ static void launch_lagrow2(aln_ctx *ctx, int n, int maxWy)
            ctx->dpairs, ctx->tw);
 }
 
-#define ALN_CASES_L(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
+template <int LL>
+static void launch_lagimg2(aln_ctx *ctx, int n, int maxWy, bool both)
+{
+    constexpr int T = RegFFT<LL, +1>::T;
+    const int thr = std::max(256, T), G = thr / T;
+    const size_t sm = (size_t)G * (padded(LL) + 2) * (both ? 2 : 1) * sizeof(float2);
+    cudaFuncSetAttribute(k2_lagimg<LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    LAUNCH(ctx, "k2_lagimg", k2_lagimg<LL>, dim3((maxWy + G - 1) / G, n), thr, sm, ctx->dpairs,
+           ctx->tw);
+}
+
+#define ALN_CASES_L(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
 #define ALN_CASES_NY(X) ALN_CASES_L(X) X(8192)
 
 // register-FFT pipeline for one chunk: rows (both images), fused columns,
 // lag rows.  L = Nx/2 in [16, 4096], Ny in [16, 8192].
-static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int maxWy)
+static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int maxWy,
+                               int mode = JOB_PATCHES, bool both = false)
 {
     switch (L) {
 #define X(v) case v: launch_rowfft2<v>(ctx, n, maxh); break;
@@ -1419,11 +1547,20 @@ static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int
 #undef X
     default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "column length %d", Ny);
     }
-    switch (L) {
+    if (mode == JOB_PATCHES) {
+        switch (L) {
 #define X(v) case v: launch_lagrow2<v>(ctx, n, maxWy); break;
-        ALN_CASES_L(X)
+            ALN_CASES_L(X)
 #undef X
-    default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
+        default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
+        }
+    } else {
+        switch (L) {
+#define X(v) case v: launch_lagimg2<v>(ctx, n, maxWy, both); break;
+            ALN_CASES_L(X)
+#undef X
+        default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
+        }
     }
     return ALN_OK;
 }
@@ -1528,9 +1665,13 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int par, char
            ctx->dpairs);
     LAUNCH(ctx, "k_mean", k_mean, dim3(2, n), 256, 0, ctx->dpairs);
     LAUNCH(ctx, "k2_sat2", k2_sat2, dim3(maxslots, 2, n), 256, 0, ctx->dpairs);
-    if (L >= 16 && L <= 4096 && Ny >= 16 && Ny <= 8192) {
-        if (int rc = launch_fft_pipeline(ctx, L, Ny, n, maxh, maxWy))
+    const int mode = hd[0].mode;
+    if (L >= 8 && L <= 4096 && Ny >= 8 && Ny <= 8192) {
+        if (int rc = launch_fft_pipeline(ctx, L, Ny, n, maxh, maxWy, mode,
+                                         hd[0].want_r && hd[0].want_s))
             return rc;
+    } else if (mode != JOB_PATCHES) {
+        return set_err(ctx, ALN_ERR_UNSUPPORTED, "CorrImages FFT size %d x %d", Nx, Ny);
     } else {
         {
             const int RB = rows_per_cta(L);
@@ -1552,8 +1693,11 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int par, char
                    ctx->dpairs, ctx->tw, RBL);
         }
     }
-    LAUNCH(ctx, "k_final", k_final, n, 256, 0, ctx->dpairs, ctx->dres, chunk[0]->frame_nx1,
-           chunk[0]->frame_ny1);
+    if (mode == JOB_PATCHES)
+        LAUNCH(ctx, "k_final", k_final, n, 256, 0, ctx->dpairs, ctx->dres, chunk[0]->frame_nx1,
+               chunk[0]->frame_ny1);
+    else
+        LAUNCH(ctx, "k_final_img", k_final_img, n, 256, 0, ctx->dpairs, ctx->dres);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(hres_out, ctx->dres, n * sizeof(ResultDev), cudaMemcpyDeviceToHost, st));
     ctx->d2h_bytes += n * sizeof(ResultDev);
@@ -1587,8 +1731,10 @@ static int ensure_hres(aln_ctx *ctx, size_t n)
     return ALN_OK;
 }
 
-extern "C" int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *pairs,
-                                      aln_result *out)
+// Runs CorrPatches (specs == NULL) or CorrImages jobs in chunks of equal FFT
+// size and job kind through the two-stage pipeline.
+static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const ImgSpec *specs,
+                      aln_result *out)
 {
     if (!ctx || npairs < 0 || (npairs && (!pairs || !out)))
         return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
@@ -1597,15 +1743,18 @@ extern "C" int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *
     for (int k = 0; k < npairs; ++k) {
         plans[k].src = &pairs[k];
         plans[k].index = k;
-        if (int rc = plan_pair(ctx, pairs[k], plans[k], true))
+        if (int rc = plan_pair(ctx, pairs[k], plans[k], specs == nullptr,
+                               specs ? &specs[k] : nullptr))
             return rc;
     }
-    // group by FFT size, keep submission order inside a group, split into
-    // chunks bounded by the workspace budget
-    std::map<std::tuple<int, int, int, int>, std::vector<PairPlan *>> groups;
+    // group by FFT size and job kind, keep submission order inside a group,
+    // split into chunks bounded by the workspace budget
+    std::map<std::tuple<int, int, int, int, int, int, int>, std::vector<PairPlan *>> groups;
     for (auto &pl : plans)
         if (pl.d.status == 0)
-            groups[std::make_tuple(pl.d.Nx, pl.d.Ny, pl.frame_nx1, pl.frame_ny1)].push_back(&pl);
+            groups[std::make_tuple(pl.d.Nx, pl.d.Ny, pl.frame_nx1, pl.frame_ny1, pl.d.mode,
+                                   pl.d.want_r, pl.d.want_s)]
+                .push_back(&pl);
     std::vector<std::vector<PairPlan *>> chunks;
     size_t max_stage = 0, max_work = 0, max_n = 1;
     for (auto &g : groups) {
@@ -1669,6 +1818,62 @@ extern "C" int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *
     for (int k = 0; k < npairs; ++k)
         fill_result(plans[k], &out[k]);
     return ALN_OK;
+}
+
+extern "C" int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *pairs,
+                                      aln_result *out)
+{
+    return batch_impl(ctx, npairs, pairs, nullptr, out);
+}
+
+extern "C" int aln_corr_images_batch(aln_ctx *ctx, int njobs, const aln_image_job *jobs,
+                                     aln_result *out)
+{
+    if (!ctx || njobs < 0 || (njobs && (!jobs || !out)))
+        return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
+    std::vector<aln_pair> pairs(njobs);
+    std::vector<ImgSpec> specs(njobs);
+    for (int k = 0; k < njobs; ++k) {
+        const aln_image_job &J = jobs[k];
+        if (J.kind != ALN_CORR_R && J.kind != ALN_CORR_S)
+            return set_err(ctx, ALN_ERR_UNSUPPORTED,
+                           "CorrImages kind %d: the F (isolated-peak) variant is not built yet",
+                           J.kind);
+        memset(&pairs[k], 0, sizeof(aln_pair));
+        pairs[k].a = J.a;
+        pairs[k].b = J.b;
+        pairs[k].radius = 1 << 20;   // the whole R image; MaskA's oval is separate
+        pairs[k].legal = J.legal;
+        specs[k].kind = J.kind == ALN_CORR_S ? 2 : 1;
+        specs[k].mincor = J.mincor;
+        specs[k].ox = J.ox;
+        specs[k].oy = J.oy;
+        specs[k].rx = J.rx;
+        specs[k].ry = J.ry;
+    }
+    return batch_impl(ctx, njobs, pairs.data(), specs.data(), out);
+}
+
+extern "C" int aln_corr_images(aln_ctx *ctx, int kind, const aln_image *a, const aln_image *b,
+                               const aln_legal *legal, double mincor, double nbmaxht, int ox,
+                               int oy, int rx, int ry, aln_result *out)
+{
+    if (!ctx || !a || !b || !out)
+        return ctx ? set_err(ctx, ALN_ERR_ARG, "null argument") : ALN_ERR_ARG;
+    aln_image_job J;
+    memset(&J, 0, sizeof J);
+    J.a = *a;
+    J.b = *b;
+    J.kind = kind;
+    if (legal)
+        J.legal = *legal;
+    J.mincor = mincor;
+    J.nbmaxht = nbmaxht;
+    J.ox = ox;
+    J.oy = oy;
+    J.rx = rx;
+    J.ry = ry;
+    return aln_corr_images_batch(ctx, 1, &J, out);
 }
 
 extern "C" int aln_corr_patches(aln_ctx *ctx, const aln_image *a, const aln_image *b, int ox,

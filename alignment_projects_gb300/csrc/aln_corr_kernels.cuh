@@ -8,8 +8,12 @@
 // Best legal lag of one lag row (written by the lag kernel).
 struct RowBest {
     double r;        // best r in the row, -1e30 if no legal lag
-    long long key;   // storage index iy*Nx + ix of that lag (tie-break: smallest)
+    long long key;   // tie-break index of that lag (smallest wins)
+    double ssum, ssum2;   // CorrImagesS: sums of S and S^2 over the row
 };
+
+// job kinds
+enum { JOB_PATCHES = 0, JOB_IMAGES_R = 1, JOB_IMAGES_S = 2 };
 
 // Compact per-pair result copied back to the host.
 struct ResultDev {
@@ -58,9 +62,19 @@ struct PairDev {
     double *segS[2], *segQ[2];   // per column-walk segment: exclusive column offsets
     int *segN[2];
     double *colsum[2];           // per-column totals (mean shift)
-    double *rr;                  // r over the lag window [j][x - xlo]
+    double *rr;                  // r over the lag window [j][x - xlo] (the key image)
     RowBest *rb;                 // per lag row
     double mu[2];                // mean shift applied before the FFT
+    // CorrImagesR/S (0_GEN/Correlation.cpp:1851-3290)
+    int mode;                    // JOB_*
+    int want_r, want_s;          // which inverse transforms the job needs
+    int no_shift;                // S is not shift-invariant: mu = 0
+    double mincor;               // candidates need R > mincor when > 0
+    int oval_on, ocx, ocy, orx, ory;   // MaskA oval in R-image indices
+    double oasq, orx2;
+    int cx, cy, wR, hR;          // R image: lag (x, y) at index (x + cx) + wR (y + cy)
+    float2 *Q2;                  // whitened inverse rows when both R and S are needed
+    double *rr2;                 // R image when the key is S and mincor > 0
     // result
     double r, dx, dy;
     int status, px, py;

@@ -494,18 +494,52 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
 #pragma unroll
     for (int r = 0; r < R; ++r)
         va[r] = cmulc(sb[r * T + t], va[r]);   // X2 * conj(X1)
-    FI::run(va, sm, t, tw);
-    if (!live)
-        return;
+    // CorrPatches / CorrImagesR need the plain inverse; CorrImagesS the inverse
+    // of the whitened product P / sqrt(|P|) (0_GEN/Correlation.cpp:2311-2317)
+    const bool want_r = p.mode == JOB_PATCHES || p.want_r;
+    const bool want_s = p.want_s != 0;
+    if (want_r && want_s) {
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            sb[r * T + t] = va[r];
+    }
     const int Wy = p.yhi - p.ylo + 1;
     const int nnegy = p.h[0] - 1;
-    float2 *Q = p.Q + (long long)kx * Wy;
+    if (want_r) {
+        FI::run(va, sm, t, tw);
+        if (live) {
+            float2 *Q = p.Q + (long long)kx * Wy;
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const int ys = t + r * T;
-        const int y = ys >= NY - nnegy ? ys - NY : ys;
-        if (y >= p.ylo && y <= p.yhi)
-            Q[y - p.ylo] = va[r];
+            for (int r = 0; r < R; ++r) {
+                const int ys = t + r * T;
+                const int y = ys >= NY - nnegy ? ys - NY : ys;
+                if (y >= p.ylo && y <= p.yhi)
+                    Q[y - p.ylo] = va[r];
+            }
+        }
+    }
+    if (want_s) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            float2 v = want_r ? sb[r * T + t] : va[r];
+            const float m = hypotf(v.x, v.y);
+            if (m > 1e-10f) {
+                const float q = 1.0f / sqrtf(m);
+                v = make_float2(v.x * q, v.y * q);
+            }
+            va[r] = v;
+        }
+        FI::run(va, sm, t, tw);
+        if (live) {
+            float2 *Q = (want_r ? p.Q2 : p.Q) + (long long)kx * Wy;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int ys = t + r * T;
+                const int y = ys >= NY - nnegy ? ys - NY : ys;
+                if (y >= p.ylo && y <= p.yhi)
+                    Q[y - p.ylo] = va[r];
+            }
+        }
     }
 }
 
@@ -614,4 +648,239 @@ __global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
         p.rb[j].r = br;
         p.rb[j].key = bk;
     }
+}
+
+// ---------------------------------------------------------------------------
+// CorrImagesR/S lag images (CCorImg::MakeRandA / MakeSandRandA + OrderF +
+// SimpleMax, 0_GEN/Correlation.cpp:2060-2380,2509-2569,2939-2948)
+// ---------------------------------------------------------------------------
+
+// Per lag row: inverse real FFT of the S rows (whitened product) and/or the
+// R rows (plain product), S and R per lag, A = legality & oval (& R > mincor),
+// the row's best candidate (key S or R; ties -> smallest R-image index) and
+// the row's S sums.
+template <int L>
+__global__ void k2_lagimg(PairDev *pairs, const float2 *__restrict__ tw)
+{
+    using F = RegFFT<L, +1>;
+    constexpr int R = F::R, T = F::T;
+    constexpr int PITCH = padded(L) + 2;
+    extern __shared__ float2 smem[];
+    __shared__ double red_r[32], red_s[32], red_s2[32];
+    __shared__ long long red_k[32];
+    PairDev &p = pairs[blockIdx.y];
+    if (p.status != 0)
+        return;
+    const int Wy = p.yhi - p.ylo + 1, Wx = p.xhi - p.xlo + 1;
+    const int G = blockDim.x / T;
+    const int team = threadIdx.x / T, t = threadIdx.x - team * T;
+    const int j0 = blockIdx.x * G;
+    if (j0 >= Wy)
+        return;
+    const int j = j0 + team;
+    const bool live = j < Wy;
+    const int jc = live ? j : Wy - 1;
+    const bool want_r = p.want_r != 0, want_s = p.want_s != 0;
+    const bool both = want_r && want_s;
+    float2 *sm = smem + team * PITCH * (both ? 2 : 1);
+    const int Nx = p.Nx, Ny = p.Ny;
+    const float *CS = nullptr, *CR = nullptr;
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool doS = pass == 0;
+        if ((doS && !want_s) || (!doS && !want_r))
+            continue;
+        const float2 *Qs = doS ? (both ? p.Q2 : p.Q) : p.Q;
+        float2 *reg = sm + ((both && !doS) ? PITCH : 0);
+        __syncthreads();
+        for (int k = t; k <= L; k += T)
+            reg[padi(k)] = Qs[(long long)k * Wy + jc];
+        __syncthreads();
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int k = t + r * T;
+            float2 a = reg[padi(k)];
+            float2 b = cconj(reg[padi(L - k)]);
+            if (k == 0) {
+                a.y = 0.f;
+                b.y = 0.f;
+            }
+            const float2 e = cadd(a, b);
+            const float2 dd = csub(a, b);
+            float2 wv = __ldg(&tw[2 * L + k]);
+            wv.y = -wv.y;
+            const float2 o = cmul(dd, wv);
+            v[r] = make_float2(e.x - o.y, e.y + o.x);
+        }
+        F::run(v, reg, t, tw);
+        __syncthreads();
+        float *C = (float *)reg;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int n = t + r * T;
+            C[2 * n] = v[r].x;
+            C[2 * n + 1] = v[r].y;
+        }
+        if (doS)
+            CS = C;
+        else
+            CR = C;
+    }
+    __syncthreads();
+    const double inv = 1.0 / ((double)Nx * (double)Ny);
+    double br = -1.0e30, ss = 0.0, ss2 = 0.0;
+    long long bk = 0x7fffffffffffffffLL;
+    if (live) {
+        const int y = p.ylo + j, iy = y + p.cy;
+        const bool keyS = p.mode == JOB_IMAGES_S;
+        for (int x = p.xlo + t; x <= p.xhi; x += T) {
+            const int xs = x < 0 ? x + Nx : x;
+            double S = 0.0, rv = 0.0;
+            if (want_s) {
+                S = (double)CS[xs] * inv;
+                ss += S;
+                ss2 += S * S;
+            }
+            const bool legal = lag_eval(p, x, y, want_r ? (double)CR[xs] * inv : 0.0, want_r, rv);
+            const double key = keyS ? S : rv;
+            const long long o = (long long)j * Wx + (x - p.xlo);
+            p.rr[o] = key;
+            if (keyS && want_r)
+                p.rr2[o] = rv;
+            const int ix = x + p.cx;
+            if (legal && oval_ok(p, ix, iy) && (p.mincor <= 0.0 || rv > p.mincor))
+                best_merge(br, bk, key, (long long)iy * p.wR + ix);
+        }
+    }
+    const int lane = threadIdx.x & 31;
+    for (int o = 16; o > 0; o >>= 1) {
+        const double r2 = __shfl_down_sync(0xffffffff, br, o);
+        const long long k2 = __shfl_down_sync(0xffffffff, bk, o);
+        const double a2 = __shfl_down_sync(0xffffffff, ss, o);
+        const double b2 = __shfl_down_sync(0xffffffff, ss2, o);
+        if (lane + o < 32 && (lane + o) / T == lane / T) {
+            best_merge(br, bk, r2, k2);
+            ss += a2;
+            ss2 += b2;
+        }
+    }
+    if (T <= 32) {
+        if (live && t == 0) {
+            p.rb[j].r = br;
+            p.rb[j].key = bk;
+            p.rb[j].ssum = ss;
+            p.rb[j].ssum2 = ss2;
+        }
+        return;
+    }
+    const int wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        red_r[wid] = br;
+        red_k[wid] = bk;
+        red_s[wid] = ss;
+        red_s2[wid] = ss2;
+    }
+    __syncthreads();
+    if (live && t == 0) {
+        const int w0 = team * (T / 32);
+        for (int q = 1; q < T / 32; ++q) {
+            best_merge(br, bk, red_r[w0 + q], red_k[w0 + q]);
+            ss += red_s[w0 + q];
+            ss2 += red_s2[w0 + q];
+        }
+        p.rb[j].r = br;
+        p.rb[j].key = bk;
+        p.rb[j].ssum = ss;
+        p.rb[j].ssum2 = ss2;
+    }
+}
+
+// grid (npairs), block 256: argmax over rows, ParabPeak on the key image
+// (neighbours must be > 0, 0_GEN/Correlation.cpp:2975-3010), ReturnR's
+// offsets (:3016-3043); CorrImagesS returns 10 (S - mean) / (sd sqrt(nR))
+// with the sample sd over the whole S image (:3285-3289).
+__global__ void k_final_img(PairDev *pairs, ResultDev *res)
+{
+    __shared__ double red_r[32], red_s[32], red_s2[32];
+    __shared__ long long red_k[32];
+    PairDev &p = pairs[blockIdx.x];
+    if (p.status != 0)
+        return;
+    const int Wy = p.yhi - p.ylo + 1;
+    double br = -1.0e30, ss = 0.0, ss2 = 0.0;
+    long long bk = 0x7fffffffffffffffLL;
+    for (int j = threadIdx.x; j < Wy; j += blockDim.x) {
+        best_merge(br, bk, p.rb[j].r, p.rb[j].key);
+        ss += p.rb[j].ssum;
+        ss2 += p.rb[j].ssum2;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double r2 = __shfl_down_sync(0xffffffff, br, o);
+        const long long k2 = __shfl_down_sync(0xffffffff, bk, o);
+        const double a2 = __shfl_down_sync(0xffffffff, ss, o);
+        const double b2 = __shfl_down_sync(0xffffffff, ss2, o);
+        best_merge(br, bk, r2, k2);
+        ss += a2;
+        ss2 += b2;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        red_r[wid] = br;
+        red_k[wid] = bk;
+        red_s[wid] = ss;
+        red_s2[wid] = ss2;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0)
+        return;
+    for (int q = 1; q < (int)(blockDim.x >> 5); ++q) {
+        best_merge(br, bk, red_r[q], red_k[q]);
+        ss += red_s[q];
+        ss2 += red_s2[q];
+    }
+    ResultDev &o = res[blockIdx.x];
+    if (br < -2.0) {
+        p.status = ALN_NO_PEAK;
+        o.r = o.dx = o.dy = 0.0;
+        o.status = ALN_NO_PEAK;
+        o.px = o.py = 0;
+        return;
+    }
+    const int wR = p.wR, hR = p.hR;
+    const int ry = (int)(bk / wR), rx = (int)(bk - (long long)ry * wR);
+    const double *I = p.rr;   // the key image: the window is the whole R image
+    double xpk = rx, ypk = ry;
+    const double z1 = I[rx + (long long)wR * ry];
+    double z0, z2;
+    if (rx - 1 >= 0 && rx + 1 < wR && (z0 = I[rx - 1 + (long long)wR * ry]) > 0.0 &&
+        (z2 = I[rx + 1 + (long long)wR * ry]) > 0.0) {
+        z0 = (z0 - z2) / (2 * (z0 + z2 - z1 - z1));
+        if (fabs(z0) <= 8)
+            xpk += z0;
+    }
+    if (ry - 1 >= 0 && ry + 1 < hR && (z0 = I[rx + (long long)wR * (ry - 1)]) > 0.0 &&
+        (z2 = I[rx + (long long)wR * (ry + 1)]) > 0.0) {
+        z0 = (z0 - z2) / (2 * (z0 + z2 - z1 - z1));
+        if (fabs(z0) <= 8)
+            ypk += z0;
+    }
+    double r = z1;
+    if (p.mode == JOB_IMAGES_S) {
+        const double n = (double)wR * hR;
+        const double mn = ss / n;
+        const double sd = sqrt(fmax(ss2 - n * mn * mn, 0.0) / (n - 1.0));
+        r = 10.0 * (z1 - mn) / (sd * sqrt(n));
+    }
+    p.r = r;
+    p.dx = xpk + (p.x0[1] - p.x0[0]) - p.cx;
+    p.dy = ypk + (p.y0[1] - p.y0[0]) - p.cy;
+    p.px = rx - p.cx;
+    p.py = ry - p.cy;
+    p.status = ALN_OK;
+    o.r = p.r;
+    o.dx = p.dx;
+    o.dy = p.dy;
+    o.status = ALN_OK;
+    o.px = p.px;
+    o.py = p.py;
 }

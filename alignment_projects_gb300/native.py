@@ -47,6 +47,15 @@ class AlnResult(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class AlnImageJob(C.Structure):
+    _fields_ = [("a", AlnImage), ("b", AlnImage), ("kind", C.c_int), ("legal", AlnLegal),
+                ("mincor", C.c_double), ("nbmaxht", C.c_double), ("ox", C.c_int),
+                ("oy", C.c_int), ("rx", C.c_int), ("ry", C.c_int)]
+
+
+CORR_F, CORR_R, CORR_S = 0, 1, 2
+
+
 class AlnPair(C.Structure):
     _fields_ = [("a", AlnImage), ("b", AlnImage), ("ox", C.c_int), ("oy", C.c_int),
                 ("radius", C.c_int), ("legal", AlnLegal)]
@@ -70,6 +79,12 @@ def lib():
                                        C.POINTER(AlnResult)]
         L.aln_corr_patches_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnPair),
                                              C.POINTER(AlnResult)]
+        L.aln_corr_images.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnImage),
+                                      C.POINTER(AlnImage), C.POINTER(AlnLegal), C.c_double,
+                                      C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      C.POINTER(AlnResult)]
+        L.aln_corr_images_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnImageJob),
+                                            C.POINTER(AlnResult)]
         L.aln_fft_2d.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         L.aln_ift_2d.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         L.aln_ctx_set_profiling.argtypes = [C.c_void_p, C.c_int]
@@ -203,6 +218,39 @@ class Context:
                                              C.byref(lg) if lg is not None else None,
                                              C.byref(res)))
         return res.as_dict()
+
+    # -- CorrImagesR / CorrImagesS ------------------------------------------
+    def corr_images(self, kind, a, b, lg=None, mincor=0.0, nbmaxht=0.75, ox=0, oy=0, rx=-1,
+                    ry=-1, a_origin=(0, 0), b_origin=(0, 0)) -> dict:
+        ia = image(a, *a_origin)
+        ib = image(b, *b_origin)
+        res = AlnResult()
+        self._check(self._L.aln_corr_images(self.h, kind, C.byref(ia), C.byref(ib),
+                                            C.byref(lg) if lg is not None else None,
+                                            mincor, nbmaxht, ox, oy, rx, ry, C.byref(res)))
+        return res.as_dict()
+
+    def corr_images_batch(self, jobs) -> list:
+        """jobs: dicts with kind, a, b, [legal, mincor, nbmaxht, ox, oy, rx, ry,
+        a_origin, b_origin]."""
+        jobs = list(jobs)
+        arr = (AlnImageJob * len(jobs))()
+        keep = []
+        for k, j in enumerate(jobs):
+            ia = image(j["a"], *j.get("a_origin", (0, 0)))
+            ib = image(j["b"], *j.get("b_origin", (0, 0)))
+            keep += [ia, ib]
+            arr[k].a, arr[k].b, arr[k].kind = ia, ib, j["kind"]
+            if j.get("legal") is not None:
+                keep.append(j["legal"])
+                arr[k].legal = j["legal"]
+            arr[k].mincor = j.get("mincor", 0.0)
+            arr[k].nbmaxht = j.get("nbmaxht", 0.75)
+            arr[k].ox, arr[k].oy = j.get("ox", 0), j.get("oy", 0)
+            arr[k].rx, arr[k].ry = j.get("rx", -1), j.get("ry", -1)
+        out = (AlnResult * len(jobs))()
+        self._check(self._L.aln_corr_images_batch(self.h, len(jobs), arr, out))
+        return [o.as_dict() for o in out]
 
     def corr_patches_batch(self, pairs) -> list:
         """pairs: iterable of dicts with a, b, [ox, oy, radius, legal, a_origin, b_origin]."""

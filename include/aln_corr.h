@@ -181,6 +181,34 @@ typedef struct aln_pair {
 int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *pairs,
                            aln_result *out);
 
+/* ---- CorrImagesF/R/S: 0_GEN/Correlation.h:159-220 ------------------ */
+
+enum { ALN_CORR_F = 0, ALN_CORR_R = 1, ALN_CORR_S = 2 };
+
+/* One CorrImages call: the R (and S) image over every lag, A = legality &
+ * the oval MaskA (Rx, Ry > 0: semi-axes around (Ox, Oy), as
+ * 0_GEN/Correlation.cpp:2011-2054), candidates A (and R > mincor when
+ * mincor > 0), peak by maximal R (kind R) or maximal S, the FFT-whitened
+ * correlation (kind S), ParabPeak refinement.  out->r is R at the peak
+ * (kind R) or 10 (S - mean(S)) / (sd(S) sqrt(wR hR)) (kind S).  Images
+ * smaller than the reference's SetDims limit give ALN_NO_PEAK.  nbmaxht is
+ * used by kind F only. */
+typedef struct aln_image_job {
+    aln_image a, b;
+    int kind;           /* ALN_CORR_R or ALN_CORR_S (ALN_CORR_F: not built yet) */
+    aln_legal legal;
+    double mincor, nbmaxht;
+    int ox, oy, rx, ry;
+} aln_image_job;
+
+/* CorrImagesR / CorrImagesS, 0_GEN/Correlation.cpp:3144-3199, 3222-3290 */
+int aln_corr_images(aln_ctx *ctx, int kind, const aln_image *a, const aln_image *b,
+                    const aln_legal *legal, double mincor, double nbmaxht, int ox, int oy,
+                    int rx, int ry, aln_result *out);
+/* Many CorrImages calls in one submission (any mix of sizes). */
+int aln_corr_images_batch(aln_ctx *ctx, int njobs, const aln_image_job *jobs,
+                          aln_result *out);
+
 /* ---- allocation-free CorrPatches: no counterpart in the reference ---- */
 
 /* Size of the device scratch array behind aln_corr_patches_noalloc. */
