@@ -29,4 +29,10 @@ from .native import (  # noqa: F401
     CORR_F,
     CORR_R,
     CORR_S,
+    THM_DENOVO,
+    THM_RFROMANGLE,
+    THM_PRIOR,
+    THM_SCAN_HUNT,
+    THM_SCAN_MAXR,
+    thumbs_from_points,
 )

@@ -12,7 +12,8 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libaln_corr.so")
 
 SOURCES = ["aln_corr.cu"]
-HEADERS = ["aln_fft.cuh", "aln_corr_kernels.cuh"]
+HEADERS = ["aln_fft.cuh", "aln_fft_reg.cuh", "aln_corr_kernels.cuh", "aln_pipeline.cuh",
+           "aln_sweep.cuh"]
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-O3", "-lineinfo", "-std=c++17",

@@ -2241,3 +2241,5 @@ extern "C" int aln_corr_patches_noalloc(const aln_image *a, const aln_image *b, 
     out->peak_y = hr.py;
     return ALN_OK;
 }
+
+#include "aln_sweep.cuh"

@@ -1,0 +1,777 @@
+// aln_sweep.cuh -- the CThmScan rotation sweep (0_GEN/CThmScan.cpp) on the
+// GPU, included at the end of aln_corr.cu.
+//
+// Every correlator call of the sweep (RFromAngle -> CorrImagesS,
+// CThmScan.cpp:329-366) becomes a job: the thumbnail-A grid points are
+// rotated by C.T = R(deg*PI/180) * (Tdfm * Tptwk) (FP64, the reference's
+// operation order, PI truncated as GenDefs.h:16), splatted bilinearly into
+// the bounding box of the rotated points (k_splat), and correlated with
+// thumbnail B by the CorrImagesS pipeline.  A host controller runs the
+// sweep logic for many pairs at once: each stage (coarse scan, fine scan,
+// one bracket step of PeakHunt, one Pretweaks round) is one GPU batch over
+// all pairs still in that stage.
+#pragma once
+
+#define ALN_PI_REF 3.14159265358   // GenDefs.h:16, truncated as the reference uses it
+
+// One rotate-and-splat job: rotated A points -> FP32 raster [h1][w1].
+struct SplatJob {
+    double t0, t1, t3, t4;   // linear part of C.T
+    int L, B, w1, h1;        // bounding box of the rotated points
+    float *out;
+    const double *a;         // A values on the grid, a[x + stride*y]
+    const unsigned char *mask;   // presence (NULL: all present)
+    int aw, ah, astride, ax0, ay0;
+};
+
+// grid (ceil(maxw/32), ceil(maxh/32), njobs), block 256.  Each CTA owns a
+// 32 x 32 tile of the output and gathers every grid point whose bilinear
+// footprint reaches it (inverse-rotated tile, +1 px), accumulating the four
+// weights (DistributePixel, 0_GEN/Maths.h:236-276) in shared memory.  The
+// accumulation is in 2^-32 fixed point with integer atomics, so the raster
+// does not depend on the order of the additions: the same transform always
+// gives the same raster, bit for bit, as the sweep's tie rules require.
+__device__ __forceinline__ void splat_add(unsigned long long *cell, float c)
+{
+    atomicAdd(cell, (unsigned long long)llrintf(c * 4294967296.0f));
+}
+
+__global__ void k_splat(const SplatJob *jobs)
+{
+    __shared__ unsigned long long tile[32][33];
+    const SplatJob &J = jobs[blockIdx.z];
+    const int tx0 = blockIdx.x * 32, ty0 = blockIdx.y * 32;
+    if (tx0 >= J.w1 || ty0 >= J.h1)
+        return;
+    for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x)
+        tile[e >> 5][e & 31] = 0ull;
+    __syncthreads();
+    // source range: inverse map of the rotated-frame rectangle covering the
+    // tile's footprint [tx0-1, tx0+32) x [ty0-1, ty0+32) (+ the box origin)
+    const double det = J.t0 * J.t4 - J.t1 * J.t3;
+    const double X0 = tx0 - 1 + J.L, X1 = tx0 + 32 + J.L;
+    const double Y0 = ty0 - 1 + J.B, Y1 = ty0 + 32 + J.B;
+    double umin = 1e300, umax = -1e300, vmin = 1e300, vmax = -1e300;
+    for (int c = 0; c < 4; ++c) {
+        const double X = (c & 1) ? X1 : X0, Y = (c & 2) ? Y1 : Y0;
+        const double u = (J.t4 * X - J.t1 * Y) / det;
+        const double v = (-J.t3 * X + J.t0 * Y) / det;
+        umin = fmin(umin, u);
+        umax = fmax(umax, u);
+        vmin = fmin(vmin, v);
+        vmax = fmax(vmax, v);
+    }
+    const int gx0 = max(0, (int)floor(umin) - 1 - J.ax0), gx1 = min(J.aw - 1, (int)ceil(umax) + 1 - J.ax0);
+    const int gy0 = max(0, (int)floor(vmin) - 1 - J.ay0), gy1 = min(J.ah - 1, (int)ceil(vmax) + 1 - J.ay0);
+    if (gx0 <= gx1 && gy0 <= gy1) {
+        const int nx = gx1 - gx0 + 1;
+        const int total = nx * (gy1 - gy0 + 1);
+        for (int e = threadIdx.x; e < total; e += blockDim.x) {
+            const int gy = gy0 + e / nx, gx = gx0 + (e - (e / nx) * nx);
+            if (J.mask && !J.mask[gx + (long long)J.astride * gy])
+                continue;
+            const double px = (double)(gx + J.ax0), py = (double)(gy + J.ay0);
+            // Apply_R_Part (TAffine.cpp:407-423) then the box shift
+            const double xr = __dadd_rn(__dmul_rn(px, J.t0), __dmul_rn(py, J.t1));
+            const double yr = __dadd_rn(__dmul_rn(px, J.t3), __dmul_rn(py, J.t4));
+            const double x = __dsub_rn(xr, (double)J.L), y = __dsub_rn(yr, (double)J.B);
+            const int ix = (int)floor(x), iy = (int)floor(y);
+            const float alpha = (float)__dsub_rn(x, (double)ix);
+            const float beta = (float)__dsub_rn(y, (double)iy);
+            const float val = (float)J.a[gx + (long long)J.astride * gy];
+            const int lx = ix - tx0, ly = iy - ty0;
+            if (ix >= 0 && ix < J.w1) {
+                if (iy >= 0 && iy < J.h1 && lx >= 0 && lx < 32 && ly >= 0 && ly < 32)
+                    splat_add(&tile[ly][lx], (1.0f - alpha) * (1.0f - beta) * val);
+                if (iy + 1 < J.h1 && iy + 1 >= 0 && lx >= 0 && lx < 32 && ly + 1 >= 0 && ly + 1 < 32)
+                    splat_add(&tile[ly + 1][lx], (1.0f - alpha) * beta * val);
+            }
+            if (ix + 1 >= 0 && ix + 1 < J.w1) {
+                if (iy >= 0 && iy < J.h1 && lx + 1 >= 0 && lx + 1 < 32 && ly >= 0 && ly < 32)
+                    splat_add(&tile[ly][lx + 1], alpha * (1.0f - beta) * val);
+                if (iy + 1 < J.h1 && iy + 1 >= 0 && lx + 1 >= 0 && lx + 1 < 32 && ly + 1 >= 0 &&
+                    ly + 1 < 32)
+                    splat_add(&tile[ly + 1][lx + 1], alpha * beta * val);
+            }
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
+        const int ly = e >> 5, lx = e & 31;
+        const int x = tx0 + lx, y = ty0 + ly;
+        if (x < J.w1 && y < J.h1)
+            J.out[(long long)y * J.w1 + x] =
+                (float)((double)(long long)tile[ly][lx] * (1.0 / 4294967296.0));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host: affine algebra of TAffine (TAffine.cpp:60-135,220-232)
+// ---------------------------------------------------------------------------
+
+static void aff_one(double t[6])
+{
+    t[0] = 1; t[1] = 0; t[2] = 0;
+    t[3] = 0; t[4] = 1; t[5] = 0;
+}
+
+static void aff_mul(double r[6], const double L[6], const double R[6])
+{
+    double t[6];
+    t[0] = L[0] * R[0] + L[1] * R[3];
+    t[1] = L[0] * R[1] + L[1] * R[4];
+    t[2] = L[0] * R[2] + L[1] * R[5] + L[2];
+    t[3] = L[3] * R[0] + L[4] * R[3];
+    t[4] = L[3] * R[1] + L[4] * R[4];
+    t[5] = L[3] * R[2] + L[4] * R[5] + L[5];
+    memcpy(r, t, sizeof t);
+}
+
+// NUSelect: 0 Scl, 1 XScl, 2 YScl, 3 XSkw, 4 YSkw, 5 Rot
+static void aff_nu(double t[6], int sel, double a)
+{
+    aff_one(t);
+    switch (sel) {
+    case 1: t[0] = a; break;
+    case 2: t[4] = a; break;
+    case 3: t[1] = a; break;
+    case 4: t[3] = a; break;
+    case 5: {
+        const double c = cos(a), s = sin(a);
+        t[0] = c; t[1] = -s; t[3] = s; t[4] = c;
+        break;
+    }
+    default: t[0] = a; t[4] = a; break;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host: one pair's sweep state
+// ---------------------------------------------------------------------------
+
+struct ThmRec {
+    double A, X, Y, R;
+    double T[6];
+};
+
+struct ThmPair {
+    const aln_thumbs *in;
+    std::vector<std::pair<long long, long long>> hull;   // convex hull of A's points
+    double Tptwk[6];
+    const double *dev_a;            // device copies
+    const unsigned char *dev_mask;
+    aln_image dev_b;
+    // pretweak sweep records (TCD.vT)
+    std::vector<int> Tsel;
+    std::vector<double> Ta;
+    int ncalls;
+    int err;
+    ThmRec best;
+};
+
+struct Eval {
+    int pair;
+    double deg;
+    int iaux;    // pretweak record, -1: none
+    ThmRec *out;
+};
+
+static double cross3(const std::pair<long long, long long> &o, const std::pair<long long, long long> &a,
+                     const std::pair<long long, long long> &b)
+{
+    return (double)(a.first - o.first) * (double)(b.second - o.second) -
+           (double)(a.second - o.second) * (double)(b.first - o.first);
+}
+
+// Monotone-chain hull of the present A grid points (absolute coordinates).
+static void make_hull(ThmPair &tp)
+{
+    const aln_thumbs &T = *tp.in;
+    std::vector<std::pair<long long, long long>> pts;
+    for (int y = 0; y < T.a_h; ++y) {
+        int xl = -1, xr = -1;   // extreme present points of the row suffice
+        for (int x = 0; x < T.a_w; ++x)
+            if (!T.a_mask || T.a_mask[x + (size_t)T.a_stride * y]) {
+                if (xl < 0)
+                    xl = x;
+                xr = x;
+            }
+        if (xl >= 0) {
+            pts.push_back({xl + T.a_x0, y + T.a_y0});
+            if (xr != xl)
+                pts.push_back({xr + T.a_x0, y + T.a_y0});
+        }
+    }
+    std::sort(pts.begin(), pts.end());
+    pts.erase(std::unique(pts.begin(), pts.end()), pts.end());
+    if (pts.size() < 3) {
+        tp.hull = pts;
+        return;
+    }
+    std::vector<std::pair<long long, long long>> h(2 * pts.size());
+    size_t k = 0;
+    for (size_t i = 0; i < pts.size(); ++i) {
+        while (k >= 2 && cross3(h[k - 2], h[k - 1], pts[i]) <= 0)
+            --k;
+        h[k++] = pts[i];
+    }
+    for (size_t i = pts.size() - 1, t = k + 1; i > 0; --i) {
+        while (k >= t && cross3(h[k - 2], h[k - 1], pts[i - 1]) <= 0)
+            --k;
+        h[k++] = pts[i - 1];
+    }
+    h.resize(k - 1);
+    tp.hull = h;
+}
+
+struct SweepCtx {
+    aln_ctx *ctx;
+    std::vector<ThmPair> pairs;
+    aln_thm_params P;
+    char *arena = nullptr;   // splat rasters
+    size_t arena_cap = 0;
+    SplatJob *djobs = nullptr;
+    size_t djobs_cap = 0;
+};
+
+// RFromAngle (CThmScan.cpp:329-366) for a list of evaluations: one GPU batch.
+static int eval_batch(SweepCtx &S, std::vector<Eval> &ev)
+{
+    aln_ctx *ctx = S.ctx;
+    const size_t CH = 8192;
+    for (size_t c0 = 0; c0 < ev.size(); c0 += CH) {
+        const size_t n = std::min(CH, ev.size() - c0);
+        std::vector<SplatJob> jobs(n);
+        std::vector<aln_pair> pairs(n);
+        std::vector<ImgSpec> specs(n);
+        size_t bytes = 0;
+        for (size_t k = 0; k < n; ++k) {
+            Eval &E = ev[c0 + k];
+            ThmPair &tp = S.pairs[E.pair];
+            ThmRec &C = *E.out;
+            double R[6], T[6], D[6];
+            C.A = E.deg;
+            aff_nu(R, 5, E.deg * ALN_PI_REF / 180.0);
+            memcpy(T, tp.Tptwk, sizeof T);
+            if (E.iaux >= 0 && E.iaux < (int)tp.Tsel.size()) {
+                double M[6];
+                aff_nu(M, tp.Tsel[E.iaux], tp.Ta[E.iaux]);
+                aff_mul(T, M, tp.Tptwk);
+            }
+            aff_mul(D, S.P.tdfm, T);
+            aff_mul(C.T, R, D);
+            SplatJob &J = jobs[k];
+            J.t0 = C.T[0];
+            J.t1 = C.T[1];
+            J.t3 = C.T[3];
+            J.t4 = C.T[4];
+            double xlo = 1e300, xhi = -1e300, ylo = 1e300, yhi = -1e300;
+            for (auto &h : tp.hull) {
+                const double px = (double)h.first, py = (double)h.second;
+                const double x = px * J.t0 + py * J.t1, y = px * J.t3 + py * J.t4;
+                xlo = std::min(xlo, x);
+                xhi = std::max(xhi, x);
+                ylo = std::min(ylo, y);
+                yhi = std::max(yhi, y);
+            }
+            J.L = (int)floor(xlo);
+            J.B = (int)floor(ylo);
+            J.w1 = (int)ceil(xhi) - J.L + 1;
+            J.h1 = (int)ceil(yhi) - J.B + 1;
+            J.a = tp.dev_a;
+            J.mask = tp.dev_mask;
+            J.aw = tp.in->a_w;
+            J.ah = tp.in->a_h;
+            J.astride = tp.in->a_stride;
+            J.ax0 = tp.in->a_x0;
+            J.ay0 = tp.in->a_y0;
+            bytes += al256((size_t)J.w1 * J.h1 * sizeof(float));
+        }
+        if (bytes > S.arena_cap) {
+            CK(cudaStreamSynchronize(ctx->stream));
+            cudaFree(S.arena);
+            S.arena = nullptr;
+            S.arena_cap = 0;
+            cudaError_t e = cudaMalloc(&S.arena, bytes + bytes / 4);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return set_err(ctx, ALN_ERR_NOMEM, "sweep arena: %s", cudaGetErrorString(e));
+            }
+            S.arena_cap = bytes + bytes / 4;
+        }
+        if (n > S.djobs_cap) {
+            CK(cudaStreamSynchronize(ctx->stream));
+            cudaFree(S.djobs);
+            CK(cudaMalloc(&S.djobs, n * sizeof(SplatJob)));
+            S.djobs_cap = n;
+        }
+        char *p = S.arena;
+        int mw = 1, mh = 1;
+        for (size_t k = 0; k < n; ++k) {
+            SplatJob &J = jobs[k];
+            J.out = (float *)p;
+            p += al256((size_t)J.w1 * J.h1 * sizeof(float));
+            mw = std::max(mw, J.w1);
+            mh = std::max(mh, J.h1);
+            const Eval &E = ev[c0 + k];
+            const ThmPair &tp = S.pairs[E.pair];
+            aln_pair &Pp = pairs[k];
+            memset(&Pp, 0, sizeof Pp);
+            Pp.a.data = J.out;
+            Pp.a.dtype = ALN_F32;
+            Pp.a.w = J.w1;
+            Pp.a.h = J.h1;
+            Pp.a.stride = J.w1;
+            Pp.a.x0 = J.L;
+            Pp.a.y0 = J.B;
+            Pp.a.on_device = 1;
+            Pp.b = tp.dev_b;
+            Pp.radius = 1 << 20;
+            // BigEnough / EnoughPoints (CThmScan.cpp:28-42) with thm.reqArea
+            Pp.legal.rgn_kind = ALN_RGN_MIN;
+            Pp.legal.rgn_a = Pp.legal.rgn_b = tp.in->olap1d;
+            Pp.legal.rgn_area = tp.in->req_area;
+            Pp.legal.cnt_kind = ALN_CNT_GT;
+            Pp.legal.cnt_n = tp.in->req_area;
+            specs[k].kind = 2;
+            specs[k].mincor = 0.0;
+            specs[k].ox = S.P.ox;
+            specs[k].oy = S.P.oy;
+            specs[k].rx = S.P.rx;
+            specs[k].ry = S.P.ry;
+        }
+        CK(cudaMemcpyAsync(S.djobs, jobs.data(), n * sizeof(SplatJob), cudaMemcpyHostToDevice,
+                           ctx->stream));
+        LAUNCH(ctx, "k_splat", k_splat, dim3((mw + 31) / 32, (mh + 31) / 32, (unsigned)n), 256, 0,
+               S.djobs);
+        CK(cudaGetLastError());
+        std::vector<aln_result> res(n);
+        if (int rc = batch_impl(ctx, (int)n, pairs.data(), specs.data(), res.data()))
+            return rc;
+        for (size_t k = 0; k < n; ++k) {
+            ThmRec &C = *ev[c0 + k].out;
+            C.R = res[k].status == ALN_OK ? res[k].r : 0.0;
+            C.X = res[k].status == ALN_OK ? res[k].dx : 0.0;
+            C.Y = res[k].status == ALN_OK ? res[k].dy : 0.0;
+            S.pairs[ev[c0 + k].pair].ncalls++;
+        }
+    }
+    return ALN_OK;
+}
+
+static int round_ref(double x) { return x >= 0.0 ? (int)(x + 0.5) : (int)(x - 0.5); }
+
+// LineFit lincor (Maths.cpp:457-507)
+static double linefit_r(const double *x, const double *y, int n)
+{
+    double cnt = 0, sx = 0, sy = 0, sxx = 0, syy = 0, sxy = 0;
+    for (int i = 0; i < n; ++i) {
+        const double X = x[i], Y = y[i];
+        sx += X;
+        sy += Y;
+        sxx += X * X;
+        syy += Y * Y;
+        sxy += X * Y;
+        ++cnt;
+    }
+    const double r = cnt * sxy - sx * sy;
+    const double vx = cnt * sxx - sx * sx;
+    const double vy = cnt * syy - sy * sy;
+    return r / sqrt(vx * vy);
+}
+
+// AngleScanSel (CThmScan.cpp:627-641) over a set of pairs: ConstXY
+// (:514-621) or MaxR (:431-493).
+static int scan_sel(SweepCtx &S, const std::vector<int> &ids, const std::vector<double> &center,
+                    double hlfwid, double step, bool favorCenter, bool constxy)
+{
+    std::vector<std::vector<ThmRec>> vC(ids.size());
+    std::vector<Eval> ev;
+    for (size_t q = 0; q < ids.size(); ++q) {
+        std::vector<double> angs;
+        const double c = center[q];
+        if (constxy) {
+            for (double a = c - hlfwid; a <= c + hlfwid; a += step)
+                angs.push_back(a);
+        } else {
+            angs.push_back(c);
+            if (favorCenter) {
+                const double cwide = 2.0 * step, cstep = step / 3.0;
+                for (double a = c - cwide; a <= c + cwide; a += cstep)
+                    angs.push_back(a);
+                if (hlfwid >= 180) {
+                    const double opc = c + 180;
+                    for (double a = opc - cwide; a <= opc + cwide; a += cstep)
+                        angs.push_back(a);
+                }
+            }
+            for (double a = c - hlfwid; a <= c + hlfwid; a += step)
+                angs.push_back(a);
+        }
+        vC[q].resize(angs.size());
+        for (size_t k = 0; k < angs.size(); ++k)
+            ev.push_back(Eval{ids[q], angs[k], -1, &vC[q][k]});
+    }
+    if (int rc = eval_batch(S, ev))
+        return rc;
+    for (size_t q = 0; q < ids.size(); ++q) {
+        ThmRec &best = S.pairs[ids[q]].best;
+        std::vector<ThmRec> &C = vC[q];
+        const int nC = (int)C.size();
+        if (!constxy) {
+            best = C[0];
+            for (int ic = 1; ic < nC; ++ic)
+                if (C[ic].R > best.R)
+                    best = C[ic];
+            continue;
+        }
+        best.X = best.Y = best.A = best.R = 0.0;
+        std::vector<int> order(nC);
+        for (int i = 0; i < nC; ++i)
+            order[i] = i;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int a, int b) { return C[a].R > C[b].R; });
+        const double rthresh = 0.7;
+        const int m = 3, M = 2 * m + 1;
+        for (int i = 0; i < nC; ++i) {
+            const int ic = order[i];
+            if (ic < m || nC - 1 - ic < m)
+                continue;
+            double A[7], X[7], Y[7];
+            int n = 0;
+            for (int j = ic - m; j <= ic + m; ++j) {
+                A[n] = C[j].A;
+                X[n] = round_ref(C[j].X);
+                Y[n] = round_ref(C[j].Y);
+                ++n;
+            }
+            double lc = linefit_r(A, X, M);
+            if (std::isfinite(lc) && fabs(lc) < rthresh)
+                continue;
+            lc = linefit_r(A, Y, M);
+            if (std::isfinite(lc) && fabs(lc) < rthresh)
+                continue;
+            best = C[ic];
+            break;
+        }
+    }
+    return ALN_OK;
+}
+
+// PeakHunt (CThmScan.cpp:676-728): bracket bisection, all pairs in lockstep
+// rounds (each pair stops on its own when its bracket is below 1e-4).
+static int peak_hunt(SweepCtx &S, const std::vector<int> &ids, double hlfwid)
+{
+    const size_t n = ids.size();
+    std::vector<ThmRec> B0(n), C(n);
+    std::vector<double> L(n), R(n), M(n), a(n);
+    std::vector<char> on(n, 1);
+    std::vector<Eval> ev;
+    for (size_t q = 0; q < n; ++q) {
+        ThmRec &best = S.pairs[ids[q]].best;
+        B0[q] = best;
+        L[q] = best.A - hlfwid;
+        R[q] = best.A + hlfwid;
+        M[q] = (L[q] + R[q]) / 2.0;
+        ev.push_back(Eval{ids[q], M[q], -1, &best});
+    }
+    if (int rc = eval_batch(S, ev))
+        return rc;
+    for (;;) {
+        ev.clear();
+        for (size_t q = 0; q < n; ++q) {
+            on[q] = R[q] - L[q] > 0.0001;
+            if (on[q]) {
+                a[q] = (L[q] + M[q]) / 2.0;
+                ev.push_back(Eval{ids[q], a[q], -1, &C[q]});
+            }
+        }
+        if (ev.empty())
+            break;
+        if (int rc = eval_batch(S, ev))
+            return rc;
+        ev.clear();
+        for (size_t q = 0; q < n; ++q) {
+            if (!on[q])
+                continue;
+            ThmRec &best = S.pairs[ids[q]].best;
+            if (C[q].R >= best.R) {
+                R[q] = M[q];
+                best = C[q];
+                M[q] = a[q];
+            } else
+                L[q] = a[q];
+            a[q] = (M[q] + R[q]) / 2.0;
+            ev.push_back(Eval{ids[q], a[q], -1, &C[q]});
+        }
+        if (int rc = eval_batch(S, ev))
+            return rc;
+        for (size_t q = 0; q < n; ++q) {
+            if (!on[q])
+                continue;
+            ThmRec &best = S.pairs[ids[q]].best;
+            if (C[q].R >= best.R) {
+                L[q] = M[q];
+                best = C[q];
+                M[q] = a[q];
+            } else
+                R[q] = a[q];
+        }
+    }
+    for (size_t q = 0; q < n; ++q)
+        if (B0[q].R > S.pairs[ids[q]].best.R)
+            S.pairs[ids[q]].best = B0[q];
+    return ALN_OK;
+}
+
+// Pretweaks (CThmScan.cpp:205-323) for one pair; returns whether Tptwk changed.
+static int pretweaks(SweepCtx &S, int id, double bestR, double deg, bool *changed)
+{
+    ThmPair &tp = S.pairs[id];
+    int vused[5] = {0, 0, 0, 0, 0};
+    const double astep = 0.02;
+    const int nstep = 5;
+    *changed = false;
+    for (int itype = 0; itype < 5; ++itype) {
+        tp.Tsel.clear();
+        tp.Ta.clear();
+        for (int sel = 0; sel < 5; ++sel) {
+            if (vused[sel])
+                continue;
+            const double abase = (sel >= 0 && sel <= 2) ? 1.0 : 0.0;
+            for (int j = -nstep; j <= nstep; ++j) {
+                tp.Tsel.push_back(sel);
+                tp.Ta.push_back(abase + j * astep);
+            }
+        }
+        const int nc = (int)tp.Tsel.size();
+        std::vector<ThmRec> vC(nc);
+        std::vector<Eval> ev;
+        for (int ic = 0; ic < nc; ++ic)
+            ev.push_back(Eval{id, deg, ic, &vC[ic]});
+        if (int rc = eval_batch(S, ev))
+            return rc;
+        double rbest = 0;
+        int ibest = -1;
+        for (int ic = 0; ic < nc; ++ic)
+            if (vC[ic].R > rbest) {
+                rbest = vC[ic].R;
+                ibest = ic;
+            }
+        if (ibest == -1)
+            break;
+        const int bsel = tp.Tsel[ibest];
+        double x1 = tp.Ta[ibest];
+        // PTWInterp (CThmScan.cpp:119-155) on record 0
+        const double y1 = rbest, d = astep;
+        ThmRec C;
+        std::vector<Eval> one(1, Eval{id, deg, 0, &C});
+        tp.Tsel[0] = bsel;
+        tp.Ta[0] = x1 - d;
+        if (int rc = eval_batch(S, one))
+            return rc;
+        const double y0 = C.R;
+        tp.Ta[0] = x1 + d;
+        if (int rc = eval_batch(S, one))
+            return rc;
+        const double y2 = C.R;
+        double xnew = x1;
+        {
+            const double D = d * (y0 - y2) / (2 * (y0 + y2 - y1 - y1));
+            if (fabs(D) <= 2 * d)
+                xnew = x1 + D;
+        }
+        tp.Ta[0] = xnew;
+        if (int rc = eval_batch(S, one))
+            return rc;
+        double ynew = C.R;
+        if (ynew < y1) {
+            xnew = x1;
+            ynew = y1;
+        }
+        rbest = ynew;
+        if (rbest > bestR) {
+            double M[6];
+            aff_nu(M, bsel, xnew);
+            aff_mul(tp.Tptwk, M, tp.Tptwk);
+            vused[bsel] = 1;
+            bestR = rbest;
+            *changed = true;
+        } else
+            break;
+    }
+    tp.Tsel.clear();
+    tp.Ta.clear();
+    return ALN_OK;
+}
+
+// AngleScanWithTweaks (CThmScan.cpp:647-668)
+static int scan_with_tweaks(SweepCtx &S, const std::vector<int> &ids,
+                            const std::vector<double> &center, double hlfwid, double step)
+{
+    if (int rc = scan_sel(S, ids, center, hlfwid, step, true, S.P.constxy != 0))
+        return rc;
+    if (!S.P.pretweak)
+        return ALN_OK;
+    std::vector<int> redo;
+    std::vector<double> rc_center;
+    for (size_t q = 0; q < ids.size(); ++q) {
+        ThmRec &best = S.pairs[ids[q]].best;
+        if (best.R < S.P.rthresh) {
+            bool changed = false;
+            if (int rc = pretweaks(S, ids[q], best.R, best.R > 0.0 ? best.A : center[q], &changed))
+                return rc;
+            if (changed) {
+                redo.push_back(ids[q]);
+                rc_center.push_back(center[q]);
+            }
+        }
+    }
+    if (!redo.empty())
+        return scan_sel(S, redo, rc_center, hlfwid, step, true, S.P.constxy != 0);
+    return ALN_OK;
+}
+
+extern "C" int aln_thm_search_batch(aln_ctx *ctx, int npairs, const aln_thumbs *thumbs,
+                                    const aln_thm_params *params, int mode, double ang0,
+                                    double hfang, double step, aln_thm_result *out)
+{
+    if (!ctx || npairs < 0 || (npairs && (!thumbs || !params || !out)))
+        return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
+    if (!params->usecorrr)
+        return set_err(ctx, ALN_ERR_UNSUPPORTED,
+                       "sweep with CorrImagesF (useCorrR off) is not built yet");
+    CK(cudaSetDevice(ctx->device));
+    SweepCtx S;
+    S.ctx = ctx;
+    S.P = *params;
+    S.pairs.resize(npairs);
+    // device copies of the thumbnails
+    size_t bytes = 0;
+    for (int k = 0; k < npairs; ++k) {
+        const aln_thumbs &T = thumbs[k];
+        if (!T.a || T.a_w < 1 || T.a_h < 1 || T.a_stride < T.a_w || !T.b.data ||
+            T.b.dtype != ALN_F64 || T.b.w < 1 || T.b.h < 1 || T.b.stride < T.b.w)
+            return set_err(ctx, ALN_ERR_ARG, "thumbnail pair %d: bad grid/raster", k);
+        bytes += al256((size_t)T.a_stride * T.a_h * 8) + al256((size_t)T.a_stride * T.a_h) +
+                 al256((size_t)T.b.stride * T.b.h * 8);
+    }
+    char *dbuf = nullptr;
+    if (bytes) {
+        cudaError_t e = cudaMalloc(&dbuf, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(ctx, ALN_ERR_NOMEM, "thumbnails: %s", cudaGetErrorString(e));
+        }
+    }
+    char *p = dbuf;
+    int rc = ALN_OK;
+    for (int k = 0; k < npairs && rc == ALN_OK; ++k) {
+        const aln_thumbs &T = thumbs[k];
+        ThmPair &tp = S.pairs[k];
+        tp.in = &T;
+        tp.ncalls = 0;
+        tp.err = 0;
+        aff_one(tp.Tptwk);
+        const size_t ab = (size_t)T.a_stride * T.a_h * 8;
+        tp.dev_a = (const double *)p;
+        if (cudaMemcpyAsync(p, T.a, ab, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+            rc = set_err(ctx, ALN_ERR_CUDA, "thumbnail copy");
+        p += al256(ab);
+        tp.dev_mask = nullptr;
+        if (T.a_mask) {
+            tp.dev_mask = (const unsigned char *)p;
+            if (cudaMemcpyAsync(p, T.a_mask, (size_t)T.a_stride * T.a_h, cudaMemcpyHostToDevice,
+                                ctx->stream) != cudaSuccess)
+                rc = set_err(ctx, ALN_ERR_CUDA, "mask copy");
+        }
+        p += al256((size_t)T.a_stride * T.a_h);
+        const size_t bb = (size_t)T.b.stride * T.b.h * 8;
+        tp.dev_b = T.b;
+        tp.dev_b.data = p;
+        tp.dev_b.on_device = 1;
+        if (cudaMemcpyAsync(p, T.b.data, bb, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+            rc = set_err(ctx, ALN_ERR_CUDA, "thumbnail copy");
+        p += al256(bb);
+        make_hull(tp);
+        if (tp.hull.empty())
+            rc = set_err(ctx, ALN_ERR_ARG, "thumbnail pair %d: no A points", k);
+        tp.best.X = tp.best.Y = tp.best.A = tp.best.R = -999.0;   // CThmScan::Initialize
+    }
+    std::vector<int> all(npairs);
+    for (int k = 0; k < npairs; ++k)
+        all[k] = k;
+    std::vector<double> c0(npairs, ang0);
+    auto failing = [&](const std::vector<int> &ids) {
+        std::vector<int> keep;
+        for (int id : ids)
+            if (S.pairs[id].best.R < S.P.rthresh)
+                S.pairs[id].err = (mode == ALN_THM_PRIOR) ? 2 : 1;
+            else
+                keep.push_back(id);
+        return keep;
+    };
+    if (rc == ALN_OK) {
+        switch (mode) {
+        case ALN_THM_DENOVO: {
+            // DenovoBestAngle (CThmScan.cpp:764-790)
+            rc = scan_with_tweaks(S, all, c0, hfang, step);
+            std::vector<int> ids = failing(all);
+            if (rc == ALN_OK && !ids.empty()) {
+                std::vector<double> cen;
+                for (int id : ids)
+                    cen.push_back(S.pairs[id].best.A);
+                rc = scan_sel(S, ids, cen, step * 2.0, step * 0.05, false, S.P.constxy != 0);
+            }
+            ids = failing(ids);
+            if (rc == ALN_OK && !ids.empty())
+                rc = peak_hunt(S, ids, step * 0.05 * 1.5);
+            failing(ids);
+            break;
+        }
+        case ALN_THM_RFROMANGLE: {
+            std::vector<Eval> ev;
+            for (int k = 0; k < npairs; ++k)
+                ev.push_back(Eval{k, ang0, -1, &S.pairs[k].best});
+            rc = eval_batch(S, ev);
+            break;
+        }
+        case ALN_THM_PRIOR: {
+            // UsePriorAngles (CThmScan.cpp:734-758)
+            rc = scan_with_tweaks(S, all, c0, hfang, 0.1);
+            std::vector<int> ids = failing(all);
+            if (rc == ALN_OK && !ids.empty())
+                rc = peak_hunt(S, ids, 0.1 * 1.5);
+            failing(ids);
+            break;
+        }
+        case ALN_THM_SCAN_HUNT:
+            rc = scan_sel(S, all, c0, hfang, step, false, S.P.constxy != 0);
+            if (rc == ALN_OK)
+                rc = peak_hunt(S, all, step * 0.05 * 1.5);
+            break;
+        case ALN_THM_SCAN_MAXR:
+            rc = scan_sel(S, all, c0, hfang, step, true, false);
+            break;
+        default:
+            rc = set_err(ctx, ALN_ERR_ARG, "bad sweep mode %d", mode);
+        }
+    }
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(S.arena);
+    cudaFree(S.djobs);
+    cudaFree(dbuf);
+    if (rc != ALN_OK)
+        return rc;
+    for (int k = 0; k < npairs; ++k) {
+        const ThmPair &tp = S.pairs[k];
+        out[k].A = tp.best.A;
+        out[k].X = tp.best.X;
+        out[k].Y = tp.best.Y;
+        out[k].R = tp.best.R;
+        memcpy(out[k].T, tp.best.T, sizeof out[k].T);
+        out[k].err = tp.err;
+        out[k].ncalls = tp.ncalls;
+    }
+    return ALN_OK;
+}

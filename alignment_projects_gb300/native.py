@@ -54,6 +54,52 @@ class AlnImageJob(C.Structure):
 
 
 CORR_F, CORR_R, CORR_S = 0, 1, 2
+THM_DENOVO, THM_RFROMANGLE, THM_PRIOR, THM_SCAN_HUNT, THM_SCAN_MAXR = 0, 1, 2, 3, 4
+
+
+class AlnThumbs(C.Structure):
+    _fields_ = [("a", C.c_void_p), ("a_mask", C.c_void_p), ("a_w", C.c_int), ("a_h", C.c_int),
+                ("a_stride", C.c_int), ("a_x0", C.c_int), ("a_y0", C.c_int), ("b", AlnImage),
+                ("req_area", C.c_longlong), ("olap1d", C.c_int)]
+
+
+class AlnThmParams(C.Structure):
+    _fields_ = [("rthresh", C.c_double), ("nbmaxht", C.c_double), ("constxy", C.c_int),
+                ("pretweak", C.c_int), ("usecorrr", C.c_int), ("ox", C.c_int), ("oy", C.c_int),
+                ("rx", C.c_int), ("ry", C.c_int), ("tdfm", C.c_double * 6)]
+
+
+class AlnThmResult(C.Structure):
+    _fields_ = [("A", C.c_double), ("X", C.c_double), ("Y", C.c_double), ("R", C.c_double),
+                ("T", C.c_double * 6), ("err", C.c_int), ("ncalls", C.c_int)]
+
+
+def thumbs_from_points(pa, va, pb, vb, req_area, olap1d=0):
+    """Point lists with integer coordinates (a ThmRec) -> AlnThumbs.  A
+    becomes a grid with a presence mask; B a raster over its bounding box."""
+    pa = np.asarray(pa, np.float64).reshape(-1, 2)
+    pb = np.asarray(pb, np.float64).reshape(-1, 2)
+    assert np.all(pa == np.round(pa)) and np.all(pb == np.round(pb))
+    ax, ay = pa[:, 0].astype(np.int64), pa[:, 1].astype(np.int64)
+    ax0, ay0 = int(ax.min()), int(ay.min())
+    aw, ah = int(ax.max()) - ax0 + 1, int(ay.max()) - ay0 + 1
+    agrid = np.zeros((ah, aw), np.float64)
+    amask = np.zeros((ah, aw), np.uint8)
+    agrid[ay - ay0, ax - ax0] = np.asarray(va, np.float64)
+    amask[ay - ay0, ax - ax0] = 1
+    bx, by = pb[:, 0].astype(np.int64), pb[:, 1].astype(np.int64)
+    bx0, by0 = int(bx.min()), int(by.min())
+    bw, bh = int(bx.max()) - bx0 + 1, int(by.max()) - by0 + 1
+    braster = np.zeros((bh, bw), np.float64)
+    np.add.at(braster, (by - by0, bx - bx0), np.asarray(vb, np.float64))
+    T = AlnThumbs()
+    T.a = agrid.ctypes.data
+    T.a_mask = None if amask.all() else amask.ctypes.data
+    T.a_w, T.a_h, T.a_stride, T.a_x0, T.a_y0 = aw, ah, aw, ax0, ay0
+    T.b = image(braster, bx0, by0)
+    T.req_area, T.olap1d = req_area, olap1d
+    T._keep = (agrid, amask, braster)
+    return T
 
 
 class AlnPair(C.Structure):
@@ -85,6 +131,9 @@ def lib():
                                       C.POINTER(AlnResult)]
         L.aln_corr_images_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnImageJob),
                                             C.POINTER(AlnResult)]
+        L.aln_thm_search_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnThumbs),
+                                           C.POINTER(AlnThmParams), C.c_int, C.c_double,
+                                           C.c_double, C.c_double, C.POINTER(AlnThmResult)]
         L.aln_fft_2d.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         L.aln_ift_2d.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         L.aln_ctx_set_profiling.argtypes = [C.c_void_p, C.c_int]
@@ -251,6 +300,26 @@ class Context:
         out = (AlnResult * len(jobs))()
         self._check(self._L.aln_corr_images_batch(self.h, len(jobs), arr, out))
         return [o.as_dict() for o in out]
+
+    # -- CThmScan sweep -------------------------------------------------------
+    def thm_search_batch(self, thumbs, rthresh=0.3, nbmaxht=0.75, pretweak=0, constxy=1,
+                         usecorrr=1, disc=(0, 0, -1, -1), mode=THM_DENOVO, ang0=0.0,
+                         hfang=10.0, step=0.5, tdfm=None) -> list:
+        thumbs = list(thumbs)
+        arr = (AlnThumbs * len(thumbs))()
+        for k, t in enumerate(thumbs):
+            arr[k] = t
+        P = AlnThmParams()
+        P.rthresh, P.nbmaxht = rthresh, nbmaxht
+        P.constxy, P.pretweak, P.usecorrr = constxy, pretweak, usecorrr
+        P.ox, P.oy, P.rx, P.ry = disc
+        for i, v in enumerate(tdfm if tdfm is not None else (1, 0, 0, 0, 1, 0)):
+            P.tdfm[i] = v
+        out = (AlnThmResult * len(thumbs))()
+        self._check(self._L.aln_thm_search_batch(self.h, len(thumbs), arr, C.byref(P), mode,
+                                                 ang0, hfang, step, out))
+        return [{"A": o.A, "X": o.X, "Y": o.Y, "R": o.R, "err": o.err, "ncalls": o.ncalls,
+                 "T": list(o.T)} for o in out]
 
     def corr_patches_batch(self, pairs) -> list:
         """pairs: iterable of dicts with a, b, [ox, oy, radius, legal, a_origin, b_origin]."""

@@ -209,6 +209,53 @@ int aln_corr_images(aln_ctx *ctx, int kind, const aln_image *a, const aln_image 
 int aln_corr_images_batch(aln_ctx *ctx, int njobs, const aln_image_job *jobs,
                           aln_result *out);
 
+/* ---- CThmScan angle sweep: 0_GEN/CThmScan.h:57-223 ------------------ */
+
+/* Thumbnails of one pair, the ThmRec of 0_GEN/CThmScan.h:27-34.
+ * A: values on an integer grid, point (x + a_x0, y + a_y0) holds
+ *    a[x + a_stride*y] (present unless a_mask[...] == 0); the sweep rotates
+ *    these points about the origin.
+ * B: FP64 raster over the bounding box of B's points (ALN_F64, holes 0). */
+typedef struct aln_thumbs {
+    const double *a;
+    const unsigned char *a_mask;   /* NULL: every grid point present */
+    int a_w, a_h, a_stride, a_x0, a_y0;
+    aln_image b;
+    long long req_area;            /* ThmRec reqArea */
+    int olap1d;                    /* ThmRec olap1D */
+} aln_thumbs;
+
+/* CThmScan settings (its setters, 0_GEN/CThmScan.h:115-157). */
+typedef struct aln_thm_params {
+    double rthresh, nbmaxht;
+    int constxy, pretweak, usecorrr;   /* usecorrr must be 1 (CorrImagesS) */
+    int ox, oy, rx, ry;                /* SetDisc */
+    double tdfm[6];                    /* SetTdfm (TAffine t[0..5]) */
+} aln_thm_params;
+
+/* CorRec (0_GEN/CThmScan.h:36-44) plus the search's err and call count. */
+typedef struct aln_thm_result {
+    double A, X, Y, R;
+    double T[6];
+    int err;       /* errOK 0, errLowRDenov 1, errLowRPrior 2 */
+    int ncalls;    /* correlator calls made for this pair */
+} aln_thm_result;
+
+enum {
+    ALN_THM_DENOVO = 0,      /* DenovoBestAngle(ang0, hfang, step), CThmScan.cpp:764-790 */
+    ALN_THM_RFROMANGLE = 1,  /* RFromAngle(ang0), CThmScan.cpp:329-366 */
+    ALN_THM_PRIOR = 2,       /* UsePriorAngles(ang0, hfang), CThmScan.cpp:734-758 */
+    ALN_THM_SCAN_HUNT = 3,   /* AngleScanSel(ang0, hfang, step, false) + PeakHunt(step*0.075) */
+    ALN_THM_SCAN_MAXR = 4    /* AngleScanMaxR(ang0, hfang, step, favorCenter), :431-493 */
+};
+
+/* Runs one CThmScan search per pair, all pairs together: every correlator
+ * call of a stage (scan, fine scan, each bracket step) over all pairs is one
+ * GPU batch.  Results equal the reference's search on each pair. */
+int aln_thm_search_batch(aln_ctx *ctx, int npairs, const aln_thumbs *thumbs,
+                         const aln_thm_params *params, int mode, double ang0,
+                         double hfang, double step, aln_thm_result *out);
+
 /* ---- allocation-free CorrPatches: no counterpart in the reference ---- */
 
 /* Size of the device scratch array behind aln_corr_patches_noalloc. */
