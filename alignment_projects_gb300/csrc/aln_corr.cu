@@ -1197,9 +1197,12 @@ static inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // CorrImagesF/R/S parameters of a job (0_GEN/Correlation.h:159-220).
 struct ImgSpec {
-    int kind;   // 1 R, 2 S
+    int kind;   // 1 R, 2 S, 3 CorrPatchToImage
     double mincor;
     int ox, oy, rx, ry;
+    // CorrPatchToImage
+    int p2i_w1, p2i_h1, p2i_w2, p2i_h2, p2i_filter;
+    double p2i_norm;
 };
 
 // Host-side plan of one pair: sizes, window, needed SAT rows, workspace.
@@ -1327,7 +1330,36 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
         return set_err(ctx, ALN_ERR_ARG, "legality table missing");
     if (d.rgn_kind < 0 || d.rgn_kind > ALN_RGN_TABLE)
         return set_err(ctx, ALN_ERR_ARG, "bad rgn_kind %d", d.rgn_kind);
-    if (spec) {
+    if (spec && spec->kind == 3) {
+        // CorrPatchToImage: both images are the N x N frame; every storage
+        // row/column of the inverse is kept; no summed-area tables
+        d.mode = JOB_P2I;
+        d.no_shift = 1;
+        d.Nx = d.w[0];   // circular correlation on the N x N frame itself
+        d.Ny = d.h[0];
+        d.logNx = ilog2(d.Nx);
+        d.logNy = ilog2(d.Ny);
+        pl.orig_nx = d.Nx;
+        pl.orig_ny = d.Ny;
+        pl.frame_nx1 = pl.frame_ny1 = 0;
+        d.p2i_filter = spec->p2i_filter;
+        d.p2i_w1 = spec->p2i_w1;
+        d.p2i_h1 = spec->p2i_h1;
+        d.p2i_w2 = spec->p2i_w2;
+        d.p2i_h2 = spec->p2i_h2;
+        d.p2i_norm = spec->p2i_norm;
+        d.ox = spec->ox;
+        d.oy = spec->oy;
+        d.rsqr = (long long)spec->rx * spec->rx;   // rx carries the radius
+        d.xlo = 0;
+        d.xhi = d.Nx - 1;
+        d.ylo = 0;
+        d.yhi = d.Ny - 1;
+        for (int i = 0; i < 2; ++i) {
+            d.need_lo[i][0] = d.need_lo[i][1] = 1;
+            d.need_hi[i][0] = d.need_hi[i][1] = 0;
+        }
+    } else if (spec) {
         // CCorImg::SetDims "too small" rule, 0_GEN/Correlation.cpp:1991-2000
         const int mindelta = 11 / 2 + 1;
         if (d.w[0] - 1 < mindelta || d.w[1] < mindelta || d.h[0] - 1 < mindelta ||
@@ -1362,8 +1394,9 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
         pl.in_bytes[0] = pl.in_bytes[1] = 0;
         return ALN_OK;
     }
-    for (int i = 0; i < 2; ++i)
-        need_rows(d, i, d.need_lo[i], d.need_hi[i]);
+    if (d.mode != JOB_P2I)
+        for (int i = 0; i < 2; ++i)
+            need_rows(d, i, d.need_lo[i], d.need_hi[i]);
     const int L1 = d.Nx / 2 + 1;
     const int Wy = d.yhi - d.ylo + 1, Wx = d.xhi - d.xlo + 1;
     size_t b = 0;
@@ -1517,6 +1550,17 @@ static void launch_lagrow2(aln_ctx *ctx, int n, int maxWy)
 }
 
 template <int LL>
+static void launch_lagp2i(aln_ctx *ctx, int n, int maxWy)
+{
+    constexpr int T = RegFFT<LL, +1>::T;
+    const int thr = std::max(256, T), G = thr / T;
+    const size_t sm = (size_t)G * (padded(LL) + 2) * sizeof(float2);
+    cudaFuncSetAttribute(k2_lagp2i<LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    LAUNCH(ctx, "k2_lagp2i", k2_lagp2i<LL>, dim3((maxWy + G - 1) / G, n), thr, sm, ctx->dpairs,
+           ctx->tw);
+}
+
+template <int LL>
 static void launch_lagimg2(aln_ctx *ctx, int n, int maxWy, bool both)
 {
     constexpr int T = RegFFT<LL, +1>::T;
@@ -1550,6 +1594,13 @@ static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int
     if (mode == JOB_PATCHES) {
         switch (L) {
 #define X(v) case v: launch_lagrow2<v>(ctx, n, maxWy); break;
+            ALN_CASES_L(X)
+#undef X
+        default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
+        }
+    } else if (mode == JOB_P2I) {
+        switch (L) {
+#define X(v) case v: launch_lagp2i<v>(ctx, n, maxWy); break;
             ALN_CASES_L(X)
 #undef X
         default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
@@ -1661,11 +1712,13 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int par, char
             LAUNCH(ctx, "k_transpose", k_transpose, dim3((sw + 31) / 32, (sh + 31) / 32, 2 * n),
                    dim3(32, 8), 0, ctx->dpairs);
     }
-    LAUNCH(ctx, "k3_sat", k3_sat, dim3((maxw + 31) / 32, 2 * n), dim3(32, SAT_WARPS), 0,
-           ctx->dpairs);
-    LAUNCH(ctx, "k_mean", k_mean, dim3(2, n), 256, 0, ctx->dpairs);
-    LAUNCH(ctx, "k2_sat2", k2_sat2, dim3(maxslots, 2, n), 256, 0, ctx->dpairs);
     const int mode = hd[0].mode;
+    if (mode != JOB_P2I) {
+        LAUNCH(ctx, "k3_sat", k3_sat, dim3((maxw + 31) / 32, 2 * n), dim3(32, SAT_WARPS), 0,
+               ctx->dpairs);
+        LAUNCH(ctx, "k_mean", k_mean, dim3(2, n), 256, 0, ctx->dpairs);
+        LAUNCH(ctx, "k2_sat2", k2_sat2, dim3(maxslots, 2, n), 256, 0, ctx->dpairs);
+    }
     if (L >= 8 && L <= 4096 && Ny >= 8 && Ny <= 8192) {
         if (int rc = launch_fft_pipeline(ctx, L, Ny, n, maxh, maxWy, mode,
                                          hd[0].want_r && hd[0].want_s))
@@ -1696,6 +1749,8 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int par, char
     if (mode == JOB_PATCHES)
         LAUNCH(ctx, "k_final", k_final, n, 256, 0, ctx->dpairs, ctx->dres, chunk[0]->frame_nx1,
                chunk[0]->frame_ny1);
+    else if (mode == JOB_P2I)
+        LAUNCH(ctx, "k_final_p2i", k_final_p2i, n, 256, 0, ctx->dpairs, ctx->dres);
     else
         LAUNCH(ctx, "k_final_img", k_final_img, n, 256, 0, ctx->dpairs, ctx->dres);
     CK(cudaGetLastError());
@@ -1852,6 +1907,70 @@ extern "C" int aln_corr_images_batch(aln_ctx *ctx, int njobs, const aln_image_jo
         specs[k].ry = J.ry;
     }
     return batch_impl(ctx, njobs, pairs.data(), specs.data(), out);
+}
+
+extern "C" int aln_corr_patch_to_image(aln_ctx *ctx, const double *xy1, const double *v1,
+                                       int n1, const double *i2, int n2sq, int ox, int oy,
+                                       int radius, int bfilter, aln_result *out)
+{
+    if (!ctx || !xy1 || !v1 || !i2 || !out || n1 < 1 || n2sq < 1)
+        return ctx ? set_err(ctx, ALN_ERR_ARG, "patch_to_image: bad arguments") : ALN_ERR_ARG;
+    const int N = (int)sqrt((double)n2sq);
+    if (N < 16 || (N & (N - 1)) || N > ALN_MAX_N)
+        return set_err(ctx, ALN_ERR_UNSUPPORTED,
+                       "patch_to_image: image side %d (powers of two 16..%d)", N, ALN_MAX_N);
+    // BBoxFromPoints of the patch (0_GEN/Geometry.cpp:78-106)
+    double xlo = xy1[0], xhi = xy1[0], ylo = xy1[1], yhi = xy1[1];
+    for (int i = 1; i < n1; ++i) {
+        const double x = xy1[2 * i], y = xy1[2 * i + 1];
+        if (x < xlo)
+            xlo = x;
+        else if (x > xhi)
+            xhi = x;
+        if (y < ylo)
+            ylo = y;
+        else if (y > yhi)
+            yhi = y;
+    }
+    // the caller-embedded image's nonzero extent, and the patch image (points
+    // truncated to pixels, later points overwrite: Correlation.cpp:1222-1249)
+    int w2 = 0, h2 = 0;
+    for (int i = 0; i < N * N; ++i)
+        if (i2[i] != 0.0) {
+            const int y = i / N, x = i - N * y;
+            if (y > h2)
+                h2 = y;
+            if (x > w2)
+                w2 = x;
+        }
+    std::vector<double> im1((size_t)N * N, 0.0);
+    for (int i = 0; i < n1; ++i) {
+        const int x = (int)xy1[2 * i], y = (int)xy1[2 * i + 1];
+        if (x < 0 || y < 0 || x >= N || y >= N)
+            return set_err(ctx, ALN_ERR_ARG, "patch_to_image: point %d outside the image", i);
+        im1[x + (size_t)N * y] = v1[i];
+    }
+    aln_pair P;
+    memset(&P, 0, sizeof P);
+    P.a.data = im1.data();
+    P.b.data = i2;
+    P.a.dtype = P.b.dtype = ALN_F64;
+    P.a.w = P.a.h = P.a.stride = N;
+    P.b.w = P.b.h = P.b.stride = N;
+    P.radius = 1 << 20;
+    ImgSpec sp;
+    memset(&sp, 0, sizeof sp);
+    sp.kind = 3;
+    sp.ox = ox;
+    sp.oy = oy;
+    sp.rx = radius;
+    sp.p2i_w1 = (int)ceil(xhi) - (int)floor(xlo) + 1;
+    sp.p2i_h1 = (int)ceil(yhi) - (int)floor(ylo) + 1;
+    sp.p2i_w2 = w2 + 1;
+    sp.p2i_h2 = h2 + 1;
+    sp.p2i_filter = bfilter != 0;
+    sp.p2i_norm = (double)n1 * ((double)N * N);
+    return batch_impl(ctx, 1, &P, &sp, out);
 }
 
 extern "C" int aln_corr_images(aln_ctx *ctx, int kind, const aln_image *a, const aln_image *b,

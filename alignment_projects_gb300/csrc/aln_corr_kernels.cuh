@@ -13,7 +13,7 @@ struct RowBest {
 };
 
 // job kinds
-enum { JOB_PATCHES = 0, JOB_IMAGES_R = 1, JOB_IMAGES_S = 2 };
+enum { JOB_PATCHES = 0, JOB_IMAGES_R = 1, JOB_IMAGES_S = 2, JOB_P2I = 3 };
 
 // Compact per-pair result copied back to the host.
 struct ResultDev {
@@ -75,6 +75,10 @@ struct PairDev {
     int cx, cy, wR, hR;          // R image: lag (x, y) at index (x + cx) + wR (y + cy)
     float2 *Q2;                  // whitened inverse rows when both R and S are needed
     double *rr2;                 // R image when the key is S and mincor > 0
+    // CorrPatchToImage (0_GEN/Correlation.cpp:1186-1355)
+    int p2i_filter;              // Gaussian low-pass of the cross spectrum
+    int p2i_w1, p2i_h1, p2i_w2, p2i_h2;   // patch bbox size, image nonzero extent
+    double p2i_norm;             // np1 * N^2
     // result
     double r, dx, dy;
     int status, px, py;

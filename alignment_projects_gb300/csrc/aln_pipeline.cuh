@@ -494,9 +494,22 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
 #pragma unroll
     for (int r = 0; r < R; ++r)
         va[r] = cmulc(sb[r * T + t], va[r]);   // X2 * conj(X1)
+    if (p.mode == JOB_P2I && p.p2i_filter) {
+        // CorrPatchToImage's low-pass (0_GEN/Correlation.cpp:1255-1283): the
+        // reference names the row index "x" (wrapped) and the column "y"
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            int x = t + r * T;
+            if (x >= NY / 2)
+                x -= NY;
+            const double rad2 = ((double)x * x + (double)kxc * kxc) / 10000.0;
+            const float filt = rad2 > 10.0 ? 0.f : (float)exp(-rad2);
+            va[r] = make_float2(va[r].x * filt, va[r].y * filt);
+        }
+    }
     // CorrPatches / CorrImagesR need the plain inverse; CorrImagesS the inverse
     // of the whitened product P / sqrt(|P|) (0_GEN/Correlation.cpp:2311-2317)
-    const bool want_r = p.mode == JOB_PATCHES || p.want_r;
+    const bool want_r = p.mode == JOB_PATCHES || p.mode == JOB_P2I || p.want_r;
     const bool want_s = p.want_s != 0;
     if (want_r && want_s) {
 #pragma unroll
@@ -507,7 +520,12 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
     const int nnegy = p.h[0] - 1;
     if (want_r) {
         FI::run(va, sm, t, tw);
-        if (live) {
+        if (live && p.mode == JOB_P2I) {   // every storage row, in storage order
+            float2 *Q = p.Q + (long long)kx * NY;
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                Q[t + r * T] = va[r];
+        } else if (live) {
             float2 *Q = p.Q + (long long)kx * Wy;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
@@ -883,4 +901,195 @@ __global__ void k_final_img(PairDev *pairs, ResultDev *res)
     o.status = ALN_OK;
     o.px = p.px;
     o.py = p.py;
+}
+
+// ---------------------------------------------------------------------------
+// CorrPatchToImage (0_GEN/Correlation.cpp:1186-1355): raw correlation over an
+// N x N frame, its own lag zones, ParabPeakFFT on the raw inverse
+// ---------------------------------------------------------------------------
+
+// Per storage row: inverse real FFT -> raw values (kept for the neighbour
+// look-ups), the row's best lag by the reference's zone rules:
+// y > N - h1 negative, else y >= h2 dead (likewise x), disc on (x, y).
+template <int L>
+__global__ void k2_lagp2i(PairDev *pairs, const float2 *__restrict__ tw)
+{
+    using F = RegFFT<L, +1>;
+    constexpr int R = F::R, T = F::T;
+    constexpr int PITCH = padded(L) + 2;
+    extern __shared__ float2 smem[];
+    __shared__ double red_r[32];
+    __shared__ long long red_k[32];
+    PairDev &p = pairs[blockIdx.y];
+    if (p.status != 0)
+        return;
+    const int N = p.Nx, Wy = p.Ny;
+    const int G = blockDim.x / T;
+    const int team = threadIdx.x / T, t = threadIdx.x - team * T;
+    const int j0 = blockIdx.x * G;
+    if (j0 >= Wy)
+        return;
+    const int j = j0 + team;
+    const bool live = j < Wy;
+    const int jc = live ? j : Wy - 1;
+    float2 *sm = smem + team * PITCH;
+    for (int k = t; k <= L; k += T)
+        sm[padi(k)] = p.Q[(long long)k * Wy + jc];
+    __syncthreads();
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int k = t + r * T;
+        float2 a = sm[padi(k)];
+        float2 b = cconj(sm[padi(L - k)]);
+        if (k == 0) {
+            a.y = 0.f;
+            b.y = 0.f;
+        }
+        const float2 e = cadd(a, b);
+        const float2 dd = csub(a, b);
+        float2 wv = __ldg(&tw[2 * L + k]);
+        wv.y = -wv.y;
+        const float2 o = cmul(dd, wv);
+        v[r] = make_float2(e.x - o.y, e.y + o.x);
+    }
+    F::run(v, sm, t, tw);
+    double br = -1.0e30;
+    long long bk = 0x7fffffffffffffffLL;
+    if (live) {
+        // storage row j; its lag row by the reference's rule
+        int y = j;
+        bool ydead = false;
+        if (y > N - p.p2i_h1)
+            y -= N;
+        else if (y >= p.p2i_h2)
+            ydead = true;
+        const long long dy = y - p.oy;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int n = t + r * T;
+            for (int h = 0; h < 2; ++h) {
+                const int xs = 2 * n + h;
+                const double val = h ? (double)v[r].y : (double)v[r].x;
+                p.rr[(long long)j * N + xs] = val;
+                if (ydead)
+                    continue;
+                int x = xs;
+                if (x > N - p.p2i_w1)
+                    x -= N;
+                else if (x >= p.p2i_w2)
+                    continue;
+                const long long dx = x - p.ox;
+                if (dx * dx + dy * dy > p.rsqr)
+                    continue;
+                best_merge(br, bk, val, (long long)j * N + xs);
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31;
+    for (int o = 16; o > 0; o >>= 1) {
+        const double r2 = __shfl_down_sync(0xffffffff, br, o);
+        const long long k2 = __shfl_down_sync(0xffffffff, bk, o);
+        if (lane + o < 32 && (lane + o) / T == lane / T)
+            best_merge(br, bk, r2, k2);
+    }
+    if (T <= 32) {
+        if (live && t == 0) {
+            p.rb[j].r = br;
+            p.rb[j].key = bk;
+        }
+        return;
+    }
+    const int wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        red_r[wid] = br;
+        red_k[wid] = bk;
+    }
+    __syncthreads();
+    if (live && t == 0) {
+        const int w0 = team * (T / 32);
+        for (int q = 1; q < T / 32; ++q)
+            best_merge(br, bk, red_r[w0 + q], red_k[w0 + q]);
+        p.rb[j].r = br;
+        p.rb[j].key = bk;
+    }
+}
+
+__global__ void k_final_p2i(PairDev *pairs, ResultDev *res)
+{
+    __shared__ double red_r[32];
+    __shared__ long long red_k[32];
+    PairDev &p = pairs[blockIdx.x];
+    if (p.status != 0)
+        return;
+    const int N = p.Nx;
+    double br = -1.0e30;
+    long long bk = 0x7fffffffffffffffLL;
+    for (int j = threadIdx.x; j < N; j += blockDim.x)
+        best_merge(br, bk, p.rb[j].r, p.rb[j].key);
+    for (int o = 16; o > 0; o >>= 1) {
+        const double r2 = __shfl_down_sync(0xffffffff, br, o);
+        const long long k2 = __shfl_down_sync(0xffffffff, bk, o);
+        best_merge(br, bk, r2, k2);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        red_r[wid] = br;
+        red_k[wid] = bk;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0)
+        return;
+    for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
+        best_merge(br, bk, red_r[q], red_k[q]);
+    ResultDev &o = res[blockIdx.x];
+    int bigx = -1, bigy = -1;
+    double biggest = -1.0E30;
+    if (br > -1.0e30) {
+        const int ys = (int)(bk / N), xs = (int)(bk - (long long)ys * N);
+        bigy = ys > N - p.p2i_h1 ? ys - N : ys;
+        bigx = xs > N - p.p2i_w1 ? xs - N : xs;
+        biggest = br;
+    }
+    biggest /= p.p2i_norm;
+    // ParabPeakFFT, d = 1, LkFFT on the raw inverse (0_GEN/Correlation.cpp:268-298,482-517)
+    const double *I = p.rr;
+    auto lk = [&](int x, int y) {
+        if (x < 0)
+            x += N;
+        if (y < 0)
+            y += N;
+        return I[x + (long long)N * y];
+    };
+    double xpk = bigx, ypk = bigy;
+    const int ix = bigx, iy = bigy;
+    if (ix > -N && iy > -N) {
+        const double z1 = lk(ix, iy);
+        double z0, z2;
+        if (ix - 1 >= 0 && ix + 1 < N && (z0 = lk(ix - 1, iy)) != 0.0 &&
+            (z2 = lk(ix + 1, iy)) != 0.0) {
+            z0 = (z0 - z2) / (2 * (z0 + z2 - z1 - z1));
+            if (fabs(z0) <= 8)
+                xpk += z0;
+        }
+        if (iy - 1 >= 0 && iy + 1 < N && (z0 = lk(ix, iy - 1)) != 0.0 &&
+            (z2 = lk(ix, iy + 1)) != 0.0) {
+            z0 = (z0 - z2) / (2 * (z0 + z2 - z1 - z1));
+            if (fabs(z0) <= 8)
+                ypk += z0;
+        }
+    }
+    p.r = biggest;
+    p.dx = xpk;
+    p.dy = ypk;
+    p.px = bigx;
+    p.py = bigy;
+    // the reference exits (44) on a normalised peak above 1.0001
+    p.status = biggest > 1.0001 ? ALN_NO_PEAK : ALN_OK;
+    o.r = p.r;
+    o.dx = p.dx;
+    o.dy = p.dy;
+    o.status = p.status;
+    o.px = bigx;
+    o.py = bigy;
 }

@@ -134,6 +134,9 @@ def lib():
         L.aln_thm_search_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnThumbs),
                                            C.POINTER(AlnThmParams), C.c_int, C.c_double,
                                            C.c_double, C.c_double, C.POINTER(AlnThmResult)]
+        L.aln_corr_patch_to_image.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                              C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                              C.c_int, C.POINTER(AlnResult)]
         L.aln_fft_2d.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         L.aln_ift_2d.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         L.aln_ctx_set_profiling.argtypes = [C.c_void_p, C.c_int]
@@ -266,6 +269,18 @@ class Context:
         self._check(self._L.aln_corr_patches(self.h, C.byref(ia), C.byref(ib), ox, oy, radius,
                                              C.byref(lg) if lg is not None else None,
                                              C.byref(res)))
+        return res.as_dict()
+
+    # -- CorrPatchToImage -----------------------------------------------------
+    def corr_patch_to_image(self, pts, vals, img2, ox=0, oy=0, radius=4096,
+                            bfilter=False) -> dict:
+        xy = np.ascontiguousarray(pts, np.float64).reshape(-1, 2)
+        v = np.ascontiguousarray(vals, np.float64)
+        i2 = np.ascontiguousarray(img2, np.float64)
+        res = AlnResult()
+        self._check(self._L.aln_corr_patch_to_image(self.h, xy.ctypes.data, v.ctypes.data,
+                                                    len(v), i2.ctypes.data, i2.size, ox, oy,
+                                                    radius, int(bfilter), C.byref(res)))
         return res.as_dict()
 
     # -- CorrImagesR / CorrImagesS ------------------------------------------

@@ -181,6 +181,17 @@ typedef struct aln_pair {
 int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *pairs,
                            aln_result *out);
 
+/* CorrPatchToImage, 0_GEN/Correlation.cpp:1186-1355: the patch's points
+ * (xy1[2i], xy1[2i+1], truncated to pixels) against a caller-embedded
+ * square image i2 (N x N, N = sqrt(n2sq), a power of two 16..8192), raw
+ * correlation / (n1 N^2), optional low-pass (bfilter), ParabPeakFFT on the
+ * raw correlation.  out->dx, dy are the refined peak (no box offsets, as the
+ * reference).  A normalised peak above 1.0001 (where the reference exits)
+ * returns ALN_NO_PEAK. */
+int aln_corr_patch_to_image(aln_ctx *ctx, const double *xy1, const double *v1, int n1,
+                            const double *i2, int n2sq, int ox, int oy, int radius,
+                            int bfilter, aln_result *out);
+
 /* ---- CorrImagesF/R/S: 0_GEN/Correlation.h:159-220 ------------------ */
 
 enum { ALN_CORR_F = 0, ALN_CORR_R = 1, ALN_CORR_S = 2 };

@@ -121,3 +121,35 @@ def test_images_batch_equals_single(ctx):
         single = ctx.corr_images(j["kind"], j["a"], j["b"], j["legal"], a_origin=j["a_origin"],
                                  b_origin=j["b_origin"])
         assert r == single
+
+
+# ---------------------------------------------------------------- CorrPatchToImage
+
+@pytest.mark.parametrize("case", ["p2i_f0", "p2i_f1"])
+def test_patch_to_image_golden(ctx, orc, case):
+    d = load_golden("patch_to_image")[case]
+    bf = bool(int(d["bfilter"]))
+    g = ctx.corr_patch_to_image(d["pa"], d["va"], d["img2"], 0, 0, 4096, bf)
+    o = orc.corr_patch_to_image(d["pa"], d["va"], d["img2"], 0, 0, 4096, bf)
+    assert abs(o["r"] - float(d["r"])) < 1e-12
+    assert g["status"] == 0
+    assert (g["peak_x"], g["peak_y"]) == (o["bigx"], o["bigy"])
+    # raw (unnormalised) correlation in FP32: 1e-5 relative
+    assert abs(g["r"] - float(d["r"])) <= 1e-5 * abs(float(d["r"]))
+    assert abs(g["dx"] - float(d["dx"])) <= PX_TOL and abs(g["dy"] - float(d["dy"])) <= PX_TOL
+
+
+def test_patch_to_image_disc_and_offsets(ctx, orc):
+    from alignment_projects_gb300 import synth
+    import oracle
+    p = synth.plain_pair(12, n=90, margin=8)
+    A, VA = oracle.image_to_points(p.a, 20, 30)
+    VA = (VA - VA.mean()) / VA.std() / 30
+    img2 = np.zeros((256, 256))
+    img2[30:120, 20:110] = (p.b - p.b.mean()) / p.b.std() / 30
+    for (ox, oy, rad) in [(0, 0, 4096), (3, -2, 10)]:
+        g = ctx.corr_patch_to_image(A, VA, img2, ox, oy, rad)
+        o = orc.corr_patch_to_image(A, VA, img2, ox, oy, rad)
+        assert (g["peak_x"], g["peak_y"]) == (o["bigx"], o["bigy"]), (g, o)
+        assert abs(g["r"] - o["r"]) <= 1e-5 * abs(o["r"])
+        assert abs(g["dx"] - o["dx"]) <= PX_TOL and abs(g["dy"] - o["dy"]) <= PX_TOL
