@@ -200,7 +200,7 @@ __device__ __forceinline__ bool lag_eval(const PairDev &p, int x, int y, double 
     bool ok = true;
     if (p.rgn_kind != ALN_RGN_NONE && !rgn_ok(p, olw, olh))
         ok = false;
-    if (p.cnt_kind == ALN_CNT_GT) {
+    if (ok && p.cnt_kind == ALN_CNT_GT) {
         const int c1 = sat_box_n(p.satN[0], p, 0, L1, R1, B1, T1);
         const int c2 = sat_box_n(p.satN[1], p, 1, L2, R2, B2, T2);
         if (!(c1 > p.cnt_n && c2 > p.cnt_n))
@@ -320,6 +320,11 @@ __global__ void k_mean(PairDev *pairs)
     const int i = blockIdx.x;
     if (p.status != 0)
         return;
+    if (p.sat_nonly) {   // no value sums: CorrImagesS correlates unshifted images
+        if (threadIdx.x == 0)
+            p.mu[i] = 0.0;
+        return;
+    }
     __shared__ double part[256];
     double s = 0.0;
     for (int c = threadIdx.x; c < p.w[i]; c += blockDim.x)
@@ -901,6 +906,18 @@ struct ProfRec {
     cudaEvent_t a, b;
 };
 
+// One cached spectrum of an image b (the reference's fft2 / ftc cache
+// argument): X2 in the layout k2_corrcol reads, for one FFT size and frame.
+struct SpecEntry {
+    float2 *X2;
+    size_t bytes;
+    unsigned long long tick;   // last chunk that used it
+};
+// (namespace, key, Nx, Ny, transposed, no_shift); namespace 0: the caller's
+// keys, 1: keys the library makes (the sweep's thumbnails).  no_shift: the
+// spectrum is of b itself (CorrImagesS) rather than of b minus its mean.
+typedef std::tuple<int, unsigned long long, int, int, int, int> SpecKey;
+
 struct aln_ctx {
     int device;
     cudaStream_t stream;
@@ -926,6 +943,15 @@ struct aln_ctx {
     std::vector<cudaEvent_t> ev_pool;
     std::map<std::string, std::pair<long long, double>> prof_acc;  // name -> (launches, ms)
     std::vector<std::string> prof_names;  // stable storage for returned names
+    // spectrum cache (device-resident X2 per keyed image b)
+    std::map<SpecKey, SpecEntry> spec;
+    std::multimap<size_t, float2 *> spec_free;   // evicted buffers by size
+    size_t spec_bytes, spec_cap;                 // all buffers held / limit
+    unsigned long long spec_tick;
+    long long spec_hits, spec_fills;
+    int *dsel;                                   // cache-fill job lists
+    size_t dsel_cap;
+    unsigned long long sweep_serial;             // key namespace of each sweep call
 };
 
 static cudaEvent_t ev_get(aln_ctx *c)
@@ -1044,6 +1070,13 @@ extern "C" int aln_ctx_create(int device, aln_ctx **out)
     ctx->launches = 0;
     ctx->prof_on = 0;
     ctx->ws_budget = (size_t)4 << 30;
+    ctx->spec_bytes = 0;
+    ctx->spec_cap = (size_t)8 << 30;
+    ctx->spec_tick = 0;
+    ctx->spec_hits = ctx->spec_fills = 0;
+    ctx->dsel = nullptr;
+    ctx->dsel_cap = 0;
+    ctx->sweep_serial = 0;
     if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&ctx->cstream, cudaStreamNonBlocking)) != cudaSuccess) {
         set_err(nullptr, ALN_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
@@ -1097,6 +1130,11 @@ extern "C" void aln_ctx_destroy(aln_ctx *ctx)
     cudaStreamSynchronize(ctx->cstream);
     cudaFree(ctx->dpairs_base);
     cudaFree(ctx->dres_base);
+    for (auto &e : ctx->spec)
+        cudaFree(e.second.X2);
+    for (auto &f : ctx->spec_free)
+        cudaFree(f.second);
+    cudaFree(ctx->dsel);
     if (ctx->hres)
         cudaFreeHost(ctx->hres);
     for (int q = 0; q < 2; ++q) {
@@ -1216,7 +1254,66 @@ struct PairPlan {
     size_t tr_bytes[2];          // transposed copies
     const aln_pair *src;
     int index;
+    int key_ns;                  // spectrum-cache key of image b (0: none)
+    unsigned long long key;
 };
+
+// A device buffer for a new cache entry of `bytes`, evicting entries not used
+// by the current chunk (least recently used first).  Buffers are reused on
+// the context's stream, so a kernel still reading an evicted entry finishes
+// before the buffer is filled again.  Returns NULL when nothing fits.
+static float2 *spec_alloc(aln_ctx *ctx, size_t bytes)
+{
+    auto f = ctx->spec_free.find(bytes);
+    if (f != ctx->spec_free.end()) {
+        float2 *b = f->second;
+        ctx->spec_free.erase(f);
+        return b;
+    }
+    while (ctx->spec_bytes + bytes > ctx->spec_cap) {
+        if (!ctx->spec_free.empty()) {
+            auto g = std::prev(ctx->spec_free.end());
+            cudaFree(g->second);   // waits for the device: rare
+            ctx->spec_bytes -= g->first;
+            ctx->spec_free.erase(g);
+            continue;
+        }
+        auto lru = ctx->spec.end();
+        for (auto it = ctx->spec.begin(); it != ctx->spec.end(); ++it)
+            if (it->second.tick < ctx->spec_tick &&
+                (lru == ctx->spec.end() || it->second.tick < lru->second.tick))
+                lru = it;
+        if (lru == ctx->spec.end())
+            return nullptr;
+        float2 *b = lru->second.X2;
+        const size_t lb = lru->second.bytes;
+        ctx->spec.erase(lru);
+        if (lb == bytes)
+            return b;
+        ctx->spec_free.insert(std::make_pair(lb, b));
+    }
+    float2 *b = nullptr;
+    if (cudaMalloc(&b, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    ctx->spec_bytes += bytes;
+    return b;
+}
+
+// Drops every entry of namespace ns with key in [k0, k1] (buffers kept for reuse).
+static void spec_drop(aln_ctx *ctx, int ns, unsigned long long k0, unsigned long long k1)
+{
+    for (auto it = ctx->spec.begin(); it != ctx->spec.end();) {
+        if (std::get<0>(it->first) == ns && std::get<1>(it->first) >= k0 &&
+            std::get<1>(it->first) <= k1) {
+            ctx->spec_free.insert(std::make_pair(it->second.bytes, it->second.X2));
+            it = ctx->spec.erase(it);
+        } else {
+            ++it;
+        }
+    }
+}
 
 static void need_rows(const PairDev &d, int img, int lo[2], int hi[2])
 {
@@ -1373,6 +1470,9 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
         d.want_s = spec->kind == 2;
         d.want_r = spec->kind == 1 || (spec->kind == 2 && spec->mincor > 0.0);
         d.no_shift = d.want_s;
+        // S key alone: no value sums, only counts; FP32 keys in the lag scan
+        d.sat_nonly = d.mode == JOB_IMAGES_S && !d.want_r;
+        d.s_float = d.sat_nonly;
         d.mincor = spec->mincor;
         d.cx = d.w[0] - 1;
         d.cy = d.h[0] - 1;
@@ -1394,9 +1494,14 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
         pl.in_bytes[0] = pl.in_bytes[1] = 0;
         return ALN_OK;
     }
-    if (d.mode != JOB_P2I)
+    if (d.mode != JOB_P2I && !(d.sat_nonly && d.cnt_kind != ALN_CNT_GT))
         for (int i = 0; i < 2; ++i)
             need_rows(d, i, d.need_lo[i], d.need_hi[i]);
+    else if (d.mode != JOB_P2I)
+        for (int i = 0; i < 2; ++i) {   // no table is read
+            d.need_lo[i][0] = d.need_lo[i][1] = 1;
+            d.need_hi[i][0] = d.need_hi[i][1] = 0;
+        }
     const int L1 = d.Nx / 2 + 1;
     const int Wy = d.yhi - d.ylo + 1, Wx = d.xhi - d.xlo + 1;
     size_t b = 0;
@@ -1524,18 +1629,43 @@ static void launch_rowfft2(aln_ctx *ctx, int n, int maxh)
     const size_t sm = (size_t)G * (padded(LL) + 2) * sizeof(float2);
     cudaFuncSetAttribute(k2_rowfft<LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     LAUNCH(ctx, "k2_rowfft", k2_rowfft<LL>, dim3((maxh + G - 1) / G, 2, n), thr, sm,
-           ctx->dpairs, ctx->tw, -1);
+           ctx->dpairs, ctx->tw, -1, (const int *)nullptr);
+}
+
+// spectrum-cache fills: b's rows and columns of the selected jobs -> X2
+template <int LL>
+static void launch_fill_rows(aln_ctx *ctx, int nsel, int maxh)
+{
+    constexpr int T = RegFFT<LL, -1>::T;
+    const int thr = rowfft_threads(T), G = thr / T;
+    const size_t sm = (size_t)G * (padded(LL) + 2) * sizeof(float2);
+    cudaFuncSetAttribute(k2_rowfft<LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    LAUNCH(ctx, "k2_rowfft", k2_rowfft<LL>, dim3((maxh + G - 1) / G, 1, nsel), thr, sm,
+           ctx->dpairs, ctx->tw, 1, (const int *)ctx->dsel);
 }
 
 template <int NY>
-static void launch_corrcol2(aln_ctx *ctx, int n, int L, int cached)
+static void launch_fill_cols(aln_ctx *ctx, int nsel, int L)
+{
+    constexpr int T = RegFFT<NY, -1>::T;
+    const int thr = std::max(256, T), G = thr / T;
+    const size_t sm = (size_t)G * padded(NY) * sizeof(float2);
+    cudaFuncSetAttribute(k2_colspec<NY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    LAUNCH(ctx, "k2_colspec", k2_colspec<NY>, dim3((L + 1 + G - 1) / G, nsel), thr, sm,
+           ctx->dpairs, ctx->tw, (const int *)ctx->dsel);
+}
+
+template <int NY>
+static void launch_corrcol2(aln_ctx *ctx, int n, int L, int cached, bool plain)
 {
     constexpr int T = RegFFT<NY, -1>::T;
     const int thr = std::max(256, T), G = thr / T;
     const size_t sm = (size_t)G * (padded(NY) + NY) * sizeof(float2);
-    cudaFuncSetAttribute(k2_corrcol<NY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    LAUNCH(ctx, "k2_corrcol", k2_corrcol<NY>, dim3((L + 1 + G - 1) / G, n), thr, sm,
-           ctx->dpairs, ctx->tw, cached);
+    void (*kern)(PairDev *, const float2 *, int) =
+        plain ? k2_corrcol<NY, true> : k2_corrcol<NY, false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    LAUNCH(ctx, "k2_corrcol", kern, dim3((L + 1 + G - 1) / G, n), thr, sm, ctx->dpairs, ctx->tw,
+           cached);
 }
 
 template <int LL>
@@ -1586,7 +1716,7 @@ static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int
     default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
     }
     switch (Ny) {
-#define X(v) case v: launch_corrcol2<v>(ctx, n, L, 0); break;
+#define X(v) case v: launch_corrcol2<v>(ctx, n, L, 0, mode == JOB_PATCHES); break;
         ALN_CASES_NY(X)
 #undef X
     default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "column length %d", Ny);
@@ -1645,10 +1775,36 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int par, char
         run_dst = nullptr;
         return ALN_OK;
     };
+    const bool reg_path = Nx / 2 >= 8 && Nx / 2 <= 4096 && Ny >= 8 && Ny <= 8192;
+    std::vector<int> fill;   // jobs whose b spectrum is computed into a new entry
+    int fill_maxh = 1;
+    ++ctx->spec_tick;
     for (int k = 0; k < n; ++k) {
         PairPlan &pl = *chunk[k];
         const aln_pair &P = *pl.src;
         work += carve(pl, work, P, &stage);
+        pl.d.b_cached = 0;
+        if (pl.key && reg_path && pl.d.mode != JOB_P2I && ctx->spec_cap > 0) {
+            const SpecKey K(pl.key_ns, pl.key, pl.d.Nx, pl.d.Ny, pl.d.transposed,
+                            pl.d.no_shift);
+            auto it = ctx->spec.find(K);
+            if (it != ctx->spec.end()) {
+                it->second.tick = ctx->spec_tick;
+                pl.d.b_cached = 1;
+                pl.d.X2 = it->second.X2;
+                ctx->spec_hits++;
+            } else {
+                const size_t bytes = al256((size_t)(pl.d.Nx / 2 + 1) * pl.d.Ny * sizeof(float2));
+                if (float2 *buf = spec_alloc(ctx, bytes)) {
+                    ctx->spec[K] = SpecEntry{buf, bytes, ctx->spec_tick};
+                    pl.d.b_cached = 1;
+                    pl.d.X2 = buf;
+                    fill.push_back(k);
+                    fill_maxh = std::max(fill_maxh, pl.d.h[1]);
+                    ctx->spec_fills++;
+                }
+            }
+        }
         const aln_image *im[2] = {&P.a, &P.b};
         for (int i = 0; i < 2; ++i) {
             if (pl.in_bytes[i]) {
@@ -1717,7 +1873,37 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int par, char
         LAUNCH(ctx, "k3_sat", k3_sat, dim3((maxw + 31) / 32, 2 * n), dim3(32, SAT_WARPS), 0,
                ctx->dpairs);
         LAUNCH(ctx, "k_mean", k_mean, dim3(2, n), 256, 0, ctx->dpairs);
-        LAUNCH(ctx, "k2_sat2", k2_sat2, dim3(maxslots, 2, n), 256, 0, ctx->dpairs);
+        if (maxw <= SAT2W_MAXW)
+            LAUNCH(ctx, "k2_sat2w", k2_sat2w, dim3((maxslots + 7) / 8, 2, n), 256, 0,
+                   ctx->dpairs);
+        else
+            LAUNCH(ctx, "k2_sat2", k2_sat2, dim3(maxslots, 2, n), 256, 0, ctx->dpairs);
+    }
+    if (!fill.empty()) {
+        if (fill.size() > ctx->dsel_cap) {
+            CK(cudaStreamSynchronize(st));
+            cudaFree(ctx->dsel);
+            ctx->dsel = nullptr;
+            ctx->dsel_cap = 0;
+            const size_t cap = std::max<size_t>(fill.size(), 4096);
+            CK(cudaMalloc(&ctx->dsel, cap * sizeof(int)));
+            ctx->dsel_cap = cap;
+        }
+        CK(cudaMemcpyAsync(ctx->dsel, fill.data(), fill.size() * sizeof(int),
+                           cudaMemcpyHostToDevice, st));
+        const int ns = (int)fill.size();
+        switch (L) {
+#define X(v) case v: launch_fill_rows<v>(ctx, ns, fill_maxh); break;
+            ALN_CASES_L(X)
+#undef X
+        default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
+        }
+        switch (Ny) {
+#define X(v) case v: launch_fill_cols<v>(ctx, ns, L); break;
+            ALN_CASES_NY(X)
+#undef X
+        default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "column length %d", Ny);
+        }
     }
     if (L >= 8 && L <= 4096 && Ny >= 8 && Ny <= 8192) {
         if (int rc = launch_fft_pipeline(ctx, L, Ny, n, maxh, maxWy, mode,
@@ -1789,7 +1975,7 @@ static int ensure_hres(aln_ctx *ctx, size_t n)
 // Runs CorrPatches (specs == NULL) or CorrImages jobs in chunks of equal FFT
 // size and job kind through the two-stage pipeline.
 static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const ImgSpec *specs,
-                      aln_result *out)
+                      aln_result *out, const unsigned long long *int_keys = nullptr)
 {
     if (!ctx || npairs < 0 || (npairs && (!pairs || !out)))
         return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
@@ -1798,6 +1984,8 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
     for (int k = 0; k < npairs; ++k) {
         plans[k].src = &pairs[k];
         plans[k].index = k;
+        plans[k].key_ns = int_keys ? 1 : 0;
+        plans[k].key = int_keys ? int_keys[k] : pairs[k].b_key;
         if (int rc = plan_pair(ctx, pairs[k], plans[k], specs == nullptr,
                                specs ? &specs[k] : nullptr))
             return rc;
@@ -1899,6 +2087,7 @@ extern "C" int aln_corr_images_batch(aln_ctx *ctx, int njobs, const aln_image_jo
         pairs[k].b = J.b;
         pairs[k].radius = 1 << 20;   // the whole R image; MaskA's oval is separate
         pairs[k].legal = J.legal;
+        pairs[k].b_key = J.b_key;
         specs[k].kind = J.kind == ALN_CORR_S ? 2 : 1;
         specs[k].mincor = J.mincor;
         specs[k].ox = J.ox;
@@ -2151,6 +2340,7 @@ extern "C" void aln_ctx_profile_reset(aln_ctx *ctx)
     ctx->prof_acc.clear();
     ctx->launches = 0;
     ctx->h2d_bytes = ctx->d2h_bytes = 0;
+    ctx->spec_hits = ctx->spec_fills = 0;
 }
 
 extern "C" int aln_ctx_profile(aln_ctx *ctx, int cap, const char **names,
@@ -2186,8 +2376,39 @@ extern "C" long long aln_ctx_counter(aln_ctx *ctx, int which)
     case 0: return ctx->launches;
     case 1: return ctx->h2d_bytes;
     case 2: return ctx->d2h_bytes;
+    case 3: return ctx->spec_hits;
+    case 4: return ctx->spec_fills;
+    case 5: return (long long)ctx->spec_bytes;
     default: return -1;
     }
+}
+
+extern "C" int aln_ctx_set_spectrum_cache(aln_ctx *ctx, size_t bytes)
+{
+    if (!ctx)
+        return ALN_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->spec_cap = bytes;
+    ++ctx->spec_tick;   // nothing is in use now: every entry may go
+    while (ctx->spec_bytes > bytes) {
+        if (!ctx->spec_free.empty()) {
+            auto g = std::prev(ctx->spec_free.end());
+            cudaFree(g->second);
+            ctx->spec_bytes -= g->first;
+            ctx->spec_free.erase(g);
+            continue;
+        }
+        if (ctx->spec.empty())
+            break;
+        auto lru = ctx->spec.begin();
+        for (auto it = ctx->spec.begin(); it != ctx->spec.end(); ++it)
+            if (it->second.tick < lru->second.tick)
+                lru = it;
+        ctx->spec_free.insert(std::make_pair(lru->second.bytes, lru->second.X2));
+        ctx->spec.erase(lru);
+    }
+    return ALN_OK;
 }
 
 extern "C" int aln_ctx_set_workspace_limit(aln_ctx *ctx, size_t bytes)

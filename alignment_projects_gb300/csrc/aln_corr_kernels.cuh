@@ -55,10 +55,15 @@ struct PairDev {
     float2 *T[2];       // row-pass output [kx][y], stride Ts[i]
     int Ts[2];
     float2 *X2;         // spectrum of image 1 (b): [kx][ky], stride Ny
+    int b_cached;       // 1: X2 holds b's spectrum already (a cache entry);
+                        // the row pass skips b and the column pass reads X2
     float2 *Q;          // column-inverse output [kx][j], j = y - ylo, stride Wy
     double *satS[2], *satQ[2];   // summed-area tables of v and v^2, [y][x] stride w
     int *satN[2];                // summed-area table of (v != 0)
     int sat_int;                 // bit i: image i's S, Q tables hold int64
+    int sat_nonly;               // 1: only the count table N is needed (S key alone)
+    int s_float;                 // S key alone: rr holds the FP32 correlation c,
+                                 // RowBest r/ssum/ssum2 are in c units (S = c / NxNy)
     double *segS[2], *segQ[2];   // per column-walk segment: exclusive column offsets
     int *segN[2];
     double *colsum[2];           // per-column totals (mean shift)

@@ -17,6 +17,17 @@
 
 __device__ __forceinline__ bool int_pixels(int dt) { return dt == ALN_U8 || dt == ALN_U16; }
 
+// s + e += x with the rounding error of the sum kept in e (Knuth's TwoSum;
+// explicit round-to-nearest operations, so nothing is contracted or reordered)
+__device__ __forceinline__ void two_sum_acc(float &s, float &e, float x)
+{
+    const float t = __fadd_rn(s, x);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(x, bp));
+    e = __fadd_rn(e, err);
+    s = t;
+}
+
 // Column prefix sums of v, v^2 and (v != 0) at the rows the lag window needs
 // (IntegrateImage's sums, 0_GEN/Correlation.cpp:49-105, restricted to the
 // rows IntegralTable will read).  grid (ceil(w/32), 2*npairs), block
@@ -27,7 +38,7 @@ __device__ __forceinline__ bool int_pixels(int dt) { return dt == ALN_U8 || dt =
 // otherwise.  Also writes the column totals (mean shift).
 #define SAT_WARPS 16
 
-template <typename TA, typename PIX>
+template <typename TA, typename PIX, bool SQ = true>
 __device__ __forceinline__ void sat_cols(const PairDev &p, int i, TA *shS, TA *shQ, int *shN)
 {
     const int w = p.w[i], h = p.h[i];
@@ -61,8 +72,10 @@ __device__ __forceinline__ void sat_cols(const PairDev &p, int i, TA *shS, TA *s
 #pragma unroll 8
             for (; y < stop; ++y) {
                 const TA v = (TA)__ldg(&col[y * st]);
-                s += v;
-                q += v * v;
+                if (SQ) {
+                    s += v;
+                    q += v * v;
+                }
                 if (want_n)
                     n += (v != 0);
             }
@@ -74,12 +87,14 @@ __device__ __forceinline__ void sat_cols(const PairDev &p, int i, TA *shS, TA *s
             const long long base = first ? (long long)(y - lo0) : (long long)(len0 + y - lo1);
             for (long long o = base * w + c; y <= rend; ++y, o += w) {
                 const TA v = (TA)__ldg(&col[y * st]);
-                s += v;
-                q += v * v;
+                if (SQ) {
+                    s += v;
+                    q += v * v;
+                    S[o] = s;
+                    Q[o] = q;
+                }
                 if (want_n)
                     n += (v != 0);
-                S[o] = s;
-                Q[o] = q;
                 N[o] = n;
             }
         }
@@ -97,11 +112,13 @@ __device__ __forceinline__ void sat_cols(const PairDev &p, int i, TA *shS, TA *s
         oq += shQ[g * 32 + tx];
         on += shN[g * 32 + tx];
     }
-    ((TA *)p.segS[i])[ty * w + c] = os;
-    ((TA *)p.segQ[i])[ty * w + c] = oq;
+    if (SQ) {
+        ((TA *)p.segS[i])[ty * w + c] = os;
+        ((TA *)p.segQ[i])[ty * w + c] = oq;
+        if (ty == SAT_WARPS - 1)
+            p.colsum[i][c] = (double)(os + s);
+    }
     p.segN[i][ty * w + c] = on;
-    if (ty == SAT_WARPS - 1)
-        p.colsum[i][c] = (double)(os + s);
 }
 
 __global__ void k3_sat(PairDev *pairs)
@@ -112,6 +129,17 @@ __global__ void k3_sat(PairDev *pairs)
     const int i = blockIdx.y & 1;
     if (p.status != 0 || blockIdx.x * 32 >= p.w[i])
         return;
+    if (p.sat_nonly) {   // counts only (CorrImagesS without a mincor)
+        if (p.cnt_kind != ALN_CNT_GT)
+            return;
+        switch (p.dt[i]) {
+        case ALN_U8: sat_cols<long long, uint8_t, false>(p, i, shS, shQ, shN); break;
+        case ALN_U16: sat_cols<long long, uint16_t, false>(p, i, shS, shQ, shN); break;
+        case ALN_F32: sat_cols<double, float, false>(p, i, (double *)shS, (double *)shQ, shN); break;
+        default: sat_cols<double, double, false>(p, i, (double *)shS, (double *)shQ, shN); break;
+        }
+        return;
+    }
     switch (p.dt[i]) {
     case ALN_U8:
         sat_cols<long long, uint8_t>(p, i, shS, shQ, shN);
@@ -329,6 +357,168 @@ __global__ void k2_sat2(PairDev *pairs)
         sat2_row<double>(p, i, slot, y, p.satS[i], p.satQ[i]);
 }
 
+// The same row pass with one warp per slot row (rows up to SAT2W_MAXW
+// columns): lane l owns a contiguous run of ceil(w/32) columns, the lane
+// totals are scanned with shuffles.  No block-wide synchronisation, so a
+// CTA carries eight rows and small images do not pay one CTA per row.
+#define SAT2W_MAXW 4096
+
+template <typename TA, bool SQ = true>
+__device__ __forceinline__ void sat2_row_warp(const PairDev &p, int i, int slot, int y, TA *S,
+                                              TA *Q, int lane)
+{
+    const int w = p.w[i];
+    const int seg = y / ((p.h[i] + SAT_WARPS - 1) / SAT_WARPS);
+    const TA *__restrict__ oS = (const TA *)p.segS[i] + (long long)seg * w;
+    const TA *__restrict__ oQ = (const TA *)p.segQ[i] + (long long)seg * w;
+    const int *__restrict__ oN = p.segN[i] + (long long)seg * w;
+    TA *__restrict__ rS = S + (long long)slot * w;
+    TA *__restrict__ rQ = Q + (long long)slot * w;
+    int *__restrict__ rN = p.satN[i] + (long long)slot * w;
+    const int per = (w + 31) >> 5;
+    const int c0 = lane * per, c1 = min(w, c0 + per);
+    TA s = 0, q = 0;
+    int n = 0;
+    for (int c = c0; c < c1; ++c) {
+        if (SQ) {
+            s += rS[c] + oS[c];
+            q += rQ[c] + oQ[c];
+            rS[c] = s;
+            rQ[c] = q;
+        }
+        n += rN[c] + oN[c];
+        rN[c] = n;
+    }
+    TA ts = s, tq = q;
+    int tn = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int c2 = __shfl_up_sync(0xffffffff, tn, o);
+        if (SQ) {
+            const TA a2 = __shfl_up_sync(0xffffffff, ts, o);
+            const TA b2 = __shfl_up_sync(0xffffffff, tq, o);
+            if (lane >= o) {
+                ts += a2;
+                tq += b2;
+            }
+        }
+        if (lane >= o)
+            tn += c2;
+    }
+    const TA os = ts - s, oq = tq - q;
+    const int on = tn - n;
+    if (lane == 0)
+        return;
+    for (int c = c0; c < c1; ++c) {
+        if (SQ) {
+            rS[c] += os;
+            rQ[c] += oq;
+        }
+        rN[c] += on;
+    }
+}
+
+// Register form of the warp row pass for rows up to 32*PER columns: each
+// lane loads its PER columns at once (unrolled), keeps the running sums in
+// registers and stores each element once.
+template <typename TA, bool SQ, int PER>
+__device__ __forceinline__ void sat2_row_reg(const PairDev &p, int i, int slot, int y, TA *S,
+                                             TA *Q, int lane)
+{
+    const int w = p.w[i];
+    const int seg = y / ((p.h[i] + SAT_WARPS - 1) / SAT_WARPS);
+    const TA *__restrict__ oS = (const TA *)p.segS[i] + (long long)seg * w;
+    const TA *__restrict__ oQ = (const TA *)p.segQ[i] + (long long)seg * w;
+    const int *__restrict__ oN = p.segN[i] + (long long)seg * w;
+    TA *__restrict__ rS = S + (long long)slot * w;
+    TA *__restrict__ rQ = Q + (long long)slot * w;
+    int *__restrict__ rN = p.satN[i] + (long long)slot * w;
+    const int c0 = lane * PER;
+    TA vs[PER], vq[PER];
+    int vn[PER];
+    TA s = 0, q = 0;
+    int n = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int c = c0 + k;
+        if (c < w) {
+            if (SQ) {
+                s += rS[c] + oS[c];
+                q += rQ[c] + oQ[c];
+            }
+            n += rN[c] + oN[c];
+        }
+        vs[k] = s;
+        vq[k] = q;
+        vn[k] = n;
+    }
+    TA ts = s, tq = q;
+    int tn = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int c2 = __shfl_up_sync(0xffffffff, tn, o);
+        if (SQ) {
+            const TA a2 = __shfl_up_sync(0xffffffff, ts, o);
+            const TA b2 = __shfl_up_sync(0xffffffff, tq, o);
+            if (lane >= o) {
+                ts += a2;
+                tq += b2;
+            }
+        }
+        if (lane >= o)
+            tn += c2;
+    }
+    const TA os = ts - s, oq = tq - q;
+    const int on = tn - n;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int c = c0 + k;
+        if (c < w) {
+            if (SQ) {
+                rS[c] = vs[k] + os;
+                rQ[c] = vq[k] + oq;
+            }
+            rN[c] = vn[k] + on;
+        }
+    }
+}
+
+template <typename TA, bool SQ>
+__device__ __forceinline__ void sat2_row_any(const PairDev &p, int i, int slot, int y, TA *S,
+                                             TA *Q, int lane)
+{
+    const int w = p.w[i];
+    if (w <= 128)
+        sat2_row_reg<TA, SQ, 4>(p, i, slot, y, S, Q, lane);
+    else if (w <= 256)
+        sat2_row_reg<TA, SQ, 8>(p, i, slot, y, S, Q, lane);
+    else if (w <= 512)
+        sat2_row_reg<TA, SQ, 16>(p, i, slot, y, S, Q, lane);
+    else
+        sat2_row_warp<TA, SQ>(p, i, slot, y, S, Q, lane);
+}
+
+// grid (ceil(maxslots / 8), 2, npairs), block 256: warp k takes slot 8*bx + k
+__global__ void k2_sat2w(PairDev *pairs)
+{
+    const PairDev &p = pairs[blockIdx.z];
+    const int i = blockIdx.y;
+    const int slot = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (p.status != 0 || slot >= nslots(p, i))
+        return;
+    const int len0 = p.need_hi[i][0] - p.need_lo[i][0] + 1;
+    const int y = slot < len0 ? p.need_lo[i][0] + slot : p.need_lo[i][1] + slot - len0;
+    const int lane = threadIdx.x & 31;
+    if (p.sat_nonly)
+        sat2_row_any<long long, false>(p, i, slot, y, (long long *)p.satS[i],
+                                       (long long *)p.satQ[i], lane);
+    else if (int_pixels(p.dt[i]))
+        sat2_row_any<long long, true>(p, i, slot, y, (long long *)p.satS[i],
+                                      (long long *)p.satQ[i], lane);
+    else
+        sat2_row_any<double, true>(p, i, slot, y, p.satS[i], p.satQ[i], lane);
+}
+
 // ---------------------------------------------------------------------------
 // forward rows
 // ---------------------------------------------------------------------------
@@ -339,15 +529,16 @@ __host__ __device__ constexpr int rowfft_threads(int T) { return T * 4 > 512 ? 5
 // Each team of RegFFT<L>::T threads transforms one row.  G = blockDim.x / T
 // rows per CTA; smem: G * (padded(L) + 2) float2 per CTA.
 template <int L>
-__global__ void k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img)
+__global__ void k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int *sel)
 {
     using F = RegFFT<L, -1>;
     constexpr int R = F::R, T = F::T;
     constexpr int G = rowfft_threads(T) / T;
     extern __shared__ float2 smem[];
-    PairDev &p = pairs[blockIdx.z];
+    // sel: the jobs of this launch are pairs[sel[z]] (spectrum-cache fills)
+    PairDev &p = pairs[sel ? sel[blockIdx.z] : blockIdx.z];
     const int i = only_img >= 0 ? only_img : blockIdx.y;
-    if (p.status != 0)
+    if (p.status != 0 || (i == 1 && p.b_cached && !sel))
         return;
     const int team = threadIdx.x / T, t = threadIdx.x - team * T;
     const int h = p.h[i], w = p.w[i], dt = p.dt[i];
@@ -439,7 +630,9 @@ __global__ void k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int onl
 // columns: forward b and a, product, inverse, window rows
 // ---------------------------------------------------------------------------
 
-template <int NY>
+// PLAIN: CorrPatches chunks (plain inverse only, no low-pass, no whitening),
+// compiled without the other jobs' branches.
+template <int NY, bool PLAIN>
 __global__ void __launch_bounds__(NY >= 8192 ? 512 : 256, NY >= 8192 ? 1 : 2)
 k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
 {
@@ -463,7 +656,7 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
     float2 va[R];
     {
         float2 vb[R];
-        if (use_cached_b) {
+        if (use_cached_b || p.b_cached) {
 #pragma unroll
             for (int r = 0; r < R; ++r)
                 vb[r] = p.X2[(long long)kxc * NY + t + r * T];
@@ -494,7 +687,8 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
 #pragma unroll
     for (int r = 0; r < R; ++r)
         va[r] = cmulc(sb[r * T + t], va[r]);   // X2 * conj(X1)
-    if (p.mode == JOB_P2I && p.p2i_filter) {
+    const bool is_p2i = !PLAIN && p.mode == JOB_P2I;
+    if (is_p2i && p.p2i_filter) {
         // CorrPatchToImage's low-pass (0_GEN/Correlation.cpp:1255-1283): the
         // reference names the row index "x" (wrapped) and the column "y"
 #pragma unroll
@@ -509,8 +703,8 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
     }
     // CorrPatches / CorrImagesR need the plain inverse; CorrImagesS the inverse
     // of the whitened product P / sqrt(|P|) (0_GEN/Correlation.cpp:2311-2317)
-    const bool want_r = p.mode == JOB_PATCHES || p.mode == JOB_P2I || p.want_r;
-    const bool want_s = p.want_s != 0;
+    const bool want_r = PLAIN || p.mode == JOB_PATCHES || is_p2i || p.want_r;
+    const bool want_s = !PLAIN && p.want_s != 0;
     if (want_r && want_s) {
 #pragma unroll
         for (int r = 0; r < R; ++r)
@@ -520,7 +714,7 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
     const int nnegy = p.h[0] - 1;
     if (want_r) {
         FI::run(va, sm, t, tw);
-        if (live && p.mode == JOB_P2I) {   // every storage row, in storage order
+        if (live && is_p2i) {   // every storage row, in storage order
             float2 *Q = p.Q + (long long)kx * NY;
 #pragma unroll
             for (int r = 0; r < R; ++r)
@@ -558,6 +752,45 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
                     Q[y - p.ylo] = va[r];
             }
         }
+    }
+}
+
+// Spectrum of image b alone into X2 (a cache entry): per column kx, the
+// column FFT of b's row-pass output, stored as k2_corrcol reads a cached
+// spectrum.  The same RegFFT code as the fused path, so the cached and the
+// recomputed spectra are the same numbers.  grid (ceil((L+1)/G), nsel): the
+// jobs are pairs[sel[y]].
+template <int NY>
+__global__ void __launch_bounds__(NY >= 8192 ? 512 : 256)
+k2_colspec(PairDev *pairs, const float2 *__restrict__ tw, const int *sel)
+{
+    using FF = RegFFT<NY, -1>;
+    constexpr int R = FF::R, T = FF::T;
+    extern __shared__ float2 smem[];
+    PairDev &p = pairs[sel[blockIdx.y]];
+    if (p.status != 0)
+        return;
+    const int L1 = (p.Nx >> 1) + 1;
+    const int G = blockDim.x / T;
+    const int team = threadIdx.x / T, t = threadIdx.x - team * T;
+    const int kx = blockIdx.x * G + team;
+    if (blockIdx.x * G >= L1)
+        return;
+    float2 *sm = smem + team * FF::SMEM;
+    const int kxc = kx < L1 ? kx : L1 - 1;
+    const float2 *Tb = p.T[1] + (long long)kxc * p.Ts[1];
+    const int hb = p.h[1];
+    float2 vb[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int y = t + r * T;
+        vb[r] = y < hb ? Tb[y] : make_float2(0.f, 0.f);
+    }
+    FF::run(vb, sm, t, tw);
+    if (kx < L1) {
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            p.X2[(long long)kx * NY + t + r * T] = vb[r];
     }
 }
 
@@ -748,7 +981,35 @@ __global__ void k2_lagimg(PairDev *pairs, const float2 *__restrict__ tw)
     const double inv = 1.0 / ((double)Nx * (double)Ny);
     double br = -1.0e30, ss = 0.0, ss2 = 0.0;
     long long bk = 0x7fffffffffffffffLL;
-    if (live) {
+    if (live && p.s_float) {
+        // S key alone: S = c / (Nx Ny) is strictly increasing in the FP32
+        // inverse value c, so the scan compares c itself (same argmax, same
+        // ties); the S statistics are compensated FP32 sums of c and c^2.
+        const int y = p.ylo + j, iy = y + p.cy;
+        float fs = 0.f, fe = 0.f, fq = 0.f, fqe = 0.f, bc = 0.f;
+        float *rf = (float *)p.rr + (long long)j * Wx - p.xlo;
+        for (int x = p.xlo + t; x <= p.xhi; x += T) {
+            const float c = CS[x < 0 ? x + Nx : x];
+            two_sum_acc(fs, fe, c);
+            const float c2 = __fmul_rn(c, c);
+            two_sum_acc(fq, fqe, c2);
+            fqe = __fadd_rn(fqe, __fmaf_rn(c, c, -c2));
+            rf[x] = c;
+            double rv;
+            const int ix = x + p.cx;
+            if (lag_eval(p, x, y, 0.0, false, rv) && oval_ok(p, ix, iy)) {
+                const long long key = (long long)iy * p.wR + ix;
+                if (bk == 0x7fffffffffffffffLL || c > bc || (c == bc && key < bk)) {
+                    bc = c;
+                    bk = key;
+                }
+            }
+        }
+        if (bk != 0x7fffffffffffffffLL)
+            br = (double)bc;
+        ss = (double)fs + (double)fe;
+        ss2 = (double)fq + (double)fqe;
+    } else if (live) {
         const int y = p.ylo + j, iy = y + p.cy;
         const bool keyS = p.mode == JOB_IMAGES_S;
         for (int x = p.xlo + t; x <= p.xhi; x += T) {
@@ -857,7 +1118,7 @@ __global__ void k_final_img(PairDev *pairs, ResultDev *res)
         ss2 += red_s2[q];
     }
     ResultDev &o = res[blockIdx.x];
-    if (br < -2.0) {
+    if (bk == 0x7fffffffffffffffLL) {   // no candidate lag
         p.status = ALN_NO_PEAK;
         o.r = o.dx = o.dy = 0.0;
         o.status = ALN_NO_PEAK;
@@ -866,18 +1127,23 @@ __global__ void k_final_img(PairDev *pairs, ResultDev *res)
     }
     const int wR = p.wR, hR = p.hR;
     const int ry = (int)(bk / wR), rx = (int)(bk - (long long)ry * wR);
-    const double *I = p.rr;   // the key image: the window is the whole R image
+    // the key image (the window is the whole R image); FP32 c when s_float:
+    // ParabPeak's ratios and the S score are the same in c units
+    const double *Id = p.rr;
+    const float *If = (const float *)p.rr;
+    const bool fl = p.s_float != 0;
+    auto I = [&](long long k) -> double { return fl ? (double)If[k] : Id[k]; };
     double xpk = rx, ypk = ry;
-    const double z1 = I[rx + (long long)wR * ry];
+    const double z1 = I(rx + (long long)wR * ry);
     double z0, z2;
-    if (rx - 1 >= 0 && rx + 1 < wR && (z0 = I[rx - 1 + (long long)wR * ry]) > 0.0 &&
-        (z2 = I[rx + 1 + (long long)wR * ry]) > 0.0) {
+    if (rx - 1 >= 0 && rx + 1 < wR && (z0 = I(rx - 1 + (long long)wR * ry)) > 0.0 &&
+        (z2 = I(rx + 1 + (long long)wR * ry)) > 0.0) {
         z0 = (z0 - z2) / (2 * (z0 + z2 - z1 - z1));
         if (fabs(z0) <= 8)
             xpk += z0;
     }
-    if (ry - 1 >= 0 && ry + 1 < hR && (z0 = I[rx + (long long)wR * (ry - 1)]) > 0.0 &&
-        (z2 = I[rx + (long long)wR * (ry + 1)]) > 0.0) {
+    if (ry - 1 >= 0 && ry + 1 < hR && (z0 = I(rx + (long long)wR * (ry - 1))) > 0.0 &&
+        (z2 = I(rx + (long long)wR * (ry + 1))) > 0.0) {
         z0 = (z0 - z2) / (2 * (z0 + z2 - z1 - z1));
         if (fabs(z0) <= 8)
             ypk += z0;

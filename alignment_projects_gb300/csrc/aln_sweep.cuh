@@ -17,6 +17,9 @@
 // One rotate-and-splat job: rotated A points -> FP32 raster [h1][w1].
 struct SplatJob {
     double t0, t1, t3, t4;   // linear part of C.T
+    long long T0, T1, T3, T4;   // the same in 2^-40 fixed point
+    float i00, i01, i10, i11;   // inverse of the linear part
+    float eu, ev;            // half-extents of the preimage of a 2 x 2 pixel square
     int L, B, w1, h1;        // bounding box of the rotated points
     float *out;
     const double *a;         // A values on the grid, a[x + stride*y]
@@ -24,84 +27,57 @@ struct SplatJob {
     int aw, ah, astride, ax0, ay0;
 };
 
-// grid (ceil(maxw/32), ceil(maxh/32), njobs), block 256.  Each CTA owns a
-// 32 x 32 tile of the output and gathers every grid point whose bilinear
-// footprint reaches it (inverse-rotated tile, +1 px), accumulating the four
-// weights (DistributePixel, 0_GEN/Maths.h:236-276) in shared memory.  The
-// accumulation is in 2^-32 fixed point with integer atomics, so the raster
-// does not depend on the order of the additions: the same transform always
-// gives the same raster, bit for bit, as the sweep's tie rules require.
-__device__ __forceinline__ void splat_add(unsigned long long *cell, float c)
-{
-    atomicAdd(cell, (unsigned long long)llrintf(c * 4294967296.0f));
-}
+#define SPLAT_FX 40   // fractional bits of the fixed-point coordinates
 
-__global__ void k_splat(const SplatJob *jobs)
+// grid (ceil(maxw/32), ceil(maxh/32), njobs), block 256: each thread gathers
+// four output pixels of a 32 x 32 tile.  A point p = (px, py) lands at
+// x = t0 px + t1 py - L, y = t3 px + t4 py - B and adds its value to the
+// pixels around it with the bilinear weights of DistributePixel
+// (0_GEN/Maths.h:236-276): pixel X receives the weight 1 - |x - X| when
+// |x - X| < 1 (that is 1 - alpha at floor(x), alpha at floor(x) + 1), and
+// the same in y.  Per pixel the candidate points are the grid points of the
+// preimage of the square (X +- 1, Y +- 1); the test itself runs in 2^-40
+// fixed point (exact integer arithmetic, 64-bit), the weights and the sum in
+// FP32 in a fixed order, so the same transform always gives the same raster
+// bit for bit, as the sweep's tie rules need.
+__global__ void __launch_bounds__(256) k_splat(const SplatJob *jobs)
 {
-    __shared__ unsigned long long tile[32][33];
     const SplatJob &J = jobs[blockIdx.z];
     const int tx0 = blockIdx.x * 32, ty0 = blockIdx.y * 32;
     if (tx0 >= J.w1 || ty0 >= J.h1)
         return;
-    for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x)
-        tile[e >> 5][e & 31] = 0ull;
-    __syncthreads();
-    // source range: inverse map of the rotated-frame rectangle covering the
-    // tile's footprint [tx0-1, tx0+32) x [ty0-1, ty0+32) (+ the box origin)
-    const double det = J.t0 * J.t4 - J.t1 * J.t3;
-    const double X0 = tx0 - 1 + J.L, X1 = tx0 + 32 + J.L;
-    const double Y0 = ty0 - 1 + J.B, Y1 = ty0 + 32 + J.B;
-    double umin = 1e300, umax = -1e300, vmin = 1e300, vmax = -1e300;
-    for (int c = 0; c < 4; ++c) {
-        const double X = (c & 1) ? X1 : X0, Y = (c & 2) ? Y1 : Y0;
-        const double u = (J.t4 * X - J.t1 * Y) / det;
-        const double v = (-J.t3 * X + J.t0 * Y) / det;
-        umin = fmin(umin, u);
-        umax = fmax(umax, u);
-        vmin = fmin(vmin, v);
-        vmax = fmax(vmax, v);
-    }
-    const int gx0 = max(0, (int)floor(umin) - 1 - J.ax0), gx1 = min(J.aw - 1, (int)ceil(umax) + 1 - J.ax0);
-    const int gy0 = max(0, (int)floor(vmin) - 1 - J.ay0), gy1 = min(J.ah - 1, (int)ceil(vmax) + 1 - J.ay0);
-    if (gx0 <= gx1 && gy0 <= gy1) {
-        const int nx = gx1 - gx0 + 1;
-        const int total = nx * (gy1 - gy0 + 1);
-        for (int e = threadIdx.x; e < total; e += blockDim.x) {
-            const int gy = gy0 + e / nx, gx = gx0 + (e - (e / nx) * nx);
-            if (J.mask && !J.mask[gx + (long long)J.astride * gy])
-                continue;
-            const double px = (double)(gx + J.ax0), py = (double)(gy + J.ay0);
-            // Apply_R_Part (TAffine.cpp:407-423) then the box shift
-            const double xr = __dadd_rn(__dmul_rn(px, J.t0), __dmul_rn(py, J.t1));
-            const double yr = __dadd_rn(__dmul_rn(px, J.t3), __dmul_rn(py, J.t4));
-            const double x = __dsub_rn(xr, (double)J.L), y = __dsub_rn(yr, (double)J.B);
-            const int ix = (int)floor(x), iy = (int)floor(y);
-            const float alpha = (float)__dsub_rn(x, (double)ix);
-            const float beta = (float)__dsub_rn(y, (double)iy);
-            const float val = (float)J.a[gx + (long long)J.astride * gy];
-            const int lx = ix - tx0, ly = iy - ty0;
-            if (ix >= 0 && ix < J.w1) {
-                if (iy >= 0 && iy < J.h1 && lx >= 0 && lx < 32 && ly >= 0 && ly < 32)
-                    splat_add(&tile[ly][lx], (1.0f - alpha) * (1.0f - beta) * val);
-                if (iy + 1 < J.h1 && iy + 1 >= 0 && lx >= 0 && lx < 32 && ly + 1 >= 0 && ly + 1 < 32)
-                    splat_add(&tile[ly + 1][lx], (1.0f - alpha) * beta * val);
-            }
-            if (ix + 1 >= 0 && ix + 1 < J.w1) {
-                if (iy >= 0 && iy < J.h1 && lx + 1 >= 0 && lx + 1 < 32 && ly >= 0 && ly < 32)
-                    splat_add(&tile[ly][lx + 1], alpha * (1.0f - beta) * val);
-                if (iy + 1 < J.h1 && iy + 1 >= 0 && lx + 1 >= 0 && lx + 1 < 32 && ly + 1 >= 0 &&
-                    ly + 1 < 32)
-                    splat_add(&tile[ly + 1][lx + 1], alpha * beta * val);
+    const long long ONE = 1ll << SPLAT_FX;
+    const float SCL = 1.0f / (float)(1ll << SPLAT_FX);
+    const int X = tx0 + (threadIdx.x & 31);
+    const int gx_lo = J.ax0, gx_hi = J.ax0 + J.aw - 1;
+    const int gy_lo = J.ay0, gy_hi = J.ay0 + J.ah - 1;
+    for (int k = 0; k < 4; ++k) {
+        const int Y = ty0 + (threadIdx.x >> 5) + 8 * k;
+        if (X >= J.w1 || Y >= J.h1)
+            continue;
+        const int Xa = X + J.L, Ya = Y + J.B;   // rotated-frame coordinates
+        const float uc = J.i00 * (float)Xa + J.i01 * (float)Ya;
+        const float vc = J.i10 * (float)Xa + J.i11 * (float)Ya;
+        const int u0 = max(gx_lo, (int)ceilf(uc - J.eu)), u1 = min(gx_hi, (int)floorf(uc + J.eu));
+        const int v0 = max(gy_lo, (int)ceilf(vc - J.ev)), v1 = min(gy_hi, (int)floorf(vc + J.ev));
+        const long long Xf = (long long)Xa << SPLAT_FX, Yf = (long long)Ya << SPLAT_FX;
+        float acc = 0.0f;
+        for (int v = v0; v <= v1; ++v) {
+            const long long bx = (long long)v * J.T1 - Xf, by = (long long)v * J.T4 - Yf;
+            const long long row = (long long)J.astride * (v - J.ay0) - J.ax0;
+            for (int u = u0; u <= u1; ++u) {
+                const long long dx = (long long)u * J.T0 + bx;
+                const long long dy = (long long)u * J.T3 + by;
+                if (dx <= -ONE || dx >= ONE || dy <= -ONE || dy >= ONE)
+                    continue;
+                if (J.mask && !J.mask[row + u])
+                    continue;
+                const float wx = (float)(ONE - (dx < 0 ? -dx : dx)) * SCL;
+                const float wy = (float)(ONE - (dy < 0 ? -dy : dy)) * SCL;
+                acc += wx * wy * (float)__ldg(&J.a[row + u]);
             }
         }
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
-        const int ly = e >> 5, lx = e & 31;
-        const int x = tx0 + lx, y = ty0 + ly;
-        if (x < J.w1 && y < J.h1)
-            J.out[(long long)y * J.w1 + x] =
-                (float)((double)(long long)tile[ly][lx] * (1.0 / 4294967296.0));
+        J.out[(long long)Y * J.w1 + X] = acc;
     }
 }
 
@@ -232,6 +208,7 @@ struct SweepCtx {
     size_t arena_cap = 0;
     SplatJob *djobs = nullptr;
     size_t djobs_cap = 0;
+    unsigned long long key_base = 0;   // thumbnail B of pair k: spectrum key key_base + k + 1
 };
 
 // RFromAngle (CThmScan.cpp:329-366) for a list of evaluations: one GPU batch.
@@ -244,6 +221,7 @@ static int eval_batch(SweepCtx &S, std::vector<Eval> &ev)
         std::vector<SplatJob> jobs(n);
         std::vector<aln_pair> pairs(n);
         std::vector<ImgSpec> specs(n);
+        std::vector<unsigned long long> keys(n);   // B's spectrum is reused across angles
         size_t bytes = 0;
         for (size_t k = 0; k < n; ++k) {
             Eval &E = ev[c0 + k];
@@ -265,6 +243,24 @@ static int eval_batch(SweepCtx &S, std::vector<Eval> &ev)
             J.t1 = C.T[1];
             J.t3 = C.T[3];
             J.t4 = C.T[4];
+            const double fx = (double)(1ll << SPLAT_FX);
+            J.T0 = llrint(J.t0 * fx);
+            J.T1 = llrint(J.t1 * fx);
+            J.T3 = llrint(J.t3 * fx);
+            J.T4 = llrint(J.t4 * fx);
+            {
+                const double det = J.t0 * J.t4 - J.t1 * J.t3;
+                const double m00 = J.t4 / det, m01 = -J.t1 / det;
+                const double m10 = -J.t3 / det, m11 = J.t0 / det;
+                J.i00 = (float)m00;
+                J.i01 = (float)m01;
+                J.i10 = (float)m10;
+                J.i11 = (float)m11;
+                // half-extents plus a margin for the FP32 centre (the exact
+                // test decides)
+                J.eu = (float)(fabs(m00) + fabs(m01)) + 1e-2f;
+                J.ev = (float)(fabs(m10) + fabs(m11)) + 1e-2f;
+            }
             double xlo = 1e300, xhi = -1e300, ylo = 1e300, yhi = -1e300;
             for (auto &h : tp.hull) {
                 const double px = (double)h.first, py = (double)h.second;
@@ -333,6 +329,7 @@ static int eval_batch(SweepCtx &S, std::vector<Eval> &ev)
             Pp.legal.rgn_area = tp.in->req_area;
             Pp.legal.cnt_kind = ALN_CNT_GT;
             Pp.legal.cnt_n = tp.in->req_area;
+            keys[k] = S.key_base + (unsigned long long)E.pair + 1;
             specs[k].kind = 2;
             specs[k].mincor = 0.0;
             specs[k].ox = S.P.ox;
@@ -346,7 +343,8 @@ static int eval_batch(SweepCtx &S, std::vector<Eval> &ev)
                S.djobs);
         CK(cudaGetLastError());
         std::vector<aln_result> res(n);
-        if (int rc = batch_impl(ctx, (int)n, pairs.data(), specs.data(), res.data()))
+        if (int rc = batch_impl(ctx, (int)n, pairs.data(), specs.data(), res.data(),
+                                keys.data()))
             return rc;
         for (size_t k = 0; k < n; ++k) {
             ThmRec &C = *ev[c0 + k].out;
@@ -646,6 +644,7 @@ extern "C" int aln_thm_search_batch(aln_ctx *ctx, int npairs, const aln_thumbs *
     S.ctx = ctx;
     S.P = *params;
     S.pairs.resize(npairs);
+    S.key_base = (++ctx->sweep_serial) << 32;
     // device copies of the thumbnails
     size_t bytes = 0;
     for (int k = 0; k < npairs; ++k) {
@@ -693,6 +692,7 @@ extern "C" int aln_thm_search_batch(aln_ctx *ctx, int npairs, const aln_thumbs *
         if (cudaMemcpyAsync(p, T.b.data, bb, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
             rc = set_err(ctx, ALN_ERR_CUDA, "thumbnail copy");
         p += al256(bb);
+        ctx->h2d_bytes += (long long)(ab + bb + (T.a_mask ? (size_t)T.a_stride * T.a_h : 0));
         make_hull(tp);
         if (tp.hull.empty())
             rc = set_err(ctx, ALN_ERR_ARG, "thumbnail pair %d: no A points", k);
@@ -758,6 +758,7 @@ extern "C" int aln_thm_search_batch(aln_ctx *ctx, int npairs, const aln_thumbs *
         }
     }
     cudaStreamSynchronize(ctx->stream);
+    spec_drop(ctx, 1, S.key_base, S.key_base + (unsigned long long)npairs + 1);
     cudaFree(S.arena);
     cudaFree(S.djobs);
     cudaFree(dbuf);

@@ -50,7 +50,7 @@ class AlnResult(C.Structure):
 class AlnImageJob(C.Structure):
     _fields_ = [("a", AlnImage), ("b", AlnImage), ("kind", C.c_int), ("legal", AlnLegal),
                 ("mincor", C.c_double), ("nbmaxht", C.c_double), ("ox", C.c_int),
-                ("oy", C.c_int), ("rx", C.c_int), ("ry", C.c_int)]
+                ("oy", C.c_int), ("rx", C.c_int), ("ry", C.c_int), ("b_key", C.c_ulonglong)]
 
 
 CORR_F, CORR_R, CORR_S = 0, 1, 2
@@ -104,7 +104,7 @@ def thumbs_from_points(pa, va, pb, vb, req_area, olap1d=0):
 
 class AlnPair(C.Structure):
     _fields_ = [("a", AlnImage), ("b", AlnImage), ("ox", C.c_int), ("oy", C.c_int),
-                ("radius", C.c_int), ("legal", AlnLegal)]
+                ("radius", C.c_int), ("legal", AlnLegal), ("b_key", C.c_ulonglong)]
 
 
 _lib = None
@@ -146,6 +146,7 @@ def lib():
         L.aln_ctx_counter.argtypes = [C.c_void_p, C.c_int]
         L.aln_ctx_counter.restype = C.c_longlong
         L.aln_ctx_set_workspace_limit.argtypes = [C.c_void_p, C.c_size_t]
+        L.aln_ctx_set_spectrum_cache.argtypes = [C.c_void_p, C.c_size_t]
         L.aln_parab_peak_fft.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
                                          C.c_void_p, C.c_int, C.c_int]
         _lib = L
@@ -240,7 +241,13 @@ class Context:
     def counters(self) -> dict:
         return {"launches": self._L.aln_ctx_counter(self.h, 0),
                 "h2d_bytes": self._L.aln_ctx_counter(self.h, 1),
-                "d2h_bytes": self._L.aln_ctx_counter(self.h, 2)}
+                "d2h_bytes": self._L.aln_ctx_counter(self.h, 2),
+                "spec_hits": self._L.aln_ctx_counter(self.h, 3),
+                "spec_fills": self._L.aln_ctx_counter(self.h, 4),
+                "spec_bytes": self._L.aln_ctx_counter(self.h, 5)}
+
+    def set_spectrum_cache(self, nbytes: int):
+        self._check(self._L.aln_ctx_set_spectrum_cache(self.h, nbytes))
 
     def set_workspace_limit(self, nbytes: int):
         self._check(self._L.aln_ctx_set_workspace_limit(self.h, nbytes))
@@ -296,7 +303,7 @@ class Context:
 
     def corr_images_batch(self, jobs) -> list:
         """jobs: dicts with kind, a, b, [legal, mincor, nbmaxht, ox, oy, rx, ry,
-        a_origin, b_origin]."""
+        a_origin, b_origin, b_key]."""
         jobs = list(jobs)
         arr = (AlnImageJob * len(jobs))()
         keep = []
@@ -312,6 +319,7 @@ class Context:
             arr[k].nbmaxht = j.get("nbmaxht", 0.75)
             arr[k].ox, arr[k].oy = j.get("ox", 0), j.get("oy", 0)
             arr[k].rx, arr[k].ry = j.get("rx", -1), j.get("ry", -1)
+            arr[k].b_key = j.get("b_key", 0)
         out = (AlnResult * len(jobs))()
         self._check(self._L.aln_corr_images_batch(self.h, len(jobs), arr, out))
         return [o.as_dict() for o in out]
@@ -337,7 +345,8 @@ class Context:
                  "T": list(o.T)} for o in out]
 
     def corr_patches_batch(self, pairs) -> list:
-        """pairs: iterable of dicts with a, b, [ox, oy, radius, legal, a_origin, b_origin]."""
+        """pairs: iterable of dicts with a, b, [ox, oy, radius, legal, a_origin, b_origin,
+        b_key (spectrum-cache key of b, 0 = none)]."""
         pairs = list(pairs)
         arr = (AlnPair * len(pairs))()
         keep = []
@@ -354,6 +363,7 @@ class Context:
             if lg is not None:
                 keep.append(lg)
                 arr[k].legal = lg
+            arr[k].b_key = p.get("b_key", 0)
         out = (AlnResult * len(pairs))()
         self._check(self._L.aln_corr_patches_batch(self.h, len(pairs), arr, out))
         return [o.as_dict() for o in out]

@@ -256,3 +256,50 @@ def montage_batch_torch(seed: int, n: int, device, long_side: int = 2048, wmin: 
         out.append(dict(a=a8, b=b8, truth=(-tx, -ty), decoy=decoy, ox=0, oy=0, radius=64,
                         lr=lr, W=W))
     return out
+
+
+def thumb_batch_torch(seed: int, n: int, device, tile: int = 2048, dec: int = 8,
+                      max_deg=10.0, max_t=30.0, noise=5.0):
+    """n cross-layer thumbnail pairs (as thumb_pair) generated with torch on
+    `device`: tile x tile tiles, B resampled at R(theta) p + t (bilinear),
+    gain U[0.9, 1.1], N(0, noise^2), both box-averaged by `dec`, then each
+    thumbnail normalised to mean 0, sample std 1 (MakeThumbs).  Pair i depends
+    only on (seed, i).  Returns dicts with FP64 tensors ta, tb (on `device`),
+    theta (deg) and t (full-resolution px)."""
+    import torch
+
+    out = []
+    pad = int(tile * 0.25) + int(max_t) + 4
+    size = tile + 2 * pad
+    k = torch.arange(tile, device=device, dtype=torch.float64)
+    yy, xx = torch.meshgrid(k, k, indexing="ij")
+    cx = cy = tile / 2.0
+    for i in range(n):
+        s = seed * 1000003 + i
+        rng = np.random.default_rng(s)
+        theta = float(rng.uniform(-max_deg, max_deg))
+        t = rng.uniform(-max_t, max_t, 2)
+        gain = float(rng.uniform(0.9, 1.1))
+        gen = torch.Generator(device=device)
+        gen.manual_seed(s)
+        f = field_torch(gen, size, size, device)
+        a = f[pad:pad + tile, pad:pad + tile]
+        c, sn = math.cos(math.radians(theta)), math.sin(math.radians(theta))
+        X = c * (xx - cx) - sn * (yy - cy) + cx + float(t[0]) + pad
+        Y = sn * (xx - cx) + c * (yy - cy) + cy + float(t[1]) + pad
+        x0 = X.floor().long().clamp(0, size - 2)
+        y0 = Y.floor().long().clamp(0, size - 2)
+        ax = (X - x0).clamp(0.0, 1.0)
+        ay = (Y - y0).clamp(0.0, 1.0)
+        b = ((1 - ax) * (1 - ay) * f[y0, x0] + ax * (1 - ay) * f[y0, x0 + 1]
+             + (1 - ax) * ay * f[y0 + 1, x0] + ax * ay * f[y0 + 1, x0 + 1])
+        b = gain * b + noise * torch.randn((tile, tile), generator=gen, device=device,
+                                           dtype=torch.float64)
+        m = tile // dec
+        ta = a.reshape(m, dec, m, dec).mean(dim=(1, 3)).float().double()
+        tb = b.reshape(m, dec, m, dec).mean(dim=(1, 3)).float().double()
+        ta = (ta - ta.mean()) / ta.std()
+        tb = (tb - tb.mean()) / tb.std()
+        out.append(dict(ta=ta.contiguous(), tb=tb.contiguous(), theta=theta,
+                        t=(float(t[0]), float(t[1]))))
+    return out

@@ -134,8 +134,21 @@ void aln_ctx_profile_reset(aln_ctx *ctx);
 int aln_ctx_profile(aln_ctx *ctx, int cap, const char **names, long long *launches,
                     double *ms);
 /* which: 0 = kernel launches, 1 = host-to-device bytes, 2 = device-to-host
- * bytes, counted since the last aln_ctx_profile_reset. */
+ * bytes, 3 = spectrum-cache hits, 4 = spectrum-cache fills (counted since
+ * the last aln_ctx_profile_reset), 5 = device bytes the cache holds. */
 long long aln_ctx_counter(aln_ctx *ctx, int which);
+
+/* Spectrum cache: the device-resident form of the reference's fft2 / ftc
+ * cache arguments (CorrPatches' `vector<CD> &fft2`, 0_GEN/Correlation.cpp:
+ * 901-915, 965-985; CorrImages' `ftc`, :3144-3290).  A job whose b_key is
+ * non-zero names image b: the first job with that key (for its FFT size and
+ * frame) stores b's spectrum in device memory, later jobs read it instead of
+ * transforming b again.  Equal keys must mean equal images b (the caller's
+ * promise, as in the reference, which reuses fft2 whenever its size
+ * matches).  Results are the same numbers with or without the cache.
+ * `bytes` bounds the device memory the cache holds (default 8 GiB; 0 turns
+ * it off and releases it); least recently used entries are evicted. */
+int aln_ctx_set_spectrum_cache(aln_ctx *ctx, size_t bytes);
 
 /* ---- FFT support: 0_GEN/Correlation.h:14-31 ------------------------- */
 
@@ -173,6 +186,7 @@ typedef struct aln_pair {
     aln_image a, b;
     int ox, oy, radius;
     aln_legal legal;
+    unsigned long long b_key;   /* != 0: image b's spectrum cache key (fft2) */
 } aln_pair;
 
 /* Many CorrPatches calls in one submission (pairs of any mix of sizes).
@@ -210,6 +224,7 @@ typedef struct aln_image_job {
     aln_legal legal;
     double mincor, nbmaxht;
     int ox, oy, rx, ry;
+    unsigned long long b_key;   /* != 0: image b's spectrum cache key (ftc) */
 } aln_image_job;
 
 /* CorrImagesR / CorrImagesS, 0_GEN/Correlation.cpp:3144-3199, 3222-3290 */

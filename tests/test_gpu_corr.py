@@ -239,3 +239,50 @@ def test_bad_arguments_raise(ctx):
     big = np.zeros((5000, 8), np.uint8)
     with pytest.raises(aln.AlnError):
         ctx.corr_patches(big, big)   # FFT size 16384 > 8192
+
+
+def test_spectrum_cache_same_numbers(ctx):
+    """Jobs sharing image b under one key (the reference's fft2 cache) give
+    exactly the results of uncached calls: the first job of a key fills the
+    entry, the rest (same batch and later batches) read it."""
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300 import synth
+    rng = np.random.default_rng(7)
+    b = synth.plain_pair(300, n=160, margin=12).b
+    pairs = []
+    for s in range(6):
+        a = synth.plain_pair(310 + s, n=150, margin=10).a
+        pairs.append(dict(a=a, b=b, ox=int(rng.integers(-5, 6)), oy=int(rng.integers(-5, 6)),
+                          radius=40, legal=aln.legal(aln.RGN_MIN, 16, 16, 0)))
+    # a wide pair (solved transposed) and a different-size pair under the same key
+    w = synth.montage_pair(21)
+    pairs.append(dict(a=w.a, b=w.b, ox=w.ox, oy=w.oy, radius=w.radius,
+                      legal=aln.legal(aln.RGN_SECTION, 1500, 1500, 30000)))
+    plain = ctx.corr_patches_batch(pairs)
+    ctx.profile_reset()
+    keyed = [dict(p, b_key=(99 if k < 6 else 100)) for k, p in enumerate(pairs)]
+    first = ctx.corr_patches_batch(keyed)
+    c1 = ctx.counters()
+    again = ctx.corr_patches_batch(keyed)
+    c2 = ctx.counters()
+    assert first == plain and again == plain
+    assert c1["spec_fills"] == 2 and c1["spec_hits"] == 5
+    assert c2["spec_fills"] == 2 and c2["spec_hits"] == 12
+
+
+def test_spectrum_cache_images_and_off(ctx):
+    """CorrImages jobs with a keyed b, and the cache switched off and on."""
+    import alignment_projects_gb300 as aln
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal((90, 110))
+    jobs = [dict(kind=aln.CORR_S if k % 2 else aln.CORR_R, a=rng.standard_normal((80, 70)),
+                 b=b, legal=aln.legal(aln.RGN_MIN, 0, 0, 400, aln.CNT_GT, 400))
+            for k in range(5)]
+    plain = ctx.corr_images_batch(jobs)
+    keyed = [dict(j, b_key=7) for j in jobs]
+    assert ctx.corr_images_batch(keyed) == plain
+    ctx.set_spectrum_cache(0)
+    assert ctx.counters()["spec_bytes"] == 0
+    assert ctx.corr_images_batch(keyed) == plain
+    ctx.set_spectrum_cache(1 << 30)
+    assert ctx.corr_images_batch(keyed) == plain
