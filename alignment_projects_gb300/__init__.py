@@ -8,6 +8,10 @@ Python host side of that ABI.
 from .native import (  # noqa: F401
     AlnError,
     Context,
+    Server,
+    REQ_PATCHES,
+    REQ_IMAGES,
+    REQ_SWEEP,
     legal,
     image,
     lib,

@@ -1235,7 +1235,7 @@ static inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // CorrImagesF/R/S parameters of a job (0_GEN/Correlation.h:159-220).
 struct ImgSpec {
-    int kind;   // 1 R, 2 S, 3 CorrPatchToImage
+    int kind;   // 0 CorrPatches (no spec), 1 R, 2 S, 3 CorrPatchToImage
     double mincor;
     int ox, oy, rx, ry;
     // CorrPatchToImage
@@ -1986,8 +1986,8 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
         plans[k].index = k;
         plans[k].key_ns = int_keys ? 1 : 0;
         plans[k].key = int_keys ? int_keys[k] : pairs[k].b_key;
-        if (int rc = plan_pair(ctx, pairs[k], plans[k], specs == nullptr,
-                               specs ? &specs[k] : nullptr))
+        const ImgSpec *sp = (specs && specs[k].kind != 0) ? &specs[k] : nullptr;
+        if (int rc = plan_pair(ctx, pairs[k], plans[k], sp == nullptr, sp))
             return rc;
     }
     // group by FFT size and job kind, keep submission order inside a group,
@@ -2583,3 +2583,4 @@ extern "C" int aln_corr_patches_noalloc(const aln_image *a, const aln_image *b, 
 }
 
 #include "aln_sweep.cuh"
+#include "aln_server.cuh"

@@ -107,6 +107,25 @@ class AlnPair(C.Structure):
                 ("radius", C.c_int), ("legal", AlnLegal), ("b_key", C.c_ulonglong)]
 
 
+class AlnServerParams(C.Structure):
+    _fields_ = [("device", C.c_int), ("workers", C.c_int), ("mem_budget", C.c_size_t),
+                ("max_batch", C.c_int), ("cache_bytes", C.c_size_t)]
+
+
+REQ_PATCHES, REQ_IMAGES, REQ_SWEEP = 0, 1, 2
+
+
+class AlnRequest(C.Structure):
+    _fields_ = [("kind", C.c_int), ("pair", AlnPair), ("job", AlnImageJob),
+                ("thumbs", AlnThumbs), ("thm", AlnThmParams), ("thm_mode", C.c_int),
+                ("ang0", C.c_double), ("hfang", C.c_double), ("step", C.c_double)]
+
+
+class AlnReply(C.Structure):
+    _fields_ = [("status", C.c_int), ("corr", AlnResult), ("sweep", AlnThmResult),
+                ("queue_ms", C.c_double), ("total_ms", C.c_double), ("batch_size", C.c_int)]
+
+
 _lib = None
 
 
@@ -149,6 +168,17 @@ def lib():
         L.aln_ctx_set_spectrum_cache.argtypes = [C.c_void_p, C.c_size_t]
         L.aln_parab_peak_fft.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
                                          C.c_void_p, C.c_int, C.c_int]
+        L.aln_server_create.argtypes = [C.POINTER(AlnServerParams), C.POINTER(C.c_void_p)]
+        L.aln_server_destroy.argtypes = [C.c_void_p]
+        L.aln_server_submit.argtypes = [C.c_void_p, C.POINTER(AlnRequest),
+                                        C.POINTER(C.c_ulonglong)]
+        L.aln_server_wait.argtypes = [C.c_void_p, C.c_ulonglong, C.c_int, C.POINTER(AlnReply)]
+        L.aln_server_collect.argtypes = [C.c_void_p, C.c_int, C.c_int,
+                                         C.POINTER(C.c_ulonglong), C.POINTER(AlnReply)]
+        L.aln_server_counter.argtypes = [C.c_void_p, C.c_int]
+        L.aln_server_counter.restype = C.c_longlong
+        L.aln_server_last_error.argtypes = [C.c_void_p]
+        L.aln_server_last_error.restype = C.c_char_p
         _lib = L
     return _lib
 
@@ -374,3 +404,127 @@ def parab_peak_fft(xpk, ypk, d, I):
     x, y = C.c_double(xpk), C.c_double(ypk)
     lib().aln_parab_peak_fft(C.byref(x), C.byref(y), d, I.ctypes.data, I.shape[1], I.shape[0])
     return x.value, y.value
+
+
+def _thm_params(rthresh=0.3, nbmaxht=0.75, pretweak=0, constxy=1, usecorrr=1,
+                disc=(0, 0, -1, -1), tdfm=None) -> AlnThmParams:
+    P = AlnThmParams()
+    P.rthresh, P.nbmaxht = rthresh, nbmaxht
+    P.constxy, P.pretweak, P.usecorrr = constxy, pretweak, usecorrr
+    P.ox, P.oy, P.rx, P.ry = disc
+    for i, v in enumerate(tdfm if tdfm is not None else (1, 0, 0, 0, 1, 0)):
+        P.tdfm[i] = v
+    return P
+
+
+def _reply_dict(rep: AlnReply, kind: int) -> dict:
+    d = {"status": rep.status, "queue_ms": rep.queue_ms, "total_ms": rep.total_ms,
+         "batch_size": rep.batch_size}
+    if kind == REQ_SWEEP:
+        o = rep.sweep
+        d.update({"A": o.A, "X": o.X, "Y": o.Y, "R": o.R, "err": o.err, "ncalls": o.ncalls,
+                  "T": list(o.T)})
+    else:
+        d.update(rep.corr.as_dict())
+        d["status"] = rep.status if rep.status < 0 else rep.corr.status
+    return d
+
+
+class Server:
+    """Continuous-batching request server (aln_server_* in include/aln_corr.h).
+
+    submit_* queue one request and return its ticket; wait(ticket) or
+    collect() hand the replies over.  Inputs stay referenced here until their
+    reply has been handed over."""
+
+    def __init__(self, device: int = 0, workers: int = 2, mem_budget: int = 0,
+                 max_batch: int = 0, cache_bytes: int = 0):
+        self._L = lib()
+        P = AlnServerParams(device, workers, mem_budget, max_batch, cache_bytes)
+        h = C.c_void_p()
+        rc = self._L.aln_server_create(C.byref(P), C.byref(h))
+        if rc != ALN_OK:
+            raise AlnError(rc, self._L.aln_last_error(None).decode())
+        self.h = h
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.aln_server_destroy(self.h)
+            self.h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _submit(self, req: AlnRequest, keep) -> int:
+        t = C.c_ulonglong()
+        rc = self._L.aln_server_submit(self.h, C.byref(req), C.byref(t))
+        if rc < 0:
+            raise AlnError(rc, "submit refused")
+        self._keep[t.value] = (req.kind, keep)
+        return t.value
+
+    def submit_patches(self, a, b, ox=0, oy=0, radius=4096, lg=None, b_key=0,
+                       a_origin=(0, 0), b_origin=(0, 0)) -> int:
+        req = AlnRequest()
+        req.kind = REQ_PATCHES
+        ia, ib = image(a, *a_origin), image(b, *b_origin)
+        req.pair.a, req.pair.b = ia, ib
+        req.pair.ox, req.pair.oy, req.pair.radius = ox, oy, radius
+        if lg is not None:
+            req.pair.legal = lg
+        req.pair.b_key = b_key
+        return self._submit(req, (ia, ib, lg))
+
+    def submit_images(self, kind, a, b, lg=None, mincor=0.0, ox=0, oy=0, rx=-1, ry=-1,
+                      b_key=0, a_origin=(0, 0), b_origin=(0, 0)) -> int:
+        req = AlnRequest()
+        req.kind = REQ_IMAGES
+        ia, ib = image(a, *a_origin), image(b, *b_origin)
+        j = req.job
+        j.a, j.b, j.kind = ia, ib, kind
+        if lg is not None:
+            j.legal = lg
+        j.mincor, j.nbmaxht = mincor, 0.75
+        j.ox, j.oy, j.rx, j.ry = ox, oy, rx, ry
+        j.b_key = b_key
+        return self._submit(req, (ia, ib, lg))
+
+    def submit_sweep(self, thumbs: AlnThumbs, mode=0, ang0=0.0, hfang=10.0, step=0.5,
+                     **params) -> int:
+        req = AlnRequest()
+        req.kind = REQ_SWEEP
+        req.thumbs = thumbs
+        req.thm = _thm_params(**params)
+        req.thm_mode, req.ang0, req.hfang, req.step = mode, ang0, hfang, step
+        return self._submit(req, (thumbs,))
+
+    def wait(self, ticket: int, timeout_ms: int = -1) -> dict:
+        rep = AlnReply()
+        rc = self._L.aln_server_wait(self.h, ticket, timeout_ms, C.byref(rep))
+        if rc < 0:
+            raise AlnError(rc, "wait")
+        kind, _ = self._keep.pop(ticket)
+        return _reply_dict(rep, kind)
+
+    def collect(self, cap: int = 4096, timeout_ms: int = 100) -> list:
+        """Up to cap finished replies as (ticket, reply dict)."""
+        tk = (C.c_ulonglong * cap)()
+        reps = (AlnReply * cap)()
+        n = self._L.aln_server_collect(self.h, cap, timeout_ms, tk, reps)
+        if n < 0:
+            raise AlnError(n, "collect")
+        out = []
+        for i in range(n):
+            kind, _ = self._keep.pop(tk[i])
+            out.append((tk[i], _reply_dict(reps[i], kind)))
+        return out
+
+    def counters(self) -> dict:
+        c = self._L.aln_server_counter
+        return {"submitted": c(self.h, 0), "finished": c(self.h, 1), "batches": c(self.h, 2),
+                "waiting": c(self.h, 3), "spec_hits": c(self.h, 4)}

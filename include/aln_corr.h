@@ -320,6 +320,77 @@ int aln_corr_patches_noalloc(const aln_image *a, const aln_image *b, int ox, int
                              int radius, const aln_legal *legal, void *stream,
                              aln_result *out);
 
+/* ---- serving: continuous batching of pair-match requests -------------
+ * No reference counterpart (the reference calls the correlator once per
+ * pair from its worker threads, 0_GEN/CThmScan.cpp:67-107,
+ * 1_DMesh/InSectionOverlap.cpp:190).
+ *
+ * A server owns `workers` host threads, each with its own context (CUDA
+ * streams and workspace) on one device.  Requests wait in one FIFO queue.
+ * Whenever a worker is free it takes every waiting request it can admit --
+ * up to max_batch requests whose planned device workspace fits its share of
+ * mem_budget -- and runs them as one batch; requests that arrive meanwhile
+ * form the next batch, and the workers' batches run on the device at the
+ * same time.  Sweep requests (ALN_REQ_SWEEP) are batched with each other.
+ * A request's result does not depend on the batch it ran in: every job of a
+ * batch is computed by the same kernels on its own data.
+ *
+ * The caller keeps every buffer a request points to alive and unchanged
+ * until its reply has been read.  Image b of a request may carry a spectrum
+ * key (aln_pair.b_key, aln_image_job.b_key): each worker keeps such spectra
+ * resident (cache_bytes per worker) for reuse by later requests. */
+typedef struct aln_server aln_server;
+
+typedef struct aln_server_params {
+    int device;
+    int workers;          /* batches in flight on the device (0: 2) */
+    size_t mem_budget;    /* device bytes for request workspaces, all workers
+                             together (0: half of the free device memory, at most 16 GiB) */
+    int max_batch;        /* requests per batch (0: 4096) */
+    size_t cache_bytes;   /* spectrum cache per worker (0: 2 GiB) */
+} aln_server_params;
+
+enum { ALN_REQ_PATCHES = 0, ALN_REQ_IMAGES = 1, ALN_REQ_SWEEP = 2 };
+
+typedef struct aln_request {
+    int kind;                 /* ALN_REQ_* */
+    aln_pair pair;            /* ALN_REQ_PATCHES: CorrPatches */
+    aln_image_job job;        /* ALN_REQ_IMAGES: CorrImagesR/S */
+    aln_thumbs thumbs;        /* ALN_REQ_SWEEP: one CThmScan search ... */
+    aln_thm_params thm;       /* ... with these settings */
+    int thm_mode;             /* ALN_THM_* */
+    double ang0, hfang, step;
+} aln_request;
+
+typedef struct aln_reply {
+    int status;               /* ALN_OK, or the request's negative error */
+    aln_result corr;          /* ALN_REQ_PATCHES / ALN_REQ_IMAGES */
+    aln_thm_result sweep;     /* ALN_REQ_SWEEP */
+    double queue_ms;          /* submission -> its batch started */
+    double total_ms;          /* submission -> result ready */
+    int batch_size;           /* requests in that batch */
+} aln_reply;
+
+int aln_server_create(const aln_server_params *params, aln_server **out);
+/* Stops the workers after their current batch; requests still waiting are
+ * answered ALN_ERR_CANCELLED. */
+void aln_server_destroy(aln_server *s);
+/* Queue one request; *ticket identifies its reply.  ALN_ERR_REFUSED once
+ * the server is stopping. */
+int aln_server_submit(aln_server *s, const aln_request *req, unsigned long long *ticket);
+/* Wait up to timeout_ms (< 0: no limit) for the reply of `ticket`; the reply
+ * is handed over once (a second wait returns ALN_ERR_ARG).  ALN_ERR_TIMEOUT
+ * if it is not ready in time. */
+int aln_server_wait(aln_server *s, unsigned long long ticket, int timeout_ms, aln_reply *out);
+/* Hand over up to `cap` finished replies (any tickets), waiting up to
+ * timeout_ms for the first; returns how many. */
+int aln_server_collect(aln_server *s, int cap, int timeout_ms, unsigned long long *tickets,
+                       aln_reply *out);
+/* which: 0 requests submitted, 1 finished, 2 batches run, 3 waiting now,
+ * 4 spectrum-cache hits (all workers). */
+long long aln_server_counter(aln_server *s, int which);
+const char *aln_server_last_error(aln_server *s);
+
 #ifdef __cplusplus
 }
 #endif
