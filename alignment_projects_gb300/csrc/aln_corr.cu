@@ -1691,14 +1691,14 @@ static void launch_lagp2i(aln_ctx *ctx, int n, int maxWy)
 }
 
 template <int LL>
-static void launch_lagimg2(aln_ctx *ctx, int n, int maxWy, bool both)
+static void launch_lagimg2(aln_ctx *ctx, int n, int maxWy, bool both, bool sonly)
 {
     constexpr int T = RegFFT<LL, +1>::T;
     const int thr = std::max(256, T), G = thr / T;
     const size_t sm = (size_t)G * (padded(LL) + 2) * (both ? 2 : 1) * sizeof(float2);
-    cudaFuncSetAttribute(k2_lagimg<LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    LAUNCH(ctx, "k2_lagimg", k2_lagimg<LL>, dim3((maxWy + G - 1) / G, n), thr, sm, ctx->dpairs,
-           ctx->tw);
+    void (*kern)(PairDev *, const float2 *) = sonly ? k2_lagimg<LL, true> : k2_lagimg<LL, false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    LAUNCH(ctx, "k2_lagimg", kern, dim3((maxWy + G - 1) / G, n), thr, sm, ctx->dpairs, ctx->tw);
 }
 
 #define ALN_CASES_L(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
@@ -1707,7 +1707,7 @@ static void launch_lagimg2(aln_ctx *ctx, int n, int maxWy, bool both)
 // register-FFT pipeline for one chunk: rows (both images), fused columns,
 // lag rows.  L = Nx/2 in [16, 4096], Ny in [16, 8192].
 static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int maxWy,
-                               int mode = JOB_PATCHES, bool both = false)
+                               int mode = JOB_PATCHES, bool both = false, bool sonly = false)
 {
     switch (L) {
 #define X(v) case v: launch_rowfft2<v>(ctx, n, maxh); break;
@@ -1737,7 +1737,7 @@ static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int
         }
     } else {
         switch (L) {
-#define X(v) case v: launch_lagimg2<v>(ctx, n, maxWy, both); break;
+#define X(v) case v: launch_lagimg2<v>(ctx, n, maxWy, both, sonly); break;
             ALN_CASES_L(X)
 #undef X
         default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
@@ -1907,7 +1907,7 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int par, char
     }
     if (L >= 8 && L <= 4096 && Ny >= 8 && Ny <= 8192) {
         if (int rc = launch_fft_pipeline(ctx, L, Ny, n, maxh, maxWy, mode,
-                                         hd[0].want_r && hd[0].want_s))
+                                         hd[0].want_r && hd[0].want_s, hd[0].s_float != 0))
             return rc;
     } else if (mode != JOB_PATCHES) {
         return set_err(ctx, ALN_ERR_UNSUPPORTED, "CorrImages FFT size %d x %d", Nx, Ny);
@@ -1974,8 +1974,14 @@ static int ensure_hres(aln_ctx *ctx, size_t n)
 
 // Runs CorrPatches (specs == NULL) or CorrImages jobs in chunks of equal FFT
 // size and job kind through the two-stage pipeline.
+// spectrum key of a job's image b: namespace (0 caller, 1 library) and key
+struct JobKey {
+    int ns;
+    unsigned long long key;
+};
+
 static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const ImgSpec *specs,
-                      aln_result *out, const unsigned long long *int_keys = nullptr)
+                      aln_result *out, const JobKey *keys = nullptr)
 {
     if (!ctx || npairs < 0 || (npairs && (!pairs || !out)))
         return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
@@ -1984,8 +1990,8 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
     for (int k = 0; k < npairs; ++k) {
         plans[k].src = &pairs[k];
         plans[k].index = k;
-        plans[k].key_ns = int_keys ? 1 : 0;
-        plans[k].key = int_keys ? int_keys[k] : pairs[k].b_key;
+        plans[k].key_ns = keys ? keys[k].ns : 0;
+        plans[k].key = keys ? keys[k].key : pairs[k].b_key;
         const ImgSpec *sp = (specs && specs[k].kind != 0) ? &specs[k] : nullptr;
         if (int rc = plan_pair(ctx, pairs[k], plans[k], sp == nullptr, sp))
             return rc;

@@ -798,6 +798,28 @@ k2_colspec(PairDev *pairs, const float2 *__restrict__ tw, const int *sel)
 // lag rows
 // ---------------------------------------------------------------------------
 
+// The L+1 spectrum bins of lag row jc (Q is [kx][j], stride Wy) into the
+// team's shared row: all of a thread's loads are issued before the first
+// store, so their latencies overlap.
+template <int L, int T>
+__device__ __forceinline__ void load_lag_row(float2 *dst, const float2 *__restrict__ Q, int Wy,
+                                             int jc, int t)
+{
+    constexpr int K = L / T + 1;
+    float2 v[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+        const int k = t + q * T;
+        v[q] = k <= L ? __ldg(&Q[(long long)k * Wy + jc]) : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+        const int k = t + q * T;
+        if (k <= L)
+            dst[padi(k)] = v[q];
+    }
+}
+
 template <int L>
 __global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
 {
@@ -822,8 +844,7 @@ __global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
     float2 *sm = smem + team * PITCH;
     const int Nx = p.Nx, Ny = p.Ny;
     // spectrum bins of this lag row (strided over kx)
-    for (int k = t; k <= L; k += T)
-        sm[padi(k)] = p.Q[(long long)k * Wy + jc];
+    load_lag_row<L, T>(sm, p.Q, Wy, jc, t);
     __syncthreads();
     float2 v[R];
 #pragma unroll
@@ -910,8 +931,10 @@ __global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
 // R rows (plain product), S and R per lag, A = legality & oval (& R > mincor),
 // the row's best candidate (key S or R; ties -> smallest R-image index) and
 // the row's S sums.
-template <int L>
-__global__ void k2_lagimg(PairDev *pairs, const float2 *__restrict__ tw)
+// SONLY: chunks of S-key jobs without a mincor (the sweep's correlator):
+// one inverse per row and the FP32-key scan only, compiled without the rest.
+template <int L, bool SONLY>
+__global__ void __launch_bounds__(256, 2) k2_lagimg(PairDev *pairs, const float2 *__restrict__ tw)
 {
     using F = RegFFT<L, +1>;
     constexpr int R = F::R, T = F::T;
@@ -931,11 +954,12 @@ __global__ void k2_lagimg(PairDev *pairs, const float2 *__restrict__ tw)
     const int j = j0 + team;
     const bool live = j < Wy;
     const int jc = live ? j : Wy - 1;
-    const bool want_r = p.want_r != 0, want_s = p.want_s != 0;
+    const bool want_r = !SONLY && p.want_r != 0, want_s = SONLY || p.want_s != 0;
     const bool both = want_r && want_s;
     float2 *sm = smem + team * PITCH * (both ? 2 : 1);
     const int Nx = p.Nx, Ny = p.Ny;
     const float *CS = nullptr, *CR = nullptr;
+#pragma unroll 1
     for (int pass = 0; pass < 2; ++pass) {
         const bool doS = pass == 0;
         if ((doS && !want_s) || (!doS && !want_r))
@@ -943,8 +967,7 @@ __global__ void k2_lagimg(PairDev *pairs, const float2 *__restrict__ tw)
         const float2 *Qs = doS ? (both ? p.Q2 : p.Q) : p.Q;
         float2 *reg = sm + ((both && !doS) ? PITCH : 0);
         __syncthreads();
-        for (int k = t; k <= L; k += T)
-            reg[padi(k)] = Qs[(long long)k * Wy + jc];
+        load_lag_row<L, T>(reg, Qs, Wy, jc, t);
         __syncthreads();
         float2 v[R];
 #pragma unroll
@@ -981,7 +1004,7 @@ __global__ void k2_lagimg(PairDev *pairs, const float2 *__restrict__ tw)
     const double inv = 1.0 / ((double)Nx * (double)Ny);
     double br = -1.0e30, ss = 0.0, ss2 = 0.0;
     long long bk = 0x7fffffffffffffffLL;
-    if (live && p.s_float) {
+    if (live && (SONLY || p.s_float)) {
         // S key alone: S = c / (Nx Ny) is strictly increasing in the FP32
         // inverse value c, so the scan compares c itself (same argmax, same
         // ties); the S statistics are compensated FP32 sums of c and c^2.
@@ -995,13 +1018,14 @@ __global__ void k2_lagimg(PairDev *pairs, const float2 *__restrict__ tw)
             two_sum_acc(fq, fqe, c2);
             fqe = __fadd_rn(fqe, __fmaf_rn(c, c, -c2));
             rf[x] = c;
-            double rv;
-            const int ix = x + p.cx;
-            if (lag_eval(p, x, y, 0.0, false, rv) && oval_ok(p, ix, iy)) {
-                const long long key = (long long)iy * p.wR + ix;
-                if (bk == 0x7fffffffffffffffLL || c > bc || (c == bc && key < bk)) {
+            // legality only for a lag that would become this thread's best
+            // (its lags come in increasing key order: a tie never wins)
+            if (bk == 0x7fffffffffffffffLL || c > bc) {
+                double rv;
+                const int ix = x + p.cx;
+                if (lag_eval(p, x, y, 0.0, false, rv) && oval_ok(p, ix, iy)) {
                     bc = c;
-                    bk = key;
+                    bk = (long long)iy * p.wR + ix;
                 }
             }
         }
@@ -1009,7 +1033,7 @@ __global__ void k2_lagimg(PairDev *pairs, const float2 *__restrict__ tw)
             br = (double)bc;
         ss = (double)fs + (double)fe;
         ss2 = (double)fq + (double)fqe;
-    } else if (live) {
+    } else if (!SONLY && live) {
         const int y = p.ylo + j, iy = y + p.cy;
         const bool keyS = p.mode == JOB_IMAGES_S;
         for (int x = p.xlo + t; x <= p.xhi; x += T) {
@@ -1199,8 +1223,7 @@ __global__ void k2_lagp2i(PairDev *pairs, const float2 *__restrict__ tw)
     const bool live = j < Wy;
     const int jc = live ? j : Wy - 1;
     float2 *sm = smem + team * PITCH;
-    for (int k = t; k <= L; k += T)
-        sm[padi(k)] = p.Q[(long long)k * Wy + jc];
+    load_lag_row<L, T>(sm, p.Q, Wy, jc, t);
     __syncthreads();
     float2 v[R];
 #pragma unroll

@@ -62,12 +62,14 @@ __global__ void __launch_bounds__(256) k_splat(const SplatJob *jobs)
         const int v0 = max(gy_lo, (int)ceilf(vc - J.ev)), v1 = min(gy_hi, (int)floorf(vc + J.ev));
         const long long Xf = (long long)Xa << SPLAT_FX, Yf = (long long)Ya << SPLAT_FX;
         float acc = 0.0f;
-        for (int v = v0; v <= v1; ++v) {
-            const long long bx = (long long)v * J.T1 - Xf, by = (long long)v * J.T4 - Yf;
+        // (dx, dy) = fixed-point offset of point (u, v) from the pixel,
+        // stepped exactly: +T0/+T3 per u, +T1/+T4 per v
+        long long rx = (long long)u0 * J.T0 + (long long)v0 * J.T1 - Xf;
+        long long ry = (long long)u0 * J.T3 + (long long)v0 * J.T4 - Yf;
+        for (int v = v0; v <= v1; ++v, rx += J.T1, ry += J.T4) {
             const long long row = (long long)J.astride * (v - J.ay0) - J.ax0;
-            for (int u = u0; u <= u1; ++u) {
-                const long long dx = (long long)u * J.T0 + bx;
-                const long long dy = (long long)u * J.T3 + by;
+            long long dx = rx, dy = ry;
+            for (int u = u0; u <= u1; ++u, dx += J.T0, dy += J.T3) {
                 if (dx <= -ONE || dx >= ONE || dy <= -ONE || dy >= ONE)
                     continue;
                 if (J.mask && !J.mask[row + u])
@@ -208,7 +210,8 @@ struct SweepCtx {
     size_t arena_cap = 0;
     SplatJob *djobs = nullptr;
     size_t djobs_cap = 0;
-    unsigned long long key_base = 0;   // thumbnail B of pair k: spectrum key key_base + k + 1
+    unsigned long long key_base = 0;   // thumbnail B of pair k without a caller key:
+                                       // library key key_base + k + 1
 };
 
 // RFromAngle (CThmScan.cpp:329-366) for a list of evaluations: one GPU batch.
@@ -221,7 +224,7 @@ static int eval_batch(SweepCtx &S, std::vector<Eval> &ev)
         std::vector<SplatJob> jobs(n);
         std::vector<aln_pair> pairs(n);
         std::vector<ImgSpec> specs(n);
-        std::vector<unsigned long long> keys(n);   // B's spectrum is reused across angles
+        std::vector<JobKey> keys(n);   // B's spectrum is reused across angles (and calls)
         size_t bytes = 0;
         for (size_t k = 0; k < n; ++k) {
             Eval &E = ev[c0 + k];
@@ -329,7 +332,10 @@ static int eval_batch(SweepCtx &S, std::vector<Eval> &ev)
             Pp.legal.rgn_area = tp.in->req_area;
             Pp.legal.cnt_kind = ALN_CNT_GT;
             Pp.legal.cnt_n = tp.in->req_area;
-            keys[k] = S.key_base + (unsigned long long)E.pair + 1;
+            if (tp.in->b_key)
+                keys[k] = JobKey{0, tp.in->b_key};
+            else
+                keys[k] = JobKey{1, S.key_base + (unsigned long long)E.pair + 1};
             specs[k].kind = 2;
             specs[k].mincor = 0.0;
             specs[k].ox = S.P.ox;

@@ -60,7 +60,7 @@ THM_DENOVO, THM_RFROMANGLE, THM_PRIOR, THM_SCAN_HUNT, THM_SCAN_MAXR = 0, 1, 2, 3
 class AlnThumbs(C.Structure):
     _fields_ = [("a", C.c_void_p), ("a_mask", C.c_void_p), ("a_w", C.c_int), ("a_h", C.c_int),
                 ("a_stride", C.c_int), ("a_x0", C.c_int), ("a_y0", C.c_int), ("b", AlnImage),
-                ("req_area", C.c_longlong), ("olap1d", C.c_int)]
+                ("req_area", C.c_longlong), ("olap1d", C.c_int), ("b_key", C.c_ulonglong)]
 
 
 class AlnThmParams(C.Structure):

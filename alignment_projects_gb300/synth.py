@@ -303,3 +303,66 @@ def thumb_batch_torch(seed: int, n: int, device, tile: int = 2048, dec: int = 8,
         out.append(dict(ta=ta.contiguous(), tb=tb.contiguous(), theta=theta,
                         t=(float(t[0]), float(t[1]))))
     return out
+
+
+def neighbour_group_torch(seed: int, k: int, device, tile: int = 2048, dec: int = 8,
+                          max_deg=10.0, max_t=30.0, noise=5.0):
+    """One tile B and k neighbours A_1..A_k of it (different offsets of one
+    field), as 256^2-class thumbnails: B is the field resampled at
+    R(theta) p + t_B (bilinear, gain, noise), each A_i the field shifted by
+    its own u_i in [-max_t, max_t]^2.  All box-averaged by `dec` and
+    normalised (MakeThumbs).  Returns (tb, [ta_1..ta_k], theta) as FP64
+    numpy arrays on the host."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    theta = float(rng.uniform(-max_deg, max_deg))
+    t = rng.uniform(-max_t, max_t, 2)
+    u = rng.uniform(-max_t, max_t, (k, 2))
+    gain = float(rng.uniform(0.9, 1.1))
+    pad = int(tile * 0.25) + 2 * int(max_t) + 4
+    size = tile + 2 * pad
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    f = field_torch(gen, size, size, device)
+    kk = torch.arange(tile, device=device, dtype=torch.float64)
+    yy, xx = torch.meshgrid(kk, kk, indexing="ij")
+    c, sn = math.cos(math.radians(theta)), math.sin(math.radians(theta))
+    cx = cy = tile / 2.0
+    X = c * (xx - cx) - sn * (yy - cy) + cx + float(t[0]) + pad
+    Y = sn * (xx - cx) + c * (yy - cy) + cy + float(t[1]) + pad
+    x0 = X.floor().long().clamp(0, size - 2)
+    y0 = Y.floor().long().clamp(0, size - 2)
+    ax = (X - x0).clamp(0.0, 1.0)
+    ay = (Y - y0).clamp(0.0, 1.0)
+    b = ((1 - ax) * (1 - ay) * f[y0, x0] + ax * (1 - ay) * f[y0, x0 + 1]
+         + (1 - ax) * ay * f[y0 + 1, x0] + ax * ay * f[y0 + 1, x0 + 1])
+    b = gain * b + noise * torch.randn((tile, tile), generator=gen, device=device,
+                                       dtype=torch.float64)
+    m = tile // dec
+
+    def thumb(img):
+        th = img.reshape(m, dec, m, dec).mean(dim=(1, 3)).float().double()
+        return ((th - th.mean()) / th.std()).cpu().numpy()
+
+    tas = []
+    for i in range(k):
+        ox, oy = pad + int(round(u[i, 0])), pad + int(round(u[i, 1]))
+        tas.append(thumb(f[oy:oy + tile, ox:ox + tile]))
+    return thumb(b), tas, theta
+
+
+def patch_group(seed: int, k: int, n: int = 512, margin: int = 64, noise=8.0):
+    """One n x n uint8 tile B and k neighbours A_i (the field at offsets
+    t_i in [-margin, margin]^2, plus noise).  Returns (b, [a_i], [truth_i])."""
+    size = n + 2 * margin
+    f = field_np(seed, size, size)
+    rng = np.random.default_rng(seed + 1000003)
+    b = to_u8(f[margin:margin + n, margin:margin + n] + rng.normal(0.0, noise, (n, n)))
+    a_s, truths = [], []
+    for _ in range(k):
+        tx, ty = (int(v) for v in rng.integers(-margin, margin + 1, 2))
+        af = f[margin + ty:margin + ty + n, margin + tx:margin + tx + n]
+        a_s.append(to_u8(af + rng.normal(0.0, noise, af.shape)))
+        truths.append((tx, ty))
+    return b, a_s, truths

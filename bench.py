@@ -59,9 +59,14 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=48)
     ap.add_argument("--parity-sample", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="montage", choices=["montage", "sweep"],
-                    help="montage: the strip batch (default); sweep: the thumbnail angle sweep")
+    ap.add_argument("--workload", default="montage", choices=["montage", "sweep", "served"],
+                    help="montage: the strip batch (default); sweep: the thumbnail angle "
+                         "sweep; served: the Poisson request stream through the server")
     ap.add_argument("--sweep-pairs", type=int, default=1024)
+    ap.add_argument("--served-rates", default="2000,5000,10000,20000,50000")
+    ap.add_argument("--served-requests", type=int, default=2000)
+    ap.add_argument("--served-strips", type=int, default=512)
+    ap.add_argument("--served-groups", type=int, default=32)
     return ap.parse_args()
 
 
@@ -414,6 +419,27 @@ def run_gpu(args):
     cnt = ctx.counters()
     e2e_value = ws * n * args.steps / (ms_e2e / 1000.0)
 
+    # the host link alone: one pinned-to-device copy of the step's strips
+    # (bounds e2e when the copies cannot hide behind the kernels)
+    probe = torch.empty(strip_bytes, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+    e0.record()
+    probe.copy_(pinned, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    h2d_gbs = strip_bytes / (e0.elapsed_time(e1) / 1000.0) / 1e9
+    # the same bytes as four concurrent copies (several copy engines)
+    streams = [torch.cuda.Stream(device=dev) for _ in range(4)]
+    q = (strip_bytes + 3) // 4
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k, st in enumerate(streams):
+        with torch.cuda.stream(st):
+            probe[k * q:(k + 1) * q].copy_(pinned[k * q:(k + 1) * q], non_blocking=True)
+    torch.cuda.synchronize()
+    h2d_gbs4 = strip_bytes / (time.perf_counter() - t0) / 1e9
+    del probe
+
     # results agree between the two input paths
     same = all((out_d[k].status, out_d[k].peak_x, out_d[k].peak_y, out_d[k].r) ==
                (out_h[k].status, out_h[k].peak_x, out_h[k].peak_y, out_h[k].r)
@@ -474,7 +500,9 @@ def run_gpu(args):
                        "parallelism": "replicas x%d" % ws},
             "e2e": {"value": e2e_value, "unit": "pairs/s",
                     "h2d_bytes_per_step": cnt["h2d_bytes"] // args.steps,
-                    "d2h_bytes_per_step": cnt["d2h_bytes"] // args.steps},
+                    "d2h_bytes_per_step": cnt["d2h_bytes"] // args.steps,
+                    "h2d_link_gbs": h2d_gbs, "h2d_link_gbs_4_streams": h2d_gbs4,
+                    "copy_bound_pairs_per_s": n / (strip_bytes / (h2d_gbs * 1e9))},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "alg_bytes_per_launch": alg_per_launch,
@@ -681,10 +709,228 @@ def run_sweep(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# served request stream (--workload served)
+# ---------------------------------------------------------------------------
+
+SERVED_WORKLOAD = ("served request stream: Poisson arrivals at swept rates; 70% montage strip "
+                   "pairs (CorrPatches, disc 64), 20% thumbnail sweeps (DenovoBestAngle on 256^2 "
+                   "thumbnails), 10% 512^2 uint8 patch pairs (CorrPatches, full window); sweep "
+                   "and patch tiles B each serve 6 neighbours (spectrum keys); continuous-batching "
+                   "server, 2 workers")
+SERVED_MIX = (0.7, 0.2, 0.1)
+
+
+def served_pools(seed, dev, n_strips, n_groups):
+    """Host inputs: montage strip pairs, thumbnail groups, patch groups."""
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300 import synth
+    strips = [(p["a"].cpu().numpy(), p["b"].cpu().numpy(), p["ox"], p["oy"], p["radius"])
+              for p in synth.montage_batch_torch(seed, n_strips, dev)]
+    thumbs = []
+    for g in range(n_groups):
+        tb, tas, _ = synth.neighbour_group_torch(seed * 1000 + g, 6, dev)
+        for ta in tas:
+            T = aln.native.AlnThumbs()
+            T.a = ta.ctypes.data
+            T.a_mask = None
+            T.a_h, T.a_w = ta.shape
+            T.a_stride = ta.shape[1]
+            T.a_x0 = T.a_y0 = 0
+            T.b = aln.image(tb)
+            T.req_area = SWEEP_REQ_AREA
+            T.olap1d = 0
+            T.b_key = 1_000_000 + g
+            T._keep = (ta, tb)
+            thumbs.append(T)
+    patches = []
+    for g in range(n_groups):
+        b, a_s, _ = synth.patch_group(seed * 1000 + 500 + g, 6)
+        for a in a_s:
+            patches.append((a, b, 2_000_000 + g))
+    return strips, thumbs, patches
+
+
+def served_requests(pools, n, seed):
+    """n prepared AlnRequest structs drawn with the 70/20/10 mix."""
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300.native import AlnRequest, _thm_params
+    strips, thumbs, patches = pools
+    rng = np.random.default_rng(seed)
+    cls = rng.choice(3, size=n, p=SERVED_MIX)
+    lg_s = aln.legal(aln.RGN_SECTION, 1500, 1500, 30000)
+    lg_p = aln.legal(aln.RGN_MIN, 32, 32, 0)
+    thm = _thm_params()
+    reqs, keep = [], [lg_s, lg_p]
+    ci = [0, 0, 0]
+    for c in cls:
+        r = AlnRequest()
+        if c == 0:
+            a, b, ox, oy, rad = strips[ci[0] % len(strips)]
+            r.kind = aln.REQ_PATCHES
+            r.pair.a, r.pair.b = aln.image(a), aln.image(b)
+            r.pair.ox, r.pair.oy, r.pair.radius = ox, oy, rad
+            r.pair.legal = lg_s
+        elif c == 1:
+            r.kind = aln.REQ_SWEEP
+            r.thumbs = thumbs[ci[1] % len(thumbs)]
+            r.thm = thm
+            r.thm_mode, r.ang0, r.hfang, r.step = aln.THM_DENOVO, 0.0, 10.0, 0.5
+        else:
+            a, b, key = patches[ci[2] % len(patches)]
+            r.kind = aln.REQ_PATCHES
+            r.pair.a, r.pair.b = aln.image(a), aln.image(b)
+            r.pair.radius = 4096
+            r.pair.legal = lg_p
+            r.pair.b_key = key
+        ci[c] += 1
+        reqs.append(r)
+    return reqs, cls, keep
+
+
+def served_run(srv, reqs, rate, seed):
+    """Submit reqs at Poisson times of `rate` per second; collect every reply.
+    Returns (wall seconds first submit -> last reply, replies by index)."""
+    import ctypes as C
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300.native import AlnReply
+    L = aln.lib()
+    n = len(reqs)
+    gaps = np.random.default_rng(seed).exponential(1.0 / rate, n)
+    t_arr = np.cumsum(gaps) - gaps[0]
+    tickets = [0] * n
+    index = {}
+    done = {}
+    lock = threading.Lock()
+
+    def feed():
+        t0 = time.perf_counter()
+        tk = C.c_ulonglong()
+        for i in range(n):
+            while time.perf_counter() - t0 < t_arr[i]:
+                pass
+            rc = L.aln_server_submit(srv.h, C.byref(reqs[i]), C.byref(tk))
+            if rc < 0:
+                raise RuntimeError("submit refused")
+            with lock:
+                tickets[i] = tk.value
+                index[tk.value] = i
+
+    t_start = time.perf_counter()
+    th = threading.Thread(target=feed)
+    th.start()
+    cap = 4096
+    tk_buf = (C.c_ulonglong * cap)()
+    rep_buf = (AlnReply * cap)()
+    while len(done) < n:
+        k = L.aln_server_collect(srv.h, cap, 200, tk_buf, rep_buf)
+        for j in range(k):
+            with lock:
+                i = index.get(tk_buf[j])
+            while i is None:   # reply raced ahead of the feeder's bookkeeping
+                time.sleep(0)
+                with lock:
+                    i = index.get(tk_buf[j])
+            r = rep_buf[j]
+            done[i] = (r.status, r.total_ms, r.queue_ms, r.batch_size)
+    wall = time.perf_counter() - t_start
+    th.join()
+    return wall, done
+
+
+def run_served(args):
+    import torch
+    import alignment_projects_gb300 as aln
+
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the reference has no request server; its per-pair CPU paths are "
+                              "timed by --workload montage and --workload sweep"}), flush=True)
+        return 0
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pools = served_pools(5, dev, args.served_strips, args.served_groups)
+    torch.cuda.synchronize()
+    srv = aln.Server(local, workers=2)
+    rates = [float(r) for r in args.served_rates.split(",")]
+    # warm-up: every class through the server
+    reqs, cls, keep = served_requests(pools, 200, 11)
+    served_run(srv, reqs, 2000.0, 12)
+    clk = ClockSampler(local)
+    clk.start()
+    table = []
+    for k, rate in enumerate(rates):
+        reqs, cls, keep = served_requests(pools, args.served_requests, 100 + k)
+        wall, done = served_run(srv, reqs, rate, 200 + k)
+        lat = np.array([done[i][1] for i in range(len(reqs))])
+        bad = sum(1 for i in range(len(reqs)) if done[i][0] < 0)
+        row = {"offered_rate": rate, "requests": len(reqs), "throughput": len(reqs) / wall,
+               "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+               "mean_batch": float(np.mean([done[i][3] for i in range(len(reqs))])),
+               "errors": bad}
+        for c, name in enumerate(("strips", "sweeps", "patches")):
+            m = cls == c
+            if m.any():
+                row[name + "_p50_ms"] = float(np.percentile(lat[m], 50))
+                row[name + "_p99_ms"] = float(np.percentile(lat[m], 99))
+        table.append(row)
+    clocks = clk.stop()
+    counters = srv.counters()
+    srv.close()
+    # the plain one-request-per-call path on the same mix
+    ctx = aln.Context(local)
+    strips, thumbs, patches = pools
+    lg_s = aln.legal(aln.RGN_SECTION, 1500, 1500, 30000)
+    lg_p = aln.legal(aln.RGN_MIN, 32, 32, 0)
+    per = []
+    for j in range(9):
+        a, b, ox, oy, rad = strips[j]
+        t0 = time.perf_counter()
+        ctx.corr_patches(a, b, ox, oy, rad, lg_s)
+        per.append(time.perf_counter() - t0)
+    t_strip = float(np.median(per[1:]))
+    per = []
+    for j in range(5):
+        t0 = time.perf_counter()
+        ctx.thm_search_batch([thumbs[j]], mode=aln.THM_DENOVO)
+        per.append(time.perf_counter() - t0)
+    t_sweep = float(np.median(per[1:]))
+    per = []
+    for j in range(9):
+        a, b, _ = patches[j]
+        t0 = time.perf_counter()
+        ctx.corr_patches(a, b, 0, 0, 4096, lg_p)
+        per.append(time.perf_counter() - t0)
+    t_patch = float(np.median(per[1:]))
+    ctx.close()
+    plain = 1.0 / (SERVED_MIX[0] * t_strip + SERVED_MIX[1] * t_sweep + SERVED_MIX[2] * t_patch)
+    best = max(table, key=lambda r: r["throughput"])
+    print(json.dumps({
+        "metric": METRIC, "value": best["throughput"], "unit": "requests/s", "n_gpus": 1,
+        "steps": len(rates), "warmup": 1, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": SERVED_WORKLOAD, "requests_per_rate": args.served_requests,
+                   "rates": rates, "note": "one step = one offered rate; value = best throughput"},
+        "e2e": {"value": best["throughput"], "unit": "requests/s",
+                "note": "host inputs through the server API: value is end to end"},
+        "rates": table,
+        "plain": {"requests_per_s": plain, "strip_ms": 1000 * t_strip, "sweep_ms": 1000 * t_sweep,
+                  "patch_ms": 1000 * t_patch},
+        "served_over_plain": best["throughput"] / plain,
+        "server_counters": counters, "clocks": clocks}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.workload == "sweep":
         return run_sweep(args)
+    if args.workload == "served":
+        return run_served(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

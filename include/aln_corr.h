@@ -249,6 +249,8 @@ typedef struct aln_thumbs {
     aln_image b;
     long long req_area;            /* ThmRec reqArea */
     int olap1d;                    /* ThmRec olap1D */
+    unsigned long long b_key;      /* != 0: B's spectrum-cache key (ThmRec ftc),
+                                      kept across calls; 0: cached for this call only */
 } aln_thumbs;
 
 /* CThmScan settings (its setters, 0_GEN/CThmScan.h:115-157). */
