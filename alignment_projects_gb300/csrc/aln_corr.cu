@@ -924,13 +924,15 @@ struct aln_ctx {
     float2 *tw;
     char *ws;
     size_t ws_cap;
-    PairDev *dpairs;          // the current chunk's job table (one of two parities)
+    PairDev *dpairs;          // the current chunk's entries of the batch job table
     ResultDev *dres;
     PairDev *dpairs_base;
+    PairDev *htab;            // pinned host job tables, one per parity
     ResultDev *dres_base;
-    size_t dpairs_cap;        // jobs per parity
+    size_t dpairs_cap;        // jobs the batch tables hold
     cudaStream_t cstream;     // host-to-device staging copies
-    cudaEvent_t ev_copy[2], ev_done[2];
+    cudaEvent_t ev_copy[2];               // a window's staging is copied
+    cudaEvent_t ev_wdone[2];              // a window's kernels are done (staging free)
     ResultDev *hres;          // pinned result buffer
     size_t hres_cap;
     size_t ws_budget;
@@ -949,9 +951,12 @@ struct aln_ctx {
     size_t spec_bytes, spec_cap;                 // all buffers held / limit
     unsigned long long spec_tick;
     long long spec_hits, spec_fills;
-    int *dsel;                                   // cache-fill job lists
+    int *dsel;                                   // cache-fill job lists (whole batch)
     size_t dsel_cap;
+    int *dsel_cur;                               // the current chunk's list
     unsigned long long sweep_serial;             // key namespace of each sweep call
+    long long chunks;                            // chunks run since the last reset
+    long long h2d_copies;                        // staging transfers issued
 };
 
 static cudaEvent_t ev_get(aln_ctx *c)
@@ -983,6 +988,25 @@ static void prof_end(aln_ctx *c)
 {
     if (c->prof_on && !c->prof.empty())
         cudaEventRecord(c->prof.back().b, c->stream);
+}
+
+// the same for work on the copy stream (host-to-device staging)
+static void prof_begin_copy(aln_ctx *c, const char *name)
+{
+    if (!c->prof_on)
+        return;
+    ProfRec r;
+    r.name = name;
+    r.a = ev_get(c);
+    r.b = ev_get(c);
+    cudaEventRecord(r.a, c->cstream);
+    c->prof.push_back(r);
+}
+
+static void prof_end_copy(aln_ctx *c)
+{
+    if (c->prof_on && !c->prof.empty())
+        cudaEventRecord(c->prof.back().b, c->cstream);
 }
 
 // fold finished records into the per-kernel totals (stream must be idle)
@@ -1029,6 +1053,21 @@ static int set_err(aln_ctx *c, int code, const char *fmt, ...)
 
 static const int kSmemMax = 200 * 1024;
 
+// Raise a kernel's dynamic shared-memory limit once per (device, kernel),
+// not before every launch: the attribute call is a driver round trip.
+static std::mutex g_attr_lock;
+static std::map<std::pair<int, const void *>, int> g_attr_set;
+
+static void smem_attr(int device, const void *fn, size_t bytes)
+{
+    std::lock_guard<std::mutex> lk(g_attr_lock);
+    int &cur = g_attr_set[std::make_pair(device, fn)];
+    if ((int)bytes > cur) {
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        cur = (int)bytes;
+    }
+}
+
 static int configure_kernels()
 {
     const void *ks[] = {(const void *)k_rowfft, (const void *)k_colfft,
@@ -1060,6 +1099,7 @@ extern "C" int aln_ctx_create(int device, aln_ctx **out)
     ctx->dpairs = nullptr;
     ctx->dres = nullptr;
     ctx->dpairs_base = nullptr;
+    ctx->htab = nullptr;
     ctx->dres_base = nullptr;
     ctx->dpairs_cap = 0;
     ctx->cstream = nullptr;
@@ -1076,7 +1116,10 @@ extern "C" int aln_ctx_create(int device, aln_ctx **out)
     ctx->spec_hits = ctx->spec_fills = 0;
     ctx->dsel = nullptr;
     ctx->dsel_cap = 0;
+    ctx->dsel_cur = nullptr;
     ctx->sweep_serial = 0;
+    ctx->chunks = 0;
+    ctx->h2d_copies = 0;
     if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&ctx->cstream, cudaStreamNonBlocking)) != cudaSuccess) {
         set_err(nullptr, ALN_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
@@ -1086,7 +1129,7 @@ extern "C" int aln_ctx_create(int device, aln_ctx **out)
     for (int q = 0; q < 2; ++q)
         if ((e = cudaEventCreateWithFlags(&ctx->ev_copy[q], cudaEventDisableTiming)) !=
                 cudaSuccess ||
-            (e = cudaEventCreateWithFlags(&ctx->ev_done[q], cudaEventDisableTiming)) !=
+            (e = cudaEventCreateWithFlags(&ctx->ev_wdone[q], cudaEventDisableTiming)) !=
                 cudaSuccess) {
             set_err(nullptr, ALN_ERR_CUDA, "events: %s", cudaGetErrorString(e));
             delete ctx;
@@ -1130,6 +1173,8 @@ extern "C" void aln_ctx_destroy(aln_ctx *ctx)
     cudaStreamSynchronize(ctx->cstream);
     cudaFree(ctx->dpairs_base);
     cudaFree(ctx->dres_base);
+    if (ctx->htab)
+        cudaFreeHost(ctx->htab);
     for (auto &e : ctx->spec)
         cudaFree(e.second.X2);
     for (auto &f : ctx->spec_free)
@@ -1139,7 +1184,7 @@ extern "C" void aln_ctx_destroy(aln_ctx *ctx)
         cudaFreeHost(ctx->hres);
     for (int q = 0; q < 2; ++q) {
         cudaEventDestroy(ctx->ev_copy[q]);
-        cudaEventDestroy(ctx->ev_done[q]);
+        cudaEventDestroy(ctx->ev_wdone[q]);
     }
     cudaStreamDestroy(ctx->cstream);
     prof_collect(ctx);
@@ -1212,19 +1257,24 @@ static int ensure_ws(aln_ctx *ctx, size_t bytes)
 
 static int ensure_pairs(aln_ctx *ctx, size_t n)
 {
+    ctx->dpairs = ctx->dpairs_base;
+    ctx->dres = ctx->dres_base;
     if (n <= ctx->dpairs_cap)
         return ALN_OK;
     if (ctx->dpairs_base) {
         CK(cudaStreamSynchronize(ctx->stream));
         cudaFree(ctx->dpairs_base);
         cudaFree(ctx->dres_base);
+        cudaFreeHost(ctx->htab);
+        ctx->htab = nullptr;
         ctx->dpairs = ctx->dpairs_base = nullptr;
         ctx->dres = ctx->dres_base = nullptr;
         ctx->dpairs_cap = 0;
     }
-    size_t cap = std::max<size_t>(n, 64);
-    CK(cudaMalloc(&ctx->dpairs_base, 2 * cap * sizeof(PairDev)));
-    CK(cudaMalloc(&ctx->dres_base, 2 * cap * sizeof(ResultDev)));
+    size_t cap = std::max<size_t>(n + n / 4, 64);
+    CK(cudaMalloc(&ctx->dpairs_base, cap * sizeof(PairDev)));
+    CK(cudaHostAlloc((void **)&ctx->htab, cap * sizeof(PairDev), cudaHostAllocDefault));
+    CK(cudaMalloc(&ctx->dres_base, cap * sizeof(ResultDev)));
     ctx->dpairs = ctx->dpairs_base;
     ctx->dres = ctx->dres_base;
     ctx->dpairs_cap = cap;
@@ -1256,6 +1306,7 @@ struct PairPlan {
     int index;
     int key_ns;                  // spectrum-cache key of image b (0: none)
     unsigned long long key;
+    char *staged[2];             // device staging of host inputs (set per window)
 };
 
 // A device buffer for a new cache entry of `bytes`, evicting entries not used
@@ -1537,12 +1588,9 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
     return ALN_OK;
 }
 
-// carve a pair's workspace starting at base; returns bytes used
-// carve a pair's workspace starting at base; returns bytes used.  With a
-// staging cursor, host-input staging goes there instead, packed back to back
-// (aligned to the element size only) so that adjacent host images can be
-// copied with one transfer.
-static size_t carve(PairPlan &pl, char *base, const aln_pair &P, char **stage = nullptr)
+// carve a pair's workspace starting at base; returns bytes used.  Host
+// inputs already staged by their window keep that staging.
+static size_t carve(PairPlan &pl, char *base, const aln_pair &P)
 {
     PairDev &d = pl.d;
     char *p = base;
@@ -1550,14 +1598,11 @@ static size_t carve(PairPlan &pl, char *base, const aln_pair &P, char **stage = 
     const int Wy = d.yhi - d.ylo + 1, Wx = d.xhi - d.xlo + 1;
     for (int i = 0; i < 2; ++i) {
         if (pl.in_bytes[i]) {
-            // staging of a host input, in the caller's layout (packed)
-            char *q = p;
-            if (stage) {
-                const size_t es = dtype_size(d.dt[i]);
-                *stage = (char *)(((uintptr_t)*stage + es - 1) & ~(uintptr_t)(es - 1));
-                q = *stage;
-                *stage += (size_t)d.w[i] * d.h[i] * es;
-            } else {
+            // staging of a host input, in the caller's layout: the window's
+            // staging buffer when set, else the pair's own workspace
+            char *q = pl.staged[i];
+            if (!q) {
+                q = p;
                 p += pl.in_bytes[i];
             }
             if (pl.transposed) {
@@ -1627,7 +1672,7 @@ static void launch_rowfft2(aln_ctx *ctx, int n, int maxh)
     constexpr int T = RegFFT<LL, -1>::T;
     const int thr = rowfft_threads(T), G = thr / T;
     const size_t sm = (size_t)G * (padded(LL) + 2) * sizeof(float2);
-    cudaFuncSetAttribute(k2_rowfft<LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    smem_attr(ctx->device, (const void *)k2_rowfft<LL>, sm);
     LAUNCH(ctx, "k2_rowfft", k2_rowfft<LL>, dim3((maxh + G - 1) / G, 2, n), thr, sm,
            ctx->dpairs, ctx->tw, -1, (const int *)nullptr);
 }
@@ -1639,9 +1684,9 @@ static void launch_fill_rows(aln_ctx *ctx, int nsel, int maxh)
     constexpr int T = RegFFT<LL, -1>::T;
     const int thr = rowfft_threads(T), G = thr / T;
     const size_t sm = (size_t)G * (padded(LL) + 2) * sizeof(float2);
-    cudaFuncSetAttribute(k2_rowfft<LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    smem_attr(ctx->device, (const void *)k2_rowfft<LL>, sm);
     LAUNCH(ctx, "k2_rowfft", k2_rowfft<LL>, dim3((maxh + G - 1) / G, 1, nsel), thr, sm,
-           ctx->dpairs, ctx->tw, 1, (const int *)ctx->dsel);
+           ctx->dpairs, ctx->tw, 1, (const int *)ctx->dsel_cur);
 }
 
 template <int NY>
@@ -1650,9 +1695,9 @@ static void launch_fill_cols(aln_ctx *ctx, int nsel, int L)
     constexpr int T = RegFFT<NY, -1>::T;
     const int thr = std::max(256, T), G = thr / T;
     const size_t sm = (size_t)G * padded(NY) * sizeof(float2);
-    cudaFuncSetAttribute(k2_colspec<NY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    smem_attr(ctx->device, (const void *)k2_colspec<NY>, sm);
     LAUNCH(ctx, "k2_colspec", k2_colspec<NY>, dim3((L + 1 + G - 1) / G, nsel), thr, sm,
-           ctx->dpairs, ctx->tw, (const int *)ctx->dsel);
+           ctx->dpairs, ctx->tw, (const int *)ctx->dsel_cur);
 }
 
 template <int NY>
@@ -1663,7 +1708,7 @@ static void launch_corrcol2(aln_ctx *ctx, int n, int L, int cached, bool plain)
     const size_t sm = (size_t)G * (padded(NY) + NY) * sizeof(float2);
     void (*kern)(PairDev *, const float2 *, int) =
         plain ? k2_corrcol<NY, true> : k2_corrcol<NY, false>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    smem_attr(ctx->device, (const void *)kern, sm);
     LAUNCH(ctx, "k2_corrcol", kern, dim3((L + 1 + G - 1) / G, n), thr, sm, ctx->dpairs, ctx->tw,
            cached);
 }
@@ -1674,7 +1719,7 @@ static void launch_lagrow2(aln_ctx *ctx, int n, int maxWy)
     constexpr int T = RegFFT<LL, +1>::T;
     const int thr = std::max(256, T), G = thr / T;
     const size_t sm = (size_t)G * (padded(LL) + 2) * sizeof(float2);
-    cudaFuncSetAttribute(k2_lagrow<LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    smem_attr(ctx->device, (const void *)k2_lagrow<LL>, sm);
     LAUNCH(ctx, "k2_lagrow", k2_lagrow<LL>, dim3((maxWy + G - 1) / G, n), thr, sm,
            ctx->dpairs, ctx->tw);
 }
@@ -1685,7 +1730,7 @@ static void launch_lagp2i(aln_ctx *ctx, int n, int maxWy)
     constexpr int T = RegFFT<LL, +1>::T;
     const int thr = std::max(256, T), G = thr / T;
     const size_t sm = (size_t)G * (padded(LL) + 2) * sizeof(float2);
-    cudaFuncSetAttribute(k2_lagp2i<LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    smem_attr(ctx->device, (const void *)k2_lagp2i<LL>, sm);
     LAUNCH(ctx, "k2_lagp2i", k2_lagp2i<LL>, dim3((maxWy + G - 1) / G, n), thr, sm, ctx->dpairs,
            ctx->tw);
 }
@@ -1697,7 +1742,7 @@ static void launch_lagimg2(aln_ctx *ctx, int n, int maxWy, bool both, bool sonly
     const int thr = std::max(256, T), G = thr / T;
     const size_t sm = (size_t)G * (padded(LL) + 2) * (both ? 2 : 1) * sizeof(float2);
     void (*kern)(PairDev *, const float2 *) = sonly ? k2_lagimg<LL, true> : k2_lagimg<LL, false>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    smem_attr(ctx->device, (const void *)kern, sm);
     LAUNCH(ctx, "k2_lagimg", kern, dim3((maxWy + G - 1) / G, n), thr, sm, ctx->dpairs, ctx->tw);
 }
 
@@ -1746,43 +1791,37 @@ static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int
     return ALN_OK;
 }
 
-// One chunk of pairs sharing (Nx, Ny), run as a two-stage pipeline step:
-// host inputs are copied on the copy stream into staging buffer `par`
-// (adjacent host images in one transfer), the kernels run on the compute
-// stream once that copy is done, and the results go to pinned host memory.
-// Nothing here waits for the GPU; the caller synchronises once per batch.
-static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int par, char *stage_base,
-                     char *work_base, ResultDev *hres_out)
+// One chunk of jobs sharing (Nx, Ny, kind): the sizes its launches need and
+// where its jobs sit in the batch's job table.
+struct ChunkLaunch {
+    int off, n;                        // jobs [off, off + n) of the batch table
+    int maxw, maxh, maxslots, maxWy;
+    int sw, sh;                        // largest caller-frame image of transposed jobs
+    int Nx, Ny, mode, both, sonly, frame_nx1, frame_ny1;
+    int fill_off, nfill, fill_maxh;    // spectrum-cache fills: sel[fill_off ...]
+};
+
+// Host side of a chunk: carve each job's workspace (the chunk's work buffer
+// is reused by every chunk, in stream order), resolve spectrum-cache keys,
+// write the job table entries hd[0..n).
+static void prep_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int off, char *work_base,
+                       PairDev *hd, std::vector<int> &fills, ChunkLaunch &cl)
 {
     const int n = (int)chunk.size();
-    ctx->dpairs = ctx->dpairs_base + (size_t)par * ctx->dpairs_cap;
-    ctx->dres = ctx->dres_base + (size_t)par * ctx->dpairs_cap;
-    std::vector<PairDev> hd(n);
-    int maxw = 1, maxh = 1, maxslots = 1, maxWy = 1;
-    const int Nx = chunk[0]->d.Nx, Ny = chunk[0]->d.Ny;
-    char *stage = stage_base, *work = work_base;
-    // staging copies, coalesced over host images adjacent in memory
-    CK(cudaStreamWaitEvent(ctx->cstream, ctx->ev_done[par], 0));
-    const char *run_src = nullptr, *run_end = nullptr;
-    char *run_dst = nullptr;
-    auto flush = [&]() -> int {
-        if (run_src && run_end > run_src) {
-            CK(cudaMemcpyAsync(run_dst, run_src, (size_t)(run_end - run_src),
-                               cudaMemcpyHostToDevice, ctx->cstream));
-            ctx->h2d_bytes += (long long)(run_end - run_src);
-        }
-        run_src = run_end = nullptr;
-        run_dst = nullptr;
-        return ALN_OK;
-    };
-    const bool reg_path = Nx / 2 >= 8 && Nx / 2 <= 4096 && Ny >= 8 && Ny <= 8192;
-    std::vector<int> fill;   // jobs whose b spectrum is computed into a new entry
-    int fill_maxh = 1;
+    cl.off = off;
+    cl.n = n;
+    cl.maxw = cl.maxh = cl.maxslots = cl.maxWy = 1;
+    cl.sw = cl.sh = 0;
+    cl.Nx = chunk[0]->d.Nx;
+    cl.Ny = chunk[0]->d.Ny;
+    cl.fill_off = (int)fills.size();
+    cl.fill_maxh = 1;
+    char *work = work_base;
+    const bool reg_path = cl.Nx / 2 >= 8 && cl.Nx / 2 <= 4096 && cl.Ny >= 8 && cl.Ny <= 8192;
     ++ctx->spec_tick;
     for (int k = 0; k < n; ++k) {
         PairPlan &pl = *chunk[k];
-        const aln_pair &P = *pl.src;
-        work += carve(pl, work, P, &stage);
+        work += carve(pl, work, *pl.src);
         pl.d.b_cached = 0;
         if (pl.key && reg_path && pl.d.mode != JOB_P2I && ctx->spec_cap > 0) {
             const SpecKey K(pl.key_ns, pl.key, pl.d.Nx, pl.d.Ny, pl.d.transposed,
@@ -1799,115 +1838,84 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int par, char
                     ctx->spec[K] = SpecEntry{buf, bytes, ctx->spec_tick};
                     pl.d.b_cached = 1;
                     pl.d.X2 = buf;
-                    fill.push_back(k);
-                    fill_maxh = std::max(fill_maxh, pl.d.h[1]);
+                    fills.push_back(k);
+                    cl.fill_maxh = std::max(cl.fill_maxh, pl.d.h[1]);
                     ctx->spec_fills++;
                 }
             }
         }
-        const aln_image *im[2] = {&P.a, &P.b};
         for (int i = 0; i < 2; ++i) {
-            if (pl.in_bytes[i]) {
-                const size_t es = dtype_size(im[i]->dtype);
-                char *dst = pl.transposed ? (char *)pl.d.src_img[i] : (char *)pl.d.img[i];
-                const size_t bytes = (size_t)im[i]->w * im[i]->h * es;
-                const char *src = (const char *)im[i]->data;
-                if (im[i]->stride == im[i]->w) {
-                    if (run_src && src == run_end && dst == run_dst + (run_end - run_src)) {
-                        run_end += bytes;
-                    } else {
-                        if (int rc = flush())
-                            return rc;
-                        run_src = src;
-                        run_end = src + bytes;
-                        run_dst = dst;
-                    }
-                } else {
-                    if (int rc = flush())
-                        return rc;
-                    CK(cudaMemcpy2DAsync(dst, (size_t)im[i]->w * es, im[i]->data,
-                                         (size_t)im[i]->stride * es, (size_t)im[i]->w * es,
-                                         im[i]->h, cudaMemcpyHostToDevice, ctx->cstream));
-                    ctx->h2d_bytes += (long long)bytes;
-                }
-            }
-            maxw = std::max(maxw, pl.d.w[i]);
-            maxh = std::max(maxh, pl.d.h[i]);
+            cl.maxw = std::max(cl.maxw, pl.d.w[i]);
+            cl.maxh = std::max(cl.maxh, pl.d.h[i]);
             int ns = 0;
             for (int q = 0; q < 2; ++q)
                 if (pl.d.need_hi[i][q] >= pl.d.need_lo[i][q])
                     ns += pl.d.need_hi[i][q] - pl.d.need_lo[i][q] + 1;
-            maxslots = std::max(maxslots, ns);
+            cl.maxslots = std::max(cl.maxslots, ns);
+            if (pl.d.transposed) {
+                cl.sw = std::max(cl.sw, pl.d.h[i]);
+                cl.sh = std::max(cl.sh, pl.d.w[i]);
+            }
         }
-        maxWy = std::max(maxWy, pl.d.yhi - pl.d.ylo + 1);
+        cl.maxWy = std::max(cl.maxWy, pl.d.yhi - pl.d.ylo + 1);
         pl.d.sat_int = (pl.d.dt[0] == ALN_U8 || pl.d.dt[0] == ALN_U16 ? 1 : 0) |
                        (pl.d.dt[1] == ALN_U8 || pl.d.dt[1] == ALN_U16 ? 2 : 0);
         hd[k] = pl.d;
     }
-    if (int rc = flush())
-        return rc;
-    CK(cudaEventRecord(ctx->ev_copy[par], ctx->cstream));
-    // job table and legality tables (pageable sources: staged before return)
+    cl.nfill = (int)fills.size() - cl.fill_off;
+    cl.mode = hd[0].mode;
+    cl.both = hd[0].want_r && hd[0].want_s;
+    cl.sonly = hd[0].s_float != 0;
+    cl.frame_nx1 = chunk[0]->frame_nx1;
+    cl.frame_ny1 = chunk[0]->frame_ny1;
+}
+
+// The chunk's kernels on the compute stream (its job table, fill list and
+// staged inputs are already on the device, in stream order).
+static int launch_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, const ChunkLaunch &cl)
+{
+    const int n = cl.n, Nx = cl.Nx, Ny = cl.Ny, L = Nx / 2;
+    ctx->chunks++;
+    ctx->dpairs = ctx->dpairs_base + cl.off;
+    ctx->dres = ctx->dres_base + cl.off;
+    ctx->dsel_cur = ctx->dsel + cl.fill_off;
     cudaStream_t st = ctx->stream;
-    for (int k = 0; k < n; ++k)
-        if (hd[k].rgn_kind == ALN_RGN_TABLE)
-            CK(cudaMemcpyAsync((void *)hd[k].table, chunk[k]->src->legal.table,
-                               (size_t)hd[k].table_w * hd[k].table_h, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(ctx->dpairs, hd.data(), n * sizeof(PairDev), cudaMemcpyHostToDevice, st));
-    CK(cudaStreamWaitEvent(st, ctx->ev_copy[par], 0));
-    const int L = Nx / 2;
-    {
-        int sw = 0, sh = 0;   // largest caller-frame image among transposed jobs
-        for (int k = 0; k < n; ++k)
-            if (hd[k].transposed)
-                for (int i = 0; i < 2; ++i) {
-                    sw = std::max(sw, hd[k].h[i]);
-                    sh = std::max(sh, hd[k].w[i]);
-                }
-        if (sw > 0)
-            LAUNCH(ctx, "k_transpose", k_transpose, dim3((sw + 31) / 32, (sh + 31) / 32, 2 * n),
-                   dim3(32, 8), 0, ctx->dpairs);
-    }
-    const int mode = hd[0].mode;
+    for (int k = 0; k < n; ++k)   // tabulated legality (pageable source: staged at the call)
+        if (chunk[k]->d.rgn_kind == ALN_RGN_TABLE)
+            CK(cudaMemcpyAsync((void *)chunk[k]->d.table, chunk[k]->src->legal.table,
+                               (size_t)chunk[k]->d.table_w * chunk[k]->d.table_h,
+                               cudaMemcpyHostToDevice, st));
+    if (cl.sw > 0)
+        LAUNCH(ctx, "k_transpose", k_transpose, dim3((cl.sw + 31) / 32, (cl.sh + 31) / 32, 2 * n),
+               dim3(32, 8), 0, ctx->dpairs);
+    const int mode = cl.mode;
     if (mode != JOB_P2I) {
-        LAUNCH(ctx, "k3_sat", k3_sat, dim3((maxw + 31) / 32, 2 * n), dim3(32, SAT_WARPS), 0,
+        LAUNCH(ctx, "k3_sat", k3_sat, dim3((cl.maxw + 31) / 32, 2 * n), dim3(32, SAT_WARPS), 0,
                ctx->dpairs);
         LAUNCH(ctx, "k_mean", k_mean, dim3(2, n), 256, 0, ctx->dpairs);
-        if (maxw <= SAT2W_MAXW)
-            LAUNCH(ctx, "k2_sat2w", k2_sat2w, dim3((maxslots + 7) / 8, 2, n), 256, 0,
+        if (cl.maxw <= SAT2W_MAXW)
+            LAUNCH(ctx, "k2_sat2w", k2_sat2w, dim3((cl.maxslots + 7) / 8, 2, n), 256, 0,
                    ctx->dpairs);
         else
-            LAUNCH(ctx, "k2_sat2", k2_sat2, dim3(maxslots, 2, n), 256, 0, ctx->dpairs);
+            LAUNCH(ctx, "k2_sat2", k2_sat2, dim3(cl.maxslots, 2, n), 256, 0, ctx->dpairs);
     }
-    if (!fill.empty()) {
-        if (fill.size() > ctx->dsel_cap) {
-            CK(cudaStreamSynchronize(st));
-            cudaFree(ctx->dsel);
-            ctx->dsel = nullptr;
-            ctx->dsel_cap = 0;
-            const size_t cap = std::max<size_t>(fill.size(), 4096);
-            CK(cudaMalloc(&ctx->dsel, cap * sizeof(int)));
-            ctx->dsel_cap = cap;
-        }
-        CK(cudaMemcpyAsync(ctx->dsel, fill.data(), fill.size() * sizeof(int),
-                           cudaMemcpyHostToDevice, st));
-        const int ns = (int)fill.size();
+    if (cl.nfill > 0) {
         switch (L) {
-#define X(v) case v: launch_fill_rows<v>(ctx, ns, fill_maxh); break;
+#define X(v) case v: launch_fill_rows<v>(ctx, cl.nfill, cl.fill_maxh); break;
             ALN_CASES_L(X)
 #undef X
         default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
         }
         switch (Ny) {
-#define X(v) case v: launch_fill_cols<v>(ctx, ns, L); break;
+#define X(v) case v: launch_fill_cols<v>(ctx, cl.nfill, L); break;
             ALN_CASES_NY(X)
 #undef X
         default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "column length %d", Ny);
         }
     }
     if (L >= 8 && L <= 4096 && Ny >= 8 && Ny <= 8192) {
-        if (int rc = launch_fft_pipeline(ctx, L, Ny, n, maxh, maxWy, mode,
-                                         hd[0].want_r && hd[0].want_s, hd[0].s_float != 0))
+        if (int rc = launch_fft_pipeline(ctx, L, Ny, n, cl.maxh, cl.maxWy, mode, cl.both != 0,
+                                         cl.sonly != 0))
             return rc;
     } else if (mode != JOB_PATCHES) {
         return set_err(ctx, ALN_ERR_UNSUPPORTED, "CorrImages FFT size %d x %d", Nx, Ny);
@@ -1915,7 +1923,7 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int par, char
         {
             const int RB = rows_per_cta(L);
             const size_t sm = 2 * (size_t)RB * (L + 1) * sizeof(float2);
-            LAUNCH(ctx, "k_rowfft", k_rowfft, dim3((maxh + RB - 1) / RB, 2, n), 256, sm,
+            LAUNCH(ctx, "k_rowfft", k_rowfft, dim3((cl.maxh + RB - 1) / RB, 2, n), 256, sm,
                    ctx->dpairs, ctx->tw, RB, -1);
         }
         {
@@ -1928,21 +1936,18 @@ static int run_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int par, char
         {
             const int RBL = std::max(1, std::min(8, 4096 / std::max(1, L)));
             const size_t sm = 2 * (size_t)RBL * (L + 1) * sizeof(float2);
-            LAUNCH(ctx, "k_lagrow", k_lagrow, dim3((maxWy + RBL - 1) / RBL, n), 256, sm,
+            LAUNCH(ctx, "k_lagrow", k_lagrow, dim3((cl.maxWy + RBL - 1) / RBL, n), 256, sm,
                    ctx->dpairs, ctx->tw, RBL);
         }
     }
     if (mode == JOB_PATCHES)
-        LAUNCH(ctx, "k_final", k_final, n, 256, 0, ctx->dpairs, ctx->dres, chunk[0]->frame_nx1,
-               chunk[0]->frame_ny1);
+        LAUNCH(ctx, "k_final", k_final, n, 256, 0, ctx->dpairs, ctx->dres, cl.frame_nx1,
+               cl.frame_ny1);
     else if (mode == JOB_P2I)
         LAUNCH(ctx, "k_final_p2i", k_final_p2i, n, 256, 0, ctx->dpairs, ctx->dres);
     else
         LAUNCH(ctx, "k_final_img", k_final_img, n, 256, 0, ctx->dpairs, ctx->dres);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(hres_out, ctx->dres, n * sizeof(ResultDev), cudaMemcpyDeviceToHost, st));
-    ctx->d2h_bytes += n * sizeof(ResultDev);
-    CK(cudaEventRecord(ctx->ev_done[par], st));
     return ALN_OK;
 }
 
@@ -1972,6 +1977,84 @@ static int ensure_hres(aln_ctx *ctx, size_t n)
     return ALN_OK;
 }
 
+// Copies a window's host inputs into staging buffer `base` on the copy
+// stream (after the kernels that last read this buffer), packed in window
+// order, adjacent host images with one transfer; records ev_copy[wp].
+// Staging addresses of a window's host inputs: packed in window order
+// (aligned to the element size only), so adjacent host images stay adjacent.
+static void assign_staging(std::vector<PairPlan *> &win, char *base)
+{
+    char *cur = base;
+    for (PairPlan *pl : win) {
+        const aln_image *im[2] = {&pl->src->a, &pl->src->b};
+        for (int i = 0; i < 2; ++i) {
+            pl->staged[i] = nullptr;
+            if (!pl->in_bytes[i])
+                continue;
+            const size_t es = dtype_size(im[i]->dtype);
+            cur = (char *)(((uintptr_t)cur + es - 1) & ~(uintptr_t)(es - 1));
+            pl->staged[i] = cur;
+            cur += (size_t)im[i]->w * im[i]->h * es;
+        }
+    }
+}
+
+static int stage_window(aln_ctx *ctx, std::vector<PairPlan *> &win, int wp)
+{
+    CK(cudaStreamWaitEvent(ctx->cstream, ctx->ev_wdone[wp], 0));
+    prof_begin_copy(ctx, "h2d_staging");
+    const char *run_src = nullptr, *run_end = nullptr;
+    char *run_dst = nullptr;
+    auto flush = [&]() -> int {
+        // one transfer per run, in pieces of at most 64 MiB
+        for (const char *q = run_src; q && q < run_end;) {
+            const size_t b = std::min((size_t)(run_end - q), (size_t)64 << 20);
+            CK(cudaMemcpyAsync(run_dst + (q - run_src), q, b, cudaMemcpyHostToDevice,
+                               ctx->cstream));
+            ctx->h2d_bytes += (long long)b;
+            ctx->h2d_copies++;
+            q += b;
+        }
+        run_src = run_end = nullptr;
+        run_dst = nullptr;
+        return ALN_OK;
+    };
+    for (PairPlan *pl : win) {
+        const aln_image *im[2] = {&pl->src->a, &pl->src->b};
+        for (int i = 0; i < 2; ++i) {
+            if (!pl->in_bytes[i])
+                continue;
+            const size_t es = dtype_size(im[i]->dtype);
+            char *dst = pl->staged[i];
+            const size_t bytes = (size_t)im[i]->w * im[i]->h * es;
+            const char *src = (const char *)im[i]->data;
+            if (im[i]->stride == im[i]->w) {
+                if (run_src && src == run_end && dst == run_dst + (run_end - run_src)) {
+                    run_end += bytes;
+                } else {
+                    if (int rc = flush())
+                        return rc;
+                    run_src = src;
+                    run_end = src + bytes;
+                    run_dst = dst;
+                }
+            } else {
+                if (int rc = flush())
+                    return rc;
+                CK(cudaMemcpy2DAsync(dst, (size_t)im[i]->w * es, im[i]->data,
+                                     (size_t)im[i]->stride * es, (size_t)im[i]->w * es, im[i]->h,
+                                     cudaMemcpyHostToDevice, ctx->cstream));
+                ctx->h2d_bytes += (long long)bytes;
+            }
+        }
+    }
+    if (int rc = flush())
+        return rc;
+    prof_end_copy(ctx);
+    CK(cudaEventRecord(ctx->ev_copy[wp], ctx->cstream));
+    return ALN_OK;
+}
+
 // Runs CorrPatches (specs == NULL) or CorrImages jobs in chunks of equal FFT
 // size and job kind through the two-stage pipeline.
 // spectrum key of a job's image b: namespace (0 caller, 1 library) and key
@@ -1996,67 +2079,140 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
         if (int rc = plan_pair(ctx, pairs[k], plans[k], sp == nullptr, sp))
             return rc;
     }
-    // group by FFT size and job kind, keep submission order inside a group,
-    // split into chunks bounded by the workspace budget
-    std::map<std::tuple<int, int, int, int, int, int, int>, std::vector<PairPlan *>> groups;
-    for (auto &pl : plans)
-        if (pl.d.status == 0)
-            groups[std::make_tuple(pl.d.Nx, pl.d.Ny, pl.frame_nx1, pl.frame_ny1, pl.d.mode,
-                                   pl.d.want_r, pl.d.want_s)]
-                .push_back(&pl);
-    std::vector<std::vector<PairPlan *>> chunks;
-    size_t max_stage = 0, max_work = 0, max_n = 1;
-    for (auto &g : groups) {
-        std::vector<PairPlan *> chunk;
-        size_t sb = 0, wb = 0;
-        auto close = [&]() {
-            max_stage = std::max(max_stage, sb);
-            max_work = std::max(max_work, wb);
-            max_n = std::max(max_n, chunk.size());
-            chunks.push_back(chunk);
-            chunk.clear();
-            sb = wb = 0;
-        };
-        for (PairPlan *pl : g.second) {
-            const size_t st = pl->in_bytes[0] + pl->in_bytes[1];
-            const size_t wk = pl->ws_bytes - st;
-            if (!chunk.empty() && (sb + st + wb + wk > ctx->ws_budget || chunk.size() >= 4096))
-                close();
-            chunk.push_back(pl);
-            sb += st + 16;
-            wb += wk;
+    // Windows: runs of consecutive jobs (submission order) whose host inputs
+    // fit one staging buffer.  A window's host images are copied in one go
+    // on the copy stream -- adjacent host images with one transfer -- while
+    // the previous window computes.  Inside a window, jobs are grouped by FFT
+    // size and job kind (submission order kept) and split into chunks
+    // bounded by the workspace budget.  Device-resident inputs need no
+    // staging: then the whole batch is one window.
+    const size_t win_cap = std::max((size_t)64 << 20, ctx->ws_budget / 8);
+    std::vector<std::vector<PairPlan *>> windows(1);
+    {
+        size_t sb = 0;
+        for (auto &pl : plans) {
+            if (pl.d.status != 0)
+                continue;
+            const size_t st = pl.in_bytes[0] + pl.in_bytes[1] + 16;
+            if (!windows.back().empty() && st > 16 && sb + st > win_cap) {
+                windows.emplace_back();
+                sb = 0;
+            }
+            windows.back().push_back(&pl);
+            sb += st;
         }
-        if (!chunk.empty())
-            close();
+    }
+    std::vector<std::vector<std::vector<PairPlan *>>> wchunks(windows.size());
+    size_t max_stage = 0, max_work = 0, max_n = 1;
+    for (size_t w = 0; w < windows.size(); ++w) {
+        std::map<std::tuple<int, int, int, int, int, int, int>, std::vector<PairPlan *>> groups;
+        size_t sb = 0;
+        for (PairPlan *pl : windows[w]) {
+            groups[std::make_tuple(pl->d.Nx, pl->d.Ny, pl->frame_nx1, pl->frame_ny1, pl->d.mode,
+                                   pl->d.want_r, pl->d.want_s)]
+                .push_back(pl);
+            sb += pl->in_bytes[0] + pl->in_bytes[1] + 16;
+        }
+        max_stage = std::max(max_stage, sb);
+        for (auto &g : groups) {
+            std::vector<PairPlan *> chunk;
+            size_t wb = 0;
+            for (PairPlan *pl : g.second) {
+                const size_t wk = pl->ws_bytes - pl->in_bytes[0] - pl->in_bytes[1];
+                if (!chunk.empty() && (wb + wk > ctx->ws_budget || chunk.size() >= 4096)) {
+                    max_work = std::max(max_work, wb);
+                    max_n = std::max(max_n, chunk.size());
+                    wchunks[w].push_back(chunk);
+                    chunk.clear();
+                    wb = 0;
+                }
+                chunk.push_back(pl);
+                wb += wk;
+            }
+            if (!chunk.empty()) {
+                max_work = std::max(max_work, wb);
+                max_n = std::max(max_n, chunk.size());
+                wchunks[w].push_back(chunk);
+            }
+        }
     }
     max_stage = al256(max_stage);
     max_work = al256(max_work);
+    (void)max_n;
     if (int rc = ensure_ws(ctx, 2 * max_stage + max_work))
         return rc;
-    if (int rc = ensure_pairs(ctx, max_n))
+    if (int rc = ensure_pairs(ctx, (size_t)std::max(npairs, 1)))
         return rc;
-    if (int rc = ensure_hres(ctx, (size_t)npairs))
+    if (int rc = ensure_hres(ctx, (size_t)std::max(npairs, 1)))
         return rc;
-    // two-stage pipeline over the chunks
-    size_t done = 0;
-    std::vector<size_t> first(chunks.size());
-    for (size_t c = 0; c < chunks.size(); ++c) {
-        const int par = (int)(c & 1);
-        first[c] = done;
-        if (int rc = run_chunk(ctx, chunks[c], par, ctx->ws + par * max_stage,
-                               ctx->ws + 2 * max_stage, ctx->hres + done)) {
-            cudaStreamSynchronize(ctx->cstream);
-            cudaStreamSynchronize(ctx->stream);
-            return rc;
+    // host side of every chunk first: staging addresses, workspaces, cache
+    // keys, one job table and one fill list for the whole batch
+    std::vector<std::vector<PairPlan *> *> order;
+    std::vector<ChunkLaunch> cls;
+    std::vector<int> fills;
+    int off = 0;
+    for (size_t w = 0; w < windows.size(); ++w) {
+        assign_staging(windows[w], ctx->ws + (w & 1) * max_stage);
+        for (auto &chunk : wchunks[w]) {
+            ChunkLaunch cl;
+            prep_chunk(ctx, chunk, off, ctx->ws + 2 * max_stage, ctx->htab + off, fills, cl);
+            cls.push_back(cl);
+            order.push_back(&chunk);
+            off += cl.n;
         }
-        done += chunks[c].size();
     }
-    CK(cudaStreamSynchronize(ctx->stream));
+    if (fills.size() > ctx->dsel_cap) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        cudaFree(ctx->dsel);
+        ctx->dsel = nullptr;
+        ctx->dsel_cap = 0;
+        const size_t cap = std::max<size_t>(fills.size(), 4096);
+        CK(cudaMalloc(&ctx->dsel, cap * sizeof(int)));
+        ctx->dsel_cap = cap;
+    }
+    cudaStream_t st = ctx->stream;
+    if (off > 0)
+        CK(cudaMemcpyAsync(ctx->dpairs_base, ctx->htab, (size_t)off * sizeof(PairDev),
+                           cudaMemcpyHostToDevice, st));
+    if (!fills.empty())
+        CK(cudaMemcpyAsync(ctx->dsel, fills.data(), fills.size() * sizeof(int),
+                           cudaMemcpyHostToDevice, st));
+    // two-stage pipeline: window w+1's copies are queued before window w's
+    // kernels, on the copy stream; the kernels wait for their window only
+    size_t ci = 0;
+    for (size_t w = 0; w <= windows.size(); ++w) {
+        if (w < windows.size()) {
+            if (int rc = stage_window(ctx, windows[w], (int)(w & 1))) {
+                cudaStreamSynchronize(ctx->cstream);
+                cudaStreamSynchronize(st);
+                return rc;
+            }
+        }
+        if (w == 0)
+            continue;
+        const size_t cw = w - 1;   // the window computed now
+        const int wp = (int)(cw & 1);
+        CK(cudaStreamWaitEvent(st, ctx->ev_copy[wp], 0));
+        for (size_t q = 0; q < wchunks[cw].size(); ++q, ++ci) {
+            if (int rc = launch_chunk(ctx, *order[ci], cls[ci])) {
+                cudaStreamSynchronize(ctx->cstream);
+                cudaStreamSynchronize(st);
+                return rc;
+            }
+        }
+        CK(cudaEventRecord(ctx->ev_wdone[wp], st));
+    }
+    if (off > 0) {
+        CK(cudaMemcpyAsync(ctx->hres, ctx->dres_base, (size_t)off * sizeof(ResultDev),
+                           cudaMemcpyDeviceToHost, st));
+        ctx->d2h_bytes += (long long)off * sizeof(ResultDev);
+    }
+    CK(cudaStreamSynchronize(st));
     prof_collect(ctx);
-    for (size_t c = 0; c < chunks.size(); ++c)
-        for (size_t k = 0; k < chunks[c].size(); ++k) {
-            const ResultDev &r = ctx->hres[first[c] + k];
-            PairDev &d = chunks[c][k]->d;
+    for (size_t c = 0; c < order.size(); ++c)
+        for (int k = 0; k < cls[c].n; ++k) {
+            const ResultDev &r = ctx->hres[cls[c].off + k];
+            PairDev &d = (*order[c])[k]->d;
             d.r = r.r;
             d.dx = r.dx;
             d.dy = r.dy;
@@ -2347,6 +2503,8 @@ extern "C" void aln_ctx_profile_reset(aln_ctx *ctx)
     ctx->launches = 0;
     ctx->h2d_bytes = ctx->d2h_bytes = 0;
     ctx->spec_hits = ctx->spec_fills = 0;
+    ctx->chunks = 0;
+    ctx->h2d_copies = 0;
 }
 
 extern "C" int aln_ctx_profile(aln_ctx *ctx, int cap, const char **names,
@@ -2385,6 +2543,8 @@ extern "C" long long aln_ctx_counter(aln_ctx *ctx, int which)
     case 3: return ctx->spec_hits;
     case 4: return ctx->spec_fills;
     case 5: return (long long)ctx->spec_bytes;
+    case 6: return ctx->chunks;
+    case 7: return ctx->h2d_copies;
     default: return -1;
     }
 }

@@ -274,7 +274,9 @@ class Context:
                 "d2h_bytes": self._L.aln_ctx_counter(self.h, 2),
                 "spec_hits": self._L.aln_ctx_counter(self.h, 3),
                 "spec_fills": self._L.aln_ctx_counter(self.h, 4),
-                "spec_bytes": self._L.aln_ctx_counter(self.h, 5)}
+                "spec_bytes": self._L.aln_ctx_counter(self.h, 5),
+                "chunks": self._L.aln_ctx_counter(self.h, 6),
+                "h2d_copies": self._L.aln_ctx_counter(self.h, 7)}
 
     def set_spectrum_cache(self, nbytes: int):
         self._check(self._L.aln_ctx_set_spectrum_cache(self.h, nbytes))

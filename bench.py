@@ -406,17 +406,22 @@ def run_gpu(args):
             raise RuntimeError(L.aln_last_error(ctx.h).decode())
 
     step_host()
+    ctx.set_profiling(True)
     ctx.profile_reset()
     barrier(dist)
     torch.cuda.synchronize()
     e0.record()
+    t_host = time.perf_counter()
     for _ in range(args.steps):
         step_host()
     e1.record()
     torch.cuda.synchronize()
+    t_host = time.perf_counter() - t_host
     barrier(dist)
     ms_e2e = max_over_ranks(dist, e0.elapsed_time(e1), dev)
     cnt = ctx.counters()
+    prof_e2e = ctx.profile()
+    ctx.set_profiling(False)
     e2e_value = ws * n * args.steps / (ms_e2e / 1000.0)
 
     # the host link alone: one pinned-to-device copy of the step's strips
@@ -511,6 +516,10 @@ def run_gpu(args):
             "clocks": clocks,
             "gpu_launches": launches,
             "kernels_ms": {k: round(v[1], 3) for k, v in sorted(ours.items())},
+            "kernels_ms_e2e": {k: round(v[1], 3) for k, v in sorted(prof_e2e.items())},
+            "e2e_host_wall_ms_per_step": 1000.0 * t_host / args.steps,
+            "chunks_per_step": cnt["chunks"] / args.steps,
+            "h2d_copies_per_step": cnt["h2d_copies"] / args.steps,
             "plain": {"pairs_per_s": plain_pps, "p50_ms": lat_ms[len(lat_ms) // 2],
                       "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))],
                       "sample": len(lat_ms)},

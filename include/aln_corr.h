@@ -135,7 +135,9 @@ int aln_ctx_profile(aln_ctx *ctx, int cap, const char **names, long long *launch
                     double *ms);
 /* which: 0 = kernel launches, 1 = host-to-device bytes, 2 = device-to-host
  * bytes, 3 = spectrum-cache hits, 4 = spectrum-cache fills (counted since
- * the last aln_ctx_profile_reset), 5 = device bytes the cache holds. */
+ * the last aln_ctx_profile_reset), 5 = device bytes the cache holds,
+ * 6 = batch chunks run, 7 = host-to-device staging transfers issued (both
+ * since the last reset). */
 long long aln_ctx_counter(aln_ctx *ctx, int which);
 
 /* Spectrum cache: the device-resident form of the reference's fft2 / ftc
