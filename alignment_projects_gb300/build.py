@@ -35,6 +35,29 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+SHIM_SRC = os.path.join(PKG, "shim", "aln_correlation_shim.cpp")
+SHIM_HDR = os.path.join(PKG, "shim", "aln_correlation.hpp")
+SHIM_LIB = os.path.join(LIBDIR, "libaln_corr_shim.so")
+
+
+def build_shim(force: bool = False, verbose: bool = False) -> str:
+    """The C++ drop-in for the Correlation.h entry points (g++), linked
+    against libaln_corr.so in the same directory."""
+    lib = build(force=force, verbose=verbose)
+    deps = [SHIM_SRC, SHIM_HDR, os.path.join(ROOT, "include", "aln_corr.h"), lib]
+    if not force and not _stale(SHIM_LIB, deps):
+        return SHIM_LIB
+    tmp = SHIM_LIB + ".tmp%d" % os.getpid()
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off",
+           "-shared", "-o", tmp, SHIM_SRC, "-L" + LIBDIR, "-laln_corr",
+           "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), file=sys.stderr)
+    subprocess.check_call(cmd)
+    os.replace(tmp, SHIM_LIB)
+    return SHIM_LIB
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
     deps = srcs + [os.path.join(CSRC, h) for h in HEADERS] + [
@@ -53,3 +76,4 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))
+    print(build_shim(verbose=True))

@@ -1,0 +1,321 @@
+// aln_correlation_shim.cpp -- libaln_corr_shim.so: the Correlation.h entry
+// points of aln_correlation.hpp over the C ABI of libaln_corr.so (GPU).
+//
+// What the shim does on the host is the boundary's format work only: point
+// lists become bounding-box rasters (BBoxFromPoints, 0_GEN/Geometry.cpp:
+// 78-106; ImageFromValuesAndPoints / DistributePixel, Geometry.cpp:661-685,
+// Maths.h:236-276), EvalType callbacks become typed legality descriptors,
+// the reference's fft2 / ftc cache vectors become spectrum-cache keys.  Every
+// correlation runs on the GPU; there is no CPU fallback: if the GPU library
+// fails, the call logs the error to flog and returns 0.0, the reference's
+// "no result" value.
+#include "aln_correlation.hpp"
+
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <atomic>
+#include <vector>
+
+#include "../../include/aln_corr.h"
+
+namespace {
+
+// one context per host thread (the reference serialises its FFTs under a
+// mutex; here each thread has its own stream and workspace)
+aln_ctx *ctx()
+{
+    static thread_local aln_ctx *c = nullptr;
+    if (!c && aln_ctx_create(0, &c) != ALN_OK)
+        c = nullptr;
+    return c;
+}
+
+struct IBoxD {
+    int L, R, B, T;
+};
+
+IBoxD bbox(const std::vector<Point> &p)
+{
+    double xlo = p[0].x, xhi = p[0].x, ylo = p[0].y, yhi = p[0].y;
+    for (size_t i = 1; i < p.size(); ++i) {
+        const double x = p[i].x, y = p[i].y;
+        if (x < xlo)
+            xlo = x;
+        else if (x > xhi)
+            xhi = x;
+        if (y < ylo)
+            ylo = y;
+        else if (y > yhi)
+            yhi = y;
+    }
+    return IBoxD{(int)floor(xlo), (int)ceil(xhi), (int)floor(ylo), (int)ceil(yhi)};
+}
+
+// The points' raster over their bounding box: bilinear weights of each
+// point's value on the four pixels around it, bounds-checked (integer
+// points land on one pixel with weight 1).
+std::vector<double> raster(const std::vector<Point> &p, const std::vector<double> &v,
+                           const IBoxD &B)
+{
+    const int w = B.R - B.L + 1, h = B.T - B.B + 1;
+    std::vector<double> I((size_t)w * h, 0.0);
+    for (size_t k = 0; k < p.size(); ++k) {
+        const double x = p[k].x - B.L, y = p[k].y - B.B;
+        int ix = (int)floor(x), iy = (int)floor(y);
+        const double a = x - ix, b = y - iy, val = v[k];
+        for (int dxp = 0; dxp < 2; ++dxp) {
+            const int X = ix + dxp;
+            if (X < 0 || X >= w)
+                continue;
+            const double wx = dxp ? a : 1.0 - a;
+            for (int dyp = 0; dyp < 2; ++dyp) {
+                const int Y = iy + dyp;
+                if (Y < 0 || Y >= h)
+                    continue;
+                I[(size_t)X + (size_t)w * Y] += wx * (dyp ? b : 1.0 - b) * val;
+            }
+        }
+    }
+    return I;
+}
+
+aln_image image_of(const std::vector<double> &I, const IBoxD &B)
+{
+    aln_image im;
+    im.data = I.data();
+    im.dtype = ALN_F64;
+    im.w = B.R - B.L + 1;
+    im.h = B.T - B.B + 1;
+    im.stride = im.w;
+    im.x0 = B.L;
+    im.y0 = B.B;
+    im.on_device = 0;
+    return im;
+}
+
+// LegalRgn -> a table over every overlap size the pair can have; LegalCnt
+// -> the count threshold n of "c1 > n && c2 > n" (EnoughPoints,
+// 0_GEN/CThmScan.cpp:39-42), found by bisection and checked; any other
+// LegalCnt shape is refused.
+bool legal_of(EvalType rgn, void *arglr, EvalType cnt, void *arglc, int w1, int h1, int w2,
+              int h2, aln_legal &lg, std::vector<unsigned char> &tab, FILE *flog)
+{
+    memset(&lg, 0, sizeof lg);
+    if (rgn) {
+        const int tw = w1 < w2 ? w1 : w2, th = h1 < h2 ? h1 : h2;
+        tab.assign((size_t)tw * th, 0);
+        for (int sy = 1; sy <= th; ++sy)
+            for (int sx = 1; sx <= tw; ++sx)
+                tab[(size_t)(sy - 1) * tw + (sx - 1)] = rgn(sx, sy, arglr) ? 1 : 0;
+        lg.rgn_kind = ALN_RGN_TABLE;
+        lg.table = tab.data();
+        lg.table_w = tw;
+        lg.table_h = th;
+    }
+    if (cnt) {
+        const long long cmax = (long long)w1 * h1 + (long long)w2 * h2 + 1;
+        if (!cnt((int)cmax, (int)cmax, arglc)) {
+            lg.cnt_kind = ALN_CNT_GT;   // never legal
+            lg.cnt_n = cmax;
+            return true;
+        }
+        long long lo = -1, hi = cmax;   // cnt(c, c) false at lo, true at hi
+        if (cnt(0, 0, arglc))
+            hi = 0;
+        while (hi - lo > 1) {
+            const long long m = (lo + hi) / 2;
+            (cnt((int)m, (int)m, arglc) ? hi : lo) = m;
+        }
+        const long long n = hi - 1;
+        const bool ok = (n < 0 || !cnt((int)n, (int)cmax, arglc)) &&
+                        (n < 0 || !cnt((int)cmax, (int)n, arglc)) &&
+                        cnt((int)hi, (int)cmax, arglc) && cnt((int)cmax, (int)hi, arglc);
+        if (!ok) {
+            fprintf(flog, "GPU correlation: LegalCnt is not of the form c1 > n && c2 > n\n");
+            return false;
+        }
+        lg.cnt_kind = ALN_CNT_GT;
+        lg.cnt_n = n;
+    }
+    return true;
+}
+
+// fft2 / ftc: the reference reuses image 2's spectrum while the vector keeps
+// the FFT's size.  The vector's contents are the shim's own: its first
+// element carries the spectrum-cache key of the image it was filled for.
+std::atomic<unsigned long long> g_key{1};
+
+unsigned long long key_of(std::vector<CD> &fft2, size_t M)
+{
+    unsigned long long k = 0;
+    if (fft2.size() == M && M > 0) {
+        const double re = fft2[0].real();
+        memcpy(&k, &re, sizeof k);
+        return k;
+    }
+    k = (g_key++ << 1) | 1;   // never 0 (0 means "no key")
+    fft2.assign(M, CD(0.0, 0.0));
+    double re;
+    memcpy(&re, &k, sizeof re);
+    if (M)
+        fft2[0] = CD(re, 0.0);
+    return k;
+}
+
+}   // namespace
+
+int FFTSize(int n1, int n2) { return aln_fft_size(n1, n2); }
+
+int FFTSizeSQR(int w1, int h1, int w2, int h2) { return aln_fft_size_sqr(w1, h1, w2, h2); }
+
+int FFT_2D(std::vector<CD> &out, const std::vector<double> &in, int Nfast, int Nslow,
+           bool cached, FILE *flog)
+{
+    const int M = Nslow * (Nfast / 2 + 1);
+    if (cached && (int)out.size() == M)
+        return M;
+    out.resize(M);
+    const int rc = aln_fft_2d(ctx(), in.data(), Nfast, Nslow, (double *)out.data());
+    if (rc < 0)
+        fprintf(flog, "FFT_2D: %s\n", aln_last_error(ctx()));
+    return M;
+}
+
+void IFT_2D(std::vector<double> &out, const std::vector<CD> &in, int Nfast, int Nslow,
+            FILE *flog)
+{
+    out.resize((size_t)Nfast * Nslow);
+    if (aln_ift_2d(ctx(), (const double *)in.data(), Nfast, Nslow, out.data()) < 0)
+        fprintf(flog, "IFT_2D: %s\n", aln_last_error(ctx()));
+}
+
+void ParabPeakFFT(double &xpk, double &ypk, int d, const double *I, int nx, int ny)
+{
+    aln_parab_peak_fft(&xpk, &ypk, d, I, nx, ny);
+}
+
+double CorrPatches(FILE *flog, int verbose, double &dx, double &dy,
+                   const std::vector<Point> &ip1, const std::vector<double> &iv1,
+                   const std::vector<Point> &ip2, const std::vector<double> &iv2, int Ox,
+                   int Oy, int radius, EvalType LegalRgn, void *arglr, EvalType LegalCnt,
+                   void *arglc, std::vector<CD> &fft2)
+{
+    if (ip1.empty() || ip2.empty())
+        return 0.0;
+    const IBoxD B1 = bbox(ip1), B2 = bbox(ip2);
+    const std::vector<double> r1 = raster(ip1, iv1, B1), r2 = raster(ip2, iv2, B2);
+    aln_pair P;
+    memset(&P, 0, sizeof P);
+    P.a = image_of(r1, B1);
+    P.b = image_of(r2, B2);
+    P.ox = Ox;
+    P.oy = Oy;
+    P.radius = radius;
+    std::vector<unsigned char> tab;
+    if (!legal_of(LegalRgn, arglr, LegalCnt, arglc, P.a.w, P.a.h, P.b.w, P.b.h, P.legal, tab,
+                  flog))
+        return 0.0;
+    const int Nx = aln_fft_size(P.a.w, P.b.w), Ny = aln_fft_size(P.a.h, P.b.h);
+    P.b_key = key_of(fft2, (size_t)Ny * (Nx / 2 + 1));
+    aln_result res;
+    if (aln_corr_patches_batch(ctx(), 1, &P, &res) < 0) {
+        fprintf(flog, "CorrPatches (GPU): %s\n", aln_last_error(ctx()));
+        return 0.0;
+    }
+    if (res.status != ALN_OK) {
+        if (verbose)
+            fprintf(flog, "NormCorr: No legal subregions at all...\n");
+        return 0.0;
+    }
+    if (verbose)
+        fprintf(flog, "NormCorr: Maximum correlation of %f at [%d,%d].\n", res.r, res.peak_x,
+                res.peak_y);
+    dx = res.dx;
+    dy = res.dy;
+    return res.r;
+}
+
+double CorrPatchToImage(double &dx, double &dy, const std::vector<Point> &ip1,
+                        const std::vector<double> &iv1, const std::vector<double> &i2, int Ox,
+                        int Oy, int radius, bool bFilter)
+{
+    aln_result res;
+    const int rc = aln_corr_patch_to_image(ctx(), (const double *)ip1.data(), iv1.data(),
+                                           (int)ip1.size(), i2.data(), (int)i2.size(), Ox, Oy,
+                                           radius, bFilter ? 1 : 0, &res);
+    if (rc < 0 || res.status != ALN_OK)
+        return 0.0;
+    dx = res.dx;
+    dy = res.dy;
+    return res.r;
+}
+
+namespace {
+
+double corr_images(int kind, FILE *flog, int verbose, double &dx, double &dy,
+                   const std::vector<Point> &ip1, const std::vector<double> &iv1,
+                   const std::vector<Point> &ip2, const std::vector<double> &iv2,
+                   EvalType LegalRgn, void *arglr, EvalType LegalCnt, void *arglc,
+                   double mincor, double nbmaxht, int Ox, int Oy, int Rx, int Ry,
+                   std::vector<CD> &fft2)
+{
+    if (ip1.empty() || ip2.empty())
+        return 0.0;
+    const IBoxD B1 = bbox(ip1), B2 = bbox(ip2);
+    const std::vector<double> r1 = raster(ip1, iv1, B1), r2 = raster(ip2, iv2, B2);
+    aln_image_job J;
+    memset(&J, 0, sizeof J);
+    J.a = image_of(r1, B1);
+    J.b = image_of(r2, B2);
+    J.kind = kind;
+    J.mincor = mincor;
+    J.nbmaxht = nbmaxht;
+    J.ox = Ox;
+    J.oy = Oy;
+    J.rx = Rx;
+    J.ry = Ry;
+    std::vector<unsigned char> tab;
+    if (!legal_of(LegalRgn, arglr, LegalCnt, arglc, J.a.w, J.a.h, J.b.w, J.b.h, J.legal, tab,
+                  flog))
+        return 0.0;
+    const int Nx = aln_fft_size(J.a.w, J.b.w), Ny = aln_fft_size(J.a.h, J.b.h);
+    J.b_key = key_of(fft2, (size_t)Ny * (Nx / 2 + 1));
+    aln_result res;
+    if (aln_corr_images_batch(ctx(), 1, &J, &res) < 0) {
+        fprintf(flog, "CorrImages (GPU): %s\n", aln_last_error(ctx()));
+        return 0.0;
+    }
+    if (res.status != ALN_OK)
+        return 0.0;
+    if (verbose)
+        fprintf(flog, "CorrImages: peak %f at [%d,%d].\n", res.r, res.peak_x, res.peak_y);
+    dx = res.dx;
+    dy = res.dy;
+    return res.r;
+}
+
+}   // namespace
+
+double CorrImagesR(FILE *flog, int verbose, double &dx, double &dy,
+                   const std::vector<Point> &ip1, const std::vector<double> &iv1,
+                   const std::vector<Point> &ip2, const std::vector<double> &iv2,
+                   EvalType LegalRgn, void *arglr, EvalType LegalCnt, void *arglc,
+                   double mincor, double nbmaxht, int Ox, int Oy, int Rx, int Ry,
+                   std::vector<CD> &fft2)
+{
+    return corr_images(ALN_CORR_R, flog, verbose, dx, dy, ip1, iv1, ip2, iv2, LegalRgn, arglr,
+                       LegalCnt, arglc, mincor, nbmaxht, Ox, Oy, Rx, Ry, fft2);
+}
+
+double CorrImagesS(FILE *flog, int verbose, double &dx, double &dy,
+                   const std::vector<Point> &ip1, const std::vector<double> &iv1,
+                   const std::vector<Point> &ip2, const std::vector<double> &iv2,
+                   EvalType LegalRgn, void *arglr, EvalType LegalCnt, void *arglc,
+                   double mincor, double nbmaxht, int Ox, int Oy, int Rx, int Ry,
+                   std::vector<CD> &fft2)
+{
+    return corr_images(ALN_CORR_S, flog, verbose, dx, dy, ip1, iv1, ip2, iv2, LegalRgn, arglr,
+                       LegalCnt, arglc, mincor, nbmaxht, Ox, Oy, Rx, Ry, fft2);
+}

@@ -1,0 +1,76 @@
+"""The C++ drop-in on the GPU: a C++ program calls CorrPatches / CorrImagesR /
+CorrImagesS / FFT_2D / IFT_2D through the reference's signatures
+(alignment_projects_gb300/shim/aln_correlation.hpp); results match the
+reference's golden outputs (r within 1e-4, offsets within 0.01 px where the
+peak is clear) and the fft2 cache vector gives the same numbers."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from shim_util import build_check, case
+
+pytestmark = pytest.mark.gpu
+
+MARGIN = 1e-3
+
+
+def _legal_args(lg):
+    kind, a, b, area, ck, cn = (int(v) for v in lg)
+    assert kind in (0, 1)
+    return dict(rgn_min=max(a, 1) if kind == 1 else 0, rgn_area=area if kind == 1 else 0,
+                cnt_n=cn if ck == 1 else -1)
+
+
+def test_cpp_callers_through_shim(tmp_path, orc):
+    import oracle
+    exe = build_check(str(tmp_path))
+    gp = load_golden("corr_patches")
+    gi = load_golden("corr_images")
+    blob, expect = b"", []
+    for k in ("kat_testnormcorr", "plain96_s1", "plain96_s2", "ragged_none", "ragged_disc",
+              "ragged_cnt", "u16_holes"):
+        d = gp[k]
+        la = _legal_args(d["legal"])
+        blob += case(0, d["pa"], d["va"], d["pb"], d["vb"], int(d["ox"]), int(d["oy"]),
+                     int(d["radius"]), **la)
+        o = orc.corr_patches(d["pa"], d["va"], d["pb"], d["vb"], int(d["ox"]), int(d["oy"]),
+                             int(d["radius"]), oracle.legal(*[int(v) for v in d["legal"]]))
+        expect.append((k, float(d["r"]), float(d["dx"]), float(d["dy"]),
+                       o["r"] - o["second"] > MARGIN, 1e-4))
+    # the same image b again through the same fft2 vector (cache path)
+    d = gp["plain96_s1"]
+    la = _legal_args(d["legal"])
+    blob += case(0, d["pa"], d["va"], d["pb"], d["vb"], int(d["ox"]), int(d["oy"]),
+                 int(d["radius"]), reuse=1, **la)
+    expect.append(("plain96_s1 cached", float(d["r"]), float(d["dx"]), float(d["dy"]), True,
+                   1e-4))
+    for k in ("img_s0_k1_d0_m0", "img_s0_k1_d1_m1", "img_s0_k2_d0_m0", "img_s0_k2_d1_m0",
+              "img_s1_k2_d1_m1"):
+        d = gi[k]
+        kind = int(d["kind"])
+        disc = [int(v) for v in d["disc"]]
+        la = _legal_args(d["legal"])
+        blob += case(kind, d["pa"], d["va"], d["pb"], d["vb"], disc[0], disc[1], 4096, disc[2],
+                     disc[3], mincor=float(d["mincor"]), **la)
+        o = orc.corr_images(kind, d["pa"], d["va"], d["pb"], d["vb"],
+                            oracle.legal(*[int(v) for v in d["legal"]]), float(d["mincor"]),
+                            0.75, *disc)
+        tol = 1e-4 if kind == 1 else 1e-4 * max(1.0, abs(float(d["r"])))
+        expect.append((k, float(d["r"]), float(d["dx"]), float(d["dy"]),
+                       o["r"] - o["second"] > MARGIN, tol))
+    cases = os.path.join(str(tmp_path), "cases.bin")
+    open(cases, "wb").write(blob)
+    out = subprocess.run([exe, cases], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.strip().splitlines()
+    assert len(lines) == len(expect) + 1
+    for (name, r, dx, dy, clear, tol), ln in zip(expect, lines):
+        gr, gdx, gdy = (float(v) for v in ln.split())
+        assert abs(gr - r) <= tol, (name, gr, r)
+        if clear:
+            assert abs(gdx - dx) <= 0.01 and abs(gdy - dy) <= 0.01, (name, gdx, gdy, dx, dy)
+    f = lines[-1].split()
+    assert f[0] == "fft" and int(f[1]) == 4 * 5 and float(f[2]) < 1e-4 and int(f[3]) == 1024

@@ -1,0 +1,84 @@
+"""The C++ drop-in (libaln_corr_shim.so) exports the reference's
+Correlation.h symbols under exactly the reference's mangled names, so its
+callers relink unchanged.  Checked against the reference's own build
+(oracle/_ref, compiled from its sources by oracle/ref/Makefile) and by linking
+one of the reference's own caller programs against the shim.  No GPU needed:
+nothing here runs a correlation."""
+import os
+import subprocess
+import tempfile
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+EXPECTED = {
+    "FFTSize": "_Z7FFTSizeii",
+    "FFTSizeSQR": "_Z10FFTSizeSQRiiii",
+    "FFT_2D": "_Z6FFT_2DRSt6vectorISt7complexIdESaIS1_EERKS_IdSaIdEEiibP8_IO_FILE",
+    "IFT_2D": "_Z6IFT_2DRSt6vectorIdSaIdEERKS_ISt7complexIdESaIS4_EEiiP8_IO_FILE",
+    "ParabPeakFFT": "_Z12ParabPeakFFTRdS_iPKdii",
+    "CorrPatches": "_Z11CorrPatchesP8_IO_FILEiRdS1_RKSt6vectorI5PointSaIS3_EERKS2_IdSaIdEES7_SB_"
+                   "iiiPFbiiPvESC_SE_SC_RS2_ISt7complexIdESaISG_EE",
+    "CorrPatchToImage": "_Z16CorrPatchToImageRdS_RKSt6vectorI5PointSaIS1_EERKS0_IdSaIdEES9_iiib",
+    "CorrImagesR": "_Z11CorrImagesRP8_IO_FILEiRdS1_RKSt6vectorI5PointSaIS3_EERKS2_IdSaIdEES7_SB_"
+                   "PFbiiPvESC_SE_SC_ddiiiiRS2_ISt7complexIdESaISG_EE",
+    "CorrImagesS": "_Z11CorrImagesSP8_IO_FILEiRdS1_RKSt6vectorI5PointSaIS3_EERKS2_IdSaIdEES7_SB_"
+                   "PFbiiPvESC_SE_SC_ddiiiiRS2_ISt7complexIdESaISG_EE",
+}
+
+
+def _exports(path):
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True,
+                         check=True).stdout
+    return {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+
+
+@pytest.fixture(scope="module")
+def shim():
+    from alignment_projects_gb300 import build as b
+    return b.build_shim()
+
+
+def test_shim_exports_reference_signatures(shim):
+    ex = _exports(shim)
+    for name, mangled in EXPECTED.items():
+        assert mangled in ex, name
+    # nothing else at namespace scope: the shim adds no stray symbols
+    assert {s for s in ex if s.startswith("_Z") and "St" not in s[:4]} <= set(EXPECTED.values())
+
+
+def test_same_names_as_the_reference_build(shim):
+    import oracle
+    if not oracle.ref_available():
+        try:
+            oracle.build_ref()
+        except Exception:
+            pass
+    if not oracle.ref_available():
+        pytest.skip("the reference's own build exists only where its sources are mounted")
+    ref = _exports(oracle.REF_SO)
+    for name, mangled in EXPECTED.items():
+        assert mangled in ref, name
+
+
+def test_reference_caller_links_against_shim(shim):
+    """The reference's own CorrPatches test program (Retired_Proj/4_TestNormCorr),
+    compiled from its sources where they lie, links against the shim in place
+    of Correlation.o."""
+    import oracle
+    src = os.path.join(oracle.REFERENCE_TREE, "Retired_Proj", "4_TestNormCorr",
+                       "testnormcorr.cpp")
+    timer = os.path.join(os.path.dirname(oracle.REF_SO), "Timer.o")
+    if not (os.path.exists(src) and oracle.ref_available() and os.path.exists(timer)):
+        pytest.skip("the reference's sources are not mounted here")
+    gen = os.path.join(oracle.REFERENCE_TREE, "0_GEN")
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "testnormcorr")
+        subprocess.check_call(["g++", "-O1", "-w", "-DTIXML_USE_STL", "-I" + gen,
+                               "-I" + os.path.join(oracle.REFERENCE_TREE, "0_UTL"),
+                               "-I" + os.path.join(ROOT, "oracle", "ref"),
+                               "-o", exe, src, timer, "-L" + os.path.dirname(shim),
+                               "-laln_corr_shim", "-laln_corr", "-lpthread",
+                               "-Wl,-rpath," + os.path.dirname(shim)])
+        assert os.path.exists(exe)
