@@ -140,6 +140,47 @@ __device__ __forceinline__ bool rgn_ok(const PairDev &p, int sx, int sy)
 // Pearson r of lag (x, y) given the shifted cross sum cs = C'/(Nx*Ny).
 // Returns false (and r = 0) for an illegal lag, as CLinCorr::CheckSize /
 // CheckDensity / GetCorr do (0_GEN/Correlation.cpp:658-757).
+// num / sqrt(d1 * d2) without an FP64 divide or square root: FP32
+// reciprocal square roots of the factors, one Newton step in FP64 on their
+// product (relative error ~1e-14).  Factors outside the FP32 range take the
+// plain formula.
+__device__ __forceinline__ double div_sqrt2(double num, double d1, double d2)
+{
+    const double d = d1 * d2;
+    if (!(d1 > 1e-30 && d1 < 1e30 && d2 > 1e-30 && d2 < 1e30))
+        return num / sqrt(d);
+    double y = (double)(rsqrtf((float)d1) * rsqrtf((float)d2));
+    y = y * (1.5 - 0.5 * d * y * y);
+    return num * y;
+}
+
+// CLinCorr::GetCorr's terms for integer pixels: n*Q - S^2 >= 0 exactly in
+// unsigned 64-bit arithmetic (valid while n*Q < 2^64: always for 8-bit
+// pixels, for 16-bit ones while n < 2^20), the shifted product
+// (S1 - n mu1)(S2 - n mu2) from exact factors (integer means).
+__device__ __forceinline__ double r_int(const PairDev &p, long long n, double cs, long long s1,
+                                        long long q1, long long s2, long long q2)
+{
+    typedef unsigned long long u64;
+    const u64 un = (u64)n;
+    const u64 d1 = un * (u64)q1 - (u64)s1 * (u64)s1, d2 = un * (u64)q2 - (u64)s2 * (u64)s2;
+    const double dd1 = (double)d1, dd2 = (double)d2, nn = (double)n;
+    if (dd1 * dd2 < nn * nn * 1.0E-9)
+        return 0.0;
+    const long long m1 = (long long)p.mu[0], m2 = (long long)p.mu[1];
+    const double num = nn * cs - (double)(s1 - n * m1) * (double)(s2 - n * m2);
+    return div_sqrt2(num, dd1, dd2);
+}
+
+// the overlap sizes for which r_int is exact on this pair's pixel types
+__device__ __forceinline__ bool r_int_ok(const PairDev &p, long long n)
+{
+    if ((p.sat_int & 3) != 3)
+        return false;
+    const bool u8 = p.dt[0] == ALN_U8 && p.dt[1] == ALN_U8;
+    return u8 || n < (1ll << 20);
+}
+
 __device__ __forceinline__ bool lag_r(const PairDev &p, int x, int y, double cs, double &r)
 {
     const int w1 = p.w[0], h1 = p.h[0], w2 = p.w[1], h2 = p.h[1];
@@ -161,6 +202,14 @@ __device__ __forceinline__ bool lag_r(const PairDev &p, int x, int y, double cs,
         if (!(c1 > p.cnt_n && c2 > p.cnt_n))
             return false;
     }
+    if (r_int_ok(p, (long long)olw * olh)) {
+        r = r_int(p, (long long)olw * olh, cs,
+                 sat_box_i64((const long long *)p.satS[0], p, 0, L1, R1, B1, T1),
+                 sat_box_i64((const long long *)p.satQ[0], p, 0, L1, R1, B1, T1),
+                 sat_box_i64((const long long *)p.satS[1], p, 1, L2, R2, B2, T2),
+                 sat_box_i64((const long long *)p.satQ[1], p, 1, L2, R2, B2, T2));
+        return true;
+    }
     const double n = (double)(olw * olh);
     double s1, q1, s2, q2;
     if (p.sat_int & 1) {
@@ -181,7 +230,7 @@ __device__ __forceinline__ bool lag_r(const PairDev &p, int x, int y, double cs,
     const double d1 = n * q1 - s1 * s1;
     const double d2 = n * q2 - s2 * s2;
     const double d = d1 * d2;
-    r = (d < n * n * 1.0E-9) ? 0.0 : num / sqrt(d);
+    r = (d < n * n * 1.0E-9) ? 0.0 : div_sqrt2(num, d1, d2);
     return true;
 }
 
@@ -228,7 +277,7 @@ __device__ __forceinline__ bool lag_eval(const PairDev &p, int x, int y, double 
         const double d1 = n * q1 - s1 * s1;
         const double d2 = n * q2 - s2 * s2;
         const double d = d1 * d2;
-        const double v = (d < n * n * 1.0E-9) ? 0.0 : num / sqrt(d);
+        const double v = (d < n * n * 1.0E-9) ? 0.0 : div_sqrt2(num, d1, d2);
         r = (v > -1.0 && v < 1.0) ? v : 0.0;
     }
     return ok;
@@ -1671,7 +1720,7 @@ static void launch_rowfft2(aln_ctx *ctx, int n, int maxh)
 {
     constexpr int T = RegFFT<LL, -1>::T;
     const int thr = rowfft_threads(T), G = thr / T;
-    const size_t sm = (size_t)G * (padded(LL) + 2) * sizeof(float2);
+    const size_t sm = (size_t)G * row_pitch(LL) * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_rowfft<LL>, sm);
     LAUNCH(ctx, "k2_rowfft", k2_rowfft<LL>, dim3((maxh + G - 1) / G, 2, n), thr, sm,
            ctx->dpairs, ctx->tw, -1, (const int *)nullptr);
@@ -1683,7 +1732,7 @@ static void launch_fill_rows(aln_ctx *ctx, int nsel, int maxh)
 {
     constexpr int T = RegFFT<LL, -1>::T;
     const int thr = rowfft_threads(T), G = thr / T;
-    const size_t sm = (size_t)G * (padded(LL) + 2) * sizeof(float2);
+    const size_t sm = (size_t)G * row_pitch(LL) * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_rowfft<LL>, sm);
     LAUNCH(ctx, "k2_rowfft", k2_rowfft<LL>, dim3((maxh + G - 1) / G, 1, nsel), thr, sm,
            ctx->dpairs, ctx->tw, 1, (const int *)ctx->dsel_cur);
@@ -1718,7 +1767,7 @@ static void launch_lagrow2(aln_ctx *ctx, int n, int maxWy)
 {
     constexpr int T = RegFFT<LL, +1>::T;
     const int thr = std::max(256, T), G = thr / T;
-    const size_t sm = (size_t)G * (padded(LL) + 2) * sizeof(float2);
+    const size_t sm = (size_t)G * row_pitch(LL) * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_lagrow<LL>, sm);
     LAUNCH(ctx, "k2_lagrow", k2_lagrow<LL>, dim3((maxWy + G - 1) / G, n), thr, sm,
            ctx->dpairs, ctx->tw);
@@ -1729,7 +1778,7 @@ static void launch_lagp2i(aln_ctx *ctx, int n, int maxWy)
 {
     constexpr int T = RegFFT<LL, +1>::T;
     const int thr = std::max(256, T), G = thr / T;
-    const size_t sm = (size_t)G * (padded(LL) + 2) * sizeof(float2);
+    const size_t sm = (size_t)G * row_pitch(LL) * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_lagp2i<LL>, sm);
     LAUNCH(ctx, "k2_lagp2i", k2_lagp2i<LL>, dim3((maxWy + G - 1) / G, n), thr, sm, ctx->dpairs,
            ctx->tw);
@@ -1740,7 +1789,7 @@ static void launch_lagimg2(aln_ctx *ctx, int n, int maxWy, bool both, bool sonly
 {
     constexpr int T = RegFFT<LL, +1>::T;
     const int thr = std::max(256, T), G = thr / T;
-    const size_t sm = (size_t)G * (padded(LL) + 2) * (both ? 2 : 1) * sizeof(float2);
+    const size_t sm = (size_t)G * row_pitch(LL) * (both ? 2 : 1) * sizeof(float2);
     void (*kern)(PairDev *, const float2 *) = sonly ? k2_lagimg<LL, true> : k2_lagimg<LL, false>;
     smem_attr(ctx->device, (const void *)kern, sm);
     LAUNCH(ctx, "k2_lagimg", kern, dim3((maxWy + G - 1) / G, n), thr, sm, ctx->dpairs, ctx->tw);

@@ -23,6 +23,11 @@ __host__ __device__ constexpr int ipowc(int b, int e) { return e == 0 ? 1 : b * 
 __device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
 __host__ __device__ constexpr int padded(int n) { return n + (n >> 4); }
 
+// float2 per team in the row kernels: the padded row plus two bins, rounded
+// up to an even count so that every team's region starts on 16 bytes (the
+// row pass stages its input with 16-byte stores)
+__host__ __device__ constexpr int row_pitch(int L) { return (padded(L) + 3) & ~1; }
+
 // exp(DIR * 2 pi i k / 16) for k = 0..7 (DIR = -1 forward)
 template <int K16, int DIR>
 __device__ __forceinline__ float2 mul_w16(float2 x)

@@ -361,7 +361,7 @@ __global__ void k2_sat2(PairDev *pairs)
 // columns): lane l owns a contiguous run of ceil(w/32) columns, the lane
 // totals are scanned with shuffles.  No block-wide synchronisation, so a
 // CTA carries eight rows and small images do not pay one CTA per row.
-#define SAT2W_MAXW 4096
+#define SAT2W_MAXW 512
 
 template <typename TA, bool SQ = true>
 __device__ __forceinline__ void sat2_row_warp(const PairDev &p, int i, int slot, int y, TA *S,
@@ -527,7 +527,7 @@ __global__ void k2_sat2w(PairDev *pairs)
 __host__ __device__ constexpr int rowfft_threads(int T) { return T * 4 > 512 ? 512 : (T * 4 < 256 ? 256 : T * 4); }
 
 // Each team of RegFFT<L>::T threads transforms one row.  G = blockDim.x / T
-// rows per CTA; smem: G * (padded(L) + 2) float2 per CTA.
+// rows per CTA; smem: G * row_pitch(L) float2 per CTA.
 template <int L>
 __global__ void k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int *sel)
 {
@@ -546,7 +546,7 @@ __global__ void k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int onl
     if (y0 >= h)
         return;
     const int y = y0 + team;
-    constexpr int PITCH = padded(L) + 2;   // even: 16-byte aligned team regions
+    constexpr int PITCH = row_pitch(L);   // even: 16-byte aligned team regions
     float2 *sm = smem + team * PITCH;
     const void *img = p.img[i];
     const long long st = p.stride[i];
@@ -825,7 +825,7 @@ __global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
 {
     using F = RegFFT<L, +1>;
     constexpr int R = F::R, T = F::T;
-    constexpr int PITCH = padded(L) + 2;   // holds L+1 bins, then 2L reals
+    constexpr int PITCH = row_pitch(L);   // holds L+1 bins, then 2L reals
     extern __shared__ float2 smem[];
     __shared__ double red_r[32];
     __shared__ long long red_k[32];
@@ -938,7 +938,7 @@ __global__ void __launch_bounds__(256, 2) k2_lagimg(PairDev *pairs, const float2
 {
     using F = RegFFT<L, +1>;
     constexpr int R = F::R, T = F::T;
-    constexpr int PITCH = padded(L) + 2;
+    constexpr int PITCH = row_pitch(L);
     extern __shared__ float2 smem[];
     __shared__ double red_r[32], red_s[32], red_s2[32];
     __shared__ long long red_k[32];
@@ -1206,7 +1206,7 @@ __global__ void k2_lagp2i(PairDev *pairs, const float2 *__restrict__ tw)
 {
     using F = RegFFT<L, +1>;
     constexpr int R = F::R, T = F::T;
-    constexpr int PITCH = padded(L) + 2;
+    constexpr int PITCH = row_pitch(L);
     extern __shared__ float2 smem[];
     __shared__ double red_r[32];
     __shared__ long long red_k[32];

@@ -366,3 +366,35 @@ def patch_group(seed: int, k: int, n: int = 512, margin: int = 64, noise=8.0):
         a_s.append(to_u8(af + rng.normal(0.0, noise, af.shape)))
         truths.append((tx, ty))
     return b, a_s, truths
+
+
+def uneven_batch_torch(seed: int, n: int, device, smin=64, smax=1024):
+    """n uneven uint16 pairs (as uneven_pair: long side log-uniform in
+    [smin, smax], aspect 1-4, orientation random, values 0-4095 with mean
+    2048 / std 480, offset within a quarter of the short side, disc radius
+    short/2), generated with torch on `device`.  Pair i depends only on
+    (seed, i).  Returns dicts with tensors a, b stored as int16 (values
+    0-4095: the same bits as uint16), the expected lag `truth` and the disc."""
+    import torch
+
+    out = []
+    for i in range(n):
+        s_ = seed * 1000003 + i
+        rng = np.random.default_rng(s_)
+        s = int(round(math.exp(rng.uniform(math.log(smin), math.log(smax)))))
+        short = max(8, int(round(s / rng.uniform(1.0, 4.0))))
+        wide = bool(rng.integers(0, 2))
+        w, h = (s, short) if wide else (short, s)
+        q = max(1, short // 4)
+        tx, ty = (int(v) for v in rng.integers(-q, q + 1, 2))
+        gen = torch.Generator(device=device)
+        gen.manual_seed(s_)
+        f = field_torch(gen, h + 2 * q, w + 2 * q, device, mean=2048.0, std=480.0)
+        a = f[q:q + h, q:q + w]
+        bf = f[q + ty:q + ty + h, q + tx:q + tx + w]
+        b = bf + 30.0 * torch.randn(bf.shape, generator=gen, device=device, dtype=torch.float64)
+        a16 = torch.clamp(torch.round(a), 0, 4095).to(torch.int32)
+        b16 = torch.clamp(torch.round(b), 0, 4095).to(torch.int32)
+        out.append(dict(a=a16.to(torch.int16).contiguous(), b=b16.to(torch.int16).contiguous(),
+                        truth=(-tx, -ty), ox=0, oy=0, radius=max(1, short // 2)))
+    return out

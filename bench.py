@@ -59,7 +59,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=128)
     ap.add_argument("--parity-sample", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="montage", choices=["montage", "sweep", "served"],
+    ap.add_argument("--workload", default="montage",
+                    choices=["montage", "sweep", "served", "uneven"],
                     help="montage: the strip batch (default); sweep: the thumbnail angle "
                          "sweep; served: the Poisson request stream through the server")
     ap.add_argument("--sweep-pairs", type=int, default=1024)
@@ -67,6 +68,7 @@ def parse():
     ap.add_argument("--served-requests", type=int, default=2000)
     ap.add_argument("--served-strips", type=int, default=512)
     ap.add_argument("--served-groups", type=int, default=32)
+    ap.add_argument("--uneven-pairs", type=int, default=20000)
     return ap.parse_args()
 
 
@@ -968,12 +970,176 @@ def run_served(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# uneven-size uint16 batch (--workload uneven)
+# ---------------------------------------------------------------------------
+
+UNEVEN_WORKLOAD = ("uneven-size batch: pairs of uint16 patches (0-4095, mean 2048, std 480), "
+                   "long side log-uniform in [64, 1024], aspect 1-4, random orientation, "
+                   "offset within a quarter of the short side; CorrPatches, disc radius "
+                   "short/2, olap >= 8 x 8; FFT sizes 128..2048 per axis")
+
+
+def run_uneven(args):
+    import ctypes as C
+    import torch
+    import alignment_projects_gb300 as aln
+    import oracle as O
+    from alignment_projects_gb300 import synth
+    from alignment_projects_gb300.native import AlnPair, AlnResult, AlnImage
+
+    ws, rank, local = dist_env()
+    threads = host_threads()
+    torch.cuda.set_device(local)
+    dist = dist_init(ws, "nccl")
+    dev = torch.device("cuda", local)
+    L = aln.lib()
+    ctx = aln.Context(local)
+    batch = synth.uneven_batch_torch(4 + 7919 * rank, args.uneven_pairs, dev)
+    torch.cuda.synchronize()
+    n = len(batch)
+    lg = aln.legal(aln.RGN_MIN, 8, 8, 0)
+
+    def pair_array(host):
+        arr = (AlnPair * n)()
+        for k, p in enumerate(batch):
+            ims = []
+            for key in ("a", "b"):
+                t = host[k][key] if host is not None else p[key]
+                ims.append(AlnImage(t.data_ptr(), aln.U16, t.shape[1], t.shape[0], t.shape[1],
+                                    0, 0, 0 if host is not None else 1))
+            arr[k].a, arr[k].b = ims
+            arr[k].ox, arr[k].oy, arr[k].radius = 0, 0, p["radius"]
+            arr[k].legal = lg
+        return arr, (AlnResult * n)()
+
+    arr_d, out_d = pair_array(None)
+
+    def run(arr, out):
+        if L.aln_corr_patches_batch(ctx.h, n, arr, out) < 0:
+            raise RuntimeError(L.aln_last_error(ctx.h).decode())
+
+    for _ in range(args.warmup):
+        run(arr_d, out_d)
+    ctx.set_profiling(True)
+    ctx.profile_reset()
+    clk = ClockSampler(local)
+    clk.start()
+    barrier(dist)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        run(arr_d, out_d)
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(dist)
+    ms = max_over_ranks(dist, e0.elapsed_time(e1), dev)
+    clocks = clk.stop()
+    prof = ctx.profile()
+    cnt = ctx.counters()
+    value = ws * n * args.steps / (ms / 1000.0)
+    # end to end: the patches in one pinned buffer, pair after pair
+    nbytes = sum(2 * (p["a"].numel() + p["b"].numel()) for p in batch)
+    pinned = torch.empty(nbytes // 2, dtype=torch.int16, pin_memory=True)
+    host, off = [], 0
+    for p in batch:
+        h = {}
+        for key in ("a", "b"):
+            t = p[key]
+            v = pinned[off:off + t.numel()].view(t.shape)
+            v.copy_(t)
+            off += t.numel()
+            h[key] = v
+        host.append(h)
+    arr_h, out_h = pair_array(host)
+    run(arr_h, out_h)
+    ctx.profile_reset()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        run(arr_h, out_h)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_e2e = max_over_ranks(dist, e0.elapsed_time(e1), dev)
+    cnt2 = ctx.counters()
+    ctx.set_profiling(False)
+    line = None
+    if rank == 0:
+        same = all((out_d[k].peak_x, out_d[k].peak_y, out_d[k].r) ==
+                   (out_h[k].peak_x, out_h[k].peak_y, out_h[k].r) for k in range(n))
+        truth = sum(1 for k, p in enumerate(batch)
+                    if (out_d[k].peak_x, out_d[k].peak_y) == p["truth"])
+        cpu = parity = None
+        if not args.no_cpu:
+            import concurrent.futures as cf
+            orc = O.Oracle()
+            lo = O.legal(O.RGN_MIN, 8, 8, 0)
+            samp = list(range(0, n, max(1, n // args.cpu_sample)))[:args.cpu_sample]
+            prep = []
+            for k in samp:
+                a = batch[k]["a"].cpu().numpy().astype(np.uint16)
+                b = batch[k]["b"].cpu().numpy().astype(np.uint16)
+                A, VA = O.image_to_points(a)
+                B, VB = O.image_to_points(b)
+                prep.append((A, VA, B, VB, batch[k]["radius"]))
+            t0 = time.perf_counter()
+            with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+                outs = list(ex.map(lambda t: orc.corr_patches(t[0], t[1], t[2], t[3], 0, 0,
+                                                                t[4], lo), prep))
+            wall = time.perf_counter() - t0
+            cpu = {"value": len(prep) / wall, "unit": "pairs/s", "cores": threads,
+                   "kind": "port", "sample": "%d pairs spread over the batch, FP64 C "
+                   "restatement of CorrPatches, %.1f s wall on %d threads"
+                   % (len(prep), wall, threads)}
+            ok = chk = 0
+            dr = dp = 0.0
+            for k, o in zip(samp, outs):
+                g = out_d[k]
+                dr = max(dr, abs(g.r - o["r"]))
+                if o["status"] == 0 and o["r"] - o["second"] > 1e-3:
+                    chk += 1
+                    ok += (g.peak_x, g.peak_y) == (o["bigx"], o["bigy"])
+                    dp = max(dp, abs(g.dx - o["dx"]), abs(g.dy - o["dy"]))
+            parity = {"pairs": len(outs), "peak_exact": ok, "peak_checked": chk,
+                      "max_abs_dr": dr, "max_abs_dsubpix": dp}
+        line = {
+            "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": UNEVEN_WORKLOAD, "pairs_per_step": n,
+                       "input_bytes_per_step": nbytes, "parallelism": "replicas x%d" % ws},
+            "e2e": {"value": ws * n * args.steps / (ms_e2e / 1000.0), "unit": "pairs/s",
+                    "h2d_bytes_per_step": (cnt2["h2d_bytes"]) // args.steps,
+                    "d2h_bytes_per_step": (cnt2["d2h_bytes"]) // args.steps},
+            "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": cnt["launches"],
+            "chunks_per_step": cnt["chunks"] / args.steps,
+            "kernels_ms": {k: round(v[1], 3) for k, v in sorted(prof.items())},
+            "parity": parity,
+            "truth": {"found": truth, "of": n},
+            "host_vs_device_inputs_identical": same,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
     if args.workload == "sweep":
         return run_sweep(args)
     if args.workload == "served":
         return run_served(args)
+    if args.workload == "uneven":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the uneven batch's CPU "
+                              "baseline is reported in the GPU line (cpu_baseline)"}), flush=True)
+            return 0
+        return run_uneven(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

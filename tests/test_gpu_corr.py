@@ -286,3 +286,26 @@ def test_spectrum_cache_images_and_off(ctx):
     assert ctx.corr_images_batch(keyed) == plain
     ctx.set_spectrum_cache(1 << 30)
     assert ctx.corr_images_batch(keyed) == plain
+
+
+@pytest.mark.parametrize("dt,w,h", [(np.uint8, 16, 20), (np.uint16, 16, 24), (np.uint8, 9, 12),
+                                    (np.uint16, 40, 16), (np.uint8, 5, 70)])
+def test_tiny_integer_patches(ctx, orc, dt, w, h):
+    """Narrow integer patches (FFT widths 16..32): the row pass's staged
+    16-byte loads land in every team's own, 16-byte aligned region."""
+    import oracle
+    import alignment_projects_gb300 as aln
+    rng = np.random.default_rng(w * 100 + h)
+    top = 255 if dt == np.uint8 else 4095
+    m = min(4, w - 1, h - 1)   # overlaps of at least m x m (two pixels are always r = 1)
+    pairs = []
+    for k in range(24):   # several pairs: many teams per CTA
+        a = rng.integers(0, top + 1, (h, w)).astype(dt)
+        b = np.roll(a, (1, 2), axis=(0, 1)).copy()
+        pairs.append(dict(a=a, b=b, legal=aln.legal(aln.RGN_MIN, m, m, 0)))
+    got = ctx.corr_patches_batch(pairs)
+    for p, g in zip(pairs, got):
+        A, VA = oracle.image_to_points(p["a"])
+        B, VB = oracle.image_to_points(p["b"])
+        o = orc.corr_patches(A, VA, B, VB, 0, 0, 4096, oracle.legal(oracle.RGN_MIN, m, m, 0))
+        assert_parity(g, o, f"{dt.__name__} {w}x{h}")
