@@ -38,5 +38,7 @@ from .native import (  # noqa: F401
     THM_PRIOR,
     THM_SCAN_HUNT,
     THM_SCAN_MAXR,
+    THM_POSTTWEAKS,
+    THM_FULLRES,
     thumbs_from_points,
 )

@@ -145,6 +145,8 @@ struct ThmPair {
     int ncalls;
     int err;
     ThmRec best;
+    int own_disc;                   // SetDisc of this pair (finishing stages)
+    int dox, doy, drx, dry;
 };
 
 struct Eval {
@@ -338,10 +340,10 @@ static int eval_batch(SweepCtx &S, std::vector<Eval> &ev)
                 keys[k] = JobKey{1, S.key_base + (unsigned long long)E.pair + 1};
             specs[k].kind = 2;
             specs[k].mincor = 0.0;
-            specs[k].ox = S.P.ox;
-            specs[k].oy = S.P.oy;
-            specs[k].rx = S.P.rx;
-            specs[k].ry = S.P.ry;
+            specs[k].ox = tp.own_disc ? tp.dox : S.P.ox;
+            specs[k].oy = tp.own_disc ? tp.doy : S.P.oy;
+            specs[k].rx = tp.own_disc ? tp.drx : S.P.rx;
+            specs[k].ry = tp.own_disc ? tp.dry : S.P.ry;
         }
         CK(cudaMemcpyAsync(S.djobs, jobs.data(), n * sizeof(SplatJob), cudaMemcpyHostToDevice,
                            ctx->stream));
@@ -636,17 +638,13 @@ static int scan_with_tweaks(SweepCtx &S, const std::vector<int> &ids,
     return ALN_OK;
 }
 
-extern "C" int aln_thm_search_batch(aln_ctx *ctx, int npairs, const aln_thumbs *thumbs,
-                                    const aln_thm_params *params, int mode, double ang0,
-                                    double hfang, double step, aln_thm_result *out)
+// Device copies of the thumbnails, hulls and the initial sweep state
+// (CThmScan::Initialize) for every pair; *dbuf receives the allocation.
+static int sweep_setup(aln_ctx *ctx, SweepCtx &S, int npairs, const aln_thumbs *thumbs,
+                       const aln_thm_params *params, char **dbuf_out)
 {
-    if (!ctx || npairs < 0 || (npairs && (!thumbs || !params || !out)))
-        return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
-    if (!params->usecorrr)
-        return set_err(ctx, ALN_ERR_UNSUPPORTED,
-                       "sweep with CorrImagesF (useCorrR off) is not built yet");
+    *dbuf_out = nullptr;
     CK(cudaSetDevice(ctx->device));
-    SweepCtx S;
     S.ctx = ctx;
     S.P = *params;
     S.pairs.resize(npairs);
@@ -703,7 +701,24 @@ extern "C" int aln_thm_search_batch(aln_ctx *ctx, int npairs, const aln_thumbs *
         if (tp.hull.empty())
             rc = set_err(ctx, ALN_ERR_ARG, "thumbnail pair %d: no A points", k);
         tp.best.X = tp.best.Y = tp.best.A = tp.best.R = -999.0;   // CThmScan::Initialize
+        tp.own_disc = 0;
     }
+    *dbuf_out = dbuf;
+    return rc;
+}
+
+extern "C" int aln_thm_search_batch(aln_ctx *ctx, int npairs, const aln_thumbs *thumbs,
+                                    const aln_thm_params *params, int mode, double ang0,
+                                    double hfang, double step, aln_thm_result *out)
+{
+    if (!ctx || npairs < 0 || (npairs && (!thumbs || !params || !out)))
+        return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
+    if (!params->usecorrr)
+        return set_err(ctx, ALN_ERR_UNSUPPORTED,
+                       "sweep with CorrImagesF (useCorrR off) is not built yet");
+    SweepCtx S;
+    char *dbuf = nullptr;
+    int rc = sweep_setup(ctx, S, npairs, thumbs, params, &dbuf);
     std::vector<int> all(npairs);
     for (int k = 0; k < npairs; ++k)
         all[k] = k;
@@ -779,6 +794,85 @@ extern "C" int aln_thm_search_batch(aln_ctx *ctx, int npairs, const aln_thumbs *
         memcpy(out[k].T, tp.best.T, sizeof out[k].T);
         out[k].err = tp.err;
         out[k].ncalls = tp.ncalls;
+    }
+    return ALN_OK;
+}
+
+// CThmScan::PostTweaks (CThmScan.cpp:796-802) and FinishAtFullRes
+// (:810-842) for many pairs, each from its prior best record and pretweak
+// transform (the CThmScan object's state).  Both set useCorrR and a disc of
+// radius 40 / 80 around the prior (X, Y) (truncated to int, as SetDisc gets
+// them).  PostTweaks runs Pretweaks(prior R, prior A), then RFromAngle at
+// the prior angle; FinishAtFullRes runs RFromAngle at the prior angle on
+// the full-resolution thumbnails and keeps the result only when X and Y
+// moved by at most 20 (then with the prior R).
+extern "C" int aln_thm_finish_batch(aln_ctx *ctx, int npairs, const aln_thumbs *thumbs,
+                                    const aln_thm_params *params, int mode,
+                                    const aln_thm_result *prior, const double *prior_tptwk,
+                                    aln_thm_result *out, double *out_tptwk)
+{
+    if (!ctx || npairs < 0 || (npairs && (!thumbs || !params || !prior || !out)))
+        return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
+    if (mode != ALN_THM_POSTTWEAKS && mode != ALN_THM_FULLRES)
+        return set_err(ctx, ALN_ERR_ARG, "bad finishing mode %d", mode);
+    aln_thm_params P = *params;
+    P.usecorrr = 1;   // SetUseCorrR(true)
+    SweepCtx S;
+    char *dbuf = nullptr;
+    int rc = sweep_setup(ctx, S, npairs, thumbs, &P, &dbuf);
+    std::vector<ThmRec> b0(npairs);
+    for (int k = 0; k < npairs && rc == ALN_OK; ++k) {
+        ThmPair &tp = S.pairs[k];
+        tp.best.A = prior[k].A;
+        tp.best.X = prior[k].X;
+        tp.best.Y = prior[k].Y;
+        tp.best.R = prior[k].R;
+        memcpy(tp.best.T, prior[k].T, sizeof tp.best.T);
+        if (prior_tptwk)
+            memcpy(tp.Tptwk, prior_tptwk + 6 * (size_t)k, sizeof tp.Tptwk);
+        tp.own_disc = 1;
+        tp.dox = (int)tp.best.X;
+        tp.doy = (int)tp.best.Y;
+        tp.drx = tp.dry = mode == ALN_THM_POSTTWEAKS ? 40 : 80;
+        b0[k] = tp.best;
+    }
+    if (rc == ALN_OK && mode == ALN_THM_POSTTWEAKS)
+        for (int k = 0; k < npairs && rc == ALN_OK; ++k) {
+            bool changed = false;
+            rc = pretweaks(S, k, S.pairs[k].best.R, S.pairs[k].best.A, &changed);
+        }
+    if (rc == ALN_OK) {
+        std::vector<Eval> ev;
+        for (int k = 0; k < npairs; ++k)
+            ev.push_back(Eval{k, S.pairs[k].best.A, -1, &S.pairs[k].best});
+        rc = eval_batch(S, ev);
+    }
+    if (rc == ALN_OK && mode == ALN_THM_FULLRES)
+        for (int k = 0; k < npairs; ++k) {
+            ThmRec &b = S.pairs[k].best;
+            if (fabs(b.X - b0[k].X) <= 20 && fabs(b.Y - b0[k].Y) <= 20)
+                b.R = b0[k].R;
+            else
+                b = b0[k];
+        }
+    cudaStreamSynchronize(ctx->stream);
+    spec_drop(ctx, 1, S.key_base, S.key_base + (unsigned long long)npairs + 1);
+    cudaFree(S.arena);
+    cudaFree(S.djobs);
+    cudaFree(dbuf);
+    if (rc != ALN_OK)
+        return rc;
+    for (int k = 0; k < npairs; ++k) {
+        const ThmPair &tp = S.pairs[k];
+        out[k].A = tp.best.A;
+        out[k].X = tp.best.X;
+        out[k].Y = tp.best.Y;
+        out[k].R = tp.best.R;
+        memcpy(out[k].T, tp.best.T, sizeof out[k].T);
+        out[k].err = 0;
+        out[k].ncalls = tp.ncalls;
+        if (out_tptwk)
+            memcpy(out_tptwk + 6 * (size_t)k, tp.Tptwk, sizeof tp.Tptwk);
     }
     return ALN_OK;
 }

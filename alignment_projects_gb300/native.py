@@ -55,6 +55,7 @@ class AlnImageJob(C.Structure):
 
 CORR_F, CORR_R, CORR_S = 0, 1, 2
 THM_DENOVO, THM_RFROMANGLE, THM_PRIOR, THM_SCAN_HUNT, THM_SCAN_MAXR = 0, 1, 2, 3, 4
+THM_POSTTWEAKS, THM_FULLRES = 5, 6
 
 
 class AlnThumbs(C.Structure):
@@ -153,6 +154,10 @@ def lib():
         L.aln_thm_search_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnThumbs),
                                            C.POINTER(AlnThmParams), C.c_int, C.c_double,
                                            C.c_double, C.c_double, C.POINTER(AlnThmResult)]
+        L.aln_thm_finish_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnThumbs),
+                                           C.POINTER(AlnThmParams), C.c_int,
+                                           C.POINTER(AlnThmResult), C.c_void_p,
+                                           C.POINTER(AlnThmResult), C.c_void_p]
         L.aln_corr_patch_to_image.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                               C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                               C.c_int, C.POINTER(AlnResult)]
@@ -375,6 +380,28 @@ class Context:
                                                  ang0, hfang, step, out))
         return [{"A": o.A, "X": o.X, "Y": o.Y, "R": o.R, "err": o.err, "ncalls": o.ncalls,
                  "T": list(o.T)} for o in out]
+
+    def thm_finish_batch(self, thumbs, mode, priors, tptwk=None, **params) -> list:
+        """PostTweaks (THM_POSTTWEAKS) / FinishAtFullRes (THM_FULLRES) per pair
+        from priors (dicts with A, X, Y, R) and pretweak transforms (6 each)."""
+        thumbs = list(thumbs)
+        n = len(thumbs)
+        arr = (AlnThumbs * n)()
+        pri = (AlnThmResult * n)()
+        for k, (t, p) in enumerate(zip(thumbs, priors)):
+            arr[k] = t
+            pri[k].A, pri[k].X, pri[k].Y, pri[k].R = p["A"], p["X"], p["Y"], p["R"]
+        tw = None
+        if tptwk is not None:
+            tw = np.ascontiguousarray(tptwk, np.float64).reshape(n, 6)
+        tout = np.zeros((n, 6), np.float64)
+        P = _thm_params(**params)
+        out = (AlnThmResult * n)()
+        self._check(self._L.aln_thm_finish_batch(
+            self.h, n, arr, C.byref(P), mode, pri,
+            tw.ctypes.data if tw is not None else None, out, tout.ctypes.data))
+        return [{"A": o.A, "X": o.X, "Y": o.Y, "R": o.R, "err": o.err, "ncalls": o.ncalls,
+                 "T": list(o.T), "tptwk": tout[k].tolist()} for k, o in enumerate(out)]
 
     def corr_patches_batch(self, pairs) -> list:
         """pairs: iterable of dicts with a, b, [ox, oy, radius, legal, a_origin, b_origin,

@@ -276,7 +276,9 @@ enum {
     ALN_THM_RFROMANGLE = 1,  /* RFromAngle(ang0), CThmScan.cpp:329-366 */
     ALN_THM_PRIOR = 2,       /* UsePriorAngles(ang0, hfang), CThmScan.cpp:734-758 */
     ALN_THM_SCAN_HUNT = 3,   /* AngleScanSel(ang0, hfang, step, false) + PeakHunt(step*0.075) */
-    ALN_THM_SCAN_MAXR = 4    /* AngleScanMaxR(ang0, hfang, step, favorCenter), :431-493 */
+    ALN_THM_SCAN_MAXR = 4,   /* AngleScanMaxR(ang0, hfang, step, favorCenter), :431-493 */
+    ALN_THM_POSTTWEAKS = 5,  /* PostTweaks(best), CThmScan.cpp:796-802 (aln_thm_finish_batch) */
+    ALN_THM_FULLRES = 6      /* FinishAtFullRes(best), CThmScan.cpp:810-842 (aln_thm_finish_batch) */
 };
 
 /* Runs one CThmScan search per pair, all pairs together: every correlator
@@ -285,6 +287,17 @@ enum {
 int aln_thm_search_batch(aln_ctx *ctx, int npairs, const aln_thumbs *thumbs,
                          const aln_thm_params *params, int mode, double ang0,
                          double hfang, double step, aln_thm_result *out);
+
+/* CThmScan's finishing stages for many pairs (mode ALN_THM_POSTTWEAKS or
+ * ALN_THM_FULLRES), each pair from prior[k] (its best record: A, X, Y, R)
+ * and the sweep object's pretweak transform prior_tptwk[6k..6k+5] (TAffine
+ * t[0..5]; NULL: identity).  For FinishAtFullRes the thumbs are the
+ * full-resolution records and prior X, Y are already scaled to them (as
+ * 1_DMesh/CThmUtil.cpp:941-949 does).  out_tptwk (may be NULL) receives the
+ * pretweak transform after the call (6 per pair). */
+int aln_thm_finish_batch(aln_ctx *ctx, int npairs, const aln_thumbs *thumbs,
+                         const aln_thm_params *params, int mode, const aln_thm_result *prior,
+                         const double *prior_tptwk, aln_thm_result *out, double *out_tptwk);
 
 /* ---- allocation-free CorrPatches: no counterpart in the reference ---- */
 

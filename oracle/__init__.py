@@ -298,6 +298,31 @@ class Oracle(_Lib):
         return {"A": best.A, "X": best.X, "Y": best.Y, "R": best.R, "err": err,
                 "ncalls": ncalls.value}
 
+    def thm_finish(self, pa, va, pb, vb, req_area, mode, prior, tptwk=None, olap1d=0,
+                   rthresh=0.3, nbmaxht=0.75, pretweak=0, constxy=1, tdfm=None):
+        """PostTweaks (mode 5) / FinishAtFullRes (mode 6) from prior (A, X, Y, R)."""
+        pa, pb = _pts(pa), _pts(pb)
+        va = np.ascontiguousarray(va, np.float64)
+        vb = np.ascontiguousarray(vb, np.float64)
+        P = ThmParams()
+        P.rthresh, P.nbmaxht = rthresh, nbmaxht
+        P.constxy, P.pretweak, P.usecorrr = constxy, pretweak, 1
+        P.Ox, P.Oy, P.Rx, P.Ry = 0, 0, -1, -1
+        t = tdfm if tdfm is not None else (1, 0, 0, 0, 1, 0)
+        for i in range(6):
+            P.tdfm[i] = t[i]
+        pr = np.ascontiguousarray(prior, np.float64)
+        tw = None if tptwk is None else np.ascontiguousarray(tptwk, np.float64)
+        tout = np.zeros(6, np.float64)
+        best = ThmRec()
+        ncalls = C.c_int(0)
+        err = self.lib.orc_thm_finish(_p(pa), _p(va), len(va), _p(pb), _p(vb), len(vb),
+                                      C.c_long(req_area), olap1d, C.byref(P), mode, _p(pr),
+                                      _p(tw) if tw is not None else None, C.byref(best),
+                                      _p(tout), C.byref(ncalls))
+        return {"A": best.A, "X": best.X, "Y": best.Y, "R": best.R, "err": err,
+                "ncalls": ncalls.value, "tptwk": tout.tolist()}
+
 
 class Ref(_Lib):
     """The reference's own code (compiled from its sources; x86 host only)."""
@@ -388,3 +413,19 @@ class Ref(_Lib):
             C.c_double(hfang), C.c_double(step), _p(td) if td is not None else None,
             _p(out), logpath.encode() if logpath else None)
         return {"A": out[0], "X": out[1], "Y": out[2], "R": out[3], "err": err}
+
+    def thm_finish(self, pa, va, pb, vb, req_area, mode, prior, tptwk=None, olap1d=0,
+                   rthresh=0.3, nbmaxht=0.75, pretweak=0, constxy=1, tdfm=None):
+        pa, pb = _pts(pa), _pts(pb)
+        va = np.ascontiguousarray(va, np.float64)
+        vb = np.ascontiguousarray(vb, np.float64)
+        pr = np.ascontiguousarray(prior, np.float64)
+        tw = None if tptwk is None else np.ascontiguousarray(tptwk, np.float64)
+        td = None if tdfm is None else np.ascontiguousarray(tdfm, np.float64)
+        out = np.zeros(10, np.float64)
+        err = self.lib.ref_thm_finish(
+            len(va), _p(pa), _p(va), len(vb), _p(pb), _p(vb), C.c_long(req_area), olap1d,
+            C.c_double(rthresh), C.c_double(nbmaxht), pretweak, constxy, 1, mode, _p(pr),
+            _p(tw) if tw is not None else None, _p(td) if td is not None else None, _p(out))
+        return {"A": out[0], "X": out[1], "Y": out[2], "R": out[3], "err": err,
+                "tptwk": out[4:10].tolist()}

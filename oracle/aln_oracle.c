@@ -1416,3 +1416,57 @@ int orc_thm_search(const double *xya, const double *va, int na,
         *ncalls = s.ncalls;
     return err;
 }
+
+/* PostTweaks (mode 5, CThmScan.cpp:796-802) and FinishAtFullRes (mode 6,
+ * :810-842) from a prior best record (prior[0..3] = A, X, Y, R) and pretweak
+ * transform; mirrors refwrap's ref_thm_finish. */
+int orc_thm_finish(const double *xya, const double *va, int na,
+                   const double *xyb, const double *vb, int nb,
+                   long reqArea, int olap1D, const orc_thm_params *P, int mode,
+                   const double *prior, const double *tptwk6, orc_thm_rec *best,
+                   double *tptwk_out, int *ncalls)
+{
+    thm_state s;
+    memset(&s, 0, sizeof s);
+    s.xya = xya;
+    s.va = va;
+    s.na = na;
+    s.xyb = xyb;
+    s.vb = vb;
+    s.nb = nb;
+    s.reqArea = reqArea;
+    s.olap1D = olap1D;
+    s.P = *P;
+    if (tptwk6)
+        memcpy(s.Tptwk, tptwk6, sizeof s.Tptwk);
+    else
+        aff_one(s.Tptwk);
+    s.pts = (double *)malloc(sizeof(double) * 2 * (size_t)(na > 0 ? na : 1));
+    memset(best, 0, sizeof *best);
+    best->A = prior[0];
+    best->X = prior[1];
+    best->Y = prior[2];
+    best->R = prior[3];
+    s.P.usecorrr = 1;                       /* SetUseCorrR(true) */
+    s.P.Ox = (int)best->X;                  /* SetDisc((int)X, (int)Y, r, r) */
+    s.P.Oy = (int)best->Y;
+    if (mode == 5) {
+        s.P.Rx = s.P.Ry = 40;
+        thm_pretweaks(&s, best->R, best->A);
+        thm_rfromangle(&s, best, best->A, -1);
+    } else {
+        orc_thm_rec b0 = *best;
+        s.P.Rx = s.P.Ry = 80;
+        thm_rfromangle(&s, best, best->A, -1);
+        if (fabs(best->X - b0.X) <= 20 && fabs(best->Y - b0.Y) <= 20)
+            best->R = b0.R;
+        else
+            *best = b0;
+    }
+    if (tptwk_out)
+        memcpy(tptwk_out, s.Tptwk, sizeof s.Tptwk);
+    free(s.pts);
+    if (ncalls)
+        *ncalls = s.ncalls;
+    return 0;
+}

@@ -118,6 +118,15 @@ int orc_thm_search(const double *xya, const double *va, int na,
                    int mode, double ang0, double hfang, double step,
                    orc_thm_rec *best, int *ncalls);
 
+/* PostTweaks (mode 5) / FinishAtFullRes (mode 6) from a prior best
+ * (A, X, Y, R) and pretweak transform (NULL: identity).  Mirrors refwrap's
+ * ref_thm_finish; tptwk_out (may be NULL) receives the transform after. */
+int orc_thm_finish(const double *xya, const double *va, int na,
+                   const double *xyb, const double *vb, int nb,
+                   long reqArea, int olap1D, const orc_thm_params *P, int mode,
+                   const double *prior, const double *tptwk6, orc_thm_rec *best,
+                   double *tptwk_out, int *ncalls);
+
 #ifdef __cplusplus
 }
 #endif

@@ -245,4 +245,58 @@ int ref_thm_search(int na, const double *xya, const double *va,
     return S.GetErr();
 }
 
+/*
+ * CThmScan's finishing stages from a prior best record and pretweak
+ * transform: mode 5 = PostTweaks(best, thm) (0_GEN/CThmScan.cpp:796-802),
+ * 6 = FinishAtFullRes(best, thm) (:810-842), thm being the full-resolution
+ * record there.  prior[0..3] = A, X, Y, R; out[0..3] = A, X, Y, R after,
+ * out[4..9] = the pretweak transform after.
+ */
+int ref_thm_finish(int na, const double *xya, const double *va,
+                   int nb, const double *xyb, const double *vb,
+                   long reqArea, int olap1D, double rthresh, double nbmaxht,
+                   int pretweak, int constxy, int usecorrr, int mode,
+                   const double *prior, const double *tptwk6, const double *tdfm6,
+                   double *out)
+{
+    FILE *flog = quiet_log();
+    ThmRec thm;
+    to_points(thm.ap, thm.av, na, xya, va);
+    to_points(thm.bp, thm.bv, nb, xyb, vb);
+    thm.ftc.clear();
+    thm.reqArea = reqArea;
+    thm.olap1D = olap1D;
+    thm.scl = 1;
+
+    CThmScan S;
+    CorRec best;
+    S.Initialize(flog, best);
+    if (tdfm6)
+        S.SetTdfm(TAffine(tdfm6));
+    if (tptwk6)
+        S.SetTptwk(TAffine(tptwk6));
+    S.SetRThresh(rthresh);
+    S.SetNbMaxHt(nbmaxht);
+    S.SetSweepConstXY(constxy);
+    S.SetSweepPretweak(pretweak);
+    S.SetUseCorrR(usecorrr);
+    best.A = prior[0];
+    best.X = prior[1];
+    best.Y = prior[2];
+    best.R = prior[3];
+    if (mode == 5)
+        S.PostTweaks(best, thm);
+    else
+        S.FinishAtFullRes(best, thm);
+    out[0] = best.A;
+    out[1] = best.X;
+    out[2] = best.Y;
+    out[3] = best.R;
+    TAffine T;
+    S.GetTptwk(T);
+    for (int i = 0; i < 6; ++i)
+        out[4 + i] = T.t[i];
+    return S.GetErr();
+}
+
 } /* extern "C" */

@@ -172,6 +172,47 @@ def thm_cases(ref):
     return out
 
 
+def thm_finish_cases(ref):
+    """PostTweaks from the de-novo result (identity and a skewed prior
+    pretweak), FinishAtFullRes on the full-resolution tile (scale 4)."""
+    out = {}
+    for seed in (0, 2):
+        ta, tb, th, t = synth.thumb_pair(seed, tile=768, dec=8)
+        A, VA = O.image_to_points(ta)
+        B, VB = O.image_to_points(tb)
+        A, VA = ref.decimate_normalize(A, VA, 96, 96, 1)
+        B, VB = ref.decimate_normalize(B, VB, 96, 96, 1)
+        req = 3125 // 16
+        best = ref.thm_search(A, VA, B, VB, req, mode=0)
+        prior = np.array([best["A"], best["X"], best["Y"], best["R"]])
+        out[f"in_s{seed}"] = dict(pa=A, va=VA, pb=B, vb=VB)
+        for name, tw in (("id", None), ("skew", [1.0, 0.02, 0.0, 0.0, 0.99, 0.0])):
+            res = ref.thm_finish(A, VA, B, VB, req, 5, prior, tptwk=tw)
+            out[f"post_s{seed}_{name}"] = dict(
+                ref_in=f"in_s{seed}", req=req, mode=5, prior=prior,
+                tptwk=np.array(tw if tw is not None else [1, 0, 0, 0, 1, 0], np.float64),
+                A=res["A"], X=res["X"], Y=res["Y"], R=res["R"], tptwk_out=res["tptwk"])
+    ta, tb, th, t = synth.thumb_pair(7, tile=128, dec=4)
+    fa, fb, _, _ = synth.thumb_pair(7, tile=128, dec=1)
+    A, VA = O.image_to_points(ta)
+    B, VB = O.image_to_points(tb)
+    A, VA = ref.decimate_normalize(A, VA, 32, 32, 1)
+    B, VB = ref.decimate_normalize(B, VB, 32, 32, 1)
+    best = ref.thm_search(A, VA, B, VB, 100, mode=0)
+    A1, V1 = O.image_to_points(fa)
+    B1, W1 = O.image_to_points(fb)
+    A1, V1 = ref.decimate_normalize(A1, V1, 128, 128, 1)
+    B1, W1 = ref.decimate_normalize(B1, W1, 128, 128, 1)
+    prior = np.array([best["A"], best["X"] * 4, best["Y"] * 4, best["R"]])
+    res = ref.thm_finish(A1, V1, B1, W1, 1600, 6, prior)
+    out["full_s7"] = dict(pa=A1.astype(np.int32), va=V1, pb=B1.astype(np.int32), vb=W1,
+                          req=1600, mode=6, prior=prior,
+                          tptwk=np.array([1, 0, 0, 0, 1, 0], np.float64),
+                          A=res["A"], X=res["X"], Y=res["Y"], R=res["R"],
+                          tptwk_out=res["tptwk"])
+    return out
+
+
 def decimate_cases(ref):
     ta, tb, th, t = synth.thumb_pair(4, tile=512, dec=2)
     A, VA = O.image_to_points(ta.astype(np.float64))
@@ -199,6 +240,7 @@ def main():
     save("convolve", convolve_cases(ref))
     save("patch_to_image", patch_to_image_cases(ref))
     save("thm_scan", thm_cases(ref))
+    save("thm_finish", thm_finish_cases(ref))
     save("decimate", decimate_cases(ref))
 
 

@@ -63,3 +63,18 @@ def test_sweep_batch_of_pairs_matches_oracle(ctx, orc):
     got = ctx.thm_search_batch(thumbs, mode=aln.THM_DENOVO)
     for k, (g, r) in enumerate(zip(got, refs)):
         compare(g, r, f"pair {k}")
+
+
+@pytest.mark.parametrize("case", sorted(load_golden("thm_finish")))
+def test_finish_golden(ctx, case):
+    """PostTweaks / FinishAtFullRes from the reference's prior, against its
+    golden results (the same bar as the sweep)."""
+    import alignment_projects_gb300 as aln
+    d = load_golden("thm_finish")[case]
+    T = aln.thumbs_from_points(d["pa"], d["va"], d["pb"], d["vb"], int(d["req"]))
+    prior = dict(zip("AXYR", (float(v) for v in d["prior"])))
+    g = ctx.thm_finish_batch([T], int(d["mode"]), [prior], tptwk=[d["tptwk"]])[0]
+    ref = dict(A=d["A"], X=d["X"], Y=d["Y"], R=d["R"], err=0)
+    compare(g, ref, case)
+    if abs(g["A"] - float(d["A"])) < 1e-9:
+        assert np.abs(np.array(g["tptwk"]) - d["tptwk_out"]).max() <= 1e-6, (g, d["tptwk_out"])

@@ -99,6 +99,17 @@ def test_thm_scan_golden(orc, case):
     assert o["err"] == int(d["err"])
 
 
+@pytest.mark.parametrize("case", sorted(load_golden("thm_finish")))
+def test_thm_finish_golden(orc, case):
+    """PostTweaks / FinishAtFullRes (CThmScan.cpp:796-842) from a prior best."""
+    d = load_golden("thm_finish")[case]
+    o = orc.thm_finish(d["pa"], d["va"], d["pb"], d["vb"], int(d["req"]), int(d["mode"]),
+                       d["prior"], tptwk=d["tptwk"])
+    for k in ("A", "X", "Y", "R"):
+        assert close(o[k], d[k]), (k, o[k], float(d[k]))
+    assert np.abs(np.array(o["tptwk"]) - d["tptwk_out"]).max() <= 1e-12
+
+
 def test_decimate_golden(orc):
     d = load_golden("decimate")["dec8"]
     xy, v = orc.decimate_normalize(d["pa"], d["va"], int(d["w"]), int(d["h"]),
