@@ -1334,8 +1334,8 @@ static inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // CorrImagesF/R/S parameters of a job (0_GEN/Correlation.h:159-220).
 struct ImgSpec {
-    int kind;   // 0 CorrPatches (no spec), 1 R, 2 S, 3 CorrPatchToImage
-    double mincor;
+    int kind;   // 0 CorrPatches (no spec), 1 R, 2 S, 3 CorrPatchToImage, 4 F
+    double mincor, nbmaxht;
     int ox, oy, rx, ry;
     // CorrPatchToImage
     int p2i_w1, p2i_h1, p2i_w2, p2i_h2, p2i_filter;
@@ -1566,9 +1566,10 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
             pl.in_bytes[0] = pl.in_bytes[1] = 0;
             return ALN_OK;
         }
-        d.mode = spec->kind == 2 ? JOB_IMAGES_S : JOB_IMAGES_R;
+        d.mode = spec->kind == 2 ? JOB_IMAGES_S : spec->kind == 4 ? JOB_IMAGES_F : JOB_IMAGES_R;
         d.want_s = spec->kind == 2;
-        d.want_r = spec->kind == 1 || (spec->kind == 2 && spec->mincor > 0.0);
+        d.want_r = spec->kind == 1 || spec->kind == 4 || (spec->kind == 2 && spec->mincor > 0.0);
+        d.nbmaxht = spec->nbmaxht;
         d.no_shift = d.want_s;
         // S key alone: no value sums, only counts; FP32 keys in the lag scan
         d.sat_nonly = d.mode == JOB_IMAGES_S && !d.want_r;
@@ -1633,6 +1634,8 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
         b += al256((size_t)L1 * Wy * sizeof(float2));
     if (d.mode == JOB_IMAGES_S && d.want_r)
         b += al256((size_t)Wx * Wy * sizeof(double));
+    if (d.mode == JOB_IMAGES_F)
+        b += al256((size_t)Wx * Wy * sizeof(double)) + al256((size_t)Wx * Wy);
     pl.ws_bytes = b;
     return ALN_OK;
 }
@@ -1707,6 +1710,12 @@ static size_t carve(PairPlan &pl, char *base, const aln_pair &P)
     if (d.mode == JOB_IMAGES_S && d.want_r) {
         d.rr2 = (double *)p;
         p += al256((size_t)Wx * Wy * sizeof(double));
+    }
+    if (d.mode == JOB_IMAGES_F) {
+        d.fimg = (double *)p;
+        p += al256((size_t)Wx * Wy * sizeof(double));
+        d.fst = (unsigned char *)p;
+        p += al256((size_t)Wx * Wy);
     }
     (void)P;
     return (size_t)(p - base);
@@ -1994,7 +2003,16 @@ static int launch_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, const Chun
                cl.frame_ny1);
     else if (mode == JOB_P2I)
         LAUNCH(ctx, "k_final_p2i", k_final_p2i, n, 256, 0, ctx->dpairs, ctx->dres);
-    else
+    else if (mode == JOB_IMAGES_F) {
+        int mw = 1, mh = 1;
+        for (auto *pl : chunk) {
+            mw = std::max(mw, pl->d.wR);
+            mh = std::max(mh, pl->d.hR);
+        }
+        LAUNCH(ctx, "k_makef", k_makef, dim3((mw + 31) / 32, (mh + 7) / 8, n), dim3(32, 8), 0,
+               ctx->dpairs);
+        LAUNCH(ctx, "k_fpeak", k_fpeak, n, FPK_THREADS, 0, ctx->dpairs, ctx->dres);
+    } else
         LAUNCH(ctx, "k_final_img", k_final_img, n, 256, 0, ctx->dpairs, ctx->dres);
     CK(cudaGetLastError());
     return ALN_OK;
@@ -2289,18 +2307,17 @@ extern "C" int aln_corr_images_batch(aln_ctx *ctx, int njobs, const aln_image_jo
     std::vector<ImgSpec> specs(njobs);
     for (int k = 0; k < njobs; ++k) {
         const aln_image_job &J = jobs[k];
-        if (J.kind != ALN_CORR_R && J.kind != ALN_CORR_S)
-            return set_err(ctx, ALN_ERR_UNSUPPORTED,
-                           "CorrImages kind %d: the F (isolated-peak) variant is not built yet",
-                           J.kind);
+        if (J.kind != ALN_CORR_R && J.kind != ALN_CORR_S && J.kind != ALN_CORR_F)
+            return set_err(ctx, ALN_ERR_ARG, "CorrImages kind %d", J.kind);
         memset(&pairs[k], 0, sizeof(aln_pair));
         pairs[k].a = J.a;
         pairs[k].b = J.b;
         pairs[k].radius = 1 << 20;   // the whole R image; MaskA's oval is separate
         pairs[k].legal = J.legal;
         pairs[k].b_key = J.b_key;
-        specs[k].kind = J.kind == ALN_CORR_S ? 2 : 1;
+        specs[k].kind = J.kind == ALN_CORR_S ? 2 : J.kind == ALN_CORR_F ? 4 : 1;
         specs[k].mincor = J.mincor;
+        specs[k].nbmaxht = J.nbmaxht;
         specs[k].ox = J.ox;
         specs[k].oy = J.oy;
         specs[k].rx = J.rx;

@@ -13,7 +13,7 @@ struct RowBest {
 };
 
 // job kinds
-enum { JOB_PATCHES = 0, JOB_IMAGES_R = 1, JOB_IMAGES_S = 2, JOB_P2I = 3 };
+enum { JOB_PATCHES = 0, JOB_IMAGES_R = 1, JOB_IMAGES_S = 2, JOB_P2I = 3, JOB_IMAGES_F = 4 };
 
 // Compact per-pair result copied back to the host.
 struct ResultDev {
@@ -75,6 +75,10 @@ struct PairDev {
     int want_r, want_s;          // which inverse transforms the job needs
     int no_shift;                // S is not shift-invariant: mu = 0
     double mincor;               // candidates need R > mincor when > 0
+    double nbmaxht;              // CorrImagesF: neighbour height limit (x peak)
+    double *fimg;                // CorrImagesF: the F image [iy][ix] (wR x hR)
+    unsigned char *fst;          // CorrImagesF: per R pixel, bit 2 candidate,
+                                 // bit 1 visited, bit 0 masked (FPeak)
     int oval_on, ocx, ocy, orx, ory;   // MaskA oval in R-image indices
     double oasq, orx2;
     int cx, cy, wR, hR;          // R image: lag (x, y) at index (x + cx) + wR (y + cy)

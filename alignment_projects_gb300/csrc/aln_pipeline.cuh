@@ -1051,7 +1051,10 @@ __global__ void __launch_bounds__(256, 2) k2_lagimg(PairDev *pairs, const float2
             if (keyS && want_r)
                 p.rr2[o] = rv;
             const int ix = x + p.cx;
-            if (legal && oval_ok(p, ix, iy) && (p.mincor <= 0.0 || rv > p.mincor))
+            const bool cand = legal && oval_ok(p, ix, iy) && (p.mincor <= 0.0 || rv > p.mincor);
+            if (p.mode == JOB_IMAGES_F)   // OrderF's candidates (A, R > mincor)
+                p.fst[o] = cand ? 4 : 0;
+            if (cand)
                 best_merge(br, bk, key, (long long)iy * p.wR + ix);
         }
     }
@@ -1096,6 +1099,55 @@ __global__ void __launch_bounds__(256, 2) k2_lagimg(PairDev *pairs, const float2
         p.rb[j].ssum = ss;
         p.rb[j].ssum2 = ss2;
     }
+}
+
+// ParabPeak on the key image at R-image pixel (rx, ry) (neighbours must be
+// > 0, 0_GEN/Correlation.cpp:2975-3010), ReturnR's offsets (:3016-3043); the
+// S score 10 (S - mean) / (sd sqrt(nR)) with the sample sd for CorrImagesS
+// (:3285-3289).  Writes the job's result.
+__device__ void img_result(PairDev &p, int rx, int ry, double ss, double ss2, ResultDev &o)
+{
+    const int wR = p.wR, hR = p.hR;
+    // the key image (the window is the whole R image); FP32 c when s_float:
+    // ParabPeak's ratios and the S score are the same in c units
+    const double *Id = p.rr;
+    const float *If = (const float *)p.rr;
+    const bool fl = p.s_float != 0;
+    auto I = [&](long long k) -> double { return fl ? (double)If[k] : Id[k]; };
+    double xpk = rx, ypk = ry;
+    const double z1 = I(rx + (long long)wR * ry);
+    double z0, z2;
+    if (rx - 1 >= 0 && rx + 1 < wR && (z0 = I(rx - 1 + (long long)wR * ry)) > 0.0 &&
+        (z2 = I(rx + 1 + (long long)wR * ry)) > 0.0) {
+        z0 = (z0 - z2) / (2 * (z0 + z2 - z1 - z1));
+        if (fabs(z0) <= 8)
+            xpk += z0;
+    }
+    if (ry - 1 >= 0 && ry + 1 < hR && (z0 = I(rx + (long long)wR * (ry - 1))) > 0.0 &&
+        (z2 = I(rx + (long long)wR * (ry + 1))) > 0.0) {
+        z0 = (z0 - z2) / (2 * (z0 + z2 - z1 - z1));
+        if (fabs(z0) <= 8)
+            ypk += z0;
+    }
+    double r = z1;
+    if (p.mode == JOB_IMAGES_S) {
+        const double n = (double)wR * hR;
+        const double mn = ss / n;
+        const double sd = sqrt(fmax(ss2 - n * mn * mn, 0.0) / (n - 1.0));
+        r = 10.0 * (z1 - mn) / (sd * sqrt(n));
+    }
+    p.r = r;
+    p.dx = xpk + (p.x0[1] - p.x0[0]) - p.cx;
+    p.dy = ypk + (p.y0[1] - p.y0[0]) - p.cy;
+    p.px = rx - p.cx;
+    p.py = ry - p.cy;
+    p.status = ALN_OK;
+    o.r = p.r;
+    o.dx = p.dx;
+    o.dy = p.dy;
+    o.status = ALN_OK;
+    o.px = p.px;
+    o.py = p.py;
 }
 
 // grid (npairs), block 256: argmax over rows, ParabPeak on the key image
@@ -1149,48 +1201,192 @@ __global__ void k_final_img(PairDev *pairs, ResultDev *res)
         o.px = o.py = 0;
         return;
     }
+    const int ry = (int)(bk / p.wR), rx = (int)(bk - (long long)ry * p.wR);
+    img_result(p, rx, ry, ss, ss2, o);
+}
+
+// ---------------------------------------------------------------------------
+// CorrImagesF (0_GEN/Correlation.cpp:3066-3122): F = the R image filtered by
+// the 3 x 3 kernel {-1 x 8, 9} (MakeF, :2412-2492), the best isolated F peak
+// (FPeak, :2580-2767), ParabPeak and ReturnR on R there
+// ---------------------------------------------------------------------------
+
+// grid (ceil(wR/32), ceil(hR/8), njobs), block (32, 8).  MakeF convolves R
+// over a frame of CeilPow2(wR) x CeilPow2(hR) and then clears a guard band of
+// 2 pixels (F and the candidate flags); inside the band every tap lies in R,
+// so the filter is the plain 3 x 3 stencil.  F keeps its positive part; the
+// reference's division by the maximum is left out: every FPeak test compares
+// F values with multiples of a peak's F, so a common positive scale changes
+// no decision.
+__global__ void k_makef(PairDev *pairs)
+{
+    PairDev &p = pairs[blockIdx.z];
+    if (p.status != 0 || p.mode != JOB_IMAGES_F)
+        return;
     const int wR = p.wR, hR = p.hR;
-    const int ry = (int)(bk / wR), rx = (int)(bk - (long long)ry * wR);
-    // the key image (the window is the whole R image); FP32 c when s_float:
-    // ParabPeak's ratios and the S score are the same in c units
-    const double *Id = p.rr;
-    const float *If = (const float *)p.rr;
-    const bool fl = p.s_float != 0;
-    auto I = [&](long long k) -> double { return fl ? (double)If[k] : Id[k]; };
-    double xpk = rx, ypk = ry;
-    const double z1 = I(rx + (long long)wR * ry);
-    double z0, z2;
-    if (rx - 1 >= 0 && rx + 1 < wR && (z0 = I(rx - 1 + (long long)wR * ry)) > 0.0 &&
-        (z2 = I(rx + 1 + (long long)wR * ry)) > 0.0) {
-        z0 = (z0 - z2) / (2 * (z0 + z2 - z1 - z1));
-        if (fabs(z0) <= 8)
-            xpk += z0;
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    if (x >= wR || y >= hR)
+        return;
+    const long long k = (long long)y * wR + x;
+    const int grd = 2;
+    if (x < grd || x >= wR - grd || y < grd || y >= hR - grd) {
+        p.fimg[k] = 0.0;
+        p.fst[k] = 0;
+        return;
     }
-    if (ry - 1 >= 0 && ry + 1 < hR && (z0 = I(rx + (long long)wR * (ry - 1))) > 0.0 &&
-        (z2 = I(rx + (long long)wR * (ry + 1))) > 0.0) {
-        z0 = (z0 - z2) / (2 * (z0 + z2 - z1 - z1));
-        if (fabs(z0) <= 8)
-            ypk += z0;
+    const double *R = p.rr;
+    double f = 9.0 * R[k];
+    for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx)
+            if (dx || dy)
+                f -= R[k + (long long)dy * wR + dx];
+    p.fimg[k] = f > 0.0 ? f : 0.0;
+}
+
+// FPeak, one CTA of 1024 threads per job.  Candidates in OrderF's order (F
+// descending; equal F: smaller index first) are taken one at a time: each
+// thread keeps the best live candidate of its own pixels (k = t mod 1024)
+// and rescans only when that one is visited or masked; a block argmax
+// picks the next.  The candidate's tests run on the whole block: the four
+// scans for the half-height radius ri (one warp each, 32 pixels per
+// ballot), the guard-band bounds, the core mask, and the ring between ri and
+// 3 ri for a neighbour above nbmaxht x peak.  The first candidate that passes
+// is the peak.
+#define FPK_THREADS 1024
+
+__device__ __forceinline__ bool fpk_better(double a, long long ia, double b, long long ib)
+{
+    return a > b || (a == b && ia < ib);
+}
+
+__global__ void __launch_bounds__(FPK_THREADS) k_fpeak(PairDev *pairs, ResultDev *res)
+{
+    __shared__ double s_v[32];
+    __shared__ long long s_i[32];
+    __shared__ int s_dist[4];
+    __shared__ long long s_pick;
+    PairDev &p = pairs[blockIdx.x];
+    if (p.status != 0 || p.mode != JOB_IMAGES_F)
+        return;
+    ResultDev &o = res[blockIdx.x];
+    const int wR = p.wR, hR = p.hR;
+    const long long nR = (long long)wR * hR;
+    const double *F = p.fimg;
+    unsigned char *st = p.fst;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    double lv = -1.0;
+    long long li = -1;   // this thread's best live candidate (-1: rescan)
+    for (;;) {
+        if (li >= 0 && (st[li] & 3))
+            li = -1;
+        if (li < 0) {
+            lv = -1.0;
+            for (long long k = tid; k < nR; k += FPK_THREADS)
+                if ((st[k] & 7) == 4 && (li < 0 || fpk_better(F[k], k, lv, li))) {
+                    lv = F[k];
+                    li = k;
+                }
+        }
+        // block argmax (value desc, index asc); li < 0 never wins
+        double bv = li >= 0 ? lv : -2.0;
+        long long bi = li >= 0 ? li : 0x7fffffffffffffffLL;
+        for (int off = 16; off > 0; off >>= 1) {
+            const double v2 = __shfl_down_sync(0xffffffff, bv, off);
+            const long long i2 = __shfl_down_sync(0xffffffff, bi, off);
+            if (fpk_better(v2, i2, bv, bi)) {
+                bv = v2;
+                bi = i2;
+            }
+        }
+        if (lane == 0) {
+            s_v[wid] = bv;
+            s_i[wid] = bi;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 1; w < FPK_THREADS / 32; ++w)
+                if (fpk_better(s_v[w], s_i[w], bv, bi)) {
+                    bv = s_v[w];
+                    bi = s_i[w];
+                }
+            s_pick = bv > -1.5 ? bi : -1;
+        }
+        __syncthreads();
+        const long long k = s_pick;
+        if (k < 0)
+            break;   // every candidate tried
+        const double fpk = F[k], half = 0.5 * fpk, tol = p.nbmaxht * fpk;
+        const int ry = (int)(k / wR), rx = (int)(k - (long long)ry * wR);
+        // ri: first pixel at or below half height up, down, left, right
+        if (wid < 4) {
+            const int dx = wid == 2 ? -1 : (wid == 3 ? 1 : 0);
+            const int dy = wid == 0 ? -1 : (wid == 1 ? 1 : 0);
+            const int lim = wid == 0 ? ry : wid == 1 ? hR - 1 - ry : wid == 2 ? rx : wR - 1 - rx;
+            int found = -1;
+            for (int d0 = 1; d0 <= lim && found < 0; d0 += 32) {
+                const int d = d0 + lane;
+                bool hit = false;
+                if (d <= lim)
+                    hit = F[(long long)(ry + dy * d) * wR + (rx + dx * d)] <= half;
+                const unsigned b = __ballot_sync(0xffffffff, hit);
+                if (b)
+                    found = d0 + __ffs(b) - 1;
+            }
+            if (lane == 0)
+                s_dist[wid] = found;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            int ri = 1 << 30, ok = 1;
+            for (int w = 0; w < 4; ++w) {
+                if (s_dist[w] < 0)
+                    ok = 0;   // Ri_edge
+                else
+                    ri = min(ri, s_dist[w]);
+            }
+            if (ok && ri <= 1 && p.rr[k] < 0.1)
+                ok = 0;   // Micropk
+            const int ro = 3 * ri;
+            if (ok && (ry - ro < 0 || ry + ro >= hR || rx - ro < 0 || rx + ro >= wR))
+                ok = 0;   // Ro_edge
+            st[k] |= 2;   // visited
+            s_dist[0] = ok ? ri : -1;
+        }
+        __syncthreads();
+        const int ri = s_dist[0];
+        if (ri >= 0) {
+            const int ro = 3 * ri, rm = max(1, ri / 3);
+            // mask the core peak region
+            const int mw = 2 * rm + 1;
+            for (int e = tid; e < mw * mw; e += FPK_THREADS) {
+                const int yy = ry - rm + e / mw, xx = rx - rm + e % mw;
+                st[(long long)yy * wR + xx] |= 1;
+            }
+            // any pixel above tol in the ring between ri and ro
+            const int ow = 2 * ro + 1;
+            const long long tot = (long long)ow * ow;
+            int hi = 0;
+            for (long long e = tid; e < tot && !hi; e += FPK_THREADS) {
+                const int yy = ry - ro + (int)(e / ow), xx = rx - ro + (int)(e % ow);
+                if (yy >= ry - ri && yy <= ry + ri && xx >= rx - ri && xx <= rx + ri)
+                    continue;
+                hi = F[(long long)yy * wR + xx] > tol;
+            }
+            hi = __syncthreads_or(hi);
+            if (!hi) {
+                if (tid == 0)
+                    img_result(p, rx, ry, 0.0, 0.0, o);
+                return;
+            }
+        }
+        __syncthreads();
     }
-    double r = z1;
-    if (p.mode == JOB_IMAGES_S) {
-        const double n = (double)wR * hR;
-        const double mn = ss / n;
-        const double sd = sqrt(fmax(ss2 - n * mn * mn, 0.0) / (n - 1.0));
-        r = 10.0 * (z1 - mn) / (sd * sqrt(n));
+    if (tid == 0) {   // All peaks rejected / no candidates
+        p.status = ALN_NO_PEAK;
+        o.r = o.dx = o.dy = 0.0;
+        o.status = ALN_NO_PEAK;
+        o.px = o.py = 0;
     }
-    p.r = r;
-    p.dx = xpk + (p.x0[1] - p.x0[0]) - p.cx;
-    p.dy = ypk + (p.y0[1] - p.y0[0]) - p.cy;
-    p.px = rx - p.cx;
-    p.py = ry - p.cy;
-    p.status = ALN_OK;
-    o.r = p.r;
-    o.dx = p.dx;
-    o.dy = p.dy;
-    o.status = ALN_OK;
-    o.px = p.px;
-    o.py = p.py;
 }
 
 // ---------------------------------------------------------------------------

@@ -59,8 +59,9 @@ static void srv_image_job(const aln_image_job &J, aln_pair &P, ImgSpec &S)
     P.radius = 1 << 20;
     P.legal = J.legal;
     P.b_key = J.b_key;
-    S.kind = J.kind == ALN_CORR_S ? 2 : 1;
+    S.kind = J.kind == ALN_CORR_S ? 2 : J.kind == ALN_CORR_F ? 4 : 1;
     S.mincor = J.mincor;
+    S.nbmaxht = J.nbmaxht;
     S.ox = J.ox;
     S.oy = J.oy;
     S.rx = J.rx;

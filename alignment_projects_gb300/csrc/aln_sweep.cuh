@@ -338,7 +338,10 @@ static int eval_batch(SweepCtx &S, std::vector<Eval> &ev)
                 keys[k] = JobKey{0, tp.in->b_key};
             else
                 keys[k] = JobKey{1, S.key_base + (unsigned long long)E.pair + 1};
-            specs[k].kind = 2;
+            // RFromAngle: CorrImagesS, or CorrImagesF when useCorrR is off
+            // (CThmScan.cpp:355-365)
+            specs[k].kind = S.P.usecorrr ? 2 : 4;
+            specs[k].nbmaxht = S.P.nbmaxht;
             specs[k].mincor = 0.0;
             specs[k].ox = tp.own_disc ? tp.dox : S.P.ox;
             specs[k].oy = tp.own_disc ? tp.doy : S.P.oy;
@@ -713,9 +716,6 @@ extern "C" int aln_thm_search_batch(aln_ctx *ctx, int npairs, const aln_thumbs *
 {
     if (!ctx || npairs < 0 || (npairs && (!thumbs || !params || !out)))
         return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
-    if (!params->usecorrr)
-        return set_err(ctx, ALN_ERR_UNSUPPORTED,
-                       "sweep with CorrImagesF (useCorrR off) is not built yet");
     SweepCtx S;
     char *dbuf = nullptr;
     int rc = sweep_setup(ctx, S, npairs, thumbs, params, &dbuf);

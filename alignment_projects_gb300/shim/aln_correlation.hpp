@@ -53,7 +53,13 @@ double CorrPatchToImage(double &dx, double &dy, const std::vector<Point> &ip1,
                         const std::vector<double> &iv1, const std::vector<double> &i2, int Ox,
                         int Oy, int radius, bool bFilter);
 
-// CorrImagesR / CorrImagesS (0_GEN/Correlation.cpp:3144-3290)
+// CorrImagesF / CorrImagesR / CorrImagesS (0_GEN/Correlation.cpp:3066-3290)
+double CorrImagesF(FILE *flog, int verbose, double &dx, double &dy,
+                   const std::vector<Point> &ip1, const std::vector<double> &iv1,
+                   const std::vector<Point> &ip2, const std::vector<double> &iv2,
+                   EvalType LegalRgn, void *arglr, EvalType LegalCnt, void *arglc,
+                   double mincor, double nbmaxht, int Ox, int Oy, int Rx, int Ry,
+                   std::vector<CD> &fft2);
 double CorrImagesR(FILE *flog, int verbose, double &dx, double &dy,
                    const std::vector<Point> &ip1, const std::vector<double> &iv1,
                    const std::vector<Point> &ip2, const std::vector<double> &iv2,

@@ -298,6 +298,17 @@ double corr_images(int kind, FILE *flog, int verbose, double &dx, double &dy,
 
 }   // namespace
 
+double CorrImagesF(FILE *flog, int verbose, double &dx, double &dy,
+                   const std::vector<Point> &ip1, const std::vector<double> &iv1,
+                   const std::vector<Point> &ip2, const std::vector<double> &iv2,
+                   EvalType LegalRgn, void *arglr, EvalType LegalCnt, void *arglc,
+                   double mincor, double nbmaxht, int Ox, int Oy, int Rx, int Ry,
+                   std::vector<CD> &fft2)
+{
+    return corr_images(ALN_CORR_F, flog, verbose, dx, dy, ip1, iv1, ip2, iv2, LegalRgn, arglr,
+                       LegalCnt, arglc, mincor, nbmaxht, Ox, Oy, Rx, Ry, fft2);
+}
+
 double CorrImagesR(FILE *flog, int verbose, double &dx, double &dy,
                    const std::vector<Point> &ip1, const std::vector<double> &iv1,
                    const std::vector<Point> &ip2, const std::vector<double> &iv2,

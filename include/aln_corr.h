@@ -218,18 +218,21 @@ enum { ALN_CORR_F = 0, ALN_CORR_R = 1, ALN_CORR_S = 2 };
  * mincor > 0), peak by maximal R (kind R) or maximal S, the FFT-whitened
  * correlation (kind S), ParabPeak refinement.  out->r is R at the peak
  * (kind R) or 10 (S - mean(S)) / (sd(S) sqrt(wR hR)) (kind S).  Images
- * smaller than the reference's SetDims limit give ALN_NO_PEAK.  nbmaxht is
- * used by kind F only. */
+ * smaller than the reference's SetDims limit give ALN_NO_PEAK.  Kind F
+ * (CorrImagesF, 0_GEN/Correlation.cpp:3066-3122) filters R by the 3 x 3
+ * kernel {-1 x 8, 9} and takes the highest well-isolated F peak (half-height
+ * radius ri, no pixel above nbmaxht x peak between ri and 3 ri), reporting R
+ * there; nbmaxht is used by kind F only. */
 typedef struct aln_image_job {
     aln_image a, b;
-    int kind;           /* ALN_CORR_R or ALN_CORR_S (ALN_CORR_F: not built yet) */
+    int kind;           /* ALN_CORR_F, ALN_CORR_R or ALN_CORR_S */
     aln_legal legal;
     double mincor, nbmaxht;
     int ox, oy, rx, ry;
     unsigned long long b_key;   /* != 0: image b's spectrum cache key (ftc) */
 } aln_image_job;
 
-/* CorrImagesR / CorrImagesS, 0_GEN/Correlation.cpp:3144-3199, 3222-3290 */
+/* CorrImagesF / R / S, 0_GEN/Correlation.cpp:3066-3122, 3144-3199, 3222-3290 */
 int aln_corr_images(aln_ctx *ctx, int kind, const aln_image *a, const aln_image *b,
                     const aln_legal *legal, double mincor, double nbmaxht, int ox, int oy,
                     int rx, int ry, aln_result *out);
@@ -258,7 +261,7 @@ typedef struct aln_thumbs {
 /* CThmScan settings (its setters, 0_GEN/CThmScan.h:115-157). */
 typedef struct aln_thm_params {
     double rthresh, nbmaxht;
-    int constxy, pretweak, usecorrr;   /* usecorrr must be 1 (CorrImagesS) */
+    int constxy, pretweak, usecorrr;   /* usecorrr: CorrImagesS (1) or CorrImagesF (0) */
     int ox, oy, rx, ry;                /* SetDisc */
     double tdfm[6];                    /* SetTdfm (TAffine t[0..5]) */
 } aln_thm_params;

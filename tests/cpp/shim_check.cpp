@@ -7,7 +7,7 @@
 // radius, Rx, Ry, int32 rgn_min (0: no LegalRgn, else olw, olh >= it and
 // area > rgn_area), int64 rgn_area, int64 cnt_n (-1: no LegalCnt), double
 // mincor, int32 reuse (1: use the previous case's fft2 vector)
-// kind 0 = CorrPatches, 1 = CorrImagesR, 2 = CorrImagesS
+// kind 0 = CorrPatches, 1 = CorrImagesR, 2 = CorrImagesS, 3 = CorrImagesF
 #include "aln_correlation.hpp"
 
 #include <cstdint>
@@ -82,6 +82,9 @@ int main(int argc, char **argv)
         if (kind == 0)
             r = CorrPatches(stderr, 0, dx, dy, p1, v1, p2, v2, Ox, Oy, rad, lr, &ra, lc, &cnv,
                             fft2);
+        else if (kind == 3)
+            r = CorrImagesF(stderr, 0, dx, dy, p1, v1, p2, v2, lr, &ra, lc, &cnv, mincor, 0.75,
+                            Ox, Oy, Rx, Ry, fft2);
         else if (kind == 1)
             r = CorrImagesR(stderr, 0, dx, dy, p1, v1, p2, v2, lr, &ra, lc, &cnv, mincor, 0.75,
                             Ox, Oy, Rx, Ry, fft2);

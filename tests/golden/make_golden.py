@@ -213,6 +213,25 @@ def thm_finish_cases(ref):
     return out
 
 
+def thm_f_cases(ref):
+    """The sweep with useCorrR off: RFromAngle through CorrImagesF."""
+    out = {}
+    ta, tb, th, t = synth.thumb_pair(3, tile=512, dec=8)
+    A, VA = O.image_to_points(ta)
+    B, VB = O.image_to_points(tb)
+    A, VA = ref.decimate_normalize(A, VA, 64, 64, 1)
+    B, VB = ref.decimate_normalize(B, VB, 64, 64, 1)
+    req = 3125 // 64
+    out["in_s3"] = dict(pa=A, va=VA, pb=B, vb=VB)
+    for name, mode, kw in [("denovo", 0, {}), ("maxr", 4, dict(hfang=3.0))]:
+        res = ref.thm_search(A, VA, B, VB, req, mode=mode, usecorrr=0, **kw)
+        out[f"thmf_s3_{name}"] = dict(
+            ref_in="in_s3", req=req, mode=mode, ang0=0.0, hfang=kw.get("hfang", 10.0),
+            step=0.5, rthresh=0.3, pretweak=0, disc=np.array((0, 0, -1, -1)),
+            A=res["A"], X=res["X"], Y=res["Y"], R=res["R"], err=res["err"])
+    return out
+
+
 def decimate_cases(ref):
     ta, tb, th, t = synth.thumb_pair(4, tile=512, dec=2)
     A, VA = O.image_to_points(ta.astype(np.float64))
@@ -241,6 +260,7 @@ def main():
     save("patch_to_image", patch_to_image_cases(ref))
     save("thm_scan", thm_cases(ref))
     save("thm_finish", thm_finish_cases(ref))
+    save("thm_scan_f", thm_f_cases(ref))
     save("decimate", decimate_cases(ref))
 
 

@@ -1,4 +1,4 @@
-"""GPU parity of CorrImagesR / CorrImagesS (0_GEN/Correlation.cpp:3144-3290)
+"""GPU parity of CorrImagesF / R / S (0_GEN/Correlation.cpp:3066-3290)
 against the oracle and the reference's golden outputs, through the C ABI.
 
 Tolerances: the integer peak equals the oracle's wherever the oracle's
@@ -53,8 +53,7 @@ def run_case(ctx, orc, kind, pa, va, pb, vb, lg, mincor, disc):
     return g, o
 
 
-@pytest.mark.parametrize("case", sorted(k for k, d in load_golden("corr_images").items()
-                                        if int(d["kind"]) in (1, 2)))
+@pytest.mark.parametrize("case", sorted(load_golden("corr_images")))
 def test_corr_images_golden(ctx, orc, case):
     d = load_golden("corr_images")[case]
     kind = int(d["kind"])
@@ -80,7 +79,7 @@ def _thumbs(seed, deg):
     return A @ R.T, VA, B, VB, th
 
 
-@pytest.mark.parametrize("seed,kind", [(s, k) for s in range(6) for k in (1, 2)])
+@pytest.mark.parametrize("seed,kind", [(s, k) for s in range(6) for k in (0, 1, 2)])
 def test_rotated_thumbnails(ctx, orc, seed, kind):
     import oracle
     pa, va, pb, vb, th = _thumbs(seed, -1.0 + 0.37 * seed)
@@ -90,7 +89,8 @@ def test_rotated_thumbnails(ctx, orc, seed, kind):
 
 
 @pytest.mark.parametrize("kind,mincor,disc", [(2, 0.05, (0, 0, -1, -1)), (2, 0.0, (4, -3, 15, 9)),
-                                              (1, 0.1, (-6, 2, 12, 20)), (2, 0.0, (0, 0, 0, 5))])
+                                              (1, 0.1, (-6, 2, 12, 20)), (2, 0.0, (0, 0, 0, 5)),
+                                              (0, 0.0, (0, 0, -1, -1)), (0, 0.2, (3, 3, 20, 16))])
 def test_mincor_and_oval(ctx, orc, kind, mincor, disc):
     import oracle
     pa, va, pb, vb, th = _thumbs(3, 0.5)

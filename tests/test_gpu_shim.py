@@ -48,13 +48,13 @@ def test_cpp_callers_through_shim(tmp_path, orc):
     expect.append(("plain96_s1 cached", float(d["r"]), float(d["dx"]), float(d["dy"]), True,
                    1e-4))
     for k in ("img_s0_k1_d0_m0", "img_s0_k1_d1_m1", "img_s0_k2_d0_m0", "img_s0_k2_d1_m0",
-              "img_s1_k2_d1_m1"):
+              "img_s1_k2_d1_m1", "img_s0_k0_d0_m0", "img_s1_k0_d1_m1"):
         d = gi[k]
         kind = int(d["kind"])
         disc = [int(v) for v in d["disc"]]
         la = _legal_args(d["legal"])
-        blob += case(kind, d["pa"], d["va"], d["pb"], d["vb"], disc[0], disc[1], 4096, disc[2],
-                     disc[3], mincor=float(d["mincor"]), **la)
+        blob += case(kind if kind else 3, d["pa"], d["va"], d["pb"], d["vb"], disc[0], disc[1],
+                     4096, disc[2], disc[3], mincor=float(d["mincor"]), **la)
         o = orc.corr_images(kind, d["pa"], d["va"], d["pb"], d["vb"],
                             oracle.legal(*[int(v) for v in d["legal"]]), float(d["mincor"]),
                             0.75, *disc)

@@ -78,3 +78,14 @@ def test_finish_golden(ctx, case):
     compare(g, ref, case)
     if abs(g["A"] - float(d["A"])) < 1e-9:
         assert np.abs(np.array(g["tptwk"]) - d["tptwk_out"]).max() <= 1e-6, (g, d["tptwk_out"])
+
+
+@pytest.mark.parametrize("case", sorted(load_golden("thm_scan_f")))
+def test_sweep_f_golden(ctx, case):
+    """useCorrR off: every correlator call is CorrImagesF."""
+    import alignment_projects_gb300 as aln
+    d = load_golden("thm_scan_f")[case]
+    T = aln.thumbs_from_points(d["pa"], d["va"], d["pb"], d["vb"], int(d["req"]))
+    g = ctx.thm_search_batch([T], usecorrr=0, mode=int(d["mode"]), ang0=float(d["ang0"]),
+                             hfang=float(d["hfang"]), step=float(d["step"]))[0]
+    compare(g, d, case)

@@ -110,6 +110,18 @@ def test_thm_finish_golden(orc, case):
     assert np.abs(np.array(o["tptwk"]) - d["tptwk_out"]).max() <= 1e-12
 
 
+@pytest.mark.parametrize("case", sorted(load_golden("thm_scan_f")))
+def test_thm_scan_f_golden(orc, case):
+    """The sweep with useCorrR off (RFromAngle through CorrImagesF)."""
+    d = load_golden("thm_scan_f")[case]
+    o = orc.thm_search(d["pa"], d["va"], d["pb"], d["vb"], int(d["req"]), usecorrr=0,
+                       mode=int(d["mode"]), ang0=float(d["ang0"]), hfang=float(d["hfang"]),
+                       step=float(d["step"]))
+    for k in ("A", "X", "Y", "R"):
+        assert close(o[k], d[k]), (k, o[k], float(d[k]))
+    assert o["err"] == int(d["err"])
+
+
 def test_decimate_golden(orc):
     d = load_golden("decimate")["dec8"]
     xy, v = orc.decimate_normalize(d["pa"], d["va"], int(d["w"]), int(d["h"]),

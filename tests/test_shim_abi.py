@@ -21,6 +21,8 @@ EXPECTED = {
     "CorrPatches": "_Z11CorrPatchesP8_IO_FILEiRdS1_RKSt6vectorI5PointSaIS3_EERKS2_IdSaIdEES7_SB_"
                    "iiiPFbiiPvESC_SE_SC_RS2_ISt7complexIdESaISG_EE",
     "CorrPatchToImage": "_Z16CorrPatchToImageRdS_RKSt6vectorI5PointSaIS1_EERKS0_IdSaIdEES9_iiib",
+    "CorrImagesF": "_Z11CorrImagesFP8_IO_FILEiRdS1_RKSt6vectorI5PointSaIS3_EERKS2_IdSaIdEES7_SB_"
+                   "PFbiiPvESC_SE_SC_ddiiiiRS2_ISt7complexIdESaISG_EE",
     "CorrImagesR": "_Z11CorrImagesRP8_IO_FILEiRdS1_RKSt6vectorI5PointSaIS3_EERKS2_IdSaIdEES7_SB_"
                    "PFbiiPvESC_SE_SC_ddiiiiRS2_ISt7complexIdESaISG_EE",
     "CorrImagesS": "_Z11CorrImagesSP8_IO_FILEiRdS1_RKSt6vectorI5PointSaIS3_EERKS2_IdSaIdEES7_SB_"
