@@ -1759,13 +1759,13 @@ static void launch_fill_cols(aln_ctx *ctx, int nsel, int L)
 }
 
 template <int NY>
-static void launch_corrcol2(aln_ctx *ctx, int n, int L, int cached, bool plain)
+static void launch_corrcol2(aln_ctx *ctx, int n, int L, int cached, int var)
 {
     constexpr int T = RegFFT<NY, -1>::T;
     const int thr = std::max(256, T), G = thr / T;
     const size_t sm = (size_t)G * (padded(NY) + NY) * sizeof(float2);
     void (*kern)(PairDev *, const float2 *, int) =
-        plain ? k2_corrcol<NY, true> : k2_corrcol<NY, false>;
+        var == 1 ? k2_corrcol<NY, 1> : var == 2 ? k2_corrcol<NY, 2> : k2_corrcol<NY, 0>;
     smem_attr(ctx->device, (const void *)kern, sm);
     LAUNCH(ctx, "k2_corrcol", kern, dim3((L + 1 + G - 1) / G, n), thr, sm, ctx->dpairs, ctx->tw,
            cached);
@@ -1819,7 +1819,7 @@ static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int
     default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
     }
     switch (Ny) {
-#define X(v) case v: launch_corrcol2<v>(ctx, n, L, 0, mode == JOB_PATCHES); break;
+#define X(v) case v: launch_corrcol2<v>(ctx, n, L, 0, mode == JOB_PATCHES ? 1 : sonly ? 2 : 0); break;
         ALN_CASES_NY(X)
 #undef X
     default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "column length %d", Ny);

@@ -630,12 +630,15 @@ __global__ void k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int onl
 // columns: forward b and a, product, inverse, window rows
 // ---------------------------------------------------------------------------
 
-// PLAIN: CorrPatches chunks (plain inverse only, no low-pass, no whitening),
-// compiled without the other jobs' branches.
-template <int NY, bool PLAIN>
+// VAR: 1 = CorrPatches chunks (plain inverse only, no low-pass, no
+// whitening), 2 = CorrImagesS without a mincor (whitened inverse only),
+// 0 = any job; the specialised forms are compiled without the other jobs'
+// branches.
+template <int NY, int VAR>
 __global__ void __launch_bounds__(NY >= 8192 ? 512 : 256, NY >= 8192 ? 1 : 2)
 k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
 {
+    constexpr bool PLAIN = VAR == 1, SONLY = VAR == 2;
     using FF = RegFFT<NY, -1>;
     using FI = RegFFT<NY, +1>;
     constexpr int R = FF::R, T = FF::T;
@@ -687,7 +690,7 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
 #pragma unroll
     for (int r = 0; r < R; ++r)
         va[r] = cmulc(sb[r * T + t], va[r]);   // X2 * conj(X1)
-    const bool is_p2i = !PLAIN && p.mode == JOB_P2I;
+    const bool is_p2i = VAR == 0 && p.mode == JOB_P2I;
     if (is_p2i && p.p2i_filter) {
         // CorrPatchToImage's low-pass (0_GEN/Correlation.cpp:1255-1283): the
         // reference names the row index "x" (wrapped) and the column "y"
@@ -703,8 +706,8 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
     }
     // CorrPatches / CorrImagesR need the plain inverse; CorrImagesS the inverse
     // of the whitened product P / sqrt(|P|) (0_GEN/Correlation.cpp:2311-2317)
-    const bool want_r = PLAIN || p.mode == JOB_PATCHES || is_p2i || p.want_r;
-    const bool want_s = !PLAIN && p.want_s != 0;
+    const bool want_r = PLAIN || (!SONLY && (p.mode == JOB_PATCHES || is_p2i || p.want_r));
+    const bool want_s = SONLY || (!PLAIN && p.want_s != 0);
     if (want_r && want_s) {
 #pragma unroll
         for (int r = 0; r < R; ++r)
@@ -797,26 +800,49 @@ k2_colspec(PairDev *pairs, const float2 *__restrict__ tw, const int *sel)
 // ---------------------------------------------------------------------------
 // lag rows
 // ---------------------------------------------------------------------------
-
-// The L+1 spectrum bins of lag row jc (Q is [kx][j], stride Wy) into the
-// team's shared row: all of a thread's loads are issued before the first
-// store, so their latencies overlap.
-template <int L, int T>
-__device__ __forceinline__ void load_lag_row(float2 *dst, const float2 *__restrict__ Q, int Wy,
-                                             int jc, int t)
+// The job's descriptor in shared memory: the lag scans read many of its
+// fields inside loops that also store through its pointers; from global
+// memory each read would be a fresh L1 round trip (the compiler cannot keep
+// them across the stores).  All threads of the CTA must call this.
+__device__ __forceinline__ const PairDev &stage_job(const PairDev *pairs, int j, PairDev &sp)
 {
-    constexpr int K = L / T + 1;
-    float2 v[K];
+    const int *src = (const int *)(pairs + j);
+    int *dst = (int *)&sp;
+    for (int i = threadIdx.x; i < (int)(sizeof(PairDev) / sizeof(int)); i += blockDim.x)
+        dst[i] = src[i];
+    __syncthreads();
+    return sp;
+}
+
+
+// The L+1 spectrum bins of the CTA's G lag rows j0 .. j0+G-1 (Q is [kx][j],
+// stride Wy; rows past Wy repeat the last one) into the teams' shared rows
+// (team g at base + g * stride), loaded by the whole CTA so that a warp's
+// loads cover whole 8-row segments of Q (G consecutive j per kx); four loads
+// per thread are in flight before their stores.
+template <int L, int T>
+__device__ __forceinline__ void load_lag_rows(float2 *base, int stride,
+                                              const float2 *__restrict__ Q, int Wy, int j0)
+{
+    constexpr int G = (T >= 256 ? T : 256) / T;
+    constexpr int TOT = (L + 1) * G;
+    const int nt = blockDim.x;
+    for (int e0 = threadIdx.x; e0 < TOT; e0 += 4 * nt) {
+        float2 v[4];
 #pragma unroll
-    for (int q = 0; q < K; ++q) {
-        const int k = t + q * T;
-        v[q] = k <= L ? __ldg(&Q[(long long)k * Wy + jc]) : make_float2(0.f, 0.f);
-    }
+        for (int q = 0; q < 4; ++q) {
+            const int e = e0 + q * nt;
+            const int kx = e / G, g = e - kx * G;
+            v[q] = e < TOT ? __ldg(&Q[(long long)kx * Wy + min(j0 + g, Wy - 1)])
+                           : make_float2(0.f, 0.f);
+        }
 #pragma unroll
-    for (int q = 0; q < K; ++q) {
-        const int k = t + q * T;
-        if (k <= L)
-            dst[padi(k)] = v[q];
+        for (int q = 0; q < 4; ++q) {
+            const int e = e0 + q * nt;
+            const int kx = e / G, g = e - kx * G;
+            if (e < TOT)
+                base[g * stride + padi(kx)] = v[q];
+        }
     }
 }
 
@@ -829,7 +855,8 @@ __global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
     extern __shared__ float2 smem[];
     __shared__ double red_r[32];
     __shared__ long long red_k[32];
-    PairDev &p = pairs[blockIdx.y];
+    __shared__ PairDev sp;
+    const PairDev &p = stage_job(pairs, blockIdx.y, sp);
     if (p.status != 0)
         return;
     const int Wy = p.yhi - p.ylo + 1, Wx = p.xhi - p.xlo + 1;
@@ -840,11 +867,10 @@ __global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
         return;
     const int j = j0 + team;
     const bool live = j < Wy;
-    const int jc = live ? j : Wy - 1;
     float2 *sm = smem + team * PITCH;
     const int Nx = p.Nx, Ny = p.Ny;
-    // spectrum bins of this lag row (strided over kx)
-    load_lag_row<L, T>(sm, p.Q, Wy, jc, t);
+    // spectrum bins of the CTA's lag rows
+    load_lag_rows<L, T>(smem, PITCH, p.Q, Wy, j0);
     __syncthreads();
     float2 v[R];
 #pragma unroll
@@ -942,7 +968,8 @@ __global__ void __launch_bounds__(256, 2) k2_lagimg(PairDev *pairs, const float2
     extern __shared__ float2 smem[];
     __shared__ double red_r[32], red_s[32], red_s2[32];
     __shared__ long long red_k[32];
-    PairDev &p = pairs[blockIdx.y];
+    __shared__ PairDev sp;
+    const PairDev &p = stage_job(pairs, blockIdx.y, sp);
     if (p.status != 0)
         return;
     const int Wy = p.yhi - p.ylo + 1, Wx = p.xhi - p.xlo + 1;
@@ -953,7 +980,6 @@ __global__ void __launch_bounds__(256, 2) k2_lagimg(PairDev *pairs, const float2
         return;
     const int j = j0 + team;
     const bool live = j < Wy;
-    const int jc = live ? j : Wy - 1;
     const bool want_r = !SONLY && p.want_r != 0, want_s = SONLY || p.want_s != 0;
     const bool both = want_r && want_s;
     float2 *sm = smem + team * PITCH * (both ? 2 : 1);
@@ -967,7 +993,8 @@ __global__ void __launch_bounds__(256, 2) k2_lagimg(PairDev *pairs, const float2
         const float2 *Qs = doS ? (both ? p.Q2 : p.Q) : p.Q;
         float2 *reg = sm + ((both && !doS) ? PITCH : 0);
         __syncthreads();
-        load_lag_row<L, T>(reg, Qs, Wy, jc, t);
+        load_lag_rows<L, T>(smem + ((both && !doS) ? PITCH : 0), PITCH * (both ? 2 : 1), Qs,
+                            Wy, j0);
         __syncthreads();
         float2 v[R];
 #pragma unroll
@@ -1417,9 +1444,8 @@ __global__ void k2_lagp2i(PairDev *pairs, const float2 *__restrict__ tw)
         return;
     const int j = j0 + team;
     const bool live = j < Wy;
-    const int jc = live ? j : Wy - 1;
     float2 *sm = smem + team * PITCH;
-    load_lag_row<L, T>(sm, p.Q, Wy, jc, t);
+    load_lag_rows<L, T>(smem, PITCH, p.Q, Wy, j0);
     __syncthreads();
     float2 v[R];
 #pragma unroll

@@ -22,12 +22,19 @@ struct SplatJob {
     float eu, ev;            // half-extents of the preimage of a 2 x 2 pixel square
     int L, B, w1, h1;        // bounding box of the rotated points
     float *out;
-    const double *a;         // A values on the grid, a[x + stride*y]
+    const float *a;          // A values on the grid, a[x + stride*y] (FP32 copy)
     const unsigned char *mask;   // presence (NULL: all present)
     int aw, ah, astride, ax0, ay0;
 };
 
 #define SPLAT_FX 40   // fractional bits of the fixed-point coordinates
+
+__global__ void k_f64_to_f32(const double *__restrict__ src, float *__restrict__ dst, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = (float)src[i];
+}
 
 // grid (ceil(maxw/32), ceil(maxh/32), njobs), block 256: each thread gathers
 // four output pixels of a 32 x 32 tile.  A point p = (px, py) lands at
@@ -47,7 +54,6 @@ __global__ void __launch_bounds__(256) k_splat(const SplatJob *jobs)
     if (tx0 >= J.w1 || ty0 >= J.h1)
         return;
     const long long ONE = 1ll << SPLAT_FX;
-    const float SCL = 1.0f / (float)(1ll << SPLAT_FX);
     const int X = tx0 + (threadIdx.x & 31);
     const int gx_lo = J.ax0, gx_hi = J.ax0 + J.aw - 1;
     const int gy_lo = J.ay0, gy_hi = J.ay0 + J.ah - 1;
@@ -74,9 +80,13 @@ __global__ void __launch_bounds__(256) k_splat(const SplatJob *jobs)
                     continue;
                 if (J.mask && !J.mask[row + u])
                     continue;
-                const float wx = (float)(ONE - (dx < 0 ? -dx : dx)) * SCL;
-                const float wy = (float)(ONE - (dy < 0 ? -dy : dy)) * SCL;
-                acc += wx * wy * (float)__ldg(&J.a[row + u]);
+                // 1 - |d| from its top 24 fractional bits: an exact 32-bit
+                // integer to FP32 conversion (64-bit ones use the FP64 pipe)
+                const float wx = (float)(int)((ONE - (dx < 0 ? -dx : dx)) >> (SPLAT_FX - 24)) *
+                                 5.9604644775390625e-8f;
+                const float wy = (float)(int)((ONE - (dy < 0 ? -dy : dy)) >> (SPLAT_FX - 24)) *
+                                 5.9604644775390625e-8f;
+                acc += wx * wy * __ldg(&J.a[row + u]);
             }
         }
         J.out[(long long)Y * J.w1 + X] = acc;
@@ -137,6 +147,7 @@ struct ThmPair {
     std::vector<std::pair<long long, long long>> hull;   // convex hull of A's points
     double Tptwk[6];
     const double *dev_a;            // device copies
+    const float *dev_af;            // A's values in FP32 (what the splat reads)
     const unsigned char *dev_mask;
     aln_image dev_b;
     // pretweak sweep records (TCD.vT)
@@ -279,7 +290,7 @@ static int eval_batch(SweepCtx &S, std::vector<Eval> &ev)
             J.B = (int)floor(ylo);
             J.w1 = (int)ceil(xhi) - J.L + 1;
             J.h1 = (int)ceil(yhi) - J.B + 1;
-            J.a = tp.dev_a;
+            J.a = tp.dev_af;
             J.mask = tp.dev_mask;
             J.aw = tp.in->a_w;
             J.ah = tp.in->a_h;
@@ -659,8 +670,8 @@ static int sweep_setup(aln_ctx *ctx, SweepCtx &S, int npairs, const aln_thumbs *
         if (!T.a || T.a_w < 1 || T.a_h < 1 || T.a_stride < T.a_w || !T.b.data ||
             T.b.dtype != ALN_F64 || T.b.w < 1 || T.b.h < 1 || T.b.stride < T.b.w)
             return set_err(ctx, ALN_ERR_ARG, "thumbnail pair %d: bad grid/raster", k);
-        bytes += al256((size_t)T.a_stride * T.a_h * 8) + al256((size_t)T.a_stride * T.a_h) +
-                 al256((size_t)T.b.stride * T.b.h * 8);
+        bytes += al256((size_t)T.a_stride * T.a_h * 8) + al256((size_t)T.a_stride * T.a_h * 4) +
+                 al256((size_t)T.a_stride * T.a_h) + al256((size_t)T.b.stride * T.b.h * 8);
     }
     char *dbuf = nullptr;
     if (bytes) {
@@ -684,6 +695,16 @@ static int sweep_setup(aln_ctx *ctx, SweepCtx &S, int npairs, const aln_thumbs *
         if (cudaMemcpyAsync(p, T.a, ab, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
             rc = set_err(ctx, ALN_ERR_CUDA, "thumbnail copy");
         p += al256(ab);
+        // the splat multiplies in FP32: convert once here instead of per
+        // gathered point (FP64 conversions run on the narrow FP64 pipe)
+        tp.dev_af = (const float *)p;
+        {
+            const size_t na = (size_t)T.a_stride * T.a_h;
+            LAUNCH(ctx, "k_f64_to_f32", k_f64_to_f32,
+                   (unsigned)std::min<size_t>((na + 255) / 256, 1024), 256, 0, tp.dev_a,
+                   (float *)p, na);
+            p += al256(na * 4);
+        }
         tp.dev_mask = nullptr;
         if (T.a_mask) {
             tp.dev_mask = (const unsigned char *)p;
