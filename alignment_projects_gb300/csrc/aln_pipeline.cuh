@@ -634,8 +634,11 @@ __global__ void k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int onl
 // whitening), 2 = CorrImagesS without a mincor (whitened inverse only),
 // 0 = any job; the specialised forms are compiled without the other jobs'
 // branches.
+// Occupancy: the CorrPatches form keeps 2 CTAs per SM (128 registers; at 3
+// its register FFTs spill heavily and run slower), the S-only form runs 3
+// (80 registers, small spills, faster).
 template <int NY, int VAR>
-__global__ void __launch_bounds__(NY >= 8192 ? 512 : 256, NY >= 8192 ? 1 : 2)
+__global__ void __launch_bounds__(NY >= 8192 ? 512 : 256, NY >= 8192 ? 1 : (VAR == 2 ? 3 : 2))
 k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
 {
     constexpr bool PLAIN = VAR == 1, SONLY = VAR == 2;
@@ -960,7 +963,7 @@ __global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
 // SONLY: chunks of S-key jobs without a mincor (the sweep's correlator):
 // one inverse per row and the FP32-key scan only, compiled without the rest.
 template <int L, bool SONLY>
-__global__ void __launch_bounds__(256, 2) k2_lagimg(PairDev *pairs, const float2 *__restrict__ tw)
+__global__ void __launch_bounds__(256, SONLY ? 3 : 2) k2_lagimg(PairDev *pairs, const float2 *__restrict__ tw)
 {
     using F = RegFFT<L, +1>;
     constexpr int R = F::R, T = F::T;
