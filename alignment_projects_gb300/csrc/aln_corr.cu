@@ -962,10 +962,11 @@ struct SpecEntry {
     size_t bytes;
     unsigned long long tick;   // last chunk that used it
 };
-// (namespace, key, Nx, Ny, transposed, no_shift); namespace 0: the caller's
-// keys, 1: keys the library makes (the sweep's thumbnails).  no_shift: the
-// spectrum is of b itself (CorrImagesS) rather than of b minus its mean.
-typedef std::tuple<int, unsigned long long, int, int, int, int> SpecKey;
+// (namespace, key, Nx, Ny, transposed, no_shift, radix); namespace 0: the
+// caller's keys, 1: keys the library makes (the sweep's thumbnails).
+// no_shift: the spectrum is of b itself (CorrImagesS) rather than of b minus
+// its mean; radix: the column FFT's per-thread radix (its rounding).
+typedef std::tuple<int, unsigned long long, int, int, int, int, int> SpecKey;
 
 struct aln_ctx {
     int device;
@@ -1747,28 +1748,54 @@ static void launch_fill_rows(aln_ctx *ctx, int nsel, int maxh)
            ctx->dpairs, ctx->tw, 1, (const int *)ctx->dsel_cur);
 }
 
-template <int NY>
-static void launch_fill_cols(aln_ctx *ctx, int nsel, int L)
+template <int NY, int RAD>
+static void launch_fill_cols_rad(aln_ctx *ctx, int nsel, int L)
 {
-    constexpr int T = RegFFT<NY, -1>::T;
+    constexpr int T = NY / RAD;
     const int thr = std::max(256, T), G = thr / T;
     const size_t sm = (size_t)G * padded(NY) * sizeof(float2);
-    smem_attr(ctx->device, (const void *)k2_colspec<NY>, sm);
-    LAUNCH(ctx, "k2_colspec", k2_colspec<NY>, dim3((L + 1 + G - 1) / G, nsel), thr, sm,
+    smem_attr(ctx->device, (const void *)k2_colspec<NY, RAD>, sm);
+    LAUNCH(ctx, "k2_colspec", (k2_colspec<NY, RAD>), dim3((L + 1 + G - 1) / G, nsel), thr, sm,
            ctx->dpairs, ctx->tw, (const int *)ctx->dsel_cur);
+}
+
+// the cache entry is computed with the radix of the column kernel that reads it
+template <int NY>
+static void launch_fill_cols(aln_ctx *ctx, int nsel, int L, int var)
+{
+    if (var == 1)
+        launch_fill_cols_rad<NY, corrcol_radix<NY, 1>()>(ctx, nsel, L);
+    else
+        launch_fill_cols_rad<NY, corrcol_radix<NY, 0>()>(ctx, nsel, L);
+}
+
+static int corrcol_radix_of(int Ny, int var)
+{
+    (void)var;   // every form uses fft_radix (corrcol_radix)
+    return fft_radix(Ny);
+}
+
+template <int NY, int VAR>
+static void launch_corrcol_var(aln_ctx *ctx, int n, int L, int cached)
+{
+    constexpr int T = NY / corrcol_radix<NY, VAR>();
+    constexpr int thr = corrcol_threads<NY, VAR>(), G = thr / T;
+    const size_t sm = (size_t)G * (padded(NY) + NY) * sizeof(float2);
+    void (*kern)(PairDev *, const float2 *, int) = k2_corrcol<NY, VAR>;
+    smem_attr(ctx->device, (const void *)kern, sm);
+    LAUNCH(ctx, "k2_corrcol", kern, dim3((L + 1 + G - 1) / G, n), thr, sm, ctx->dpairs, ctx->tw,
+           cached);
 }
 
 template <int NY>
 static void launch_corrcol2(aln_ctx *ctx, int n, int L, int cached, int var)
 {
-    constexpr int T = RegFFT<NY, -1>::T;
-    const int thr = std::max(256, T), G = thr / T;
-    const size_t sm = (size_t)G * (padded(NY) + NY) * sizeof(float2);
-    void (*kern)(PairDev *, const float2 *, int) =
-        var == 1 ? k2_corrcol<NY, 1> : var == 2 ? k2_corrcol<NY, 2> : k2_corrcol<NY, 0>;
-    smem_attr(ctx->device, (const void *)kern, sm);
-    LAUNCH(ctx, "k2_corrcol", kern, dim3((L + 1 + G - 1) / G, n), thr, sm, ctx->dpairs, ctx->tw,
-           cached);
+    if (var == 1)
+        launch_corrcol_var<NY, 1>(ctx, n, L, cached);
+    else if (var == 2)
+        launch_corrcol_var<NY, 2>(ctx, n, L, cached);
+    else
+        launch_corrcol_var<NY, 0>(ctx, n, L, cached);
 }
 
 template <int LL>
@@ -1883,7 +1910,8 @@ static void prep_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int off, ch
         pl.d.b_cached = 0;
         if (pl.key && reg_path && pl.d.mode != JOB_P2I && ctx->spec_cap > 0) {
             const SpecKey K(pl.key_ns, pl.key, pl.d.Nx, pl.d.Ny, pl.d.transposed,
-                            pl.d.no_shift);
+                            pl.d.no_shift,
+                            corrcol_radix_of(pl.d.Ny, pl.d.mode == JOB_PATCHES ? 1 : 0));
             auto it = ctx->spec.find(K);
             if (it != ctx->spec.end()) {
                 it->second.tick = ctx->spec_tick;
@@ -1965,7 +1993,7 @@ static int launch_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, const Chun
         default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
         }
         switch (Ny) {
-#define X(v) case v: launch_fill_cols<v>(ctx, cl.nfill, L); break;
+#define X(v) case v: launch_fill_cols<v>(ctx, cl.nfill, L, mode == JOB_PATCHES ? 1 : 0); break;
             ALN_CASES_NY(X)
 #undef X
         default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "column length %d", Ny);

@@ -86,9 +86,9 @@ struct DFT<1, DIR> {
 // threads and >= 4 threads per team down to N = 32).
 __host__ __device__ constexpr int fft_radix(int N) { return N >= 512 ? 16 : (N >= 8 ? 8 : N); }
 
-template <int N, int DIR>
+template <int N, int DIR, int RAD = fft_radix(N)>
 struct RegFFT {
-    static constexpr int R = fft_radix(N);
+    static constexpr int R = RAD;
     static constexpr int T = N / R;                    // threads per transform
     static constexpr int P = ilog2c(N) / ilog2c(R);    // full radix-R passes
     static constexpr int R2 = N / ipowc(R, P);         // first-pass radix (1: none)

@@ -634,16 +634,32 @@ __global__ void k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int onl
 // whitening), 2 = CorrImagesS without a mincor (whitened inverse only),
 // 0 = any job; the specialised forms are compiled without the other jobs'
 // branches.
-// Occupancy: the CorrPatches form keeps 2 CTAs per SM (128 registers; at 3
-// its register FFTs spill heavily and run slower), the S-only form runs 3
-// (80 registers, small spills, faster).
+// Per-thread radix of the column FFTs, per kernel form.  (Measured on the
+// montage batch: 8 points per thread at 4096 -- twice the threads per
+// column -- ran 45% slower than 16, so every form uses fft_radix.)
 template <int NY, int VAR>
-__global__ void __launch_bounds__(NY >= 8192 ? 512 : 256, NY >= 8192 ? 1 : (VAR == 2 ? 3 : 2))
+__host__ __device__ constexpr int corrcol_radix()
+{
+    return fft_radix(NY);
+}
+
+template <int NY, int VAR>
+__host__ __device__ constexpr int corrcol_threads()
+{
+    return NY / corrcol_radix<NY, VAR>() >= 256 ? NY / corrcol_radix<NY, VAR>() : 256;
+}
+
+// Occupancy: the CorrPatches form keeps 2 CTAs per SM; the S-only form runs
+// 3 (80 registers, small spills, faster).
+template <int NY, int VAR>
+__global__ void __launch_bounds__(corrcol_threads<NY, VAR>(),
+                                  (NY >= 8192 || corrcol_threads<NY, VAR>() > 256) ? 1
+                                                                                 : (VAR == 2 ? 3 : 2))
 k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
 {
     constexpr bool PLAIN = VAR == 1, SONLY = VAR == 2;
-    using FF = RegFFT<NY, -1>;
-    using FI = RegFFT<NY, +1>;
+    using FF = RegFFT<NY, -1, corrcol_radix<NY, VAR>()>;
+    using FI = RegFFT<NY, +1, corrcol_radix<NY, VAR>()>;
     constexpr int R = FF::R, T = FF::T;
     extern __shared__ float2 smem[];
     PairDev &p = pairs[blockIdx.y];
@@ -766,11 +782,14 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
 // spectrum.  The same RegFFT code as the fused path, so the cached and the
 // recomputed spectra are the same numbers.  grid (ceil((L+1)/G), nsel): the
 // jobs are pairs[sel[y]].
-template <int NY>
-__global__ void __launch_bounds__(NY >= 8192 ? 512 : 256)
+// RAD: the per-thread radix of the column kernel that reads the entry (the
+// same FFT code, so the cached and the recomputed spectra are the same
+// numbers).
+template <int NY, int RAD>
+__global__ void __launch_bounds__(NY / RAD >= 256 ? NY / RAD : 256)
 k2_colspec(PairDev *pairs, const float2 *__restrict__ tw, const int *sel)
 {
-    using FF = RegFFT<NY, -1>;
+    using FF = RegFFT<NY, -1, RAD>;
     constexpr int R = FF::R, T = FF::T;
     extern __shared__ float2 smem[];
     PairDev &p = pairs[sel[blockIdx.y]];
