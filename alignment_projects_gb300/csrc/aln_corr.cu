@@ -2574,6 +2574,133 @@ extern "C" int aln_ift_2d(aln_ctx *ctx, const double *in, int nfast, int nslow, 
     return ALN_OK;
 }
 
+// Convolve's kernel frame: zeros, K / nrm at the wrapped offsets
+// (0_GEN/Correlation.cpp:395-420), one thread per frame pixel.
+__global__ void k_conv_frame(double *KK, int Nx, int Ny, const double *K, int wk, int hk,
+                             double nrm)
+{
+    const long long n = (long long)Nx * Ny;
+    const int w2 = wk / 2, h2 = hk / 2;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(e % Nx), y = (int)(e / Nx);
+        const int j = x <= w2 ? x : x - Nx, i = y <= h2 ? y : y - Ny;   // offsets -w2..w2
+        double v = 0.0;
+        if (j >= -w2 && j <= w2 && i >= -h2 && i <= h2)
+            v = K[(j + w2) + wk * (i + h2)] / nrm;
+        KK[e] = v;
+    }
+}
+
+// S = X * Y (spectra in the [kx][ky] layout)
+__global__ void k_spec_mul(const float2 *X, const float2 *Y, float2 *S, long long n)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x)
+        S[e] = cmul(X[e], Y[e]);
+}
+
+// dst[x + ws*y] = out[x + Nx*y] / (Nx*Ny) for the source's extent
+__global__ void k_crop_scale(const double *out, int Nx, int Ny, double *dst, int ws, int hs)
+{
+    const long long n = (long long)ws * hs;
+    const double s = 1.0 / ((double)Nx * Ny);
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(e % ws), y = (int)(e / ws);
+        dst[e] = out[(long long)y * Nx + x] * s;
+    }
+}
+
+extern "C" int aln_convolve(aln_ctx *ctx, const double *src, int ws, int hs, const double *K,
+                            int wk, int hk, int sym, int prenorm, double *dst)
+{
+    if (!ctx || !src || !K || !dst || ws < 1 || hs < 1 || wk < 1 || hk < 1)
+        return ctx ? set_err(ctx, ALN_ERR_ARG, "convolve: bad arguments") : ALN_ERR_ARG;
+    const int Nx = aln_fft_size(ws, wk / (1 + (sym ? 1 : 0)));
+    const int Ny = aln_fft_size(hs, hk / (1 + (sym ? 1 : 0)));
+    if (Nx < 2 || Nx > ALN_MAX_N || Ny > ALN_MAX_N)
+        return set_err(ctx, ALN_ERR_UNSUPPORTED, "convolve: frame %d x %d", Nx, Ny);
+    CK(cudaSetDevice(ctx->device));
+    double nrm = 1.0;
+    if (prenorm) {   // the kernel's sum, as the reference forms it
+        nrm = 0.0;
+        for (int i = 0; i < wk * hk; ++i)
+            nrm += K[i];
+        if (!nrm)
+            nrm = 1.0;
+    }
+    const int L1 = Nx / 2 + 1;
+    const size_t M = (size_t)L1 * Ny, NN = (size_t)Nx * Ny;
+    const size_t sb = al256((size_t)ws * hs * 8), kb = al256((size_t)wk * hk * 8),
+                 fb = al256(NN * 8), Tb = al256(M * 8);
+    if (int rc = ensure_ws(ctx, sb + kb + fb + 2 * Tb + 3 * Tb + fb + sb))
+        return rc;
+    if (int rc = ensure_pairs(ctx, 2))
+        return rc;
+    char *p = ctx->ws;
+    double *dsrc = (double *)p;                 p += sb;
+    double *dK = (double *)p;                   p += kb;
+    double *KK = (double *)p;                   p += fb;
+    float2 *T0 = (float2 *)p;                   p += Tb;
+    float2 *T1 = (float2 *)p;                   p += Tb;
+    float2 *X0 = (float2 *)p;                   p += Tb;
+    float2 *X1 = (float2 *)p;                   p += Tb;
+    float2 *S = (float2 *)p;                    p += Tb;
+    double *dout = (double *)p;                 p += fb;
+    double *ddst = (double *)p;
+    cudaStream_t st = ctx->stream;
+    CK(cudaMemcpyAsync(dsrc, src, (size_t)ws * hs * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dK, K, (size_t)wk * hk * 8, cudaMemcpyHostToDevice, st));
+    const unsigned gs = (unsigned)std::min<size_t>(4096, (NN + 255) / 256);
+    LAUNCH(ctx, "k_conv_frame", k_conv_frame, gs, 256, 0, KK, Nx, Ny, dK, wk, hk, nrm);
+    // forward transforms of the source (zero-padded) and the kernel frame
+    PairDev d[2];
+    memset(d, 0, sizeof d);
+    const void *imgs[2] = {dsrc, KK};
+    const int ww[2] = {ws, Nx}, hh[2] = {hs, Ny};
+    float2 *Ts[2] = {T0, T1}, *Xs[2] = {X0, X1};
+    for (int k = 0; k < 2; ++k) {
+        d[k].img[1] = imgs[k];
+        d[k].dt[1] = ALN_F64;
+        d[k].stride[1] = ww[k];
+        d[k].w[1] = ww[k];
+        d[k].h[1] = hh[k];
+        d[k].Nx = Nx;
+        d[k].Ny = Ny;
+        d[k].logNx = ilog2(Nx);
+        d[k].logNy = ilog2(Ny);
+        d[k].T[1] = Ts[k];
+        d[k].Ts[1] = Ny;
+        d[k].X2 = Xs[k];
+    }
+    CK(cudaMemcpyAsync(ctx->dpairs, d, sizeof d, cudaMemcpyHostToDevice, st));
+    const int L = Nx / 2;
+    const int RB = rows_per_cta(L);
+    LAUNCH(ctx, "k_rowfft", k_rowfft, dim3((Ny + RB - 1) / RB, 1, 2), 256,
+           2 * (size_t)RB * (L + 1) * sizeof(float2), ctx->dpairs, ctx->tw, RB, 1);
+    const int CG = cols_per_cta(Ny);
+    LAUNCH(ctx, "k_colfft", k_colfft, dim3((L1 + CG - 1) / CG, 2), 256,
+           2 * (size_t)CG * (Ny + 1) * sizeof(float2), ctx->dpairs, ctx->tw, CG);
+    const unsigned gm = (unsigned)std::min<size_t>(4096, (M + 255) / 256);
+    LAUNCH(ctx, "k_spec_mul", k_spec_mul, gm, 256, 0, X0, X1, S, (long long)M);
+    // inverse, crop, 1 / (Nx Ny)
+    float2 *Q = T0;   // free again
+    LAUNCH(ctx, "k_icolfft", k_icolfft, (L1 + CG - 1) / CG, 256,
+           2 * (size_t)CG * (Ny + 1) * sizeof(float2), S, Q, L1, ilog2(Ny), ctx->tw, CG);
+    const int RBL = std::max(1, std::min(8, 4096 / L));
+    LAUNCH(ctx, "k_irowfft", k_irowfft, (Ny + RBL - 1) / RBL, 256,
+           2 * (size_t)RBL * (L + 1) * sizeof(float2), Q, ilog2(Nx), Ny, dout, ctx->tw, RBL);
+    LAUNCH(ctx, "k_crop_scale", k_crop_scale,
+           (unsigned)std::min<size_t>(4096, ((size_t)ws * hs + 255) / 256), 256, 0, dout, Nx, Ny,
+           ddst, ws, hs);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(dst, ddst, (size_t)ws * hs * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    prof_collect(ctx);
+    return ALN_OK;
+}
+
 // ---------------------------------------------------------------------------
 // tracing (no reference counterpart: the reference logs wall-clock Timer
 // lines, 0_GEN/Timer.cpp:25-52)

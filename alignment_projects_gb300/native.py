@@ -162,6 +162,8 @@ def lib():
                                               C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                               C.c_int, C.POINTER(AlnResult)]
         L.aln_fft_2d.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        L.aln_convolve.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                   C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
         L.aln_ift_2d.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         L.aln_ctx_set_profiling.argtypes = [C.c_void_p, C.c_int]
         L.aln_ctx_profile_reset.argtypes = [C.c_void_p]
@@ -288,6 +290,17 @@ class Context:
 
     def set_workspace_limit(self, nbytes: int):
         self._check(self._L.aln_ctx_set_workspace_limit(self.h, nbytes))
+
+    # -- Convolve (Correlation.h) -------------------------------------------
+    def convolve(self, src, K, sym=True, prenorm=True) -> np.ndarray:
+        src = np.ascontiguousarray(src, np.float64)
+        K = np.ascontiguousarray(K, np.float64)
+        dst = np.zeros_like(src)
+        hs, ws = src.shape
+        hk, wk = K.shape
+        self._check(self._L.aln_convolve(self.h, src.ctypes.data, ws, hs, K.ctypes.data, wk,
+                                         hk, int(sym), int(prenorm), dst.ctypes.data))
+        return dst
 
     # -- FFT support (Correlation.h FFT_2D / IFT_2D) -----------------------
     def fft_2d(self, x):

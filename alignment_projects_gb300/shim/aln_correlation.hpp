@@ -38,6 +38,13 @@ int FFT_2D(std::vector<CD> &out, const std::vector<double> &in, int Nfast, int N
 void IFT_2D(std::vector<double> &out, const std::vector<CD> &in, int Nfast, int Nslow,
             FILE *flog = stderr);
 
+// Convolve (0_GEN/Correlation.cpp:371-457); kfft keeps the reference's size
+// contract (its contents are not used: the GPU recomputes the kernel's
+// transform)
+void Convolve(std::vector<double> &dst, const std::vector<double> &src, int ws, int hs,
+              const double *K, int wk, int hk, bool kIsSymmetric, bool preNormK,
+              std::vector<CD> &kfft, FILE *flog);
+
 // ParabPeakFFT (0_GEN/Correlation.cpp:482-517)
 void ParabPeakFFT(double &xpk, double &ypk, int d, const double *I, int nx, int ny);
 

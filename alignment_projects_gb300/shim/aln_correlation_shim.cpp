@@ -191,6 +191,22 @@ void IFT_2D(std::vector<double> &out, const std::vector<CD> &in, int Nfast, int 
         fprintf(flog, "IFT_2D: %s\n", aln_last_error(ctx()));
 }
 
+void Convolve(std::vector<double> &dst, const std::vector<double> &src, int ws, int hs,
+              const double *K, int wk, int hk, bool kIsSymmetric, bool preNormK,
+              std::vector<CD> &kfft, FILE *flog)
+{
+    const int Nx = aln_fft_size(ws, wk / (1 + kIsSymmetric)),
+              Ny = aln_fft_size(hs, hk / (1 + kIsSymmetric));
+    std::vector<double> out((size_t)ws * hs);   // dst may be src
+    if (aln_convolve(ctx(), src.data(), ws, hs, K, wk, hk, kIsSymmetric ? 1 : 0,
+                     preNormK ? 1 : 0, out.data()) < 0) {
+        fprintf(flog, "Convolve (GPU): %s\n", aln_last_error(ctx()));
+        return;
+    }
+    dst.swap(out);
+    kfft.resize((size_t)Ny * (Nx / 2 + 1));
+}
+
 void ParabPeakFFT(double &xpk, double &ypk, int d, const double *I, int nx, int ny)
 {
     aln_parab_peak_fft(&xpk, &ypk, d, I, nx, ny);

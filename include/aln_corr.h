@@ -169,6 +169,15 @@ int aln_fft_2d(aln_ctx *ctx, const double *in, int nfast, int nslow, double *out
  * Returns 0 or a negative status. */
 int aln_ift_2d(aln_ctx *ctx, const double *in, int nfast, int nslow, double *out);
 
+/* Convolve, 0_GEN/Correlation.cpp:371-457: dst (ws x hs, host FP64) = src
+ * convolved with K (wk x hk) over the circular frame FFTSize(ws, wk/(1+sym))
+ * x FFTSize(hs, hk/(1+sym)), K divided by its sum when prenorm (a zero sum
+ * leaves it), the result divided by the frame size, as the reference.  FP32
+ * transforms on the GPU.  The reference's kfft cache is not needed: the
+ * kernel's transform is recomputed on the device. */
+int aln_convolve(aln_ctx *ctx, const double *src, int ws, int hs, const double *K, int wk,
+                 int hk, int sym, int prenorm, double *dst);
+
 /* ParabPeakFFT, 0_GEN/Correlation.cpp:482-517 (host arithmetic, O(1)). */
 void aln_parab_peak_fft(double *xpk, double *ypk, int d, const double *I,
                         int nx, int ny);

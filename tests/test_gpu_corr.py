@@ -91,6 +91,16 @@ def test_kat_time_fft(ctx):
 
 # ---------------------------------------------------------------- CorrPatches golden
 
+@pytest.mark.parametrize("case", sorted(load_golden("convolve")))
+def test_convolve_golden(ctx, case):
+    """Convolve (0_GEN/Correlation.cpp:371-457) against the reference's output:
+    FP32 transforms, so within 1e-5 of the result's range."""
+    d = load_golden("convolve")[case]
+    g = ctx.convolve(d["src"], d["K"], sym=True, prenorm=True)
+    ref = np.asarray(d["dst"])
+    assert np.abs(g - ref).max() <= 1e-5 * max(1.0, np.abs(ref).max())
+
+
 @pytest.mark.parametrize("case", sorted(load_golden("corr_patches")))
 def test_corr_patches_golden(ctx, orc, case):
     d = load_golden("corr_patches")[case]

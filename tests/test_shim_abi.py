@@ -18,6 +18,7 @@ EXPECTED = {
     "FFT_2D": "_Z6FFT_2DRSt6vectorISt7complexIdESaIS1_EERKS_IdSaIdEEiibP8_IO_FILE",
     "IFT_2D": "_Z6IFT_2DRSt6vectorIdSaIdEERKS_ISt7complexIdESaIS4_EEiiP8_IO_FILE",
     "ParabPeakFFT": "_Z12ParabPeakFFTRdS_iPKdii",
+    "Convolve": "_Z8ConvolveRSt6vectorIdSaIdEERKS1_iiPKdiibbRS_ISt7complexIdESaIS8_EEP8_IO_FILE",
     "CorrPatches": "_Z11CorrPatchesP8_IO_FILEiRdS1_RKSt6vectorI5PointSaIS3_EERKS2_IdSaIdEES7_SB_"
                    "iiiPFbiiPvESC_SE_SC_RS2_ISt7complexIdESaISG_EE",
     "CorrPatchToImage": "_Z16CorrPatchToImageRdS_RKSt6vectorI5PointSaIS1_EERKS0_IdSaIdEES9_iiib",
