@@ -762,14 +762,14 @@ __device__ double stored_value(const PairDev &p, int xs, int ys)
     const int nnegx = p.w[0] - 1, nposx = p.w[1];
     const int nnegy = p.h[0] - 1, nposy = p.h[1];
     int x, y;
-    if (xs >= p.Nx - nnegx)
-        x = xs - p.Nx;
+    if (xs >= p.rnx - nnegx)
+        x = xs - p.rnx;
     else if (xs < nposx)
         x = xs;
     else
         return 0.0;
-    if (ys >= p.Ny - nnegy)
-        y = ys - p.Ny;
+    if (ys >= p.rny - nnegy)
+        y = ys - p.rny;
     else if (ys < nposy)
         y = ys;
     else
@@ -819,12 +819,14 @@ __global__ void k_final(PairDev *pairs, ResultDev *res, int nreal_x_is_one, int 
         return;
     }
     const int Nx = p.Nx, Ny = p.Ny;
-    const int ys = (int)(bk / Nx), xs = (int)(bk - (long long)ys * Nx);
-    const int bigx = xs >= Nx - (p.w[0] - 1) ? xs - Nx : xs;
-    const int bigy = ys >= Ny - (p.h[0] - 1) ? ys - Ny : ys;
+    const int ys0 = (int)(bk / Nx), xs0 = (int)(bk - (long long)ys0 * Nx);
+    const int bigx = xs0 >= Nx - (p.w[0] - 1) ? xs0 - Nx : xs0;
+    const int bigy = ys0 >= Ny - (p.h[0] - 1) ? ys0 - Ny : ys0;
     // ParabPeakFFT, 0_GEN/Correlation.cpp:482-517, d = 1, on the reference's
-    // FFT-sized raster (nx, ny are the reference's sizes).
-    const int nx = nreal_x_is_one ? 1 : Nx, ny = nreal_y_is_one ? 1 : Ny;
+    // FFT-sized raster (nx, ny and the storage indices xs, ys are the
+    // reference's, which may be larger than the transform grid).
+    const int xs = bigx < 0 ? bigx + p.rnx : bigx, ys = bigy < 0 ? bigy + p.rny : bigy;
+    const int nx = nreal_x_is_one ? 1 : p.rnx, ny = nreal_y_is_one ? 1 : p.rny;
     double xpk = bigx, ypk = bigy;
     const int ix = bigx, iy = bigy;
     const double z1 = br;
@@ -1507,6 +1509,8 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
                        ALN_MAX_N);
     d.logNx = ilog2(d.Nx);
     d.logNy = ilog2(d.Ny);
+    d.rnx = d.Nx;
+    d.rny = d.Ny;
     const int P_ox = d.ox, P_oy = d.oy;
     const long long rad = P.radius < 0 ? -(long long)P.radius : P.radius;
     d.rsqr = rad * rad;
@@ -1596,6 +1600,26 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
         pl.in_bytes[0] = pl.in_bytes[1] = 0;
         return ALN_OK;
     }
+    if (d.mode == JOB_PATCHES) {
+        // CorrPatches reads the correlation at the disc's lags only, so the
+        // transform grid only has to keep those lags free of wrap-around: the
+        // circular correlation at lag x holds the linear one at x + m Nx for
+        // every m, whose support is [-(w0-1), w1-1]; Nx > max(w1-1-xlo,
+        // xhi+w0-1) leaves m = 0 alone for every x in [xlo, xhi].  The grid
+        // also holds both images unfolded (Nx >= w0, w1).  The plain product
+        // makes the values at those lags the same sums as on the reference's
+        // grid (the whitened S product of CorrImagesS is not grid-invariant).
+        const int nx = std::max(2, ceil_pow2(std::max(
+                                       std::max(d.w[0], d.w[1]),
+                                       std::max(d.w[1] - 1 - d.xlo, d.xhi + d.w[0] - 1) + 1)));
+        const int ny = std::max(2, ceil_pow2(std::max(
+                                       std::max(d.h[0], d.h[1]),
+                                       std::max(d.h[1] - 1 - d.ylo, d.yhi + d.h[0] - 1) + 1)));
+        d.Nx = std::min(d.Nx, nx);
+        d.Ny = std::min(d.Ny, ny);
+        d.logNx = ilog2(d.Nx);
+        d.logNy = ilog2(d.Ny);
+    }
     if (d.mode != JOB_P2I && !(d.sat_nonly && d.cnt_kind != ALN_CNT_GT))
         for (int i = 0; i < 2; ++i)
             need_rows(d, i, d.need_lo[i], d.need_hi[i]);
@@ -1639,6 +1663,20 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
         b += al256((size_t)Wx * Wy * sizeof(double)) + al256((size_t)Wx * Wy);
     pl.ws_bytes = b;
     return ALN_OK;
+}
+
+extern "C" int aln_corr_patches_grid(const aln_pair *P, int *nx, int *ny, int *transposed)
+{
+    if (!P || !nx || !ny || !transposed)
+        return ALN_ERR_ARG;
+    PairPlan pl;
+    if (int rc = plan_pair(nullptr, *P, pl, true))
+        return rc;
+    const bool empty = pl.d.status == ALN_NO_PEAK;
+    *nx = empty ? 0 : pl.d.Nx;
+    *ny = empty ? 0 : pl.d.Ny;
+    *transposed = pl.transposed ? 1 : 0;
+    return empty ? ALN_NO_PEAK : ALN_OK;
 }
 
 // carve a pair's workspace starting at base; returns bytes used.  Host

@@ -31,6 +31,10 @@ struct PairDev {
     int w[2], h[2];     // bounding boxes
     int x0[2], y0[2];   // bounding-box origins B.L, B.B
     int Nx, Ny, logNx, logNy;
+    // the reference's FFT raster (CeilPow2(w1+w2-1) x CeilPow2(h1+h2-1) in
+    // the solved frame): ParabPeakFFT reads its neighbours by that raster's
+    // storage rules, whatever grid the job is transformed on
+    int rnx, rny;
     // 1: the job is solved on transposed images (x <-> y); img/w/h/x0/y0,
     // the window and the disc are in the transposed frame, src_* describe
     // the caller's untransposed rasters for k_transpose

@@ -175,6 +175,8 @@ def lib():
         L.aln_ctx_set_spectrum_cache.argtypes = [C.c_void_p, C.c_size_t]
         L.aln_parab_peak_fft.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
                                          C.c_void_p, C.c_int, C.c_int]
+        L.aln_corr_patches_grid.argtypes = [C.POINTER(AlnPair), C.POINTER(C.c_int),
+                                            C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.aln_server_create.argtypes = [C.POINTER(AlnServerParams), C.POINTER(C.c_void_p)]
         L.aln_server_destroy.argtypes = [C.c_void_p]
         L.aln_server_submit.argtypes = [C.c_void_p, C.POINTER(AlnRequest),
@@ -439,6 +441,16 @@ class Context:
         out = (AlnResult * len(pairs))()
         self._check(self._L.aln_corr_patches_batch(self.h, len(pairs), arr, out))
         return [o.as_dict() for o in out]
+
+
+def corr_patches_grid(pair: AlnPair):
+    """(nx, ny, transposed) of the transform grid CorrPatches uses for one
+    pair, in the frame the pair is solved in; (0, 0, t) for an empty window."""
+    nx, ny, tr = C.c_int(), C.c_int(), C.c_int()
+    rc = lib().aln_corr_patches_grid(C.byref(pair), C.byref(nx), C.byref(ny), C.byref(tr))
+    if rc < 0:
+        raise AlnError(rc, "aln_corr_patches_grid")
+    return nx.value, ny.value, tr.value
 
 
 def parab_peak_fft(xpk, ypk, d, I):

@@ -166,6 +166,7 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 
 def fft_shape(w1, h1, w2, h2):
+    """The reference's FFT grid (FFTSize per axis)."""
     def cp2(n):
         p = 1
         while p < n:
@@ -174,9 +175,22 @@ def fft_shape(w1, h1, w2, h2):
     return cp2(w1 + w2 - 1), cp2(h1 + h2 - 1)
 
 
-def alg_bytes_per_pair(w, h, e=1):
-    """Per kernel, for one pair of w x h strips (both the same size here)."""
-    Nx, Ny = fft_shape(w, h, w, h)
+def solved_grid(pair):
+    """(w_s, h_s, Nx, Ny) of one AlnPair as the library solves it: the frame
+    (wide pairs transposed) and the transform grid it chooses (the smallest
+    power-of-two grid that keeps the disc's lags free of wrap-around)."""
+    import alignment_projects_gb300 as aln
+    nx, ny, tr = aln.corr_patches_grid(pair)
+    w, h = pair.a.w, pair.a.h
+    if tr:
+        w, h = h, w
+    return w, h, nx, ny
+
+
+def alg_bytes_per_pair(grid, e=1):
+    """Per kernel, for one pair of w x h strips (both the same size here),
+    on the transform grid Nx x Ny the pair is solved on."""
+    w, h, Nx, Ny = grid
     H = Ny * (Nx // 2 + 1)
     rows = 2 * (w * h * e + 8 * H)                    # r2c row passes, both images
     cols = 16 * H + 16 * H + 24 * H + 16 * H          # column passes b, a; product; c2r column pass
@@ -190,24 +204,15 @@ def alg_bytes_per_pair(w, h, e=1):
     }
 
 
-def solve_frame(w, h):
-    """The frame a strip pair is solved in (wide pairs transposed) and its
-    FFT size: (w_s, h_s, Nx, Ny)."""
-    if w > h:
-        w, h = h, w
-    Nx, Ny = fft_shape(w, h, w, h)
-    return w, h, Nx, Ny
-
-
-def dram_model_per_pair(w, h, e=1, wy=129):
+def dram_model_per_pair(grid, e=1, wy=129):
     """DRAM bytes per pair the fused kernels move (each array read or written
     once): k2_rowfft reads both strips and writes both row spectra T (rows < h
     only); k2_corrcol reads both T and writes the window rows Q; k2_lagrow
     reads Q.  k2_corrcol's figure is checked against ncu dram__bytes
     (profiles/k2_corrcol_montage.md)."""
-    ws, hs, Nx, Ny = solve_frame(w, h)
+    ws, hs, Nx, Ny = grid
     L1 = Nx // 2 + 1
-    return {"k2_rowfft": 2 * w * h * e + 16 * L1 * hs,
+    return {"k2_rowfft": 2 * ws * hs * e + 16 * L1 * hs,
             "k2_corrcol": 16 * L1 * hs + 8 * L1 * wy,
             "k2_lagrow": 8 * L1 * wy}
 
@@ -390,10 +395,14 @@ def run_gpu(args):
     ours = {k: v for k, v in prof.items()}
     dom = max(ours, key=lambda k: ours[k][1])
     dom_launches, dom_ms = ours[dom]
-    alg_total = 0
-    for p in batch:
-        h, w = p["a"].shape
-        alg_total += alg_bytes_per_pair(w, h).get(dom, 0)
+    grids = [solved_grid(arr_d[k]) for k in range(n)]
+    grid_hist, ref_hist = {}, {}
+    for g in grids:
+        key = "%dx%d" % (g[2], g[3])
+        grid_hist[key] = grid_hist.get(key, 0) + 1
+        rk = "%dx%d" % fft_shape(g[0], g[1], g[0], g[1])
+        ref_hist[rk] = ref_hist.get(rk, 0) + 1
+    alg_total = sum(alg_bytes_per_pair(g).get(dom, 0) for g in grids)
     alg_per_launch = alg_total * args.steps / max(1, dom_launches)
     achieved = alg_per_launch / (dom_ms / dom_launches / 1000.0) / 1e9
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -402,14 +411,14 @@ def run_gpu(args):
         peak_src = "measured"
     else:
         peak, peak_src = 6800.0, "fallback"
-    traffic = sum(dram_model_per_pair(p["a"].shape[1], p["a"].shape[0]).get(dom, 0)
-                  for p in batch) * args.steps / max(1, dom_launches)
+    traffic = sum(dram_model_per_pair(g).get(dom, 0)
+                  for g in grids) * args.steps / max(1, dom_launches)
     # the FFT passes together (row, column and inverse passes, with the
     # product): counted bytes over the three kernels' summed time
     fft_k = ("k2_rowfft", "k2_corrcol", "k2_lagrow")
     fft_ms = sum(ours[k][1] for k in fft_k if k in ours)
-    fft_bytes = sum(sum(alg_bytes_per_pair(p["a"].shape[1], p["a"].shape[0]).get(k, 0)
-                        for k in fft_k) for p in batch) * args.steps
+    fft_bytes = sum(sum(alg_bytes_per_pair(g).get(k, 0) for k in fft_k)
+                    for g in grids) * args.steps
     fft_gbs = fft_bytes / (fft_ms / 1000.0) / 1e9 if fft_ms > 0 else None
 
     # ---- end to end through the C ABI with pinned host buffers -------------
@@ -529,7 +538,11 @@ def run_gpu(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_dev / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "pairs_per_step": n, "fft": "512|1024 x 4096 (wide pairs solved transposed)",
+            "config": {"workload": WORKLOAD, "pairs_per_step": n,
+                       "fft": "transform grids (solved frame, wide pairs transposed): " +
+                              ", ".join("%s x%d" % (g, c) for g, c in sorted(grid_hist.items())) +
+                              "; the reference's FFTSize grids: " +
+                              ", ".join("%s x%d" % (g, c) for g, c in sorted(ref_hist.items())),
                        "l2": "inputs %.2f GB per step > 129 MB L2" % (strip_bytes / 1e9),
                        "parallelism": "replicas x%d" % ws},
             "e2e": {"value": e2e_value, "unit": "pairs/s",

@@ -206,6 +206,16 @@ typedef struct aln_pair {
 int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *pairs,
                            aln_result *out);
 
+/* The transform grid CorrPatches uses for one pair (no reference
+ * counterpart; a planning query).  The correlation at the disc's lags is
+ * computed on the smallest power-of-two grid that holds both images and
+ * keeps every lag of the disc window free of wrap-around, never larger than
+ * the reference's FFTSize grid.  nx, ny are in the frame the pair is solved
+ * in: *transposed = 1 when a wide pair is solved with x and y exchanged (as
+ * the batch entry points do).  Returns 0, ALN_NO_PEAK when the window is
+ * empty (nx = ny = 0), or a negative status. */
+int aln_corr_patches_grid(const aln_pair *pair, int *nx, int *ny, int *transposed);
+
 /* CorrPatchToImage, 0_GEN/Correlation.cpp:1186-1355: the patch's points
  * (xy1[2i], xy1[2i+1], truncated to pixels) against a caller-embedded
  * square image i2 (N x N, N = sqrt(n2sq), a power of two 16..8192), raw

@@ -68,3 +68,51 @@ def test_context_create_without_gpu_fails_loudly():
     import alignment_projects_gb300 as aln
     with pytest.raises(aln.AlnError):
         aln.Context(0)
+
+
+def _pair(w0, h0, w1, h1, ox, oy, radius, buf):
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300.native import AlnImage, AlnPair
+    P = AlnPair()
+    P.a = AlnImage(buf.ctypes.data, aln.U8, w0, h0, w0, 0, 0, 0)
+    P.b = AlnImage(buf.ctypes.data, aln.U8, w1, h1, w1, 0, 0, 0)
+    P.ox, P.oy, P.radius = ox, oy, radius
+    P.legal = aln.legal()
+    return P
+
+
+def test_corr_patches_grid_keeps_disc_lags_alias_free():
+    """The CorrPatches transform grid: a power of two, no larger than the
+    reference's FFTSize grid, holding both images, and leaving every lag of
+    the disc window free of wrap-around (x + m N outside the linear support
+    [-(w0-1), w1-1] for m != 0).  Host planning only."""
+    import numpy as np
+    import alignment_projects_gb300 as aln
+    buf = np.zeros(4096 * 4096, np.uint8)
+    rng = np.random.default_rng(5)
+    shrunk = 0
+    cases = [(256, 2048, 256, 2048, 0, 0, 64), (200, 2048, 200, 2048, 0, 0, 64),
+             (512, 512, 512, 512, 0, 0, 4096), (300, 120, 280, 100, 0, 0, 30),
+             (64, 64, 64, 64, 40, -40, 10), (1, 1, 1, 1, 0, 0, 5)]
+    for _ in range(400):
+        w0, h0, w1, h1 = (int(v) for v in rng.integers(1, 700, 4))
+        ox, oy = (int(v) for v in rng.integers(-300, 300, 2))
+        cases.append((w0, h0, w1, h1, ox, oy, int(rng.integers(0, 400))))
+    for (w0, h0, w1, h1, ox, oy, rad) in cases:
+        nx, ny, tr = aln.corr_patches_grid(_pair(w0, h0, w1, h1, ox, oy, rad, buf))
+        if tr:   # solved transposed: the grid is in the exchanged frame
+            w0, h0, w1, h1, ox, oy = h0, w0, h1, w1, oy, ox
+        xlo, xhi = max(-(w0 - 1), ox - rad), min(w1 - 1, ox + rad)
+        ylo, yhi = max(-(h0 - 1), oy - rad), min(h1 - 1, oy + rad)
+        if xlo > xhi or ylo > yhi:
+            assert (nx, ny) == (0, 0)
+            continue
+        for n, a0, a1, lo, hi in ((nx, w0, w1, xlo, xhi), (ny, h0, h1, ylo, yhi)):
+            ref = aln.lib().aln_fft_size(a0, a1)
+            assert n & (n - 1) == 0 and n <= max(2, ref), (n, ref)
+            assert n >= max(a0, a1)
+            for m in (-2, -1, 1, 2):
+                for d in (lo, hi):
+                    assert not (-(a0 - 1) <= d + m * n <= a1 - 1), (n, d, m)
+            shrunk += n < ref
+    assert shrunk > 50   # many discs allow a smaller grid

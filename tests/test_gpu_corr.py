@@ -177,6 +177,66 @@ def test_uneven_u16(ctx, orc, seed):
     assert_parity(g, o, f"uneven seed {seed}")
 
 
+def _disc_case(seed):
+    rng = np.random.default_rng(seed)
+    w, h = int(rng.integers(24, 200)), int(rng.integers(24, 200))
+    f = rng.normal(0.0, 1.0, (h + 100, w + 100))
+    for ax in (0, 1):   # a few pixels of correlation length
+        f = (f + np.roll(f, 1, ax) + np.roll(f, 2, ax)) / 3.0
+    tx, ty = (int(v) for v in rng.integers(-30, 31, 2))
+    a = f[50:50 + h, 50:50 + w]
+    b = f[50 + ty:50 + ty + h, 50 + tx:50 + tx + w] + rng.normal(0.0, 0.1, (h, w))
+    a8 = np.clip(np.round(128 + 40 * a), 0, 255).astype(np.uint8)
+    b8 = np.clip(np.round(128 + 40 * b), 0, 255).astype(np.uint8)
+    radius = int(rng.integers(3, 40))
+    # the disc around a point near the truth: some truths lie outside it,
+    # so the best lag sits on the rim
+    ox, oy = -tx + int(rng.integers(-12, 13)), -ty + int(rng.integers(-12, 13))
+    return a8, b8, ox, oy, radius
+
+
+@pytest.mark.parametrize("seed", range(40, 64))
+def test_disc_on_smaller_grid(ctx, orc, seed):
+    """Discs that let CorrPatches transform on a grid smaller than the
+    reference's FFTSize grid: the peak, r and the sub-pixel refinement
+    (whose neighbours outside the disc read 0, by the reference raster's
+    storage rules) equal the oracle's."""
+    import oracle
+    import alignment_projects_gb300 as aln
+    a8, b8, ox, oy, radius = _disc_case(seed)
+    lg_o = oracle.legal(oracle.RGN_MIN, 8, 8, 0)
+    g = ctx.corr_patches(a8, b8, ox, oy, radius, aln_legal(lg_o))
+    A, VA = oracle.image_to_points(a8)
+    B, VB = oracle.image_to_points(b8)
+    o = orc.corr_patches(A, VA, B, VB, ox, oy, radius, lg_o)
+    assert_parity(g, o, f"disc seed {seed}")
+
+
+def test_disc_grids_shrink_and_batch(ctx):
+    """The same disc cases in one batch (several transform grids) give the
+    single-call numbers, and most of them run on a smaller grid."""
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300.native import AlnPair
+    jobs, smaller = [], 0
+    for seed in range(40, 64):
+        a8, b8, ox, oy, radius = _disc_case(seed)
+        jobs.append(dict(a=a8, b=b8, ox=ox, oy=oy, radius=radius,
+                         legal=aln.legal(aln.RGN_MIN, 8, 8, 0)))
+        P = AlnPair()
+        P.a, P.b = aln.image(a8), aln.image(b8)
+        P.ox, P.oy, P.radius = ox, oy, radius
+        nx, ny, tr = aln.corr_patches_grid(P)
+        h, w = a8.shape
+        if tr:
+            w, h = h, w
+        smaller += nx * ny < aln.lib().aln_fft_size(w, w) * aln.lib().aln_fft_size(h, h)
+    assert smaller >= len(jobs) // 2
+    got = ctx.corr_patches_batch(jobs)
+    for j, g in zip(jobs, got):
+        single = ctx.corr_patches(j["a"], j["b"], j["ox"], j["oy"], j["radius"], j["legal"])
+        assert g == single
+
+
 def test_batch_equals_single(ctx):
     """A mixed-size batch gives exactly the per-pair results."""
     import alignment_projects_gb300 as aln
