@@ -820,8 +820,11 @@ __global__ void k_final(PairDev *pairs, ResultDev *res, int nreal_x_is_one, int 
     }
     const int Nx = p.Nx, Ny = p.Ny;
     const int ys0 = (int)(bk / Nx), xs0 = (int)(bk - (long long)ys0 * Nx);
-    const int bigx = xs0 >= Nx - (p.w[0] - 1) ? xs0 - Nx : xs0;
-    const int bigy = ys0 >= Ny - (p.h[0] - 1) ? ys0 - Ny : ys0;
+    // storage index -> lag: the window's non-negative lags are stored at
+    // themselves (<= xhi, yhi), the negative ones above them (x + Nx > xhi
+    // because the grid is wider than the window)
+    const int bigx = xs0 > p.xhi ? xs0 - Nx : xs0;
+    const int bigy = ys0 > p.yhi ? ys0 - Ny : ys0;
     // ParabPeakFFT, 0_GEN/Correlation.cpp:482-517, d = 1, on the reference's
     // FFT-sized raster (nx, ny and the storage indices xs, ys are the
     // reference's, which may be larger than the transform grid).
@@ -1009,6 +1012,8 @@ struct aln_ctx {
     unsigned long long sweep_serial;             // key namespace of each sweep call
     long long chunks;                            // chunks run since the last reset
     long long h2d_copies;                        // staging transfers issued
+    int seg_ns;                                  // CorrPatches column segments:
+                                                 // 0 cost model, -1 off, > 0 forced length
 };
 
 static cudaEvent_t ev_get(aln_ctx *c)
@@ -1461,7 +1466,7 @@ static void need_rows(const PairDev &d, int img, int lo[2], int hi[2])
 }
 
 static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_transpose = false,
-                     const ImgSpec *spec = nullptr)
+                     const ImgSpec *spec = nullptr, bool allow_segment = false)
 {
     if (spec)
         allow_transpose = false;   // the R image keeps the caller's orientation
@@ -1619,6 +1624,41 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
         d.Ny = std::min(d.Ny, ny);
         d.logNx = ilog2(d.Nx);
         d.logNy = ilog2(d.Ny);
+        // Segmented columns (k2_corrseg) where they take fewer FFT
+        // point-passes: 2 nseg + 1 transforms of NS points against 3 of Ny
+        // (cost per transform ~ N (log2 N + 4), loads and exchanges
+        // included); a segment of NS points serves NS - Wy + 1 rows of a.
+        const int pol = ctx ? ctx->seg_ns : 0;
+        if (allow_segment && pol >= 0 && d.Nx / 2 >= 8 && d.Nx / 2 <= 4096) {
+            const int Wy = d.yhi - d.ylo + 1;
+            auto cost = [](int n, int transforms) {
+                return (double)transforms * n * (ilog2(n) + 4);
+            };
+            double best = 0.85 * cost(d.Ny, 3);
+            int bns = 0, bseg = 0;
+            for (int ns = 64; ns <= 2048 && ns < d.Ny; ns *= 2) {
+                if (pol > 0 && ns != pol)
+                    continue;
+                const int B = ns - Wy + 1;
+                if (B < 1)
+                    continue;
+                const int nseg = (d.h[0] + B - 1) / B;
+                if (nseg > 64)
+                    continue;
+                const double c = cost(ns, 2 * nseg + 1);
+                if (pol > 0 || c < best) {
+                    best = c;
+                    bns = ns;
+                    bseg = nseg;
+                }
+            }
+            if (bns) {
+                d.Ny = bns;
+                d.logNy = ilog2(bns);
+                d.nseg = bseg;
+                d.seg_len = (d.h[0] + bseg - 1) / bseg;
+            }
+        }
     }
     if (d.mode != JOB_P2I && !(d.sat_nonly && d.cnt_kind != ALN_CNT_GT))
         for (int i = 0; i < 2; ++i)
@@ -1665,16 +1705,18 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
     return ALN_OK;
 }
 
-extern "C" int aln_corr_patches_grid(const aln_pair *P, int *nx, int *ny, int *transposed)
+extern "C" int aln_corr_patches_grid(const aln_pair *P, int *nx, int *ny, int *nseg,
+                                     int *transposed)
 {
-    if (!P || !nx || !ny || !transposed)
+    if (!P || !nx || !ny || !nseg || !transposed)
         return ALN_ERR_ARG;
     PairPlan pl;
-    if (int rc = plan_pair(nullptr, *P, pl, true))
+    if (int rc = plan_pair(nullptr, *P, pl, true, nullptr, P->b_key == 0))
         return rc;
     const bool empty = pl.d.status == ALN_NO_PEAK;
     *nx = empty ? 0 : pl.d.Nx;
     *ny = empty ? 0 : pl.d.Ny;
+    *nseg = empty ? 0 : pl.d.nseg;
     *transposed = pl.transposed ? 1 : 0;
     return empty ? ALN_NO_PEAK : ALN_OK;
 }
@@ -1807,6 +1849,18 @@ static void launch_fill_cols(aln_ctx *ctx, int nsel, int L, int var)
         launch_fill_cols_rad<NY, corrcol_radix<NY, 0>()>(ctx, nsel, L);
 }
 
+#define ALN_CASES_SEG(X) X(64) X(128) X(256) X(512) X(1024) X(2048)
+
+static int corrseg_radix_of(int ns)
+{
+    switch (ns) {
+#define X(v) case v: return corrseg_radix<v>();
+        ALN_CASES_SEG(X)
+#undef X
+    default: return fft_radix(ns);
+    }
+}
+
 static int corrcol_radix_of(int Ny, int var)
 {
     (void)var;   // every form uses fft_radix (corrcol_radix)
@@ -1834,6 +1888,16 @@ static void launch_corrcol2(aln_ctx *ctx, int n, int L, int cached, int var)
         launch_corrcol_var<NY, 2>(ctx, n, L, cached);
     else
         launch_corrcol_var<NY, 0>(ctx, n, L, cached);
+}
+
+template <int NS>
+static void launch_corrseg(aln_ctx *ctx, int n, int L)
+{
+    constexpr int T = NS / corrseg_radix<NS>(), G = 256 / T;
+    const size_t sm = (size_t)G * (padded(NS) + 2 * NS) * sizeof(float2);
+    smem_attr(ctx->device, (const void *)k2_corrseg<NS>, sm);
+    LAUNCH(ctx, "k2_corrseg", k2_corrseg<NS>, dim3((L + 1 + G - 1) / G, n), 256, sm, ctx->dpairs,
+           ctx->tw);
 }
 
 template <int LL>
@@ -1875,7 +1939,8 @@ static void launch_lagimg2(aln_ctx *ctx, int n, int maxWy, bool both, bool sonly
 // register-FFT pipeline for one chunk: rows (both images), fused columns,
 // lag rows.  L = Nx/2 in [16, 4096], Ny in [16, 8192].
 static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int maxWy,
-                               int mode = JOB_PATCHES, bool both = false, bool sonly = false)
+                               int mode = JOB_PATCHES, bool both = false, bool sonly = false,
+                               bool seg = false)
 {
     switch (L) {
 #define X(v) case v: launch_rowfft2<v>(ctx, n, maxh); break;
@@ -1883,7 +1948,14 @@ static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int
 #undef X
     default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
     }
-    switch (Ny) {
+    if (seg) {
+        switch (Ny) {
+#define X(v) case v: launch_corrseg<v>(ctx, n, L); break;
+            ALN_CASES_SEG(X)
+#undef X
+        default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "segment length %d", Ny);
+        }
+    } else switch (Ny) {
 #define X(v) case v: launch_corrcol2<v>(ctx, n, L, 0, mode == JOB_PATCHES ? 1 : sonly ? 2 : 0); break;
         ALN_CASES_NY(X)
 #undef X
@@ -1921,6 +1993,7 @@ struct ChunkLaunch {
     int maxw, maxh, maxslots, maxWy;
     int sw, sh;                        // largest caller-frame image of transposed jobs
     int Nx, Ny, mode, both, sonly, frame_nx1, frame_ny1;
+    int seg;                           // CorrPatches with segmented columns
     int fill_off, nfill, fill_maxh;    // spectrum-cache fills: sel[fill_off ...]
 };
 
@@ -1992,6 +2065,7 @@ static void prep_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int off, ch
     cl.sonly = hd[0].s_float != 0;
     cl.frame_nx1 = chunk[0]->frame_nx1;
     cl.frame_ny1 = chunk[0]->frame_ny1;
+    cl.seg = hd[0].nseg > 0;
 }
 
 // The chunk's kernels on the compute stream (its job table, fill list and
@@ -2039,7 +2113,7 @@ static int launch_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, const Chun
     }
     if (L >= 8 && L <= 4096 && Ny >= 8 && Ny <= 8192) {
         if (int rc = launch_fft_pipeline(ctx, L, Ny, n, cl.maxh, cl.maxWy, mode, cl.both != 0,
-                                         cl.sonly != 0))
+                                         cl.sonly != 0, cl.seg != 0))
             return rc;
     } else if (mode != JOB_PATCHES) {
         return set_err(ctx, ALN_ERR_UNSUPPORTED, "CorrImages FFT size %d x %d", Nx, Ny);
@@ -2209,8 +2283,33 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
         plans[k].key_ns = keys ? keys[k].ns : 0;
         plans[k].key = keys ? keys[k].key : pairs[k].b_key;
         const ImgSpec *sp = (specs && specs[k].kind != 0) ? &specs[k] : nullptr;
-        if (int rc = plan_pair(ctx, pairs[k], plans[k], sp == nullptr, sp))
+        if (int rc = plan_pair(ctx, pairs[k], plans[k], sp == nullptr, sp,
+                               sp == nullptr && plans[k].key == 0))
             return rc;
+    }
+    // Segmented columns trade parallelism for work: a team runs its column's
+    // segments one after another, so a call with too few columns to fill the
+    // GPU (fewer segment-kernel CTAs than the SMs hold, 2 per SM) is faster
+    // with one transform per column and is planned that way (unless the
+    // context forces a segment length).
+    if (ctx->seg_ns == 0) {
+        long long ctas = 0;
+        bool any = false;
+        for (auto &pl : plans)
+            if (pl.d.status == 0 && pl.d.nseg > 0) {
+                any = true;
+                const int g = 256 / (pl.d.Ny / corrseg_radix_of(pl.d.Ny));
+                ctas += ((pl.d.Nx >> 1) + 1 + g - 1) / g;
+            }
+        if (any) {
+            int sms = 0;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+            if (ctas < 2LL * std::max(sms, 1))
+                for (int k = 0; k < npairs; ++k)
+                    if (plans[k].d.status == 0 && plans[k].d.nseg > 0)
+                        if (int rc = plan_pair(ctx, pairs[k], plans[k], true, nullptr, false))
+                            return rc;
+        }
     }
     // Windows: runs of consecutive jobs (submission order) whose host inputs
     // fit one staging buffer.  A window's host images are copied in one go
@@ -2238,11 +2337,12 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
     std::vector<std::vector<std::vector<PairPlan *>>> wchunks(windows.size());
     size_t max_stage = 0, max_work = 0, max_n = 1;
     for (size_t w = 0; w < windows.size(); ++w) {
-        std::map<std::tuple<int, int, int, int, int, int, int>, std::vector<PairPlan *>> groups;
+        std::map<std::tuple<int, int, int, int, int, int, int, int>, std::vector<PairPlan *>>
+            groups;
         size_t sb = 0;
         for (PairPlan *pl : windows[w]) {
             groups[std::make_tuple(pl->d.Nx, pl->d.Ny, pl->frame_nx1, pl->frame_ny1, pl->d.mode,
-                                   pl->d.want_r, pl->d.want_s)]
+                                   pl->d.want_r, pl->d.want_s, pl->d.nseg > 0)]
                 .push_back(pl);
             sb += pl->in_bytes[0] + pl->in_bytes[1] + 16;
         }
@@ -2806,6 +2906,14 @@ extern "C" long long aln_ctx_counter(aln_ctx *ctx, int which)
     case 7: return ctx->h2d_copies;
     default: return -1;
     }
+}
+
+extern "C" int aln_ctx_set_segmenting(aln_ctx *ctx, int ns)
+{
+    if (!ctx || ns < -1 || (ns > 0 && (ns < 64 || ns > 2048 || (ns & (ns - 1)))))
+        return ctx ? set_err(ctx, ALN_ERR_ARG, "segment length %d", ns) : ALN_ERR_ARG;
+    ctx->seg_ns = ns;
+    return ALN_OK;
 }
 
 extern "C" int aln_ctx_set_spectrum_cache(aln_ctx *ctx, size_t bytes)

@@ -59,6 +59,9 @@ struct PairDev {
     float2 *T[2];       // row-pass output [kx][y], stride Ts[i]
     int Ts[2];
     float2 *X2;         // spectrum of image 1 (b): [kx][ky], stride Ny
+    int nseg, seg_len;  // CorrPatches: the column axis cut into nseg segments
+                        // of seg_len rows of a, each transformed on Ny points
+                        // (k2_corrseg); 0 = one transform of the whole column
     int b_cached;       // 1: X2 holds b's spectrum already (a cache entry);
                         // the row pass skips b and the column pass reads X2
     float2 *Q;          // column-inverse output [kx][j], j = y - ylo, stride Wy

@@ -777,6 +777,96 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
     }
 }
 
+// CorrPatches columns with the long axis cut into segments.  Only the Wy lag
+// rows [ylo, yhi] are read, so for column kx
+//   C[ylo + e] = sum_y conj(A[y]) B[y + ylo + e],   e in [0, Wy),
+// splits over segments of a's rows, y = s*seg_len + j (j < seg_len): segment
+// s pairs a's rows [s*seg_len, +seg_len) with b's rows [s*seg_len + ylo,
+// +seg_len + Wy - 1), and NS >= seg_len + Wy - 1 makes its circular
+// correlation on NS points the linear one at e in [0, Wy).  The segments'
+// spectral products are summed (one accumulator per column) and inverted
+// once: 2 nseg + 1 transforms of NS points instead of 3 of Ny.  Each thread
+// keeps its accumulator and parked a-spectrum points in its own shared-memory
+// slots (no exchange).  Output: Q[kx][e], as k2_corrcol; the column
+// transform length the lag kernel normalises by is NS (p.Ny).
+// Per-thread radix of the segment transforms.  Measured on the montage
+// strips (6 segments of 512 points): radix 8 at 3 CTAs per SM ran 25%
+// faster than radix 16 at 2 (spills, low occupancy); at 1024 and 2048 points
+// radix 16 stays ahead.
+template <int NS>
+__host__ __device__ constexpr int corrseg_radix()
+{
+    return NS == 512 ? 8 : fft_radix(NS);
+}
+
+template <int NS>
+__global__ void __launch_bounds__(256, corrseg_radix<NS>() >= 16 ? 2 : 3)
+k2_corrseg(PairDev *pairs, const float2 *__restrict__ tw)
+{
+    using FF = RegFFT<NS, -1, corrseg_radix<NS>()>;
+    using FI = RegFFT<NS, +1, corrseg_radix<NS>()>;
+    constexpr int R = FF::R, T = FF::T;
+    extern __shared__ float2 smem[];
+    const PairDev &p = pairs[blockIdx.y];
+    if (p.status != 0)
+        return;
+    const int L1 = (p.Nx >> 1) + 1;
+    const int G = blockDim.x / T;
+    const int team = threadIdx.x / T, t = threadIdx.x - team * T;
+    const int kx = blockIdx.x * G + team;
+    if (blockIdx.x * G >= L1)
+        return;
+    const bool live = kx < L1;
+    const int kxc = live ? kx : L1 - 1;   // idle teams compute a copy, store nothing
+    float2 *sm = smem + team * FF::SMEM;
+    float2 *park = smem + G * FF::SMEM + team * (2 * NS);
+    float2 *acc = park + NS;
+    const float2 *Ta = p.T[0] + (long long)kxc * p.Ts[0];
+    const float2 *Tb = p.T[1] + (long long)kxc * p.Ts[1];
+    const int ha = p.h[0], hb = p.h[1];
+    const int B = p.seg_len, nseg = p.nseg, ylo = p.ylo;
+    const int Wy = p.yhi - p.ylo + 1;
+    const int lb = B + Wy - 1;
+    for (int s = 0; s < nseg; ++s) {
+        const int y0 = s * B;
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int j = t + r * T, y = y0 + j;
+            v[r] = (j < B && y < ha) ? Ta[y] : make_float2(0.f, 0.f);
+        }
+        FF::run(v, sm, t, tw);
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            park[r * T + t] = v[r];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int j = t + r * T, y = y0 + ylo + j;
+            v[r] = (j < lb && y >= 0 && y < hb) ? Tb[y] : make_float2(0.f, 0.f);
+        }
+        FF::run(v, sm, t, tw);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const float2 q = cmulc(v[r], park[r * T + t]);   // X2 * conj(X1)
+            acc[r * T + t] = s == 0 ? q : cadd(acc[r * T + t], q);
+        }
+    }
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+        v[r] = acc[r * T + t];
+    FI::run(v, sm, t, tw);
+    if (live) {
+        float2 *Q = p.Q + (long long)kx * Wy;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int e = t + r * T;
+            if (e < Wy)
+                Q[e] = v[r];
+        }
+    }
+}
+
 // Spectrum of image b alone into X2 (a cache entry): per column kx, the
 // column FFT of b's row-pass output, stored as k2_corrcol reads a cached
 // spectrum.  The same RegFFT code as the fused path, so the cached and the

@@ -176,7 +176,9 @@ def lib():
         L.aln_parab_peak_fft.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
                                          C.c_void_p, C.c_int, C.c_int]
         L.aln_corr_patches_grid.argtypes = [C.POINTER(AlnPair), C.POINTER(C.c_int),
-                                            C.POINTER(C.c_int), C.POINTER(C.c_int)]
+                                            C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                            C.POINTER(C.c_int)]
+        L.aln_ctx_set_segmenting.argtypes = [C.c_void_p, C.c_int]
         L.aln_server_create.argtypes = [C.POINTER(AlnServerParams), C.POINTER(C.c_void_p)]
         L.aln_server_destroy.argtypes = [C.c_void_p]
         L.aln_server_submit.argtypes = [C.c_void_p, C.POINTER(AlnRequest),
@@ -286,6 +288,11 @@ class Context:
                 "spec_bytes": self._L.aln_ctx_counter(self.h, 5),
                 "chunks": self._L.aln_ctx_counter(self.h, 6),
                 "h2d_copies": self._L.aln_ctx_counter(self.h, 7)}
+
+    def set_segmenting(self, ns: int):
+        """CorrPatches column segments: 0 cost model, -1 off, or a forced
+        segment transform length (power of two, 64..2048)."""
+        self._check(self._L.aln_ctx_set_segmenting(self.h, ns))
 
     def set_spectrum_cache(self, nbytes: int):
         self._check(self._L.aln_ctx_set_spectrum_cache(self.h, nbytes))
@@ -444,13 +451,15 @@ class Context:
 
 
 def corr_patches_grid(pair: AlnPair):
-    """(nx, ny, transposed) of the transform grid CorrPatches uses for one
-    pair, in the frame the pair is solved in; (0, 0, t) for an empty window."""
-    nx, ny, tr = C.c_int(), C.c_int(), C.c_int()
-    rc = lib().aln_corr_patches_grid(C.byref(pair), C.byref(nx), C.byref(ny), C.byref(tr))
+    """(nx, ny, nseg, transposed) of the transform grid CorrPatches uses for
+    one pair, in the frame the pair is solved in (nseg > 0: the column axis
+    in nseg segments of ny points); (0, 0, 0, t) for an empty window."""
+    nx, ny, ns, tr = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    rc = lib().aln_corr_patches_grid(C.byref(pair), C.byref(nx), C.byref(ny), C.byref(ns),
+                                     C.byref(tr))
     if rc < 0:
         raise AlnError(rc, "aln_corr_patches_grid")
-    return nx.value, ny.value, tr.value
+    return nx.value, ny.value, ns.value, tr.value
 
 
 def parab_peak_fft(xpk, ypk, d, I):

@@ -176,30 +176,41 @@ def fft_shape(w1, h1, w2, h2):
 
 
 def solved_grid(pair):
-    """(w_s, h_s, Nx, Ny) of one AlnPair as the library solves it: the frame
-    (wide pairs transposed) and the transform grid it chooses (the smallest
-    power-of-two grid that keeps the disc's lags free of wrap-around)."""
+    """(w_s, h_s, Nx, Ny, nseg) of one AlnPair as the library solves it: the
+    frame (wide pairs transposed), the transform grid it chooses (the
+    smallest power-of-two grid that keeps the disc's lags free of
+    wrap-around) and the column segments (0: one column transform)."""
     import alignment_projects_gb300 as aln
-    nx, ny, tr = aln.corr_patches_grid(pair)
+    nx, ny, nseg, tr = aln.corr_patches_grid(pair)
     w, h = pair.a.w, pair.a.h
     if tr:
         w, h = h, w
-    return w, h, nx, ny
+    return w, h, nx, ny, nseg
 
 
 def alg_bytes_per_pair(grid, e=1):
-    """Per kernel, for one pair of w x h strips (both the same size here),
-    on the transform grid Nx x Ny the pair is solved on."""
-    w, h, Nx, Ny = grid
-    H = Ny * (Nx // 2 + 1)
-    rows = 2 * (w * h * e + 8 * H)                    # r2c row passes, both images
-    cols = 16 * H + 16 * H + 24 * H + 16 * H          # column passes b, a; product; c2r column pass
+    """Canonical bytes per kernel (one read + one write of the array per 1D
+    pass) for one pair of w x h strips (both the same size here), on the
+    transforms the pair is solved with.  One column transform: the two-pass
+    count on the Nx x Ny grid (H = Ny (Nx/2+1)).  Segmented columns (nseg
+    segments of Ny points): the row pass writes the h rows' spectra, each
+    column makes 2 nseg forward transforms, nseg products and one inverse."""
+    w, h, Nx, Ny, nseg = grid
+    L1 = Nx // 2 + 1
+    H = Ny * L1
     inv_rows = 8 * H + 4 * Nx * Ny                    # c2r row pass
+    if nseg:
+        rows = 2 * (w * h * e + 8 * L1 * h)
+        cols = (2 * nseg * 16 + nseg * 24 + 16) * H
+    else:
+        rows = 2 * (w * h * e + 8 * H)                # r2c row passes, both images
+        cols = 16 * H + 16 * H + 24 * H + 16 * H      # column passes b, a; product; c2r column pass
     return {
         "k_rowfft": rows, "k2_rowfft": rows,
         "k_colfft": 16 * H,
         "k_corrcol": cols - 16 * H,
-        "k2_corrcol": cols,                            # fused: b and a columns in one kernel
+        # fused: b and a columns in one kernel (the segmented form when nseg)
+        "k2_corrseg" if nseg else "k2_corrcol": cols,
         "k_lagrow": inv_rows, "k2_lagrow": inv_rows,
     }
 
@@ -207,13 +218,17 @@ def alg_bytes_per_pair(grid, e=1):
 def dram_model_per_pair(grid, e=1, wy=129):
     """DRAM bytes per pair the fused kernels move (each array read or written
     once): k2_rowfft reads both strips and writes both row spectra T (rows < h
-    only); k2_corrcol reads both T and writes the window rows Q; k2_lagrow
-    reads Q.  k2_corrcol's figure is checked against ncu dram__bytes
-    (profiles/k2_corrcol_montage.md)."""
-    ws, hs, Nx, Ny = grid
+    only); k2_corrcol reads both T and writes the window rows Q (k2_corrseg
+    reads b's rows once per segment, (seg + wy - 1) / seg times over);
+    k2_lagrow reads Q.  k2_corrcol's figure is checked against ncu
+    dram__bytes (profiles/k2_corrcol_montage.md)."""
+    ws, hs, Nx, Ny, nseg = grid
     L1 = Nx // 2 + 1
+    seg = -(-hs // nseg) if nseg else hs
+    over = (seg + wy - 1) / seg if nseg else 1.0
+    cols = (8 * L1 * hs * (1.0 + over) if nseg else 16 * L1 * hs) + 8 * L1 * wy
     return {"k2_rowfft": 2 * ws * hs * e + 16 * L1 * hs,
-            "k2_corrcol": 16 * L1 * hs + 8 * L1 * wy,
+            "k2_corrseg" if nseg else "k2_corrcol": cols,
             "k2_lagrow": 8 * L1 * wy}
 
 
@@ -398,7 +413,7 @@ def run_gpu(args):
     grids = [solved_grid(arr_d[k]) for k in range(n)]
     grid_hist, ref_hist = {}, {}
     for g in grids:
-        key = "%dx%d" % (g[2], g[3])
+        key = "%dx%d" % (g[2], g[3]) + (" in %d segments" % g[4] if g[4] else "")
         grid_hist[key] = grid_hist.get(key, 0) + 1
         rk = "%dx%d" % fft_shape(g[0], g[1], g[0], g[1])
         ref_hist[rk] = ref_hist.get(rk, 0) + 1
@@ -415,7 +430,7 @@ def run_gpu(args):
                   for g in grids) * args.steps / max(1, dom_launches)
     # the FFT passes together (row, column and inverse passes, with the
     # product): counted bytes over the three kernels' summed time
-    fft_k = ("k2_rowfft", "k2_corrcol", "k2_lagrow")
+    fft_k = ("k2_rowfft", "k2_corrcol", "k2_corrseg", "k2_lagrow")
     fft_ms = sum(ours[k][1] for k in fft_k if k in ours)
     fft_bytes = sum(sum(alg_bytes_per_pair(g).get(k, 0) for k in fft_k)
                     for g in grids) * args.steps

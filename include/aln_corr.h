@@ -147,10 +147,20 @@ long long aln_ctx_counter(aln_ctx *ctx, int which);
  * frame) stores b's spectrum in device memory, later jobs read it instead of
  * transforming b again.  Equal keys must mean equal images b (the caller's
  * promise, as in the reference, which reuses fft2 whenever its size
- * matches).  Results are the same numbers with or without the cache.
+ * matches).  Results are the same numbers with or without the cache (a
+ * keyed CorrPatches job always takes one column transform per column, so
+ * the uncached job equal to it bit for bit is the unsegmented one,
+ * aln_ctx_set_segmenting(ctx, -1); a segmented uncached job agrees within
+ * FP32 rounding).
  * `bytes` bounds the device memory the cache holds (default 8 GiB; 0 turns
  * it off and releases it); least recently used entries are evicted. */
 int aln_ctx_set_spectrum_cache(aln_ctx *ctx, size_t bytes);
+
+/* CorrPatches column segmenting for this context: 0 = the cost model
+ * (default), -1 = never (one column transform per column), or a forced
+ * segment transform length (a power of two, 64..2048; used where valid for
+ * the pair's window).  Results agree within FP32 rounding either way. */
+int aln_ctx_set_segmenting(aln_ctx *ctx, int ns);
 
 /* ---- FFT support: 0_GEN/Correlation.h:14-31 ------------------------- */
 
@@ -210,11 +220,19 @@ int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *pairs,
  * counterpart; a planning query).  The correlation at the disc's lags is
  * computed on the smallest power-of-two grid that holds both images and
  * keeps every lag of the disc window free of wrap-around, never larger than
- * the reference's FFTSize grid.  nx, ny are in the frame the pair is solved
- * in: *transposed = 1 when a wide pair is solved with x and y exchanged (as
- * the batch entry points do).  Returns 0, ALN_NO_PEAK when the window is
- * empty (nx = ny = 0), or a negative status. */
-int aln_corr_patches_grid(const aln_pair *pair, int *nx, int *ny, int *transposed);
+ * the reference's FFTSize grid.  When it takes fewer FFT passes, the column
+ * (long) axis is cut into *nseg segments of image a's rows, each correlated
+ * on ny points (ny >= segment rows + window rows - 1) and summed in the
+ * spectral domain; *nseg = 0 means one column transform of ny points.  A
+ * pair with a spectrum-cache key (b_key) is never segmented.  nx, ny are in
+ * the frame the pair is solved in: *transposed = 1 when a wide pair is
+ * solved with x and y exchanged (as the batch entry points do).  Reports
+ * the cost-model choice for a call with enough columns to fill the GPU (a
+ * call whose segmented columns would not fill it -- a single pair, say --
+ * runs them unsegmented; aln_ctx_set_segmenting overrides the choice per
+ * context).  Returns 0, ALN_NO_PEAK when the window is empty (nx = ny = 0),
+ * or a negative status. */
+int aln_corr_patches_grid(const aln_pair *pair, int *nx, int *ny, int *nseg, int *transposed);
 
 /* CorrPatchToImage, 0_GEN/Correlation.cpp:1186-1355: the patch's points
  * (xy1[2i], xy1[2i+1], truncated to pixels) against a caller-embedded

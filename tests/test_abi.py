@@ -90,7 +90,7 @@ def test_corr_patches_grid_keeps_disc_lags_alias_free():
     import alignment_projects_gb300 as aln
     buf = np.zeros(4096 * 4096, np.uint8)
     rng = np.random.default_rng(5)
-    shrunk = 0
+    shrunk = segmented = 0
     cases = [(256, 2048, 256, 2048, 0, 0, 64), (200, 2048, 200, 2048, 0, 0, 64),
              (512, 512, 512, 512, 0, 0, 4096), (300, 120, 280, 100, 0, 0, 30),
              (64, 64, 64, 64, 40, -40, 10), (1, 1, 1, 1, 0, 0, 5)]
@@ -99,7 +99,7 @@ def test_corr_patches_grid_keeps_disc_lags_alias_free():
         ox, oy = (int(v) for v in rng.integers(-300, 300, 2))
         cases.append((w0, h0, w1, h1, ox, oy, int(rng.integers(0, 400))))
     for (w0, h0, w1, h1, ox, oy, rad) in cases:
-        nx, ny, tr = aln.corr_patches_grid(_pair(w0, h0, w1, h1, ox, oy, rad, buf))
+        nx, ny, nseg, tr = aln.corr_patches_grid(_pair(w0, h0, w1, h1, ox, oy, rad, buf))
         if tr:   # solved transposed: the grid is in the exchanged frame
             w0, h0, w1, h1, ox, oy = h0, w0, h1, w1, oy, ox
         xlo, xhi = max(-(w0 - 1), ox - rad), min(w1 - 1, ox + rad)
@@ -107,7 +107,16 @@ def test_corr_patches_grid_keeps_disc_lags_alias_free():
         if xlo > xhi or ylo > yhi:
             assert (nx, ny) == (0, 0)
             continue
-        for n, a0, a1, lo, hi in ((nx, w0, w1, xlo, xhi), (ny, h0, h1, ylo, yhi)):
+        if nseg:
+            # segmented columns: each segment of a's rows plus the window's
+            # rows fits one transform, and the segments cover a's rows
+            wy = yhi - ylo + 1
+            seg_len = -(-h0 // nseg)
+            assert ny & (ny - 1) == 0 and ny < aln.lib().aln_fft_size(h0, h1)
+            assert seg_len + wy - 1 <= ny and nseg * seg_len >= h0
+            segmented += 1
+        for n, a0, a1, lo, hi in ((nx, w0, w1, xlo, xhi),) + (
+                () if nseg else ((ny, h0, h1, ylo, yhi),)):
             ref = aln.lib().aln_fft_size(a0, a1)
             assert n & (n - 1) == 0 and n <= max(2, ref), (n, ref)
             assert n >= max(a0, a1)
@@ -116,3 +125,6 @@ def test_corr_patches_grid_keeps_disc_lags_alias_free():
                     assert not (-(a0 - 1) <= d + m * n <= a1 - 1), (n, d, m)
             shrunk += n < ref
     assert shrunk > 50   # many discs allow a smaller grid
+    assert segmented > 10
+    # the montage strips (W x 2048, disc radius 64) are segmented
+    assert aln.corr_patches_grid(_pair(200, 2048, 200, 2048, 0, 0, 64, buf))[2] > 0

@@ -225,7 +225,7 @@ def test_disc_grids_shrink_and_batch(ctx):
         P = AlnPair()
         P.a, P.b = aln.image(a8), aln.image(b8)
         P.ox, P.oy, P.radius = ox, oy, radius
-        nx, ny, tr = aln.corr_patches_grid(P)
+        nx, ny, nseg, tr = aln.corr_patches_grid(P)
         h, w = a8.shape
         if tr:
             w, h = h, w
@@ -235,6 +235,35 @@ def test_disc_grids_shrink_and_batch(ctx):
     for j, g in zip(jobs, got):
         single = ctx.corr_patches(j["a"], j["b"], j["ox"], j["oy"], j["radius"], j["legal"])
         assert g == single
+
+
+@pytest.mark.parametrize("ns", [-1, 0, 256, 512, 1024, 2048])
+def test_segmented_columns(ctx, orc, ns):
+    """CorrPatches with the column axis cut into segments of every forced
+    length, by the cost model, and not at all: each form matches the oracle
+    on montage strips (disc radius 64) and on small disc cases."""
+    import oracle
+    from alignment_projects_gb300 import synth
+    jobs, refs = [], []
+    for seed in (11, 12):
+        p = synth.montage_pair(seed)
+        lg_o = oracle.legal(oracle.RGN_SECTION, 1500, 1500, 30000)
+        jobs.append(dict(a=p.a, b=p.b, ox=p.ox, oy=p.oy, radius=p.radius, legal=aln_legal(lg_o)))
+        refs.append(_oracle_pair(orc, p, lg_o))
+    for seed in range(40, 48):
+        a8, b8, ox, oy, radius = _disc_case(seed)
+        lg_o = oracle.legal(oracle.RGN_MIN, 8, 8, 0)
+        jobs.append(dict(a=a8, b=b8, ox=ox, oy=oy, radius=radius, legal=aln_legal(lg_o)))
+        A, VA = oracle.image_to_points(a8)
+        B, VB = oracle.image_to_points(b8)
+        refs.append(orc.corr_patches(A, VA, B, VB, ox, oy, radius, lg_o))
+    ctx.set_segmenting(ns)
+    try:
+        got = ctx.corr_patches_batch(jobs)
+    finally:
+        ctx.set_segmenting(0)
+    for k, (g, o) in enumerate(zip(got, refs)):
+        assert_parity(g, o, f"segments {ns} job {k}")
 
 
 def test_batch_equals_single(ctx):
@@ -328,7 +357,13 @@ def test_spectrum_cache_same_numbers(ctx):
     w = synth.montage_pair(21)
     pairs.append(dict(a=w.a, b=w.b, ox=w.ox, oy=w.oy, radius=w.radius,
                       legal=aln.legal(aln.RGN_SECTION, 1500, 1500, 30000)))
-    plain = ctx.corr_patches_batch(pairs)
+    # keyed jobs take one column transform per column: compare with the
+    # unsegmented uncached form
+    ctx.set_segmenting(-1)
+    try:
+        plain = ctx.corr_patches_batch(pairs)
+    finally:
+        ctx.set_segmenting(0)
     ctx.profile_reset()
     keyed = [dict(p, b_key=(99 if k < 6 else 100)) for k, p in enumerate(pairs)]
     first = ctx.corr_patches_batch(keyed)

@@ -114,7 +114,13 @@ def test_max_batch_and_spectrum_keys():
         tks = [srv.submit_patches(a, b, lg=lg, radius=30, b_key=1234) for a in a_s]
         keyed = [srv.wait(t) for t in tks]
         assert all(r["batch_size"] <= 4 for r in keyed)
-        assert [strip(r) for r in keyed] == [strip(r) for r in plain]
+        # keyed jobs take one column transform per column, an unkeyed one may
+        # be segmented: the same peaks, values within FP32 rounding
+        for k, p in zip(keyed, plain):
+            assert (k["peak_x"], k["peak_y"], k["status"]) == (p["peak_x"], p["peak_y"],
+                                                               p["status"])
+            assert abs(k["r"] - p["r"]) <= 1e-6
+            assert abs(k["dx"] - p["dx"]) <= 1e-4 and abs(k["dy"] - p["dy"]) <= 1e-4
         assert srv.counters()["spec_hits"] >= 8
     finally:
         srv.close()
