@@ -35,21 +35,23 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-SHIM_SRC = os.path.join(PKG, "shim", "aln_correlation_shim.cpp")
-SHIM_HDR = os.path.join(PKG, "shim", "aln_correlation.hpp")
+SHIM_SRCS = [os.path.join(PKG, "shim", s)
+             for s in ("aln_correlation_shim.cpp", "aln_thmscan_shim.cpp")]
+SHIM_HDRS = [os.path.join(PKG, "shim", h)
+             for h in ("aln_correlation.hpp", "aln_thmscan.hpp", "aln_shim_util.hpp")]
 SHIM_LIB = os.path.join(LIBDIR, "libaln_corr_shim.so")
 
 
 def build_shim(force: bool = False, verbose: bool = False) -> str:
-    """The C++ drop-in for the Correlation.h entry points (g++), linked
+    """The C++ drop-in for the Correlation.h entry points and class CThmScan (g++), linked
     against libaln_corr.so in the same directory."""
     lib = build(force=force, verbose=verbose)
-    deps = [SHIM_SRC, SHIM_HDR, os.path.join(ROOT, "include", "aln_corr.h"), lib]
+    deps = SHIM_SRCS + SHIM_HDRS + [os.path.join(ROOT, "include", "aln_corr.h"), lib]
     if not force and not _stale(SHIM_LIB, deps):
         return SHIM_LIB
     tmp = SHIM_LIB + ".tmp%d" % os.getpid()
     cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off",
-           "-shared", "-o", tmp, SHIM_SRC, "-L" + LIBDIR, "-laln_corr",
+           "-shared", "-o", tmp] + SHIM_SRCS + ["-L" + LIBDIR, "-laln_corr",
            "-Wl,-rpath,$ORIGIN"]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)

@@ -1014,6 +1014,7 @@ struct aln_ctx {
     long long h2d_copies;                        // staging transfers issued
     int seg_ns;                                  // CorrPatches column segments:
                                                  // 0 cost model, -1 off, > 0 forced length
+    int sms;                                     // SM count (0: not queried yet)
 };
 
 static cudaEvent_t ev_get(aln_ctx *c)
@@ -1851,16 +1852,6 @@ static void launch_fill_cols(aln_ctx *ctx, int nsel, int L, int var)
 
 #define ALN_CASES_SEG(X) X(64) X(128) X(256) X(512) X(1024) X(2048)
 
-static int corrseg_radix_of(int ns)
-{
-    switch (ns) {
-#define X(v) case v: return corrseg_radix<v>();
-        ALN_CASES_SEG(X)
-#undef X
-    default: return fft_radix(ns);
-    }
-}
-
 static int corrcol_radix_of(int Ny, int var)
 {
     (void)var;   // every form uses fft_radix (corrcol_radix)
@@ -1890,14 +1881,26 @@ static void launch_corrcol2(aln_ctx *ctx, int n, int L, int cached, int var)
         launch_corrcol_var<NY, 0>(ctx, n, L, cached);
 }
 
+// A team runs its column's segments one after another, so a call with few
+// columns (a single pair, say) gets fewer teams per CTA to spread them over
+// more SMs: the largest G (teams per CTA) that still gives 2 CTAs per SM,
+// down to 1.  Each column's arithmetic is the same whatever G is.
 template <int NS>
 static void launch_corrseg(aln_ctx *ctx, int n, int L)
 {
-    constexpr int T = NS / corrseg_radix<NS>(), G = 256 / T;
+    constexpr int T = NS / corrseg_radix<NS>(), GMAX = 256 / T;
+    if (!ctx->sms) {
+        cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        ctx->sms = std::max(ctx->sms, 1);
+    }
+    int G = GMAX;
+    while (G > 1 && (long long)((L + 1 + G - 1) / G) * n < 2LL * ctx->sms)
+        G /= 2;
     const size_t sm = (size_t)G * (padded(NS) + 2 * NS) * sizeof(float2);
-    smem_attr(ctx->device, (const void *)k2_corrseg<NS>, sm);
-    LAUNCH(ctx, "k2_corrseg", k2_corrseg<NS>, dim3((L + 1 + G - 1) / G, n), 256, sm, ctx->dpairs,
-           ctx->tw);
+    smem_attr(ctx->device, (const void *)k2_corrseg<NS>,
+              (size_t)GMAX * (padded(NS) + 2 * NS) * sizeof(float2));
+    LAUNCH(ctx, "k2_corrseg", k2_corrseg<NS>, dim3((L + 1 + G - 1) / G, n), G * T, sm,
+           ctx->dpairs, ctx->tw);
 }
 
 template <int LL>
@@ -2286,30 +2289,6 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
         if (int rc = plan_pair(ctx, pairs[k], plans[k], sp == nullptr, sp,
                                sp == nullptr && plans[k].key == 0))
             return rc;
-    }
-    // Segmented columns trade parallelism for work: a team runs its column's
-    // segments one after another, so a call with too few columns to fill the
-    // GPU (fewer segment-kernel CTAs than the SMs hold, 2 per SM) is faster
-    // with one transform per column and is planned that way (unless the
-    // context forces a segment length).
-    if (ctx->seg_ns == 0) {
-        long long ctas = 0;
-        bool any = false;
-        for (auto &pl : plans)
-            if (pl.d.status == 0 && pl.d.nseg > 0) {
-                any = true;
-                const int g = 256 / (pl.d.Ny / corrseg_radix_of(pl.d.Ny));
-                ctas += ((pl.d.Nx >> 1) + 1 + g - 1) / g;
-            }
-        if (any) {
-            int sms = 0;
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-            if (ctas < 2LL * std::max(sms, 1))
-                for (int k = 0; k < npairs; ++k)
-                    if (plans[k].d.status == 0 && plans[k].d.nseg > 0)
-                        if (int rc = plan_pair(ctx, pairs[k], plans[k], true, nullptr, false))
-                            return rc;
-        }
     }
     // Windows: runs of consecutive jobs (submission order) whose host inputs
     // fit one staging buffer.  A window's host images are copied in one go

@@ -358,6 +358,9 @@ static int eval_batch(SweepCtx &S, std::vector<Eval> &ev)
             specs[k].oy = tp.own_disc ? tp.doy : S.P.oy;
             specs[k].rx = tp.own_disc ? tp.drx : S.P.rx;
             specs[k].ry = tp.own_disc ? tp.dry : S.P.ry;
+            if (S.P.disc_of_angle)   // newAngProc wins over SetDisc (CThmScan.cpp:350-356)
+                S.P.disc_of_angle(S.P.disc_user, E.deg, &specs[k].ox, &specs[k].oy,
+                                  &specs[k].rx, &specs[k].ry);
         }
         CK(cudaMemcpyAsync(S.djobs, jobs.data(), n * sizeof(SplatJob), cudaMemcpyHostToDevice,
                            ctx->stream));
@@ -894,6 +897,179 @@ extern "C" int aln_thm_finish_batch(aln_ctx *ctx, int npairs, const aln_thumbs *
         out[k].ncalls = tp.ncalls;
         if (out_tptwk)
             memcpy(out_tptwk + 6 * (size_t)k, tp.Tptwk, sizeof tp.Tptwk);
+    }
+    return ALN_OK;
+}
+
+// One CThmScan member-function call per pair from the caller's object
+// state (best record, err, pretweak transform); see aln_thm_call_batch in
+// the header for the ops and their arguments.
+extern "C" int aln_thm_call_batch(aln_ctx *ctx, int npairs, const aln_thumbs *thumbs,
+                                  const aln_thm_params *params, int op, const double *args,
+                                  aln_thm_result *best, double *tptwk, double *ret)
+{
+    if (!ctx || npairs < 0 || (npairs && (!thumbs || !params || !args || !best)))
+        return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
+    if (op < ALN_THMOP_RFROMANGLE || op > ALN_THMOP_FULLRES)
+        return set_err(ctx, ALN_ERR_ARG, "bad CThmScan op %d", op);
+    const bool shared = op >= ALN_THMOP_SCAN_MAXR && op <= ALN_THMOP_DENOVO;
+    for (int k = 1; shared && k < npairs; ++k)
+        for (int j = 1; j < 4; ++j)
+            if (args[4 * k + j] != args[j])
+                return set_err(ctx, ALN_ERR_ARG, "op %d: a1..a3 differ between pairs", op);
+    aln_thm_params P = *params;
+    if (op == ALN_THMOP_POSTTWEAKS || op == ALN_THMOP_FULLRES)
+        P.usecorrr = 1;   // SetUseCorrR(true)
+    SweepCtx S;
+    char *dbuf = nullptr;
+    int rc = sweep_setup(ctx, S, npairs, thumbs, &P, &dbuf);
+    std::vector<int> all(npairs);
+    std::vector<double> a0(npairs), rv(npairs, 0.0);
+    std::vector<ThmRec> b0(npairs);
+    for (int k = 0; k < npairs && rc == ALN_OK; ++k) {
+        ThmPair &tp = S.pairs[k];
+        all[k] = k;
+        a0[k] = args[4 * k];
+        tp.best.A = best[k].A;
+        tp.best.X = best[k].X;
+        tp.best.Y = best[k].Y;
+        tp.best.R = best[k].R;
+        memcpy(tp.best.T, best[k].T, sizeof tp.best.T);
+        tp.err = best[k].err;
+        if (tptwk)
+            memcpy(tp.Tptwk, tptwk + 6 * (size_t)k, sizeof tp.Tptwk);
+        if (op == ALN_THMOP_POSTTWEAKS || op == ALN_THMOP_FULLRES) {
+            tp.own_disc = 1;   // SetDisc((int)best.X, (int)best.Y, r, r)
+            tp.dox = (int)tp.best.X;
+            tp.doy = (int)tp.best.Y;
+            tp.drx = tp.dry = op == ALN_THMOP_POSTTWEAKS ? 40 : 80;
+        }
+        b0[k] = tp.best;
+    }
+    const double a1 = npairs ? args[1] : 0.0, a2 = npairs ? args[2] : 0.0,
+                 a3 = npairs ? args[3] : 0.0;
+    auto rvals = [&](const std::vector<int> &ids) {
+        for (int id : ids)
+            rv[id] = S.pairs[id].best.R;
+    };
+    // ids still passing a stage of a `||` chain (the rest fail with err)
+    auto passing = [&](const std::vector<int> &ids, int err) {
+        std::vector<int> keep;
+        for (int id : ids)
+            if (S.pairs[id].best.R < S.P.rthresh) {
+                S.pairs[id].err = err;
+                rv[id] = 0.0;
+            } else {
+                keep.push_back(id);
+                rv[id] = 1.0;
+            }
+        return keep;
+    };
+    if (rc == ALN_OK && npairs) {
+        switch (op) {
+        case ALN_THMOP_RFROMANGLE: {
+            std::vector<Eval> ev;
+            for (int k = 0; k < npairs; ++k)
+                ev.push_back(Eval{k, a0[k], -1, &S.pairs[k].best});
+            rc = eval_batch(S, ev);
+            break;
+        }
+        case ALN_THMOP_SCAN_MAXR:
+            rc = scan_sel(S, all, a0, a1, a2, a3 != 0.0, false);
+            rvals(all);
+            break;
+        case ALN_THMOP_SCAN_CONSTXY:
+            rc = scan_sel(S, all, a0, a1, a2, false, true);
+            rvals(all);
+            break;
+        case ALN_THMOP_SCAN_SEL:
+            rc = scan_sel(S, all, a0, a1, a2, a3 != 0.0, S.P.constxy != 0);
+            rvals(all);
+            break;
+        case ALN_THMOP_SCAN_TWEAKS:
+            rc = scan_with_tweaks(S, all, a0, a1, a2);
+            rvals(all);
+            break;
+        case ALN_THMOP_PEAKHUNT:
+            rc = peak_hunt(S, all, a1);
+            rvals(all);
+            break;
+        case ALN_THMOP_PRIOR: {
+            // UsePriorAngles (CThmScan.cpp:734-758)
+            rc = scan_with_tweaks(S, all, a0, a1, 0.1);
+            std::vector<int> ids = passing(all, 2);
+            if (rc == ALN_OK && !ids.empty())
+                rc = peak_hunt(S, ids, 0.1 * 1.5);
+            passing(ids, 2);
+            break;
+        }
+        case ALN_THMOP_DENOVO: {
+            // DenovoBestAngle (CThmScan.cpp:764-790)
+            rc = scan_with_tweaks(S, all, a0, a1, a2);
+            std::vector<int> ids = passing(all, 1);
+            if (rc == ALN_OK && !ids.empty()) {
+                std::vector<double> cen;
+                for (int id : ids)
+                    cen.push_back(S.pairs[id].best.A);
+                rc = scan_sel(S, ids, cen, a2 * 2.0, a2 * 0.05, false, S.P.constxy != 0);
+            }
+            ids = passing(ids, 1);
+            if (rc == ALN_OK && !ids.empty())
+                rc = peak_hunt(S, ids, a2 * 0.05 * 1.5);
+            passing(ids, 1);
+            break;
+        }
+        case ALN_THMOP_PRETWEAKS:
+            for (int k = 0; k < npairs && rc == ALN_OK; ++k) {
+                bool changed = false;
+                rc = pretweaks(S, k, a0[k], args[4 * k + 1], &changed);
+                rv[k] = changed ? 1.0 : 0.0;
+            }
+            break;
+        case ALN_THMOP_POSTTWEAKS:
+        case ALN_THMOP_FULLRES: {
+            if (op == ALN_THMOP_POSTTWEAKS)
+                for (int k = 0; k < npairs && rc == ALN_OK; ++k) {
+                    bool changed = false;
+                    rc = pretweaks(S, k, S.pairs[k].best.R, S.pairs[k].best.A, &changed);
+                }
+            std::vector<Eval> ev;
+            for (int k = 0; k < npairs; ++k)
+                ev.push_back(Eval{k, S.pairs[k].best.A, -1, &S.pairs[k].best});
+            if (rc == ALN_OK)
+                rc = eval_batch(S, ev);
+            if (rc == ALN_OK && op == ALN_THMOP_FULLRES)
+                for (int k = 0; k < npairs; ++k) {
+                    ThmRec &b = S.pairs[k].best;
+                    if (fabs(b.X - b0[k].X) <= 20 && fabs(b.Y - b0[k].Y) <= 20)
+                        b.R = b0[k].R;
+                    else
+                        b = b0[k];
+                }
+            break;
+        }
+        }
+    }
+    cudaStreamSynchronize(ctx->stream);
+    spec_drop(ctx, 1, S.key_base, S.key_base + (unsigned long long)npairs + 1);
+    cudaFree(S.arena);
+    cudaFree(S.djobs);
+    cudaFree(dbuf);
+    if (rc != ALN_OK)
+        return rc;
+    for (int k = 0; k < npairs; ++k) {
+        const ThmPair &tp = S.pairs[k];
+        best[k].A = tp.best.A;
+        best[k].X = tp.best.X;
+        best[k].Y = tp.best.Y;
+        best[k].R = tp.best.R;
+        memcpy(best[k].T, tp.best.T, sizeof best[k].T);
+        best[k].err = tp.err;
+        best[k].ncalls = tp.ncalls;
+        if (tptwk)
+            memcpy(tptwk + 6 * (size_t)k, tp.Tptwk, sizeof tp.Tptwk);
+        if (ret)
+            ret[k] = rv[k];
     }
     return ALN_OK;
 }

@@ -64,10 +64,15 @@ class AlnThumbs(C.Structure):
                 ("req_area", C.c_longlong), ("olap1d", C.c_int), ("b_key", C.c_ulonglong)]
 
 
+DISC_OF_ANGLE = C.CFUNCTYPE(None, C.c_void_p, C.c_double, C.POINTER(C.c_int),
+                            C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int))
+
+
 class AlnThmParams(C.Structure):
     _fields_ = [("rthresh", C.c_double), ("nbmaxht", C.c_double), ("constxy", C.c_int),
                 ("pretweak", C.c_int), ("usecorrr", C.c_int), ("ox", C.c_int), ("oy", C.c_int),
-                ("rx", C.c_int), ("ry", C.c_int), ("tdfm", C.c_double * 6)]
+                ("rx", C.c_int), ("ry", C.c_int), ("tdfm", C.c_double * 6),
+                ("disc_of_angle", DISC_OF_ANGLE), ("disc_user", C.c_void_p)]
 
 
 class AlnThmResult(C.Structure):
@@ -175,6 +180,9 @@ def lib():
         L.aln_ctx_set_spectrum_cache.argtypes = [C.c_void_p, C.c_size_t]
         L.aln_parab_peak_fft.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
                                          C.c_void_p, C.c_int, C.c_int]
+        L.aln_thm_call_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnThumbs),
+                                         C.POINTER(AlnThmParams), C.c_int, C.c_void_p,
+                                         C.POINTER(AlnThmResult), C.c_void_p, C.c_void_p]
         L.aln_corr_patches_grid.argtypes = [C.POINTER(AlnPair), C.POINTER(C.c_int),
                                             C.POINTER(C.c_int), C.POINTER(C.c_int),
                                             C.POINTER(C.c_int)]
@@ -425,6 +433,35 @@ class Context:
         return [{"A": o.A, "X": o.X, "Y": o.Y, "R": o.R, "err": o.err, "ncalls": o.ncalls,
                  "T": list(o.T), "tptwk": tout[k].tolist()} for k, o in enumerate(out)]
 
+    def thm_call_batch(self, thumbs, op, args, best=None, tptwk=None, **params) -> list:
+        """One CThmScan member-function call per pair (THMOP_*; args: 4 per
+        pair, see aln_thm_call_batch), from the object state best (dicts
+        with A, X, Y, R[, T, err]) and tptwk (6 per pair)."""
+        thumbs = list(thumbs)
+        n = len(thumbs)
+        arr = (AlnThumbs * n)()
+        res = (AlnThmResult * n)()
+        for k, t in enumerate(thumbs):
+            arr[k] = t
+            b = best[k] if best is not None else {}
+            res[k].A, res[k].X = b.get("A", -999.0), b.get("X", -999.0)
+            res[k].Y, res[k].R = b.get("Y", -999.0), b.get("R", -999.0)
+            for i, v in enumerate(b.get("T", (1, 0, 0, 0, 1, 0))):
+                res[k].T[i] = v
+            res[k].err = b.get("err", 0)
+        a = np.zeros((n, 4), np.float64)
+        a[:] = np.asarray(args, np.float64).reshape(-1, 4)
+        tw = np.tile(np.array([1, 0, 0, 0, 1, 0], np.float64), (n, 1))
+        if tptwk is not None:
+            tw[:] = np.asarray(tptwk, np.float64).reshape(n, 6)
+        ret = np.zeros(n, np.float64)
+        P = _thm_params(**params)
+        self._check(self._L.aln_thm_call_batch(self.h, n, arr, C.byref(P), op, a.ctypes.data,
+                                               res, tw.ctypes.data, ret.ctypes.data))
+        return [{"A": o.A, "X": o.X, "Y": o.Y, "R": o.R, "err": o.err, "ncalls": o.ncalls,
+                 "T": list(o.T), "tptwk": tw[k].tolist(), "ret": float(ret[k])}
+                for k, o in enumerate(res)]
+
     def corr_patches_batch(self, pairs) -> list:
         """pairs: iterable of dicts with a, b, [ox, oy, radius, legal, a_origin, b_origin,
         b_key (spectrum-cache key of b, 0 = none)]."""
@@ -470,14 +507,27 @@ def parab_peak_fft(xpk, ypk, d, I):
 
 
 def _thm_params(rthresh=0.3, nbmaxht=0.75, pretweak=0, constxy=1, usecorrr=1,
-                disc=(0, 0, -1, -1), tdfm=None) -> AlnThmParams:
+                disc=(0, 0, -1, -1), tdfm=None, disc_of_angle=None) -> AlnThmParams:
+    """disc_of_angle: None, or a Python function deg -> (ox, oy, rx, ry)
+    (CThmScan's newAngProc); the returned params keep its C callback alive."""
     P = AlnThmParams()
     P.rthresh, P.nbmaxht = rthresh, nbmaxht
     P.constxy, P.pretweak, P.usecorrr = constxy, pretweak, usecorrr
     P.ox, P.oy, P.rx, P.ry = disc
     for i, v in enumerate(tdfm if tdfm is not None else (1, 0, 0, 0, 1, 0)):
         P.tdfm[i] = v
+    if disc_of_angle is not None:
+        def tramp(user, deg, ox, oy, rx, ry):
+            ox[0], oy[0], rx[0], ry[0] = (int(v) for v in disc_of_angle(deg))
+        P._cb = DISC_OF_ANGLE(tramp)
+        P.disc_of_angle = P._cb
     return P
+
+
+# CThmScan member functions for aln_thm_call_batch
+(THMOP_RFROMANGLE, THMOP_SCAN_MAXR, THMOP_SCAN_CONSTXY, THMOP_SCAN_SEL, THMOP_SCAN_TWEAKS,
+ THMOP_PEAKHUNT, THMOP_PRIOR, THMOP_DENOVO, THMOP_PRETWEAKS, THMOP_POSTTWEAKS,
+ THMOP_FULLRES) = range(11)
 
 
 def _reply_dict(rep: AlnReply, kind: int) -> dict:

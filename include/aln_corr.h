@@ -226,12 +226,11 @@ int aln_corr_patches_batch(aln_ctx *ctx, int npairs, const aln_pair *pairs,
  * spectral domain; *nseg = 0 means one column transform of ny points.  A
  * pair with a spectrum-cache key (b_key) is never segmented.  nx, ny are in
  * the frame the pair is solved in: *transposed = 1 when a wide pair is
- * solved with x and y exchanged (as the batch entry points do).  Reports
- * the cost-model choice for a call with enough columns to fill the GPU (a
- * call whose segmented columns would not fill it -- a single pair, say --
- * runs them unsegmented; aln_ctx_set_segmenting overrides the choice per
- * context).  Returns 0, ALN_NO_PEAK when the window is empty (nx = ny = 0),
- * or a negative status. */
+ * solved with x and y exchanged (as the batch entry points do).  The choice
+ * depends on the pair alone (not on the batch it comes in: a pair gives the
+ * same numbers alone and in any batch); aln_ctx_set_segmenting overrides it
+ * per context.  Returns 0, ALN_NO_PEAK when the window is empty
+ * (nx = ny = 0), or a negative status. */
 int aln_corr_patches_grid(const aln_pair *pair, int *nx, int *ny, int *nseg, int *transposed);
 
 /* CorrPatchToImage, 0_GEN/Correlation.cpp:1186-1355: the patch's points
@@ -301,6 +300,11 @@ typedef struct aln_thm_params {
     int constxy, pretweak, usecorrr;   /* usecorrr: CorrImagesS (1) or CorrImagesF (0) */
     int ox, oy, rx, ry;                /* SetDisc */
     double tdfm[6];                    /* SetTdfm (TAffine t[0..5]) */
+    /* SetNewAngProc (T_NewAngProc, CThmScan.h:46-51): when set, called on
+     * the host for every correlator call's angle (deg) to give its disc,
+     * in place of ox, oy, rx, ry (NULL: the fixed disc) */
+    void (*disc_of_angle)(void *user, double deg, int *ox, int *oy, int *rx, int *ry);
+    void *disc_user;
 } aln_thm_params;
 
 /* CorRec (0_GEN/CThmScan.h:36-44) plus the search's err and call count. */
@@ -338,6 +342,49 @@ int aln_thm_search_batch(aln_ctx *ctx, int npairs, const aln_thumbs *thumbs,
 int aln_thm_finish_batch(aln_ctx *ctx, int npairs, const aln_thumbs *thumbs,
                          const aln_thm_params *params, int mode, const aln_thm_result *prior,
                          const double *prior_tptwk, aln_thm_result *out, double *out_tptwk);
+
+/* One CThmScan member-function call per pair (0_GEN/CThmScan.cpp:205-842),
+ * from and to the object's state: best[k] is the CorRec the member function
+ * takes by reference (A, X, Y, R, T in and out; err is the object's err,
+ * set only where the member function sets it; ncalls counts this call's
+ * correlator calls) and tptwk[6k..6k+5] the object's pretweak transform
+ * (TAffine t[0..5], in and out; NULL: identity, not returned).  All pairs
+ * run together: each stage's correlator calls over all pairs are one GPU
+ * batch.  op and args[4k..4k+3] = (a0, a1, a2, a3) of pair k:
+ *   ALN_THMOP_RFROMANGLE    RFromAngle(best, deg = a0)
+ *   ALN_THMOP_SCAN_MAXR     AngleScanMaxR(best, center = a0, hlfwid = a1, step = a2,
+ *                           favorCenter = a3 != 0)
+ *   ALN_THMOP_SCAN_CONSTXY  AngleScanConstXY(best, a0, a1, a2)
+ *   ALN_THMOP_SCAN_SEL      AngleScanSel(best, a0, a1, a2, a3 != 0)
+ *   ALN_THMOP_SCAN_TWEAKS   AngleScanWithTweaks(best, a0, a1, a2)
+ *   ALN_THMOP_PEAKHUNT      PeakHunt(best, hlfwid = a1)
+ *   ALN_THMOP_PRIOR         UsePriorAngles(best, ang0 = a0, hfangpr = a1)
+ *   ALN_THMOP_DENOVO        DenovoBestAngle(best, ang0 = a0, hfangdn = a1, step = a2)
+ *   ALN_THMOP_PRETWEAKS     Pretweaks(bestR = a0, deg = a1) (best untouched)
+ *   ALN_THMOP_POSTTWEAKS    PostTweaks(best)
+ *   ALN_THMOP_FULLRES       FinishAtFullRes(best)
+ * a1..a3 must be equal for every pair of a scan or hunt call.  ret[k]
+ * (may be NULL) receives the member function's return value: R for the
+ * scans and PeakHunt, 1 / 0 for the bool ones, 0 for the void ones.
+ * PostTweaks and FinishAtFullRes also set the object's useCorrR and disc
+ * (SetDisc((int)X, (int)Y, 40 or 80, ...)): the caller applies those to its
+ * settings for later calls. */
+enum {
+    ALN_THMOP_RFROMANGLE = 0,
+    ALN_THMOP_SCAN_MAXR = 1,
+    ALN_THMOP_SCAN_CONSTXY = 2,
+    ALN_THMOP_SCAN_SEL = 3,
+    ALN_THMOP_SCAN_TWEAKS = 4,
+    ALN_THMOP_PEAKHUNT = 5,
+    ALN_THMOP_PRIOR = 6,
+    ALN_THMOP_DENOVO = 7,
+    ALN_THMOP_PRETWEAKS = 8,
+    ALN_THMOP_POSTTWEAKS = 9,
+    ALN_THMOP_FULLRES = 10
+};
+int aln_thm_call_batch(aln_ctx *ctx, int npairs, const aln_thumbs *thumbs,
+                       const aln_thm_params *params, int op, const double *args,
+                       aln_thm_result *best, double *tptwk, double *ret);
 
 /* ---- allocation-free CorrPatches: no counterpart in the reference ---- */
 

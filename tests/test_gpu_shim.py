@@ -74,3 +74,50 @@ def test_cpp_callers_through_shim(tmp_path, orc):
             assert abs(gdx - dx) <= 0.01 and abs(gdy - dy) <= 0.01, (name, gdx, gdy, dx, dy)
     f = lines[-1].split()
     assert f[0] == "fft" and int(f[1]) == 4 * 5 and float(f[2]) < 1e-4 and int(f[3]) == 1024
+
+
+def _thm_compare(g, ref, msg):
+    assert g["err"] == int(ref["err"]), (msg, g, ref)
+    A, R = float(ref["A"]), float(ref["R"])
+    assert abs(g["A"] - A) <= 0.05, (msg, g, ref)
+    assert abs(g["R"] - R) <= 1e-3 * max(1.0, abs(R)), (msg, g, ref)
+    if abs(g["A"] - A) < 1e-9:
+        assert abs(g["X"] - float(ref["X"])) <= 0.01 and \
+            abs(g["Y"] - float(ref["Y"])) <= 0.01, (msg, g, ref)
+
+
+def test_cpp_thmscan_through_shim(tmp_path):
+    """class CThmScan through the C++ drop-in: a C++ program makes the
+    reference's call sequences (DenovoBestAngle, RFromAngle, UsePriorAngles,
+    AngleScanSel with MaxR, PostTweaks, FinishAtFullRes) on the golden
+    thumbnail pairs; results match the reference's golden outputs with the
+    sweep's bar (tests/test_gpu_sweep.py)."""
+    from shim_util import build_thm_check, thm_case, parse_thm_lines
+    exe = build_thm_check(str(tmp_path))
+    blob, expect = b"", []
+    gs = load_golden("thm_scan")
+    for k in sorted(gs):
+        d = gs[k]
+        blob += thm_case(int(d["mode"]), d["pa"], d["va"], d["pb"], d["vb"], int(d["req"]),
+                         rthresh=float(d["rthresh"]), pretweak=int(d["pretweak"]),
+                         disc=tuple(int(v) for v in d["disc"]), ang0=float(d["ang0"]),
+                         hfang=float(d["hfang"]), step=float(d["step"]))
+        expect.append((k, d, None))
+    gf = load_golden("thm_finish")
+    for k in sorted(gf):
+        d = gf[k]
+        blob += thm_case(int(d["mode"]), d["pa"], d["va"], d["pb"], d["vb"], int(d["req"]),
+                         prior=tuple(float(v) for v in d["prior"]),
+                         tptwk=tuple(float(v) for v in d["tptwk"]))
+        expect.append((k, dict(A=d["A"], X=d["X"], Y=d["Y"], R=d["R"], err=0),
+                       d["tptwk_out"]))
+    cases = os.path.join(str(tmp_path), "thm_cases.bin")
+    open(cases, "wb").write(blob)
+    out = subprocess.run([exe, cases], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    got = parse_thm_lines(out.stdout)
+    assert len(got) == len(expect)
+    for (name, ref, tw), g in zip(expect, got):
+        _thm_compare(g, ref, name)
+        if tw is not None and abs(g["A"] - float(ref["A"])) < 1e-9:
+            assert np.abs(np.array(g["tptwk"]) - tw).max() <= 1e-6, (name, g, tw)

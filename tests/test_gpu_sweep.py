@@ -89,3 +89,69 @@ def test_sweep_f_golden(ctx, case):
     g = ctx.thm_search_batch([T], usecorrr=0, mode=int(d["mode"]), ang0=float(d["ang0"]),
                              hfang=float(d["hfang"]), step=float(d["step"]))[0]
     compare(g, d, case)
+
+
+def _golden_thumbs(case="thm_s0_denovo"):
+    import alignment_projects_gb300 as aln
+    d = load_golden("thm_scan")[case]
+    return aln.thumbs_from_points(d["pa"], d["va"], d["pb"], d["vb"], int(d["req"])), d
+
+
+def test_call_ops_equal_search_modes(ctx):
+    """CThmScan member functions through aln_thm_call_batch: DenovoBestAngle
+    and UsePriorAngles from a fresh object give the search entry point's
+    numbers exactly (the same engine), and a DenovoBestAngle result fed to
+    PeakHunt keeps its record or improves it."""
+    import alignment_projects_gb300 as aln
+    T, d = _golden_thumbs()
+    for op, mode, hf in ((aln.THMOP_DENOVO, aln.THM_DENOVO, 10.0),
+                         (aln.THMOP_PRIOR, aln.THM_PRIOR, 1.0)):
+        s = ctx.thm_search_batch([T], mode=mode, ang0=0.0, hfang=hf, step=0.5)[0]
+        c = ctx.thm_call_batch([T], op, [0.0, hf, 0.5, 0.0])[0]
+        for k in ("A", "X", "Y", "R", "err"):
+            assert c[k] == s[k], (op, k, c, s)
+        assert c["ret"] == (1.0 if s["err"] == 0 else 0.0)
+    b = ctx.thm_call_batch([T], aln.THMOP_DENOVO, [0.0, 10.0, 0.5, 0.0])[0]
+    h = ctx.thm_call_batch([T], aln.THMOP_PEAKHUNT, [0.0, 0.5 * 0.05 * 1.5, 0.0, 0.0],
+                           best=[b])[0]
+    assert h["R"] >= b["R"] and h["ret"] == h["R"]
+
+
+def test_call_pretweaks_then_rfromangle(ctx, orc):
+    """Pretweaks then RFromAngle (cross_thisblock's sequence) carries the
+    pretweak transform from one call to the next, as the object does; the
+    transform is a product of near-unity factors and the R it gives is at
+    least the untweaked one."""
+    import alignment_projects_gb300 as aln
+    T, d = _golden_thumbs("thm_s2_denovo")
+    ang = float(d["A"])
+    r0 = ctx.thm_call_batch([T], aln.THMOP_RFROMANGLE, [ang, 0, 0, 0])[0]
+    p = ctx.thm_call_batch([T], aln.THMOP_PRETWEAKS, [0.0, ang, 0, 0])[0]
+    r1 = ctx.thm_call_batch([T], aln.THMOP_RFROMANGLE, [ang, 0, 0, 0], tptwk=[p["tptwk"]])[0]
+    assert p["ret"] in (0.0, 1.0)
+    tw = np.array(p["tptwk"])
+    assert np.abs(tw - [1, 0, 0, 0, 1, 0]).max() < 0.2
+    if p["ret"]:
+        assert r1["R"] >= r0["R"] - 1e-9
+    else:
+        assert r1["R"] == r0["R"]
+
+
+def test_disc_of_angle_callback(ctx):
+    """newAngProc: a per-angle disc callback that returns the fixed disc gives
+    the fixed-disc numbers; one that returns a disc around the answer gives
+    the numbers of that fixed disc."""
+    import alignment_projects_gb300 as aln
+    T, d = _golden_thumbs()
+    base = ctx.thm_call_batch([T], aln.THMOP_DENOVO, [0.0, 10.0, 0.5, 0.0])[0]
+    cb = ctx.thm_call_batch([T], aln.THMOP_DENOVO, [0.0, 10.0, 0.5, 0.0],
+                            disc_of_angle=lambda deg: (0, 0, -1, -1))[0]
+    assert (cb["A"], cb["X"], cb["Y"], cb["R"]) == (base["A"], base["X"], base["Y"], base["R"])
+    disc = (int(base["X"]), int(base["Y"]), 12, 12)
+    fixed = ctx.thm_call_batch([T], aln.THMOP_DENOVO, [0.0, 10.0, 0.5, 0.0], disc=disc)[0]
+    seen = []
+    cb2 = ctx.thm_call_batch([T], aln.THMOP_DENOVO, [0.0, 10.0, 0.5, 0.0],
+                             disc_of_angle=lambda deg: seen.append(deg) or disc)[0]
+    assert (cb2["A"], cb2["X"], cb2["Y"], cb2["R"]) == (fixed["A"], fixed["X"], fixed["Y"],
+                                                        fixed["R"])
+    assert len(seen) == cb2["ncalls"]

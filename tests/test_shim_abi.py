@@ -31,6 +31,27 @@ EXPECTED = {
 }
 
 
+# class CThmScan (0_GEN/CThmScan.h:57-223): every public member function and
+# the exported BigEnough, as the reference's CThmScan.o defines them
+EXPECTED_THM = [
+    "_Z9BigEnoughiiPv",
+    "_ZN8CThmScanC1Ev", "_ZN8CThmScanC2Ev",
+    "_ZN8CThmScan10InitializeEP8_IO_FILER6CorRec",
+    "_ZN8CThmScan9PretweaksEddR6ThmRec",
+    "_ZN8CThmScan10RFromAngleER6CorRecdR6ThmReci",
+    "_ZN8CThmScan9DebugAngsEiiiidddR6ThmRec",
+    "_ZN8CThmScan13AngleScanMaxRER6CorRecdddbR6ThmRec",
+    "_ZN8CThmScan16AngleScanConstXYER6CorRecdddR6ThmRec",
+    "_ZN8CThmScan12AngleScanSelER6CorRecdddbR6ThmRec",
+    "_ZN8CThmScan19AngleScanWithTweaksER6CorRecdddR6ThmRec",
+    "_ZN8CThmScan8PeakHuntER6CorRecdR6ThmRec",
+    "_ZN8CThmScan14UsePriorAnglesER6CorReciddR6ThmRec",
+    "_ZN8CThmScan15DenovoBestAngleER6CorRecdddR6ThmRecb",
+    "_ZN8CThmScan10PostTweaksER6CorRecR6ThmRec",
+    "_ZN8CThmScan15FinishAtFullResER6CorRecR6ThmRec",
+]
+
+
 def _exports(path):
     out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True,
                          check=True).stdout
@@ -47,8 +68,11 @@ def test_shim_exports_reference_signatures(shim):
     ex = _exports(shim)
     for name, mangled in EXPECTED.items():
         assert mangled in ex, name
+    for mangled in EXPECTED_THM:
+        assert mangled in ex, mangled
     # nothing else at namespace scope: the shim adds no stray symbols
-    assert {s for s in ex if s.startswith("_Z") and "St" not in s[:4]} <= set(EXPECTED.values())
+    assert {s for s in ex if s.startswith("_Z") and "St" not in s[:4]} <= \
+        set(EXPECTED.values()) | set(EXPECTED_THM)
 
 
 def test_same_names_as_the_reference_build(shim):
@@ -63,6 +87,8 @@ def test_same_names_as_the_reference_build(shim):
     ref = _exports(oracle.REF_SO)
     for name, mangled in EXPECTED.items():
         assert mangled in ref, name
+    for mangled in EXPECTED_THM:
+        assert mangled in ref, mangled
 
 
 def test_reference_caller_links_against_shim(shim):
@@ -85,3 +111,40 @@ def test_reference_caller_links_against_shim(shim):
                                "-laln_corr_shim", "-laln_corr", "-lpthread",
                                "-Wl,-rpath," + os.path.dirname(shim)])
         assert os.path.exists(exe)
+
+
+def _reference_tree():
+    import oracle
+    if not (os.path.isdir(os.path.join(oracle.REFERENCE_TREE, "0_GEN")) and
+            oracle.ref_available()):
+        pytest.skip("the reference's sources are not mounted here")
+    return oracle.REFERENCE_TREE
+
+
+def test_thmscan_layout_matches_reference(tmp_path):
+    """class CThmScan, ThmRec and CorRec have the reference's sizes and member
+    offsets (callers built from the reference's header allocate the object
+    and run its inline setters; the shim's member functions read it)."""
+    tree = _reference_tree()
+    src = os.path.join(ROOT, "tests", "cpp", "thmscan_layout.cpp")
+    outs = []
+    for ref in (False, True):
+        exe = os.path.join(str(tmp_path), "layout%d" % ref)
+        cmd = ["g++", "-std=c++17", "-w", "-o", exe, src]
+        cmd += (["-DALN_REFERENCE_HEADERS", "-DTIXML_USE_STL",
+                 "-I" + os.path.join(tree, "0_GEN"), "-I" + os.path.join(tree, "0_UTL")]
+                if ref else ["-I" + os.path.join(ROOT, "alignment_projects_gb300", "shim")])
+        subprocess.check_call(cmd)
+        outs.append(subprocess.run([exe], capture_output=True, text=True, check=True).stdout)
+    assert outs[0] == outs[1], (outs[0], outs[1])
+
+
+def test_reference_thmscan_caller_links_against_shim(tmp_path):
+    """A CThmScan caller compiled from the reference's own headers (the call
+    sequences of ApproximateMatch / CThmUtil) links against the shim in
+    place of CThmScan.o and Correlation.o."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from shim_util import build_thm_check
+    exe = build_thm_check(str(tmp_path), reference_headers=_reference_tree())
+    assert os.path.exists(exe)
