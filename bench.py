@@ -218,15 +218,13 @@ def alg_bytes_per_pair(grid, e=1):
 def dram_model_per_pair(grid, e=1, wy=129):
     """DRAM bytes per pair the fused kernels move (each array read or written
     once): k2_rowfft reads both strips and writes both row spectra T (rows < h
-    only); k2_corrcol reads both T and writes the window rows Q (k2_corrseg
-    reads b's rows once per segment, (seg + wy - 1) / seg times over);
-    k2_lagrow reads Q.  k2_corrcol's figure is checked against ncu
-    dram__bytes (profiles/k2_corrcol_montage.md)."""
+    only); k2_corrcol and k2_corrseg read both T and write the window rows Q
+    (k2_corrseg's re-reads of b's rows shared by neighbouring segments come
+    from L2); k2_lagrow reads Q.  Checked against ncu dram__bytes
+    (profiles/k2_corrcol_montage.md, profiles/k2_corrseg_montage.md)."""
     ws, hs, Nx, Ny, nseg = grid
     L1 = Nx // 2 + 1
-    seg = -(-hs // nseg) if nseg else hs
-    over = (seg + wy - 1) / seg if nseg else 1.0
-    cols = (8 * L1 * hs * (1.0 + over) if nseg else 16 * L1 * hs) + 8 * L1 * wy
+    cols = 16 * L1 * hs + 8 * L1 * wy
     return {"k2_rowfft": 2 * ws * hs * e + 16 * L1 * hs,
             "k2_corrseg" if nseg else "k2_corrcol": cols,
             "k2_lagrow": 8 * L1 * wy}
@@ -569,7 +567,7 @@ def run_gpu(args):
                          "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic,
                          "traffic_source": "per-pair DRAM model checked against ncu "
-                                           "dram__bytes (profiles/k2_corrcol_montage.md)",
+                                           "dram__bytes (profiles/)",
                          "alg_bytes_per_launch": alg_per_launch,
                          "avg_launch_ms": dom_ms / dom_launches,
                          "accounting": "canonical two-pass FFT bytes (one read + one write "
