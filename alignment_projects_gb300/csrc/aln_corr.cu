@@ -1809,7 +1809,7 @@ static int cols_per_cta(int Ny) { return std::max(1, std::min(16, 4096 / Ny)); }
 template <int LL>
 static void launch_rowfft2(aln_ctx *ctx, int n, int maxh)
 {
-    constexpr int T = RegFFT<LL, -1>::T;
+    constexpr int T = LL / rowfft_radix(LL);
     const int thr = rowfft_threads(T), G = thr / T;
     const size_t sm = (size_t)G * row_pitch(LL) * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_rowfft<LL>, sm);
@@ -1821,7 +1821,7 @@ static void launch_rowfft2(aln_ctx *ctx, int n, int maxh)
 template <int LL>
 static void launch_fill_rows(aln_ctx *ctx, int nsel, int maxh)
 {
-    constexpr int T = RegFFT<LL, -1>::T;
+    constexpr int T = LL / rowfft_radix(LL);
     const int thr = rowfft_threads(T), G = thr / T;
     const size_t sm = (size_t)G * row_pitch(LL) * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_rowfft<LL>, sm);
@@ -1995,6 +1995,7 @@ struct ChunkLaunch {
     int off, n;                        // jobs [off, off + n) of the batch table
     int maxw, maxh, maxslots, maxWy;
     int sw, sh;                        // largest caller-frame image of transposed jobs
+    int t8;                            // every transposed job is uint8 (128-byte tiles)
     int Nx, Ny, mode, both, sonly, frame_nx1, frame_ny1;
     int seg;                           // CorrPatches with segmented columns
     int fill_off, nfill, fill_maxh;    // spectrum-cache fills: sel[fill_off ...]
@@ -2011,6 +2012,7 @@ static void prep_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int off, ch
     cl.n = n;
     cl.maxw = cl.maxh = cl.maxslots = cl.maxWy = 1;
     cl.sw = cl.sh = 0;
+    cl.t8 = 1;
     cl.Nx = chunk[0]->d.Nx;
     cl.Ny = chunk[0]->d.Ny;
     cl.fill_off = (int)fills.size();
@@ -2055,6 +2057,7 @@ static void prep_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int off, ch
             if (pl.d.transposed) {
                 cl.sw = std::max(cl.sw, pl.d.h[i]);
                 cl.sh = std::max(cl.sh, pl.d.w[i]);
+                cl.t8 &= pl.d.dt[i] == ALN_U8;
             }
         }
         cl.maxWy = std::max(cl.maxWy, pl.d.yhi - pl.d.ylo + 1);
@@ -2087,7 +2090,8 @@ static int launch_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, const Chun
                                (size_t)chunk[k]->d.table_w * chunk[k]->d.table_h,
                                cudaMemcpyHostToDevice, st));
     if (cl.sw > 0)
-        LAUNCH(ctx, "k_transpose", k_transpose, dim3((cl.sw + 31) / 32, (cl.sh + 31) / 32, 2 * n),
+        LAUNCH(ctx, "k_transpose", k_transpose,
+               dim3(cl.t8 ? (cl.sw + 127) / 128 : (cl.sw + 31) / 32, (cl.sh + 31) / 32, 2 * n),
                dim3(32, 8), 0, ctx->dpairs);
     const int mode = cl.mode;
     if (mode != JOB_P2I) {
@@ -2316,12 +2320,15 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
     std::vector<std::vector<std::vector<PairPlan *>>> wchunks(windows.size());
     size_t max_stage = 0, max_work = 0, max_n = 1;
     for (size_t w = 0; w < windows.size(); ++w) {
-        std::map<std::tuple<int, int, int, int, int, int, int, int>, std::vector<PairPlan *>>
+        std::map<std::tuple<int, int, int, int, int, int, int, int, int>,
+                 std::vector<PairPlan *>>
             groups;
         size_t sb = 0;
         for (PairPlan *pl : windows[w]) {
+            // transposed jobs apart: their chunks alone launch the transpose
             groups[std::make_tuple(pl->d.Nx, pl->d.Ny, pl->frame_nx1, pl->frame_ny1, pl->d.mode,
-                                   pl->d.want_r, pl->d.want_s, pl->d.nseg > 0)]
+                                   pl->d.want_r, pl->d.want_s, pl->d.nseg > 0,
+                                   pl->transposed ? 1 : 0)]
                 .push_back(pl);
             sb += pl->in_bytes[0] + pl->in_bytes[1] + 16;
         }

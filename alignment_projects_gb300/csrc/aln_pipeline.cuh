@@ -181,7 +181,9 @@ __device__ __forceinline__ void store_bits(char *p, int es, long long idx, unsig
 }
 
 // grid (ceil(max caller w / 32), ceil(max caller h / 32), 2*npairs), block (32, 8):
-// frame pixel (xf, yf) = caller pixel (yf, xf)
+// frame pixel (xf, yf) = caller pixel (yf, xf).  uint8 images use 32 x 128
+// tiles (blockIdx.x counts 128 columns; a launch whose transposed images are
+// all uint8 has grid x = ceil(max caller w / 128)).
 __global__ void k_transpose(PairDev *pairs)
 {
     __shared__ unsigned long long tile[32][33];
@@ -202,10 +204,19 @@ __global__ void k_transpose(PairDev *pairs)
         const int xb0 = blockIdx.x * 128;
         if (xb0 >= sw)
             return;
+        // 4-byte loads where the caller's rows allow them (4-byte aligned
+        // base and stride, the whole word inside the row)
+        const bool vec = (((uintptr_t)src | (uintptr_t)sst) & 3) == 0;
         for (int rr = threadIdx.y; rr < 32; rr += 8) {
             const int yy = y0 + rr;
+            const int xq = xb0 + 4 * threadIdx.x;
+            if (vec && yy < sh && xq + 3 < sw) {
+                *(unsigned int *)&t8[rr][4 * threadIdx.x] =
+                    *(const unsigned int *)(src + yy * sst + xq);
+                continue;
+            }
             for (int m = 0; m < 4; ++m) {
-                const int x = xb0 + 4 * threadIdx.x + m;
+                const int x = xq + m;
                 t8[rr][4 * threadIdx.x + m] =
                     (yy < sh && x < sw) ? (unsigned char)src[yy * sst + x] : 0;
             }
@@ -358,129 +369,22 @@ __global__ void k2_sat2(PairDev *pairs)
 }
 
 // The same row pass with one warp per slot row (rows up to SAT2W_MAXW
-// columns): lane l owns a contiguous run of ceil(w/32) columns, the lane
-// totals are scanned with shuffles.  No block-wide synchronisation, so a
-// CTA carries eight rows and small images do not pay one CTA per row.
+// columns; no block-wide synchronisation, so a CTA carries eight rows and
+// small images do not pay one CTA per row).  The warp walks the row 32
+// columns at a time, lane l on column c0 + l: coalesced loads and stores, an
+// inclusive shuffle scan per 32 columns and a carry between them.
 #define SAT2W_MAXW 512
 
-template <typename TA, bool SQ = true>
-__device__ __forceinline__ void sat2_row_warp(const PairDev &p, int i, int slot, int y, TA *S,
-                                              TA *Q, int lane)
+template <typename TA>
+__device__ __forceinline__ TA warp_incl_scan(TA v, int lane)
 {
-    const int w = p.w[i];
-    const int seg = y / ((p.h[i] + SAT_WARPS - 1) / SAT_WARPS);
-    const TA *__restrict__ oS = (const TA *)p.segS[i] + (long long)seg * w;
-    const TA *__restrict__ oQ = (const TA *)p.segQ[i] + (long long)seg * w;
-    const int *__restrict__ oN = p.segN[i] + (long long)seg * w;
-    TA *__restrict__ rS = S + (long long)slot * w;
-    TA *__restrict__ rQ = Q + (long long)slot * w;
-    int *__restrict__ rN = p.satN[i] + (long long)slot * w;
-    const int per = (w + 31) >> 5;
-    const int c0 = lane * per, c1 = min(w, c0 + per);
-    TA s = 0, q = 0;
-    int n = 0;
-    for (int c = c0; c < c1; ++c) {
-        if (SQ) {
-            s += rS[c] + oS[c];
-            q += rQ[c] + oQ[c];
-            rS[c] = s;
-            rQ[c] = q;
-        }
-        n += rN[c] + oN[c];
-        rN[c] = n;
-    }
-    TA ts = s, tq = q;
-    int tn = n;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const int c2 = __shfl_up_sync(0xffffffff, tn, o);
-        if (SQ) {
-            const TA a2 = __shfl_up_sync(0xffffffff, ts, o);
-            const TA b2 = __shfl_up_sync(0xffffffff, tq, o);
-            if (lane >= o) {
-                ts += a2;
-                tq += b2;
-            }
-        }
+        const TA u = __shfl_up_sync(0xffffffff, v, o);
         if (lane >= o)
-            tn += c2;
+            v += u;
     }
-    const TA os = ts - s, oq = tq - q;
-    const int on = tn - n;
-    if (lane == 0)
-        return;
-    for (int c = c0; c < c1; ++c) {
-        if (SQ) {
-            rS[c] += os;
-            rQ[c] += oq;
-        }
-        rN[c] += on;
-    }
-}
-
-// Register form of the warp row pass for rows up to 32*PER columns: each
-// lane loads its PER columns at once (unrolled), keeps the running sums in
-// registers and stores each element once.
-template <typename TA, bool SQ, int PER>
-__device__ __forceinline__ void sat2_row_reg(const PairDev &p, int i, int slot, int y, TA *S,
-                                             TA *Q, int lane)
-{
-    const int w = p.w[i];
-    const int seg = y / ((p.h[i] + SAT_WARPS - 1) / SAT_WARPS);
-    const TA *__restrict__ oS = (const TA *)p.segS[i] + (long long)seg * w;
-    const TA *__restrict__ oQ = (const TA *)p.segQ[i] + (long long)seg * w;
-    const int *__restrict__ oN = p.segN[i] + (long long)seg * w;
-    TA *__restrict__ rS = S + (long long)slot * w;
-    TA *__restrict__ rQ = Q + (long long)slot * w;
-    int *__restrict__ rN = p.satN[i] + (long long)slot * w;
-    const int c0 = lane * PER;
-    TA vs[PER], vq[PER];
-    int vn[PER];
-    TA s = 0, q = 0;
-    int n = 0;
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-        const int c = c0 + k;
-        if (c < w) {
-            if (SQ) {
-                s += rS[c] + oS[c];
-                q += rQ[c] + oQ[c];
-            }
-            n += rN[c] + oN[c];
-        }
-        vs[k] = s;
-        vq[k] = q;
-        vn[k] = n;
-    }
-    TA ts = s, tq = q;
-    int tn = n;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int c2 = __shfl_up_sync(0xffffffff, tn, o);
-        if (SQ) {
-            const TA a2 = __shfl_up_sync(0xffffffff, ts, o);
-            const TA b2 = __shfl_up_sync(0xffffffff, tq, o);
-            if (lane >= o) {
-                ts += a2;
-                tq += b2;
-            }
-        }
-        if (lane >= o)
-            tn += c2;
-    }
-    const TA os = ts - s, oq = tq - q;
-    const int on = tn - n;
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-        const int c = c0 + k;
-        if (c < w) {
-            if (SQ) {
-                rS[c] = vs[k] + os;
-                rQ[c] = vq[k] + oq;
-            }
-            rN[c] = vn[k] + on;
-        }
-    }
+    return v;
 }
 
 template <typename TA, bool SQ>
@@ -488,14 +392,45 @@ __device__ __forceinline__ void sat2_row_any(const PairDev &p, int i, int slot, 
                                              TA *Q, int lane)
 {
     const int w = p.w[i];
-    if (w <= 128)
-        sat2_row_reg<TA, SQ, 4>(p, i, slot, y, S, Q, lane);
-    else if (w <= 256)
-        sat2_row_reg<TA, SQ, 8>(p, i, slot, y, S, Q, lane);
-    else if (w <= 512)
-        sat2_row_reg<TA, SQ, 16>(p, i, slot, y, S, Q, lane);
-    else
-        sat2_row_warp<TA, SQ>(p, i, slot, y, S, Q, lane);
+    const int seg = y / ((p.h[i] + SAT_WARPS - 1) / SAT_WARPS);
+    const TA *__restrict__ oS = (const TA *)p.segS[i] + (long long)seg * w;
+    const TA *__restrict__ oQ = (const TA *)p.segQ[i] + (long long)seg * w;
+    const int *__restrict__ oN = p.segN[i] + (long long)seg * w;
+    TA *__restrict__ rS = S + (long long)slot * w;
+    TA *__restrict__ rQ = Q + (long long)slot * w;
+    int *__restrict__ rN = p.satN[i] + (long long)slot * w;
+    TA cs = 0, cq = 0;
+    int cn = 0;
+    for (int c0 = 0; c0 < w; c0 += 32) {
+        const int c = c0 + lane;
+        const bool ok = c < w;
+        TA vs = 0, vq = 0;
+        int vn = 0;
+        if (ok) {
+            if (SQ) {
+                vs = rS[c] + oS[c];
+                vq = rQ[c] + oQ[c];
+            }
+            vn = rN[c] + oN[c];
+        }
+        if (SQ) {
+            vs = warp_incl_scan(vs, lane) + cs;
+            vq = warp_incl_scan(vq, lane) + cq;
+        }
+        vn = warp_incl_scan(vn, lane) + cn;
+        if (ok) {
+            if (SQ) {
+                rS[c] = vs;
+                rQ[c] = vq;
+            }
+            rN[c] = vn;
+        }
+        if (SQ) {
+            cs = __shfl_sync(0xffffffff, vs, 31);
+            cq = __shfl_sync(0xffffffff, vq, 31);
+        }
+        cn = __shfl_sync(0xffffffff, vn, 31);
+    }
 }
 
 // grid (ceil(maxslots / 8), 2, npairs), block 256: warp k takes slot 8*bx + k
@@ -526,12 +461,17 @@ __global__ void k2_sat2w(PairDev *pairs)
 // threads per CTA of the row kernels: >= 256, four teams when teams are large
 __host__ __device__ constexpr int rowfft_threads(int T) { return T * 4 > 512 ? 512 : (T * 4 < 256 ? 256 : T * 4); }
 
-// Each team of RegFFT<L>::T threads transforms one row.  G = blockDim.x / T
-// rows per CTA; smem: G * row_pitch(L) float2 per CTA.
+// Per-thread radix of the row transforms: 16 from 128 points up (fewer
+// shared-memory exchange passes: the row kernel is bound by them), the
+// register FFT's default below.
+__host__ __device__ constexpr int rowfft_radix(int L) { return L >= 128 ? 16 : fft_radix(L); }
+
+// Each team of L / rowfft_radix(L) threads transforms one row.  G =
+// blockDim.x / T rows per CTA; smem: G * row_pitch(L) float2 per CTA.
 template <int L>
 __global__ void k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int *sel)
 {
-    using F = RegFFT<L, -1>;
+    using F = RegFFT<L, -1, rowfft_radix(L)>;
     constexpr int R = F::R, T = F::T;
     constexpr int G = rowfft_threads(T) / T;
     extern __shared__ float2 smem[];
