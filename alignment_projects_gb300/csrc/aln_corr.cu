@@ -154,22 +154,26 @@ __device__ __forceinline__ double div_sqrt2(double num, double d1, double d2)
     return num * y;
 }
 
-// CLinCorr::GetCorr's terms for integer pixels: n*Q - S^2 >= 0 exactly in
-// unsigned 64-bit arithmetic (valid while n*Q < 2^64: always for 8-bit
-// pixels, for 16-bit ones while n < 2^20), the shifted product
-// (S1 - n mu1)(S2 - n mu2) from exact factors (integer means).
-__device__ __forceinline__ double r_int(const PairDev &p, long long n, double cs, long long s1,
+// CLinCorr::GetCorr's terms for integer pixels (0_GEN/Correlation.cpp:
+// 705-757).  The normalisation terms n*Q - S^2 >= 0 are exact in unsigned
+// 64-bit arithmetic (valid while n*Q < 2^64: always for 8-bit pixels, for
+// 16-bit ones while n < 2^20), and the shifted sums S - n mu are exact
+// integers; the rest is FP32 -- the cross sum cs comes from the FP32 FFT, so
+// FP32 here adds an error of the same order (~1e-7 in r), and this GPU's
+// FP64 pipe is narrow (FP64 arithmetic bounded the lag kernel).  The
+// flat-overlap guard d1 d2 < n^2 1e-9 is evaluated in FP32 too.
+__device__ __forceinline__ double r_int(const PairDev &p, long long n, float cs, long long s1,
                                         long long q1, long long s2, long long q2)
 {
     typedef unsigned long long u64;
     const u64 un = (u64)n;
     const u64 d1 = un * (u64)q1 - (u64)s1 * (u64)s1, d2 = un * (u64)q2 - (u64)s2 * (u64)s2;
-    const double dd1 = (double)d1, dd2 = (double)d2, nn = (double)n;
-    if (dd1 * dd2 < nn * nn * 1.0E-9)
+    const float f1 = __ull2float_rn(d1), f2 = __ull2float_rn(d2), fn = __ll2float_rn(n);
+    if (f1 * f2 < fn * fn * 1.0e-9f)
         return 0.0;
     const long long m1 = (long long)p.mu[0], m2 = (long long)p.mu[1];
-    const double num = nn * cs - (double)(s1 - n * m1) * (double)(s2 - n * m2);
-    return div_sqrt2(num, dd1, dd2);
+    const float num = fmaf(fn, cs, -(__ll2float_rn(s1 - n * m1) * __ll2float_rn(s2 - n * m2)));
+    return (double)(num * (rsqrtf(f1) * rsqrtf(f2)));
 }
 
 // the overlap sizes for which r_int is exact on this pair's pixel types
@@ -181,7 +185,8 @@ __device__ __forceinline__ bool r_int_ok(const PairDev &p, long long n)
     return u8 || n < (1ll << 20);
 }
 
-__device__ __forceinline__ bool lag_r(const PairDev &p, int x, int y, double cs, double &r)
+// cs: the cross sum at this lag (the inverse transform's value over Nx Ny)
+__device__ __forceinline__ bool lag_r(const PairDev &p, int x, int y, float cs, double &r)
 {
     const int w1 = p.w[0], h1 = p.h[0], w2 = p.w[1], h2 = p.h[1];
     // BoxesFromShifts, 0_GEN/Geometry.cpp:150-176
@@ -226,7 +231,7 @@ __device__ __forceinline__ bool lag_r(const PairDev &p, int x, int y, double cs,
         s2 = sat_box(p.satS[1], p, 1, L2, R2, B2, T2);
         q2 = sat_box(p.satQ[1], p, 1, L2, R2, B2, T2);
     }
-    const double num = n * cs - (s1 - n * p.mu[0]) * (s2 - n * p.mu[1]);
+    const double num = n * (double)cs - (s1 - n * p.mu[0]) * (s2 - n * p.mu[1]);
     const double d1 = n * q1 - s1 * s1;
     const double d2 = n * q2 - s2 * s2;
     const double d = d1 * d2;
@@ -712,7 +717,7 @@ __global__ void k_lagrow(PairDev *pairs, const float2 *__restrict__ tw, int RBL)
     }
     __syncthreads();
     float2 *res = fft_cols<+1>(bZ, bX, RBL, logL, pitch, tw);
-    const double inv = 1.0 / ((double)Nx * (double)Ny);
+    const float inv = 1.0f / ((float)Nx * (float)Ny);   // a power of two: exact
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int r = 0; r < rows; ++r) {
         const int j = j0 + r, y = p.ylo + j;
@@ -728,8 +733,7 @@ __global__ void k_lagrow(PairDev *pairs, const float2 *__restrict__ tw, int RBL)
             double rv = 0.0;
             if (x >= xa && x <= xb) {
                 const int xs = x < 0 ? x + Nx : x;
-                const double cs = (double)row[xs] * inv;
-                if (lag_r(p, x, y, cs, rv))
+                if (lag_r(p, x, y, row[xs] * inv, rv))
                     best_merge(br, bk, rv, (long long)ys * Nx + xs);
             }
             p.rr[(long long)j * Wx + (x - p.xlo)] = rv;

@@ -38,9 +38,22 @@ __device__ __forceinline__ void two_sum_acc(float &s, float &e, float x)
 // otherwise.  Also writes the column totals (mean shift).
 #define SAT_WARPS 16
 
+// Accumulator of a warp's segment-local sums: 32-bit for uint8 pixels (a
+// segment is at most 512 rows -- h <= 8192 -- so the sums of v and v^2 stay
+// below 2^26), the table type otherwise.
+template <typename TA, typename PIX>
+struct SatAcc {
+    typedef TA type;
+};
+template <>
+struct SatAcc<long long, uint8_t> {
+    typedef unsigned type;
+};
+
 template <typename TA, typename PIX, bool SQ = true>
 __device__ __forceinline__ void sat_cols(const PairDev &p, int i, TA *shS, TA *shQ, int *shN)
 {
+    typedef typename SatAcc<TA, PIX>::type AC;
     const int w = p.w[i], h = p.h[i];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int c = blockIdx.x * 32 + tx;
@@ -56,7 +69,7 @@ __device__ __forceinline__ void sat_cols(const PairDev &p, int i, TA *shS, TA *s
     TA *__restrict__ S = (TA *)p.satS[i];
     TA *__restrict__ Q = (TA *)p.satQ[i];
     int *__restrict__ N = p.satN[i];
-    TA s = 0, q = 0;
+    AC s = 0, q = 0;
     int n = 0;
     if (cok) {
         const PIX *__restrict__ col = img + c;
@@ -71,7 +84,7 @@ __device__ __forceinline__ void sat_cols(const PairDev &p, int i, TA *shS, TA *s
                 stop = min(stop, max(lo1, y));
 #pragma unroll 8
             for (; y < stop; ++y) {
-                const TA v = (TA)__ldg(&col[y * st]);
+                const AC v = (AC)__ldg(&col[y * st]);
                 if (SQ) {
                     s += v;
                     q += v * v;
@@ -86,12 +99,12 @@ __device__ __forceinline__ void sat_cols(const PairDev &p, int i, TA *shS, TA *s
             const int rend = min(y1 - 1, first ? hi0 : hi1);
             const long long base = first ? (long long)(y - lo0) : (long long)(len0 + y - lo1);
             for (long long o = base * w + c; y <= rend; ++y, o += w) {
-                const TA v = (TA)__ldg(&col[y * st]);
+                const AC v = (AC)__ldg(&col[y * st]);
                 if (SQ) {
                     s += v;
                     q += v * v;
-                    S[o] = s;
-                    Q[o] = q;
+                    S[o] = (TA)s;
+                    Q[o] = (TA)q;
                 }
                 if (want_n)
                     n += (v != 0);
@@ -99,8 +112,8 @@ __device__ __forceinline__ void sat_cols(const PairDev &p, int i, TA *shS, TA *s
             }
         }
     }
-    shS[ty * 32 + tx] = s;
-    shQ[ty * 32 + tx] = q;
+    shS[ty * 32 + tx] = (TA)s;
+    shQ[ty * 32 + tx] = (TA)q;
     shN[ty * 32 + tx] = n;
     __syncthreads();
     if (!cok)
@@ -116,7 +129,7 @@ __device__ __forceinline__ void sat_cols(const PairDev &p, int i, TA *shS, TA *s
         ((TA *)p.segS[i])[ty * w + c] = os;
         ((TA *)p.segQ[i])[ty * w + c] = oq;
         if (ty == SAT_WARPS - 1)
-            p.colsum[i][c] = (double)(os + s);
+            p.colsum[i][c] = (double)(os + (TA)s);
     }
     p.segN[i][ty * w + c] = on;
 }
@@ -951,7 +964,7 @@ __global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
         C[2 * n + 1] = v[r].y;
     }
     __syncthreads();
-    const double inv = 1.0 / ((double)Nx * (double)Ny);
+    const float invf = 1.0f / ((float)Nx * (float)Ny);   // a power of two: exact
     double br = -1.0e30;
     long long bk = 0x7fffffffffffffffLL;
     if (live) {
@@ -965,7 +978,7 @@ __global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
             double rv = 0.0;
             if (x >= xa && x <= xb) {
                 const int xs = x < 0 ? x + Nx : x;
-                if (lag_r(p, x, y, (double)C[xs] * inv, rv))
+                if (lag_r(p, x, y, C[xs] * invf, rv))
                     best_merge(br, bk, rv, (long long)ys * Nx + xs);
             }
             p.rr[(long long)j * Wx + (x - p.xlo)] = rv;
