@@ -381,12 +381,15 @@ __global__ void k2_sat2(PairDev *pairs)
         sat2_row<double>(p, i, slot, y, p.satS[i], p.satQ[i]);
 }
 
-// The same row pass with one warp per slot row (rows up to SAT2W_MAXW
-// columns; no block-wide synchronisation, so a CTA carries eight rows and
-// small images do not pay one CTA per row).  The warp walks the row 32
-// columns at a time, lane l on column c0 + l: coalesced loads and stores, an
-// inclusive shuffle scan per 32 columns and a carry between them.
-#define SAT2W_MAXW 512
+// The same row pass with one warp per slot row (no block-wide
+// synchronisation, so a CTA carries eight rows and small images do not pay
+// one CTA per row).  The warp walks the row 32 columns at a time, lane l on
+// column c0 + l: coalesced loads and stores, an inclusive shuffle scan per 32
+// columns and a carry between them.  Used at every width (a plan's widths
+// are at most 4096): on the uneven uint16 batch (widths up to 1024) it took
+// 16 ms per 20000 pairs where k2_sat2 (one CTA per row) and the earlier
+// per-lane-run form took 29 ms.
+#define SAT2W_MAXW 8192
 
 template <typename TA>
 __device__ __forceinline__ TA warp_incl_scan(TA v, int lane)
