@@ -386,9 +386,9 @@ __global__ void k2_sat2(PairDev *pairs)
 // one CTA per row).  The warp walks the row 32 columns at a time, lane l on
 // column c0 + l: coalesced loads and stores, an inclusive shuffle scan per 32
 // columns and a carry between them.  Used at every width (a plan's widths
-// are at most 4096): on the uneven uint16 batch (widths up to 1024) it took
-// 16 ms per 20000 pairs where k2_sat2 (one CTA per row) and the earlier
-// per-lane-run form took 29 ms.
+// are at most 4096): on the uneven uint16 batch (widths up to 1024) the row
+// pass took 16 ms per 20000 pairs with it everywhere, 29 ms with k2_sat2 (one
+// CTA per row) on the rows wider than 512.
 #define SAT2W_MAXW 8192
 
 template <typename TA>
