@@ -5,7 +5,7 @@
 //   k3_sat    per 32-column band: warp-local column prefix sums of v, v^2,
 //             (v != 0) at the needed rows, per-warp offsets; column totals
 //             (k_mean turns them into mu)
-//   k2_sat2   per needed row: add the warp offset, x-prefix -> SAT row
+//   k2_sat2w  per needed row: add the warp offset, x-prefix -> SAT row
 //   k2_rowfft<L>   rows: (v - mu), zero pad, real FFT of length 2L, [kx][y]
 //   k2_corrcol<Ny> per column kx: FFT of b's column (or the cached spectrum),
 //             FFT of a's column, X2 * conj(X1), inverse FFT, the window's
@@ -34,7 +34,7 @@ __device__ __forceinline__ void two_sum_acc(float &s, float &e, float x)
 // (32, SAT_WARPS): each CTA owns 32 columns of one image; warp ty owns rows
 // [ty*segh, (ty+1)*segh) and walks them once, storing its local column
 // prefix at the needed rows.  The warps' exclusive offsets per column go to
-// segoff[ty][c]; k2_sat2 adds them.  Exact int64 for 8/16-bit pixels, FP64
+// segoff[ty][c]; k2_sat2w adds them.  Exact int64 for 8/16-bit pixels, FP64
 // otherwise.  Also writes the column totals (mean shift).
 #define SAT_WARPS 16
 
@@ -273,123 +273,14 @@ __global__ void k_transpose(PairDev *pairs)
     }
 }
 
-// inclusive block scan of (a, b, c) over 256 threads (warp shuffles)
-template <typename TA>
-__device__ __forceinline__ void block_scan3(TA &a, TA &b, int &c, TA *sa, TA *sb, int *sc)
-{
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const TA a2 = __shfl_up_sync(0xffffffff, a, o);
-        const TA b2 = __shfl_up_sync(0xffffffff, b, o);
-        const int c2 = __shfl_up_sync(0xffffffff, c, o);
-        if (lane >= o) {
-            a += a2;
-            b += b2;
-            c += c2;
-        }
-    }
-    if (lane == 31) {
-        sa[wid] = a;
-        sb[wid] = b;
-        sc[wid] = c;
-    }
-    __syncthreads();
-    if (wid == 0) {
-        TA x = lane < 8 ? sa[lane] : TA(0), y = lane < 8 ? sb[lane] : TA(0);
-        int z = lane < 8 ? sc[lane] : 0;
-#pragma unroll
-        for (int o = 1; o < 8; o <<= 1) {
-            const TA x2 = __shfl_up_sync(0xffffffff, x, o);
-            const TA y2 = __shfl_up_sync(0xffffffff, y, o);
-            const int z2 = __shfl_up_sync(0xffffffff, z, o);
-            if (lane >= o) {
-                x += x2;
-                y += y2;
-                z += z2;
-            }
-        }
-        if (lane < 8) {
-            sa[lane] = x;
-            sb[lane] = y;
-            sc[lane] = z;
-        }
-    }
-    __syncthreads();
-    if (wid > 0) {
-        a += sa[wid - 1];
-        b += sb[wid - 1];
-        c += sc[wid - 1];
-    }
-    __syncthreads();
-}
-
-template <typename TA>
-__device__ void sat2_row(PairDev &p, int i, int slot, int y, TA *S, TA *Q)
-{
-    __shared__ TA sa[8], sb[8];
-    __shared__ int sc[8];
-    const int w = p.w[i];
-    const int seg = y / ((p.h[i] + SAT_WARPS - 1) / SAT_WARPS);
-    const TA *oS = (const TA *)p.segS[i] + (long long)seg * w;
-    const TA *oQ = (const TA *)p.segQ[i] + (long long)seg * w;
-    const int *oN = p.segN[i] + (long long)seg * w;
-    TA *rS = S + (long long)slot * w;
-    TA *rQ = Q + (long long)slot * w;
-    int *rN = p.satN[i] + (long long)slot * w;
-    const int per = (w + 255) / 256;
-    const int c0 = threadIdx.x * per, c1 = min(w, c0 + per);
-    // full column prefix (warp segment offset + local), x-prefix of this
-    // thread's columns, then the block-wide offsets
-    TA s = 0, q = 0;
-    int n = 0;
-    for (int c = c0; c < c1; ++c) {
-        const TA cs = rS[c] + oS[c], cq = rQ[c] + oQ[c];
-        const int cn = rN[c] + oN[c];
-        s += cs;
-        q += cq;
-        n += cn;
-        rS[c] = s;
-        rQ[c] = q;
-        rN[c] = n;
-    }
-    TA ts = s, tq = q;
-    int tn = n;
-    block_scan3<TA>(ts, tq, tn, sa, sb, sc);
-    const TA os = ts - s, oq = tq - q;   // exclusive offsets
-    const int on = tn - n;
-    for (int c = c0; c < c1; ++c) {
-        rS[c] += os;
-        rQ[c] += oq;
-        rN[c] += on;
-    }
-}
-
-// grid (maxslots, 2, npairs), block 256
-__global__ void k2_sat2(PairDev *pairs)
-{
-    PairDev &p = pairs[blockIdx.z];
-    const int i = blockIdx.y;
-    const int slot = blockIdx.x;
-    if (p.status != 0 || slot >= nslots(p, i))
-        return;
-    const int len0 = p.need_hi[i][0] - p.need_lo[i][0] + 1;
-    const int y = slot < len0 ? p.need_lo[i][0] + slot : p.need_lo[i][1] + slot - len0;
-    if (int_pixels(p.dt[i]))
-        sat2_row<long long>(p, i, slot, y, (long long *)p.satS[i], (long long *)p.satQ[i]);
-    else
-        sat2_row<double>(p, i, slot, y, p.satS[i], p.satQ[i]);
-}
-
-// The same row pass with one warp per slot row (no block-wide
-// synchronisation, so a CTA carries eight rows and small images do not pay
-// one CTA per row).  The warp walks the row 32 columns at a time, lane l on
-// column c0 + l: coalesced loads and stores, an inclusive shuffle scan per 32
-// columns and a carry between them.  Used at every width (a plan's widths
-// are at most 4096): on the uneven uint16 batch (widths up to 1024) the row
-// pass took 16 ms per 20000 pairs with it everywhere, 29 ms with k2_sat2 (one
-// CTA per row) on the rows wider than 512.
-#define SAT2W_MAXW 8192
+// The row pass of the summed-area tables: per needed row, add the warp
+// segment offsets of k3_sat and take the x-prefix.  One warp per row (no
+// block-wide synchronisation, so a CTA carries eight rows and small images
+// do not pay one CTA per row); the warp walks the row 32 columns at a time,
+// lane l on column c0 + l: coalesced loads and stores, an inclusive shuffle
+// scan per 32 columns and a carry between them.  (On the uneven uint16 batch
+// this took 16 ms per 20000 pairs where a CTA-per-row scan on the rows wider
+// than 512 columns took 29 ms.)
 
 template <typename TA>
 __device__ __forceinline__ TA warp_incl_scan(TA v, int lane)
