@@ -2102,8 +2102,12 @@ static int launch_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, const Chun
         LAUNCH(ctx, "k3_sat", k3_sat, dim3((cl.maxw + 31) / 32, 2 * n), dim3(32, SAT_WARPS), 0,
                ctx->dpairs);
         LAUNCH(ctx, "k_mean", k_mean, dim3(2, n), 256, 0, ctx->dpairs);
-        LAUNCH(ctx, "k2_sat2w", k2_sat2w, dim3((cl.maxslots + 7) / 8, 2, n), 256, 0,
-               ctx->dpairs);
+        if (cl.sonly)
+            LAUNCH(ctx, "k2_sat2w", k2_sat2w<true>, dim3((cl.maxslots + 7) / 8, 2, n), 256, 0,
+                   ctx->dpairs);
+        else
+            LAUNCH(ctx, "k2_sat2w", k2_sat2w<false>, dim3((cl.maxslots + 7) / 8, 2, n), 256,
+                   0, ctx->dpairs);
     }
     if (cl.nfill > 0) {
         switch (L) {

@@ -340,7 +340,44 @@ __device__ __forceinline__ void sat2_row_any(const PairDev &p, int i, int slot, 
     }
 }
 
-// grid (ceil(maxslots / 8), 2, npairs), block 256: warp k takes slot 8*bx + k
+// Counts-only form (CorrImagesS without a mincor): K rounds of 32 columns
+// per pass, their loads issued together (one memory latency per pass), then
+// scanned in registers in column order.  (Measured on the thumbnail sweep:
+// 52 ms per 1024-pair step against 132 ms one round at a time; the same
+// batching of the int64 S and Q tables needed 91 registers and ran slower.)
+__device__ __forceinline__ void sat2_row_counts(const PairDev &p, int i, int slot, int y,
+                                                int lane)
+{
+    constexpr int K = 8;
+    const int w = p.w[i];
+    const int seg = y / ((p.h[i] + SAT_WARPS - 1) / SAT_WARPS);
+    const int *__restrict__ oN = p.segN[i] + (long long)seg * w;
+    int *__restrict__ rN = p.satN[i] + (long long)slot * w;
+    int cn = 0;
+    for (int cb = 0; cb < w; cb += 32 * K) {
+        int vn[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int c = cb + 32 * k + lane;
+            vn[k] = c < w ? rN[c] + oN[c] : 0;
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (cb + 32 * k >= w)
+                break;   // uniform over the warp
+            vn[k] = warp_incl_scan(vn[k], lane) + cn;
+            cn = __shfl_sync(0xffffffff, vn[k], 31);
+            const int c = cb + 32 * k + lane;
+            if (c < w)
+                rN[c] = vn[k];
+        }
+    }
+}
+
+// grid (ceil(maxslots / 8), 2, npairs), block 256: warp k takes slot 8*bx + k.
+// NONLY: the form launched for chunks of counts-only jobs (its registers are
+// not sized for the int64 tables).
+template <bool NONLY>
 __global__ void k2_sat2w(PairDev *pairs)
 {
     const PairDev &p = pairs[blockIdx.z];
@@ -351,7 +388,13 @@ __global__ void k2_sat2w(PairDev *pairs)
     const int len0 = p.need_hi[i][0] - p.need_lo[i][0] + 1;
     const int y = slot < len0 ? p.need_lo[i][0] + slot : p.need_lo[i][1] + slot - len0;
     const int lane = threadIdx.x & 31;
-    if (p.sat_nonly)
+    if (NONLY) {
+        if (p.sat_nonly)
+            sat2_row_counts(p, i, slot, y, lane);
+        else
+            sat2_row_any<long long, false>(p, i, slot, y, (long long *)p.satS[i],
+                                           (long long *)p.satQ[i], lane);
+    } else if (p.sat_nonly)
         sat2_row_any<long long, false>(p, i, slot, y, (long long *)p.satS[i],
                                        (long long *)p.satQ[i], lane);
     else if (int_pixels(p.dt[i]))
