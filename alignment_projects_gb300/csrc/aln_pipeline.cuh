@@ -418,8 +418,12 @@ __host__ __device__ constexpr int rowfft_radix(int L) { return L >= 128 ? 16 : f
 
 // Each team of L / rowfft_radix(L) threads transforms one row.  G =
 // blockDim.x / T rows per CTA; smem: G * row_pitch(L) float2 per CTA.
+// Occupancy: 5 CTAs per SM up to 256-point rows (48 registers, no spills),
+// 64 registers per thread above.
 template <int L>
-__global__ void k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int *sel)
+__global__ void __launch_bounds__(rowfft_threads(L / rowfft_radix(L)),
+                                  L <= 256 ? 5 : 1024 / rowfft_threads(L / rowfft_radix(L)))
+k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int *sel)
 {
     using F = RegFFT<L, -1, rowfft_radix(L)>;
     constexpr int R = F::R, T = F::T;
