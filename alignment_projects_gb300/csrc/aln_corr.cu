@@ -1,8 +1,20 @@
-// aln_corr.cu -- GB300 (sm_103a) FFT normalised cross-correlation:
-// the CorrPatches pipeline (0_GEN/Correlation.cpp:901-1170) as batched
-// kernels, plus the FFT_2D / IFT_2D drop-ins.
+// aln_corr.cu -- GB300 (sm_103a) FFT normalised cross-correlation: host
+// planning and orchestration of CorrPatches (0_GEN/Correlation.cpp:901-1170),
+// CorrImagesF/R/S, CorrPatchToImage, the FFT_2D / IFT_2D / Convolve drop-ins
+// and the C ABI of include/aln_corr.h.
 //
-// Pipeline for a group of pairs sharing one FFT size (Nx, Ny):
+// The batched pipeline (aln_pipeline.cuh) runs each chunk of jobs sharing a
+// transform grid: k_transpose (wide jobs), k3_sat + k_mean + k2_sat2w
+// (summed-area-table rows the lag window needs, mean shifts), k2_rowfft
+// (row spectra T[kx][y]), k2_corrcol or k2_corrseg (column transforms,
+// spectral product, inverse; the window's lag rows -> Q), k2_lagrow /
+// k2_lagimg / k2_lagp2i (inverse rows, r or S per lag, legality, row argmax),
+// k_final* (argmax, ParabPeakFFT / ParabPeak, S score).  The CThmScan sweep
+// (aln_sweep.cuh) and the request server (aln_server.cuh) drive it.
+//
+// The kernels defined in this file are the shared-memory FFT path: FFT_2D /
+// IFT_2D / Convolve, the allocation-free entry point, and CorrPatches grids
+// outside the register FFT's range:
 //   k_colsum    column prefix sums of v, v^2, (v != 0) -> summed-area-table
 //               rows the lag window needs; column totals
 //   k_mean      mean of each image -> shift mu (integer for integer pixels)
@@ -12,8 +24,8 @@
 //   k_colfft    image b: column FFTs -> spectrum X2[kx][ky]
 //   k_corrcol   image a: column FFTs, X2 * conj(X1), inverse column FFTs,
 //               only the lag rows of the window -> Q[kx][j]
-//   k_lagrow    per lag row: inverse real FFT, Pearson r per lag from the
-//               FP64 summed-area tables, legality, disc, row argmax
+//   k_lagrow    per lag row: inverse real FFT, Pearson r per lag, legality,
+//               disc, row argmax
 //   k_final     argmax over rows (ties: smallest storage index, as the
 //               reference's row-major scan with strict '>'), ParabPeakFFT
 //

@@ -10,7 +10,12 @@
 //   k2_corrcol<Ny> per column kx: FFT of b's column (or the cached spectrum),
 //             FFT of a's column, X2 * conj(X1), inverse FFT, the window's
 //             lag rows -> Q[kx][j].  Nothing else leaves the SM.
+//   k2_corrseg<NS> the same with the column cut into segments of a's rows
+//             (CorrPatches): per segment two NS-point FFTs and the product,
+//             summed per column, one inverse
 //   k2_lagrow<L>   per lag row: inverse real FFT, r per lag, row argmax
+//   k2_lagimg / k2_lagp2i, k_final_img / k_makef / k_fpeak / k_final_p2i:
+//             the CorrImages and CorrPatchToImage ends of the pipeline
 #pragma once
 
 #include "aln_fft_reg.cuh"
