@@ -13,7 +13,10 @@
 // double tptwk[6]
 // modes: 0 DenovoBestAngle, 1 RFromAngle, 2 UsePriorAngles,
 // 3 AngleScanSel + PeakHunt, 4 AngleScanMaxR (favorCenter), 5 PostTweaks,
-// 6 FinishAtFullRes, 7 Pretweaks then RFromAngle
+// 6 FinishAtFullRes, 7 Pretweaks then RFromAngle, 8 DenovoBestAngle with
+// SetNewAngProc giving the case's disc for every angle (and SetDisc off),
+// 9 DebugAngs(1, 2, 3, 4, ang0, hfang, step) (writes angs_1.2^3.4.log in
+// the working directory; the line reports RFromAngle at ang0)
 #ifdef ALN_REFERENCE_HEADERS
 #include "CThmScan.h"
 #else
@@ -23,6 +26,19 @@
 #include <cstdint>
 #include <cstdio>
 #include <vector>
+
+static int g_disc[4];
+static int g_disc_calls = 0;
+
+static void disc_proc(int &Ox, int &Oy, int &Rx, int &Ry, double deg)
+{
+    (void)deg;
+    Ox = g_disc[0];
+    Oy = g_disc[1];
+    Rx = g_disc[2];
+    Ry = g_disc[3];
+    ++g_disc_calls;
+}
 
 template <typename T>
 static bool rd(FILE *f, T &v)
@@ -133,6 +149,21 @@ int main(int argc, char **argv)
             break;
         case 7:
             ret = S.Pretweaks(0.0, ang0, thm);
+            S.RFromAngle(best, ang0, thm);
+            break;
+        case 8:
+            g_disc[0] = Ox;
+            g_disc[1] = Oy;
+            g_disc[2] = Rx;
+            g_disc[3] = Ry;
+            g_disc_calls = 0;
+            S.SetDisc(0, 0, -1, -1);
+            S.SetNewAngProc(disc_proc);
+            ret = S.DenovoBestAngle(best, ang0, hfang, step, thm, true);
+            ret += 10.0 * (g_disc_calls > 0);
+            break;
+        case 9:
+            S.DebugAngs(1, 2, 3, 4, ang0, hfang, step, thm);
             S.RFromAngle(best, ang0, thm);
             break;
         default:

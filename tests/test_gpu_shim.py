@@ -121,3 +121,37 @@ def test_cpp_thmscan_through_shim(tmp_path):
         _thm_compare(g, ref, name)
         if tw is not None and abs(g["A"] - float(ref["A"])) < 1e-9:
             assert np.abs(np.array(g["tptwk"]) - tw).max() <= 1e-6, (name, g, tw)
+
+
+def test_cpp_thmscan_callbacks_and_table(tmp_path):
+    """SetNewAngProc through the drop-in (a C++ callback giving a fixed disc
+    for every angle equals SetDisc with that disc), and DebugAngs' angle
+    table (one line per angle; the row at the centre angle equals
+    RFromAngle there)."""
+    from shim_util import build_thm_check, thm_case, parse_thm_lines
+    exe = build_thm_check(str(tmp_path))
+    d = load_golden("thm_scan")["thm_s0_denovo"]
+    common = dict(pa=d["pa"], va=d["va"], pb=d["pb"], vb=d["vb"], req=int(d["req"]))
+    disc = (0, 5, 12, 12)
+    blob = (thm_case(0, common["pa"], common["va"], common["pb"], common["vb"], common["req"],
+                     disc=disc)
+            + thm_case(8, common["pa"], common["va"], common["pb"], common["vb"],
+                       common["req"], disc=disc)
+            + thm_case(9, common["pa"], common["va"], common["pb"], common["vb"],
+                       common["req"], ang0=-2.0, hfang=1.0, step=0.5))
+    cases = os.path.join(str(tmp_path), "cb_cases.bin")
+    open(cases, "wb").write(blob)
+    out = subprocess.run([exe, cases], capture_output=True, text=True, timeout=600,
+                         cwd=str(tmp_path))
+    assert out.returncode == 0, out.stderr
+    fixed, cb, table = parse_thm_lines(out.stdout)
+    assert cb["ret"] == fixed["ret"] + 10.0   # the callback was called
+    for k in ("A", "X", "Y", "R", "err"):
+        assert cb[k] == fixed[k], (k, cb, fixed)
+    rows = open(os.path.join(str(tmp_path), "angs_1.2^3.4.log")).read().split("\n")
+    assert rows[0].split() == ["Deg", "R", "X", "Y"]
+    vals = [[float(v) for v in r.split()] for r in rows[1:] if r.strip()]
+    assert [round(v[0], 3) for v in vals] == [-3.0, -2.5, -2.0, -1.5, -1.0]
+    mid = vals[2]
+    assert abs(mid[1] - table["R"]) <= 1e-4 and abs(mid[2] - table["X"]) <= 1e-3 and \
+        abs(mid[3] - table["Y"]) <= 1e-3
