@@ -1073,3 +1073,176 @@ extern "C" int aln_thm_call_batch(aln_ctx *ctx, int npairs, const aln_thumbs *th
     }
     return ALN_OK;
 }
+
+// ---------------------------------------------------------------------------
+// MakeThumbs' binning and normalisation (1_DMesh/CThmUtil.cpp:470-523):
+// DecimateVector (0_GEN/Maths.cpp:1315-1364) and Normalize (:192-212)
+// ---------------------------------------------------------------------------
+
+struct DecJob {
+    const void *img;            // device copy of the raster (caller's dtype)
+    const unsigned char *mask;  // device copy of the point mask, or null
+    int dt, w, h, stride;
+    int ow, oh;                 // bin grid
+    double *vals;               // device: bin values [oh][ow]
+    unsigned char *pres;        // device: bin present
+    double sd;
+};
+
+// grid (ceil(max ow / 32), ceil(max oh / 8), n), block (32, 8): one thread
+// per bin sums its points in the point list's (raster) order, as the
+// reference's accumulation visits them; the count is the reference's uint8
+// counter (mod 256).
+__global__ void k_decimate(DecJob *jobs, int lbin)
+{
+    DecJob &J = jobs[blockIdx.z];
+    const int bx = blockIdx.x * 32 + threadIdx.x, by = blockIdx.y * 8 + threadIdx.y;
+    if (bx >= J.ow || by >= J.oh)
+        return;
+    double s = 0.0;
+    int cnt = 0;
+    const int x0 = bx * lbin, y0 = by * lbin;
+    const int x1 = min(J.w, x0 + lbin), y1 = min(J.h, y0 + lbin);
+    for (int y = y0; y < y1; ++y)
+        for (int x = x0; x < x1; ++x) {
+            const long long k = (long long)y * J.stride + x;
+            if (J.mask && !J.mask[k])
+                continue;
+            s = __dadd_rn(s, load_px(J.img, J.dt, k));
+            ++cnt;
+        }
+    cnt &= 255;
+    const long long o = (long long)by * J.ow + bx;
+    J.vals[o] = cnt ? __ddiv_rn(s, (double)cnt) : 0.0;
+    J.pres[o] = cnt != 0;
+}
+
+// Stats (Maths.cpp:132-141, MeanStd) over the present bins in raster order,
+// one thread per image in the reference's operation order (no contraction),
+// then (v - avg) / sd for every present bin.  grid n, block 256.
+__global__ void k_normalize(DecJob *jobs)
+{
+    __shared__ double sh_avg, sh_sd;
+    DecJob &J = jobs[blockIdx.x];
+    const long long nb = (long long)J.ow * J.oh;
+    if (threadIdx.x == 0) {
+        double sum = 0.0, sum2 = 0.0;
+        int n = 0;
+        for (long long k = 0; k < nb; ++k)
+            if (J.pres[k]) {
+                const double v = J.vals[k];
+                sum = __dadd_rn(sum, v);
+                sum2 = __dadd_rn(sum2, __dmul_rn(v, v));
+                ++n;
+            }
+        double avg = sum, sd = 0.0;
+        if (n > 1) {
+            avg = __ddiv_rn(avg, (double)n);
+            const double t = __dsub_rn(sum2, __dmul_rn(__dmul_rn((double)n, avg), avg));
+            sd = __dsqrt_rn(__ddiv_rn(fmax(t, 0.0), __dsub_rn((double)n, 1.0)));
+        }
+        sh_avg = avg;
+        sh_sd = sd;
+        J.sd = sd;
+    }
+    __syncthreads();
+    for (long long k = threadIdx.x; k < nb; k += blockDim.x)
+        if (J.pres[k])
+            J.vals[k] = __ddiv_rn(__dsub_rn(J.vals[k], sh_avg), sh_sd);
+}
+
+extern "C" int aln_decimate_batch(aln_ctx *ctx, int n, const aln_image *in,
+                                  const unsigned char *const *mask, int lbin, int normalize,
+                                  double *const *out_vals, unsigned char *const *out_mask,
+                                  double *out_sd)
+{
+    if (!ctx || n < 0 || (n && (!in || !out_vals || !out_mask)) || lbin < 1)
+        return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
+    if (!n)
+        return ALN_OK;
+    CK(cudaSetDevice(ctx->device));
+    std::vector<DecJob> jobs(n);
+    size_t bytes = 0;
+    int mw = 1, mh = 1;
+    for (int k = 0; k < n; ++k) {
+        const aln_image &I = in[k];
+        if (!I.data || I.w < 1 || I.h < 1 || I.stride < I.w || !dtype_size(I.dtype))
+            return set_err(ctx, ALN_ERR_ARG, "image %d: bad data/size/stride/dtype", k);
+        DecJob &J = jobs[k];
+        J.dt = I.dtype;
+        J.w = I.w;
+        J.h = I.h;
+        J.stride = I.stride;
+        J.ow = (I.w + lbin - 1) / lbin;
+        J.oh = (I.h + lbin - 1) / lbin;
+        mw = std::max(mw, J.ow);
+        mh = std::max(mh, J.oh);
+        const size_t ib = (size_t)I.stride * I.h;
+        bytes += al256(ib * dtype_size(I.dtype)) + (mask && mask[k] ? al256(ib) : 0) +
+                 al256((size_t)J.ow * J.oh * 9);
+    }
+    char *buf = nullptr;
+    {
+        cudaError_t e = cudaMalloc(&buf, bytes + al256((size_t)n * sizeof(DecJob)));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(ctx, ALN_ERR_NOMEM, "decimation buffers: %s", cudaGetErrorString(e));
+        }
+    }
+    cudaStream_t st = ctx->stream;
+    char *p = buf;
+    int rc = ALN_OK;
+    for (int k = 0; k < n && rc == ALN_OK; ++k) {
+        const aln_image &I = in[k];
+        DecJob &J = jobs[k];
+        const size_t ib = (size_t)I.stride * I.h;
+        // host or device sources alike (unified addressing)
+        if (cudaMemcpyAsync(p, I.data, ib * dtype_size(I.dtype), cudaMemcpyDefault, st) !=
+            cudaSuccess)
+            rc = set_err(ctx, ALN_ERR_CUDA, "image %d copy", k);
+        J.img = p;
+        p += al256(ib * dtype_size(I.dtype));
+        J.mask = nullptr;
+        if (mask && mask[k]) {
+            if (cudaMemcpyAsync(p, mask[k], ib, cudaMemcpyDefault, st) != cudaSuccess)
+                rc = set_err(ctx, ALN_ERR_CUDA, "mask %d copy", k);
+            J.mask = (const unsigned char *)p;
+            p += al256(ib);
+        }
+        J.vals = (double *)p;
+        J.pres = (unsigned char *)(p + (size_t)J.ow * J.oh * 8);
+        p += al256((size_t)J.ow * J.oh * 9);
+        J.sd = 0.0;
+    }
+    DecJob *dj = (DecJob *)p;
+    if (rc == ALN_OK &&
+        cudaMemcpyAsync(dj, jobs.data(), (size_t)n * sizeof(DecJob), cudaMemcpyHostToDevice,
+                        st) != cudaSuccess)
+        rc = set_err(ctx, ALN_ERR_CUDA, "job table copy");
+    if (rc == ALN_OK) {
+        LAUNCH(ctx, "k_decimate", k_decimate, dim3((mw + 31) / 32, (mh + 7) / 8, n), dim3(32, 8),
+               0, dj, lbin);
+        if (normalize)
+            LAUNCH(ctx, "k_normalize", k_normalize, n, 256, 0, dj);
+        for (int k = 0; k < n && rc == ALN_OK; ++k) {
+            const size_t nb = (size_t)jobs[k].ow * jobs[k].oh;
+            if (cudaMemcpyAsync(out_vals[k], jobs[k].vals, nb * 8, cudaMemcpyDefault, st) !=
+                    cudaSuccess ||
+                cudaMemcpyAsync(out_mask[k], jobs[k].pres, nb, cudaMemcpyDefault, st) !=
+                    cudaSuccess)
+                rc = set_err(ctx, ALN_ERR_CUDA, "result %d copy", k);
+        }
+        if (rc == ALN_OK && cudaMemcpyAsync(jobs.data(), dj, (size_t)n * sizeof(DecJob),
+                                            cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            rc = set_err(ctx, ALN_ERR_CUDA, "job table read-back");
+    }
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(buf);
+    if (rc != ALN_OK)
+        return rc;
+    CK(cudaGetLastError());
+    if (out_sd)
+        for (int k = 0; k < n; ++k)
+            out_sd[k] = jobs[k].sd;
+    return ALN_OK;
+}

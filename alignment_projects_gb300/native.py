@@ -183,6 +183,10 @@ def lib():
         L.aln_thm_call_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnThumbs),
                                          C.POINTER(AlnThmParams), C.c_int, C.c_void_p,
                                          C.POINTER(AlnThmResult), C.c_void_p, C.c_void_p]
+        L.aln_decimate_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnImage),
+                                         C.POINTER(C.c_void_p), C.c_int, C.c_int,
+                                         C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                         C.c_void_p]
         L.aln_corr_patches_grid.argtypes = [C.POINTER(AlnPair), C.POINTER(C.c_int),
                                             C.POINTER(C.c_int), C.POINTER(C.c_int),
                                             C.POINTER(C.c_int)]
@@ -432,6 +436,36 @@ class Context:
             tw.ctypes.data if tw is not None else None, out, tout.ctypes.data))
         return [{"A": o.A, "X": o.X, "Y": o.Y, "R": o.R, "err": o.err, "ncalls": o.ncalls,
                  "T": list(o.T), "tptwk": tout[k].tolist()} for k, o in enumerate(out)]
+
+    def decimate(self, images, lbin, masks=None, normalize=True) -> list:
+        """MakeThumbs' DecimateVector + Normalize of 2-D arrays (point lists
+        in raster order; masks: per image None or a 0/1 array of the same
+        shape).  Returns [(vals[oh, ow] FP64, present[oh, ow] uint8, sd)]."""
+        images = [np.ascontiguousarray(a) for a in images]
+        n = len(images)
+        ims = (AlnImage * n)()
+        mk = (C.c_void_p * n)()
+        keep = []
+        for k, a in enumerate(images):
+            ims[k] = image(a)
+            m = None if masks is None else masks[k]
+            if m is not None:
+                m = np.ascontiguousarray(m, np.uint8)
+                keep.append(m)
+                mk[k] = m.ctypes.data
+        outs = []
+        ov = (C.c_void_p * n)()
+        om = (C.c_void_p * n)()
+        for k, a in enumerate(images):
+            oh, ow = -(-a.shape[0] // lbin), -(-a.shape[1] // lbin)
+            v = np.empty((oh, ow), np.float64)
+            m = np.empty((oh, ow), np.uint8)
+            outs.append((v, m))
+            ov[k], om[k] = v.ctypes.data, m.ctypes.data
+        sd = np.zeros(n, np.float64)
+        self._check(self._L.aln_decimate_batch(self.h, n, ims, mk, lbin, int(normalize), ov, om,
+                                               sd.ctypes.data))
+        return [(v, m, float(sd[k])) for k, (v, m) in enumerate(outs)]
 
     def thm_call_batch(self, thumbs, op, args, best=None, tptwk=None, **params) -> list:
         """One CThmScan member-function call per pair (THMOP_*; args: 4 per

@@ -386,6 +386,24 @@ int aln_thm_call_batch(aln_ctx *ctx, int npairs, const aln_thumbs *thumbs,
                        const aln_thm_params *params, int op, const double *args,
                        aln_thm_result *best, double *tptwk, double *ret);
 
+/* MakeThumbs' binning and normalisation (1_DMesh/CThmUtil.cpp:470-523):
+ * DecimateVector (0_GEN/Maths.cpp:1315-1364) then, when normalize != 0,
+ * Normalize (Maths.cpp:192-212), for n overlap rasters at once.  Image k
+ * (any dtype, host or device memory) holds the point list in raster order:
+ * the pixels with mask[k][x + stride*y] != 0 (mask NULL or mask[k] NULL:
+ * every pixel), its bounding-box corner at (0, 0).  Output k (host or
+ * device memory): the ceil(w/lbin) x ceil(h/lbin) grid of bin averages
+ * out_vals[k] (FP64, [y][x]) and its presence mask out_mask[k] (1 where the
+ * bin's point count -- a uint8 counter, so taken mod 256 as the reference's
+ * -- is non-zero; absent bins hold 0), normalised to mean 0 and sample sd 1
+ * over the present bins; out_sd[k] (may be NULL) receives that sd (0 with
+ * fewer than two bins).  The numbers are the reference's bit for bit (the
+ * same sums in the same order).  The present bins are the decimated point
+ * list: an aln_thumbs A grid with a_mask = out_mask, or a B raster. */
+int aln_decimate_batch(aln_ctx *ctx, int n, const aln_image *in,
+                       const unsigned char *const *mask, int lbin, int normalize,
+                       double *const *out_vals, unsigned char *const *out_mask, double *out_sd);
+
 /* ---- allocation-free CorrPatches: no counterpart in the reference ---- */
 
 /* Size of the device scratch array behind aln_corr_patches_noalloc. */

@@ -155,3 +155,63 @@ def test_disc_of_angle_callback(ctx):
     assert (cb2["A"], cb2["X"], cb2["Y"], cb2["R"]) == (fixed["A"], fixed["X"], fixed["Y"],
                                                         fixed["R"])
     assert len(seen) == cb2["ncalls"]
+
+
+def _points_raster(pa, va, w, h):
+    """Raster-order point list (integer points, corner (0, 0)) -> image, mask."""
+    img = np.zeros((h, w), np.float64)
+    mask = np.zeros((h, w), np.uint8)
+    x = pa[:, 0].astype(np.int64)
+    y = pa[:, 1].astype(np.int64)
+    img[y, x] = va
+    mask[y, x] = 1
+    return img, mask
+
+
+def _check_decimated(g, xy, v):
+    vals, pres, sd = g
+    ys, xs = np.nonzero(pres)   # row-major: the reference's output order
+    assert np.array_equal(np.stack([xs, ys], 1), xy.astype(np.int64))
+    assert np.array_equal(vals[ys, xs], v)   # bit for bit
+
+
+def test_decimate_golden(ctx):
+    """MakeThumbs' DecimateVector + Normalize on the GPU against the
+    reference's golden output (the same sums in the same order: bitwise)."""
+    d = load_golden("decimate")["dec8"]
+    w, h, lbin = int(d["w"]), int(d["h"]), int(d["lbin"])
+    # the fixture's point list is in raster order
+    order = np.lexsort((d["pa"][:, 0], d["pa"][:, 1]))
+    assert np.array_equal(order, np.arange(len(order)))
+    img, mask = _points_raster(d["pa"], d["va"], w, h)
+    g = ctx.decimate([img], lbin, masks=[mask])[0]
+    _check_decimated(g, d["xy"], d["v"])
+
+
+@pytest.mark.parametrize("dt,lbin,masked", [(np.uint8, 8, False), (np.uint8, 8, True),
+                                            (np.uint16, 4, True), (np.float32, 8, False),
+                                            (np.float64, 5, True), (np.uint8, 16, False)])
+def test_decimate_matches_oracle(ctx, orc, dt, lbin, masked):
+    """Integer and float rasters, masks of any shape, ragged edge bins, and
+    lbin 16 (a full bin's 256 points wrap the reference's uint8 counter to 0:
+    the bin is dropped, as there)."""
+    rng = np.random.default_rng(lbin * 10 + masked)
+    h, w = 197, 261
+    if dt in (np.uint8, np.uint16):
+        img = rng.integers(0, 256 if dt == np.uint8 else 4096, (h, w)).astype(dt)
+    else:
+        img = rng.standard_normal((h, w)).astype(dt)
+    mask = None
+    if masked:
+        yy, xx = np.mgrid[0:h, 0:w]
+        mask = (((xx - 120) ** 2 + (yy - 90) ** 2) < 95 ** 2).astype(np.uint8)
+    ys, xs = np.nonzero(mask if mask is not None else np.ones((h, w), np.uint8))
+    pa = np.stack([xs, ys], 1).astype(np.float64)
+    va = img[ys, xs].astype(np.float64)
+    xy, v = orc.decimate_normalize(pa, va, w, h, lbin)
+    g = ctx.decimate([img], lbin, masks=[mask])[0]
+    _check_decimated(g, xy, v)
+    # a batch of several images gives each its own numbers
+    gb = ctx.decimate([img, img[:100, :150]], lbin, masks=None if mask is None
+                      else [mask, mask[:100, :150]])
+    assert np.array_equal(gb[0][0], g[0]) and np.array_equal(gb[0][1], g[1])
