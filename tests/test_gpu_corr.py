@@ -253,6 +253,9 @@ def test_segmented_columns(ctx, orc, ns):
     for seed in range(40, 48):
         a8, b8, ox, oy, radius = _disc_case(seed)
         lg_o = oracle.legal(oracle.RGN_MIN, 8, 8, 0)
+        if seed % 2:   # FP64 rasters: the FP64 r formula on segmented columns
+            a8 = a8.astype(np.float64) / 7.0 + 0.25
+            b8 = b8.astype(np.float64) / 7.0 - 0.5
         jobs.append(dict(a=a8, b=b8, ox=ox, oy=oy, radius=radius, legal=aln_legal(lg_o)))
         A, VA = oracle.image_to_points(a8)
         B, VB = oracle.image_to_points(b8)

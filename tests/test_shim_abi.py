@@ -148,3 +148,26 @@ def test_reference_thmscan_caller_links_against_shim(tmp_path):
     from shim_util import build_thm_check
     exe = build_thm_check(str(tmp_path), reference_headers=_reference_tree())
     assert os.path.exists(exe)
+
+
+def test_thmscan_rejects_fractional_a_points(tmp_path):
+    """The CThmScan drop-in bins thumbnail A on integer pixels; a ThmRec whose
+    A points are fractional is refused on the host (logged, R = 0) before any
+    GPU call, so this runs here without a GPU."""
+    import sys
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from shim_util import build_thm_check, thm_case, parse_thm_lines
+    exe = build_thm_check(str(tmp_path))
+    rng = np.random.default_rng(0)
+    pa = rng.random((50, 2)) * 20.0          # fractional
+    pb = np.stack(np.meshgrid(np.arange(20.0), np.arange(20.0)), -1).reshape(-1, 2)
+    cases = os.path.join(str(tmp_path), "frac.bin")
+    open(cases, "wb").write(thm_case(1, pa, rng.random(50), pb, rng.random(len(pb)), 10,
+                                     ang0=1.5))
+    log = os.path.join(str(tmp_path), "frac.log")
+    out = subprocess.run([exe, cases, log], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    g = parse_thm_lines(out.stdout)[0]
+    assert (g["A"], g["R"], g["X"], g["Y"]) == (1.5, 0.0, 0.0, 0.0)
+    assert "integer pixels" in open(log).read()
