@@ -128,3 +128,35 @@ def test_decimate_golden(orc):
                                    int(d["lbin"]))
     assert np.array_equal(xy, d["xy"])
     assert np.abs(v - d["v"]).max() <= 1e-12
+
+
+@pytest.mark.parametrize("lbin,masked", [(8, False), (8, True), (5, True), (16, False)])
+def test_decimate_against_reference_build(lbin, masked):
+    """DecimateVector + Normalize: the restatement against the reference's
+    own build on raster-order point lists, incl. lbin 16 (full bins wrap the
+    reference's uint8 counter to 0 and are dropped) -- bitwise."""
+    import oracle
+    if not oracle.ref_available():
+        try:
+            oracle.build_ref()
+        except Exception:
+            pass
+    if not oracle.ref_available():
+        pytest.skip("the reference's own build exists only where its sources are mounted")
+    orc, ref = oracle.Oracle(), oracle.Ref()
+    rng = np.random.default_rng(lbin + 100 * masked)
+    h, w = 133, 171
+    img = rng.integers(0, 256, (h, w)).astype(np.float64)
+    keep = np.ones((h, w), bool)
+    if masked:
+        yy, xx = np.mgrid[0:h, 0:w]
+        keep = ((xx - 80) ** 2 + (yy - 60) ** 2) < 70 ** 2
+    ys, xs = np.nonzero(keep)
+    pts = np.stack([xs, ys], 1).astype(np.float64)
+    vals = img[ys, xs]
+    xo, vo = orc.decimate_normalize(pts, vals, w, h, lbin)
+    xr, vr = ref.decimate_normalize(pts, vals, w, h, lbin)
+    assert np.array_equal(xo, xr)
+    assert np.array_equal(vo, vr)
+    if lbin == 16:   # a full 16 x 16 bin is dropped
+        assert len(xr) < (-(-w // 16)) * (-(-h // 16))
