@@ -1105,7 +1105,9 @@ static void prof_collect(aln_ctx *c)
         prof_end(c);                                                                 \
     } while (0)
 
-static char g_create_err[512];
+// errors of calls made without a context (aln_ctx_create, the planning
+// query, the allocation-free entry point): one message per host thread
+static thread_local char g_create_err[512];
 
 static int set_err(aln_ctx *c, int code, const char *fmt, ...)
 {

@@ -113,8 +113,9 @@ typedef struct aln_ctx aln_ctx;
  * (the reference's state is the static mutex_fft, 0_GEN/Correlation.cpp:26-27). */
 int aln_ctx_create(int device, aln_ctx **out);
 void aln_ctx_destroy(aln_ctx *ctx);
-/* Message of the last hard error on this context (or of the last failed
- * aln_ctx_create when ctx is NULL). */
+/* Message of the last hard error on this context (or, when ctx is NULL, of
+ * the calling thread's last failed call made without a context:
+ * aln_ctx_create, aln_corr_patches_grid, aln_corr_patches_noalloc). */
 const char *aln_last_error(const aln_ctx *ctx);
 
 /* Upper bound on the device workspace one batch chunk may use (default
