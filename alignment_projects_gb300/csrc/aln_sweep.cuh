@@ -1160,6 +1160,8 @@ extern "C" int aln_decimate_batch(aln_ctx *ctx, int n, const aln_image *in,
         return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
     if (!n)
         return ALN_OK;
+    if (n > 65535)   // one grid z index per image
+        return set_err(ctx, ALN_ERR_ARG, "at most 65535 images per call (%d)", n);
     CK(cudaSetDevice(ctx->device));
     std::vector<DecJob> jobs(n);
     size_t bytes = 0;

@@ -400,7 +400,8 @@ int aln_thm_call_batch(aln_ctx *ctx, int npairs, const aln_thumbs *thumbs,
  * over the present bins; out_sd[k] (may be NULL) receives that sd (0 with
  * fewer than two bins).  The numbers are the reference's bit for bit (the
  * same sums in the same order).  The present bins are the decimated point
- * list: an aln_thumbs A grid with a_mask = out_mask, or a B raster. */
+ * list: an aln_thumbs A grid with a_mask = out_mask, or a B raster.  At most
+ * 65535 images per call. */
 int aln_decimate_batch(aln_ctx *ctx, int n, const aln_image *in,
                        const unsigned char *const *mask, int lbin, int normalize,
                        double *const *out_vals, unsigned char *const *out_mask, double *out_sd);
