@@ -1659,7 +1659,9 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
                 if (pol > 0 && ns != pol)
                     continue;
                 const int B = ns - Wy + 1;
-                if (B < 1)
+                // the lag kernels key a negative lag row y by y + NS (its
+                // storage row): that must stay >= 0 for the window's rows
+                if (B < 1 || ns <= -d.ylo)
                     continue;
                 const int nseg = (d.h[0] + B - 1) / B;
                 if (nseg > 64)

@@ -212,6 +212,34 @@ def test_disc_on_smaller_grid(ctx, orc, seed):
     assert_parity(g, o, f"disc seed {seed}")
 
 
+@pytest.mark.parametrize("seed", range(8))
+def test_disc_far_from_zero_lag(ctx, orc, seed):
+    """Discs around large offsets (overlap strips cut with a big nominal
+    shift): the window's lag rows lie far from the zero lag, where the
+    storage rows of negative lags wrap; peaks and r equal the oracle's."""
+    import oracle
+    rng = np.random.default_rng(300 + seed)
+    w, h = int(rng.integers(30, 70)), int(rng.integers(250, 420))
+    f = rng.normal(0.0, 1.0, (2 * h, w + 40))
+    for ax in (0, 1):
+        f = (f + np.roll(f, 1, ax) + np.roll(f, 2, ax)) / 3.0
+    ty = int(rng.integers(h // 4, h // 2)) * (1 if seed % 2 else -1)
+    tx = int(rng.integers(-8, 9))
+    y0 = h // 2 + 10
+    a = f[y0:y0 + h, 20:20 + w]
+    b = f[y0 + ty:y0 + ty + h, 20 + tx:20 + tx + w] + rng.normal(0.0, 0.1, (h, w))
+    a8 = np.clip(np.round(128 + 40 * a), 0, 255).astype(np.uint8)
+    b8 = np.clip(np.round(128 + 40 * b), 0, 255).astype(np.uint8)
+    ox, oy, radius = -tx + int(rng.integers(-4, 5)), -ty + int(rng.integers(-4, 5)), 12
+    lg_o = oracle.legal(oracle.RGN_MIN, 8, 8, 0)
+    g = ctx.corr_patches(a8, b8, ox, oy, radius, aln_legal(lg_o))
+    A, VA = oracle.image_to_points(a8)
+    B, VB = oracle.image_to_points(b8)
+    o = orc.corr_patches(A, VA, B, VB, ox, oy, radius, lg_o)
+    assert_parity(g, o, f"far disc seed {seed}")
+    assert (g["peak_x"], g["peak_y"]) == (-tx, -ty)
+
+
 def test_disc_grids_shrink_and_batch(ctx):
     """The same disc cases in one batch (several transform grids) give the
     single-call numbers, and most of them run on a smaller grid."""

@@ -103,3 +103,45 @@ def test_some_plans_are_segmented():
     import alignment_projects_gb300 as aln
     keep = []
     assert aln.corr_patches_grid(_pair(40, 500, 40, 500, 0, 0, 10, keep))[2] > 0
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_tie_order_matches_reference_raster(seed):
+    """Ties between lags go to the first in the reference raster's row-major
+    storage order (Correlation.cpp:1040-1070); the kernels key each lag by
+    its storage index on the transform grid (ys * nx + xs, negative lags
+    wrapped by the grid size, or the segment length).  Over the disc window
+    both orders are the same."""
+    import alignment_projects_gb300 as aln
+    rng = np.random.default_rng(100 + seed)
+    w0, w1 = (int(v) for v in rng.integers(10, 120, 2))
+    h0, h1 = (int(v) for v in rng.integers(10, 600, 2))
+    ox, oy = (int(v) for v in rng.integers(-40, 41, 2))
+    if seed % 4 == 1:   # discs far from the zero lag (long strips, big offsets)
+        oy = -int(rng.integers(h0 // 4 + 1, h0 // 2 + 2))
+    if seed % 4 == 3:
+        oy = int(rng.integers(h1 // 4 + 1, h1 // 2 + 2))
+    rad = int(rng.integers(1, 60))
+    keep = []
+    nx, ny, nseg, tr = aln.corr_patches_grid(_pair(w0, h0, w1, h1, ox, oy, rad, keep))
+    if nx == 0:
+        return
+    if tr:
+        w0, h0, w1, h1, ox, oy = h0, w0, h1, w1, oy, ox
+    rnx, rny = aln.lib().aln_fft_size(w0, w1), aln.lib().aln_fft_size(h0, h1)
+    xlo, xhi, ylo, yhi = _window(w0, h0, w1, h1, ox, oy, rad)
+    if xlo > xhi or ylo > yhi:
+        return
+
+    def key(x, y, mx, my):   # the kernels' form: one wrap of negative lags
+        return ((y + my) if y < 0 else y) * mx + ((x + mx) if x < 0 else x)
+
+    lags = [(x, y) for y in range(ylo, yhi + 1) for x in range(xlo, xhi + 1)]
+    ours = np.array([key(x, y, nx, ny) for x, y in lags])
+    ref = np.array([key(x, y, rnx, rny) for x, y in lags])
+    assert ours.min() >= 0 and ref.min() >= 0
+    assert np.array_equal(np.argsort(ours, kind="stable"), np.argsort(ref, kind="stable"))
+    # k_final's decode of a storage index back to the lag
+    for (x, y), k in zip(lags, ours):
+        ys, xs = divmod(int(k), nx)
+        assert ((xs - nx) if xs > xhi else xs, (ys - ny) if ys > yhi else ys) == (x, y)
