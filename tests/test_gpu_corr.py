@@ -220,12 +220,12 @@ def test_disc_far_from_zero_lag(ctx, orc, seed):
     import oracle
     rng = np.random.default_rng(300 + seed)
     w, h = int(rng.integers(30, 70)), int(rng.integers(250, 420))
-    f = rng.normal(0.0, 1.0, (2 * h, w + 40))
+    f = rng.normal(0.0, 1.0, (3 * h, w + 40))
     for ax in (0, 1):
         f = (f + np.roll(f, 1, ax) + np.roll(f, 2, ax)) / 3.0
     ty = int(rng.integers(h // 4, h // 2)) * (1 if seed % 2 else -1)
     tx = int(rng.integers(-8, 9))
-    y0 = h // 2 + 10
+    y0 = h
     a = f[y0:y0 + h, 20:20 + w]
     b = f[y0 + ty:y0 + ty + h, 20 + tx:20 + tx + w] + rng.normal(0.0, 0.1, (h, w))
     a8 = np.clip(np.round(128 + 40 * a), 0, 255).astype(np.uint8)
