@@ -145,3 +145,40 @@ def test_tie_order_matches_reference_raster(seed):
     for (x, y), k in zip(lags, ours):
         ys, xs = divmod(int(k), nx)
         assert ((xs - nx) if xs > xhi else xs, (ys - ny) if ys > yhi else ys) == (x, y)
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_column_rows_decode_to_window_lags(seed):
+    """k2_corrcol (one column transform) keeps storage row ys as the lag
+    y = ys - Ny when ys >= Ny - (h0 - 1), else y = ys, and stores it when y
+    is in the window: on the plan's grid every window lag comes from exactly
+    its own storage row."""
+    import alignment_projects_gb300 as aln
+    rng = np.random.default_rng(500 + seed)
+    w0, w1 = (int(v) for v in rng.integers(10, 120, 2))
+    h0, h1 = (int(v) for v in rng.integers(10, 600, 2))
+    ox, oy = (int(v) for v in rng.integers(-40, 41, 2))
+    if seed % 3 == 1:
+        oy = -int(rng.integers(h0 // 4 + 1, h0 // 2 + 2))
+    if seed % 3 == 2:
+        oy = int(rng.integers(h1 // 4 + 1, h1 // 2 + 2))
+    rad = int(rng.integers(1, 60))
+    keep = []
+    P = _pair(w0, h0, w1, h1, ox, oy, rad, keep)
+    P.b_key = 7   # keyed: one column transform per column
+    nx, ny, nseg, tr = aln.corr_patches_grid(P)
+    assert nseg == 0
+    if nx == 0:
+        return
+    if tr:
+        w0, h0, w1, h1, ox, oy = h0, w0, h1, w1, oy, ox
+    xlo, xhi, ylo, yhi = _window(w0, h0, w1, h1, ox, oy, rad)
+    got = {}
+    for ys in range(ny):
+        y = ys - ny if ys >= ny - (h0 - 1) else ys
+        if ylo <= y <= yhi:
+            assert y not in got
+            got[y] = ys
+    assert sorted(got) == list(range(ylo, yhi + 1))
+    for y, ys in got.items():
+        assert ys == y % ny
