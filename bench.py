@@ -220,28 +220,14 @@ def dram_model_per_pair(grid, e=1, wy=129):
     once): k2_rowfft reads both strips and writes both row spectra T (rows < h
     only); k2_corrcol and k2_corrseg read both T and write the window rows Q
     (k2_corrseg's re-reads of b's rows shared by neighbouring segments come
-    from L2); k2_lagrow reads Q.  Checked against ncu dram__bytes
-    (profiles/k2_corrcol_montage.md, profiles/k2_corrseg_montage.md)."""
+    from L2); k2_lagrow reads Q.  Checked against ncu dram__bytes (the
+    committed ncu summaries of k2_corrcol and k2_corrseg)."""
     ws, hs, Nx, Ny, nseg = grid
     L1 = Nx // 2 + 1
     cols = 16 * L1 * hs + 8 * L1 * wy
     return {"k2_rowfft": 2 * ws * hs * e + 16 * L1 * hs,
             "k2_corrseg" if nseg else "k2_corrcol": cols,
             "k2_lagrow": 8 * L1 * wy}
-
-
-def read_traffic(kernel):
-    """DRAM bytes per pair for `kernel` from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "montage_strips_kernels.md")
-    if not os.path.exists(path):
-        return None
-    for ln in open(path):
-        if ln.startswith("traffic_per_pair ") and kernel in ln:
-            try:
-                return float(ln.split()[-1])
-            except ValueError:
-                return None
-    return None
 
 
 # ---------------------------------------------------------------------------
