@@ -10,12 +10,20 @@ aln_corr_patches_batch.
   value   pairs/s with the strips already resident in HBM (device pointers)
   e2e     pairs/s through the same C-ABI call with pinned HOST buffers:
           host-to-device copies and the result read-back inside the timed region
-  plain   the one-pair-per-call path (aln_corr_patches, host buffers) on a
-          sample of the same pairs: pairs/s and p50/p99 latency
-  roofline  dominant kernel: algorithmic bytes / CUDA-event duration against
-          the measured HBM copy bandwidth
+  plain   the one-pair-per-call path (aln_corr_patches) on a sample of the
+          same pairs: pairs/s and p50/p99 latency, with host buffers and with
+          device-resident inputs (like for like with `value` and `e2e`)
+  roofline  dominant kernel: the DRAM bytes one launch moves (the per-pair
+          model checked against ncu dram__bytes) / its CUDA-event duration,
+          against the measured HBM copy bandwidth; beside it the FP32 issue
+          figure (counted FFT / product flops against the SMs' FMA peak at
+          the sampled clock) and the canonical two-pass FFT count
   cpu_baseline  the oracle (FP64 C restatement of the reference) on the host
           cores, on a bounded sample of the same pairs
+  configs the other workloads in bounded time, each with its parity table
+          against the oracle: c1 plain 512^2 pairs, c3 the thumbnail angle
+          sweep, c4 the uneven uint16 batch, c5 the served request stream
+          (--no-extras leaves them out)
 
 --impl reference times the reference algorithm's CPU implementation (the
 oracle port; the reference's own compiled code exists only where its source
@@ -59,6 +67,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=128)
     ap.add_argument("--parity-sample", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="montage line only (no c1/c3/c4/c5 figures)")
     ap.add_argument("--workload", default="montage",
                     choices=["montage", "sweep", "served", "uneven"],
                     help="montage: the strip batch (default); sweep: the thumbnail angle "
@@ -69,6 +79,7 @@ def parse():
     ap.add_argument("--served-strips", type=int, default=512)
     ap.add_argument("--served-groups", type=int, default=32)
     ap.add_argument("--uneven-pairs", type=int, default=20000)
+    ap.add_argument("--c1-pairs", type=int, default=64)
     return ap.parse_args()
 
 
@@ -228,6 +239,47 @@ def dram_model_per_pair(grid, e=1, wy=129):
     return {"k2_rowfft": 2 * ws * hs * e + 16 * L1 * hs,
             "k2_corrseg" if nseg else "k2_corrcol": cols,
             "k2_lagrow": 8 * L1 * wy}
+
+
+def fft_flops(n):
+    """Flops of one complex FFT of n points, the standard 5 n log2 n count."""
+    return 5.0 * n * max(1, int(n).bit_length() - 1)
+
+
+def flops_per_pair(grid, wy=129):
+    """FP32 flops per pair of the fused FFT kernels (5 n log2 n per complex
+    transform, 6 per complex product plus 2 to accumulate it, a real
+    transform of n points as a complex one of n/2 plus n/2 split butterflies
+    of 10 flops).  Row pass: both images' h rows.  Columns: per column of the
+    L+1 spectrum columns, 2 nseg segment transforms of NS points, nseg
+    products and one inverse (unsegmented: 2 forward and 1 inverse of Ny).
+    Lag rows: one inverse real transform per window row."""
+    ws, hs, Nx, Ny, nseg = grid
+    L = Nx // 2
+    real_fft = fft_flops(L) + 10.0 * L
+    rows = 2 * hs * real_fft
+    if nseg:
+        cols = (L + 1) * ((2 * nseg + 1) * fft_flops(Ny) + 8.0 * nseg * Ny)
+    else:
+        cols = (L + 1) * (3 * fft_flops(Ny) + 8.0 * Ny)
+    return {"k2_rowfft": rows, "k2_corrseg" if nseg else "k2_corrcol": cols,
+            "k2_lagrow": wy * real_fft}
+
+
+def fp32_peak_tflops(sm_mhz, sms=152):
+    """FP32 FMA issue peak: SMs x 128 lanes x 2 flops x clock."""
+    return sms * 128 * 2 * sm_mhz * 1e6 / 1e12
+
+
+def fp32_block(flops, seconds, clocks):
+    """Counted FP32 flops over `seconds` against the FMA peak at the median
+    SM clock sampled in the timed region (max clock if none was sampled)."""
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz") or 2070.0
+    peak = fp32_peak_tflops(mhz)
+    ach = flops / seconds / 1e12 if seconds > 0 else 0.0
+    return {"flops": flops, "achieved_tflops": ach, "peak_tflops": peak,
+            "frac": ach / peak, "sm_mhz": mhz,
+            "accounting": "5 n log2 n per complex transform, 8 per accumulated product"}
 
 
 # ---------------------------------------------------------------------------
@@ -401,24 +453,29 @@ def run_gpu(args):
         grid_hist[key] = grid_hist.get(key, 0) + 1
         rk = "%dx%d" % fft_shape(g[0], g[1], g[0], g[1])
         ref_hist[rk] = ref_hist.get(rk, 0) + 1
-    alg_total = sum(alg_bytes_per_pair(g).get(dom, 0) for g in grids)
-    alg_per_launch = alg_total * args.steps / max(1, dom_launches)
-    achieved = alg_per_launch / (dom_ms / dom_launches / 1000.0) / 1e9
+    launch_s = dom_ms / dom_launches / 1000.0
+    per_launch = args.steps / max(1, dom_launches)
+    alg_per_launch = sum(alg_bytes_per_pair(g).get(dom, 0) for g in grids) * per_launch
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
         peak = json.load(open(peaks_path))["hbm_gbs"]
         peak_src = "measured"
     else:
         peak, peak_src = 6800.0, "fallback"
-    traffic = sum(dram_model_per_pair(g).get(dom, 0)
-                  for g in grids) * args.steps / max(1, dom_launches)
-    # the FFT passes together (row, column and inverse passes, with the
-    # product): counted bytes over the three kernels' summed time
+    # DRAM bytes one launch of the dominant kernel moves (each array read or
+    # written once; the model is checked against ncu dram__bytes)
+    traffic = sum(dram_model_per_pair(g).get(dom, 0) for g in grids) * per_launch
+    achieved = traffic / launch_s / 1e9
+    flops_launch = sum(flops_per_pair(g).get(dom, 0) for g in grids) * per_launch
+    # the FFT passes together (row, column and inverse passes with the
+    # product), on the same DRAM accounting, over the kernels' summed time
     fft_k = ("k2_rowfft", "k2_corrcol", "k2_corrseg", "k2_lagrow")
     fft_ms = sum(ours[k][1] for k in fft_k if k in ours)
-    fft_bytes = sum(sum(alg_bytes_per_pair(g).get(k, 0) for k in fft_k)
+    fft_dram = sum(sum(dram_model_per_pair(g).get(k, 0) for k in fft_k)
+                   for g in grids) * args.steps
+    fft_flops = sum(sum(flops_per_pair(g).get(k, 0) for k in fft_k)
                     for g in grids) * args.steps
-    fft_gbs = fft_bytes / (fft_ms / 1000.0) / 1e9 if fft_ms > 0 else None
+    fft_gbs = fft_dram / (fft_ms / 1000.0) / 1e9 if fft_ms > 0 else None
 
     # ---- end to end through the C ABI with pinned host buffers -------------
     # host strips in one pinned buffer, pair after pair (a, b), as a tile
@@ -505,6 +562,17 @@ def run_gpu(args):
             assert rc >= 0
         lat_ms = sorted(1000.0 * x for x in lat[1:])
         plain_pps = len(lat_ms) / (sum(lat_ms) / 1000.0)
+        # the same calls with device-resident inputs (like for like with value)
+        lat_d = []
+        for k in range(min(args.plain_sample, n)):
+            ia, ib = arr_d[k].a, arr_d[k].b
+            t0 = time.perf_counter()
+            rc = L.aln_corr_patches(ctx.h, C.byref(ia), C.byref(ib), 0, 0, 64, C.byref(lg),
+                                    C.byref(r))
+            lat_d.append(time.perf_counter() - t0)
+            assert rc >= 0
+        lat_d_ms = sorted(1000.0 * x for x in lat_d[1:])
+        plain_dev_pps = len(lat_d_ms) / (sum(lat_d_ms) / 1000.0)
 
         # ---- parity on a sample: batch result vs the oracle ------------------
         parity = None
@@ -552,14 +620,21 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic,
-                         "traffic_source": "per-pair DRAM model checked against ncu "
-                                           "dram__bytes (profiles/)",
-                         "alg_bytes_per_launch": alg_per_launch,
+                         "accounting": "achieved = DRAM bytes per launch (each array read "
+                                       "or written once: the per-pair model, checked against "
+                                       "ncu dram__bytes in profiles/) / CUDA-event launch time",
                          "avg_launch_ms": dom_ms / dom_launches,
-                         "accounting": "canonical two-pass FFT bytes (one read + one write "
-                                       "per 1D pass); the fused kernels move less",
-                         "fft_passes": {"kernels": list(fft_k), "achieved": fft_gbs,
-                                        "frac": fft_gbs / peak if fft_gbs else None}},
+                         "fp32": fp32_block(flops_launch, launch_s, clocks),
+                         "canonical_equiv_gbs": alg_per_launch / launch_s / 1e9,
+                         "canonical_note": "the canonical two-pass FFT count (one read + one "
+                                           "write of the array per 1D pass, on the transforms "
+                                           "made) over the same time; the fused kernels keep "
+                                           "those passes in registers and shared memory, so "
+                                           "this is not a DRAM figure",
+                         "fft_passes": {"kernels": list(fft_k), "dram_gbs": fft_gbs,
+                                        "frac": fft_gbs / peak if fft_gbs else None,
+                                        "fp32": fp32_block(fft_flops, fft_ms / 1000.0,
+                                                           clocks)}},
             "cpu_baseline": cpu,
             "clocks": clocks,
             "gpu_launches": launches,
@@ -570,19 +645,164 @@ def run_gpu(args):
             "h2d_copies_per_step": cnt["h2d_copies"] / args.steps,
             "plain": {"pairs_per_s": plain_pps, "p50_ms": lat_ms[len(lat_ms) // 2],
                       "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))],
-                      "sample": len(lat_ms)},
-            "batched_over_plain": value / plain_pps,
+                      "sample": len(lat_ms), "inputs": "host buffers (copies in each call)"},
+            "plain_device": {"pairs_per_s": plain_dev_pps,
+                             "p50_ms": lat_d_ms[len(lat_d_ms) // 2],
+                             "p99_ms": lat_d_ms[min(len(lat_d_ms) - 1,
+                                                    int(0.99 * len(lat_d_ms)))],
+                             "sample": len(lat_d_ms), "inputs": "device-resident"},
+            "batched_over_plain": {"device_inputs": value / plain_dev_pps,
+                                   "host_inputs": e2e_value / plain_pps},
             "batch_latency_ms": ms_dev / args.steps,
             "parity": parity,
             "truth": {"found": truth_ok, "of": n - len(decoys), "decoys_rejected": rejected,
                       "decoys": len(decoys)},
             "host_vs_device_inputs_identical": same,
         }
-        print(json.dumps(line), flush=True)
     ctx.close()
+    del batch, pinned, host_bufs, arr_h, arr_d
+    torch.cuda.empty_cache()
+    if line is not None:
+        if not args.no_extras:
+            line["configs"] = extras(args, local)
+        print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+# ---------------------------------------------------------------------------
+# the other configs in bounded time, embedded in the montage line
+# ---------------------------------------------------------------------------
+
+def c1_plain(args, local):
+    """BASELINE config 1: 512^2 uint8 pairs (FFT 1024^2, full lag window,
+    olap >= 32 x 32) through the plain one-pair-per-call path (host and
+    device inputs) and as one batch; parity and the CPU port on the host
+    cores for the same pairs."""
+    import ctypes as C
+    import torch
+    import alignment_projects_gb300 as aln
+    import oracle as O
+    from alignment_projects_gb300 import synth
+    from alignment_projects_gb300.native import AlnPair, AlnResult
+    dev = torch.device("cuda", local)
+    L = aln.lib()
+    ctx = aln.Context(local)
+    pairs = [synth.plain_pair(100 + k, n=512, margin=64) for k in range(args.c1_pairs)]
+    lg = aln.legal(aln.RGN_MIN, 32, 32, 0)
+    dts = [(torch.from_numpy(p.a).to(dev), torch.from_numpy(p.b).to(dev)) for p in pairs]
+    torch.cuda.synchronize()
+    r = AlnResult()
+    lat_h, lat_d = [], []
+    for k, p in enumerate(pairs):
+        ia, ib = aln.image(p.a), aln.image(p.b)
+        t0 = time.perf_counter()
+        assert L.aln_corr_patches(ctx.h, C.byref(ia), C.byref(ib), 0, 0, 4096, C.byref(lg),
+                                  C.byref(r)) >= 0
+        lat_h.append(time.perf_counter() - t0)
+        da, db = dts[k]
+        ia = aln.native.AlnImage(da.data_ptr(), aln.U8, 512, 512, 512, 0, 0, 1)
+        ib = aln.native.AlnImage(db.data_ptr(), aln.U8, 512, 512, 512, 0, 0, 1)
+        t0 = time.perf_counter()
+        assert L.aln_corr_patches(ctx.h, C.byref(ia), C.byref(ib), 0, 0, 4096, C.byref(lg),
+                                  C.byref(r)) >= 0
+        lat_d.append(time.perf_counter() - t0)
+    arr = (AlnPair * len(pairs))()
+    for k, p in enumerate(pairs):
+        da, db = dts[k]
+        arr[k].a = aln.native.AlnImage(da.data_ptr(), aln.U8, 512, 512, 512, 0, 0, 1)
+        arr[k].b = aln.native.AlnImage(db.data_ptr(), aln.U8, 512, 512, 512, 0, 0, 1)
+        arr[k].radius = 4096
+        arr[k].legal = lg
+    out = (AlnResult * len(pairs))()
+    L.aln_corr_patches_batch(ctx.h, len(pairs), arr, out)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    reps = 3
+    for _ in range(reps):
+        assert L.aln_corr_patches_batch(ctx.h, len(pairs), arr, out) >= 0
+    e1.record()
+    torch.cuda.synchronize()
+    batch_pps = reps * len(pairs) / (e0.elapsed_time(e1) / 1000.0)
+    ctx.close()
+
+    def pct(v, q):
+        v = sorted(1000.0 * x for x in v[1:])
+        return v[min(len(v) - 1, int(q * len(v)))]
+    res = {"workload": "512^2 uint8 pairs of the synthetic EM field, offsets U{-64..64}^2, "
+                       "noise 8 DN; CorrPatches, full window, olap >= 32 x 32; FFT 1024^2",
+           "pairs": len(pairs),
+           "plain_host": {"pairs_per_s": (len(lat_h) - 1) / sum(lat_h[1:]),
+                          "p50_ms": pct(lat_h, 0.5), "p99_ms": pct(lat_h, 0.99)},
+           "plain_device": {"pairs_per_s": (len(lat_d) - 1) / sum(lat_d[1:]),
+                            "p50_ms": pct(lat_d, 0.5), "p99_ms": pct(lat_d, 0.99)},
+           "batched_device_pairs_per_s": batch_pps,
+           "truth": sum(1 for k, p in enumerate(pairs)
+                        if (out[k].peak_x, out[k].peak_y) == p.truth)}
+    if not args.no_cpu:
+        import concurrent.futures as cf
+        orc = O.Oracle()
+        lo = O.legal(O.RGN_MIN, 32, 32, 0)
+        prep = []
+        for p in pairs[:args.parity_sample]:
+            A, VA = O.image_to_points(p.a)
+            B, VB = O.image_to_points(p.b)
+            prep.append((A, VA, B, VB))
+        threads = host_threads()
+
+        def one(t):
+            t0 = time.perf_counter()
+            o = orc.corr_patches(t[0], t[1], t[2], t[3], 0, 0, 4096, lo)
+            return o, time.perf_counter() - t0
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+            got = list(ex.map(one, prep))
+        wall = time.perf_counter() - t0
+        per = sorted(1000.0 * g[1] for g in got)
+        res["cpu_baseline"] = {"value": len(prep) / wall, "unit": "pairs/s", "cores": threads,
+                               "kind": "port", "p50_ms_one_core": per[len(per) // 2],
+                               "p99_ms_one_core": per[min(len(per) - 1, int(0.99 * len(per)))],
+                               "sample": "%d pairs" % len(prep)}
+        res["parity"] = corr_parity([out[k] for k in range(len(prep))], [g[0] for g in got])
+    return res
+
+
+def corr_parity(gpu, orc_outs):
+    """CorrPatches parity table: integer peak equal wherever the oracle's
+    top-two margin exceeds 1e-3, max |dr|, max sub-pixel difference."""
+    ok = chk = 0
+    dr = dp = 0.0
+    for g, o in zip(gpu, orc_outs):
+        dr = max(dr, abs(g.r - o["r"]))
+        if o["status"] == 0 and o["r"] - o["second"] > 1e-3:
+            chk += 1
+            ok += (g.peak_x, g.peak_y) == (o["bigx"], o["bigy"])
+            dp = max(dp, abs(g.dx - o["dx"]), abs(g.dy - o["dy"]))
+    return {"pairs": len(orc_outs), "peak_checked": chk, "peak_exact": ok,
+            "max_abs_dr": dr, "max_abs_dsubpix": dp}
+
+
+def extras(args, local):
+    """c1, c3, c4 and c5 in bounded time (rank 0 of the montage run)."""
+    import copy
+    out = {}
+    sub = copy.copy(args)
+    sub.steps = min(args.steps, 3)
+    sub.warmup = min(args.warmup, 3)
+    for name, fn in (("c1_plain", lambda: c1_plain(sub, local)),
+                     ("c3_sweep", lambda: run_sweep(sub, embedded=True)),
+                     ("c4_uneven", lambda: run_uneven(sub, embedded=True)),
+                     ("c5_served", lambda: run_served(sub, embedded=True))):
+        t0 = time.perf_counter()
+        try:
+            out[name] = fn()
+        except Exception as e:   # a failing extra must not lose the headline line
+            out[name] = {"error": repr(e)[:300]}
+        if isinstance(out[name], dict):
+            out[name]["bench_wall_s"] = round(time.perf_counter() - t0, 1)
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -637,7 +857,7 @@ def sweep_oracle(batch, threads):
     return res, time.perf_counter() - t0
 
 
-def run_sweep(args):
+def run_sweep(args, embedded=False):
     import ctypes as C
     import torch
     import alignment_projects_gb300 as aln
@@ -673,8 +893,10 @@ def run_sweep(args):
                     "d2h_bytes_per_step": 0}}), flush=True)
         return 0
 
+    if embedded:
+        ws, rank = 1, 0
     torch.cuda.set_device(local)
-    dist = dist_init(ws, "nccl")
+    dist = None if embedded else dist_init(ws, "nccl")
     dev = torch.device("cuda", local)
     L = aln.lib()
     ctx = aln.Context(local)
@@ -730,14 +952,7 @@ def run_sweep(args):
             cpu = {"value": len(samp) / wall, "unit": "pairs/s", "cores": threads, "kind": "port",
                    "sample": "%d of the sweep's pairs, FP64 C restatement of CThmScan + "
                              "CorrImagesS, %.1f s wall on %d threads" % (len(samp), wall, threads)}
-            same_err = sum(1 for g, o in zip(res, orc) if g["err"] == o["err"])
-            dA = [abs(g["A"] - o["A"]) for g, o in zip(res, orc)]
-            dR = [abs(g["R"] - o["R"]) / max(1.0, abs(o["R"])) for g, o in zip(res, orc)]
-            dxy = [max(abs(g["X"] - o["X"]), abs(g["Y"] - o["Y"]))
-                   for g, o in zip(res, orc) if abs(g["A"] - o["A"]) < 1e-9]
-            parity = {"pairs": len(orc), "same_err": same_err,
-                      "same_angle": sum(1 for d in dA if d < 1e-9), "max_abs_dA_deg": max(dA),
-                      "max_rel_dR": max(dR), "max_dxy_same_angle": max(dxy) if dxy else None}
+            parity = sweep_parity(res, orc)
         line = {
             "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -759,11 +974,30 @@ def run_sweep(args):
             "truth": {"angle_within_0.5deg": truth, "of": n,
                       "err0": sum(1 for r in res if r["err"] == 0)},
         }
-        print(json.dumps(line), flush=True)
+        if not embedded:
+            print(json.dumps(line), flush=True)
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
-    return 0
+    return line if embedded else 0
+
+
+def sweep_parity(res, orc):
+    """The sweep's parity table against the oracle (oracle/sweep_bar.py):
+    pairs whose decisions had no tie must land on the identical angle;
+    bar_failures counts pairs outside the bar."""
+    from oracle.sweep_bar import SweepStats, check
+    st = SweepStats()
+    fails = []
+    for k, (g, o) in enumerate(zip(res, orc)):
+        try:
+            st.add(check(g, o, "pair %d" % k))
+        except AssertionError:
+            fails.append(k)
+    t = st.table()
+    t["same_err"] = sum(1 for g, o in zip(res, orc) if g["err"] == o["err"])
+    t["bar_failures"] = len(fails)
+    return t
 
 
 # ---------------------------------------------------------------------------
@@ -895,11 +1129,13 @@ def served_run(srv, reqs, rate, seed):
     return wall, done
 
 
-def run_served(args):
+def run_served(args, embedded=False):
     import torch
     import alignment_projects_gb300 as aln
 
     ws, rank, local = dist_env()
+    if embedded:
+        ws, rank = 1, 0
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps({"impl": "reference", "unavailable":
@@ -966,7 +1202,7 @@ def run_served(args):
     ctx.close()
     plain = 1.0 / (SERVED_MIX[0] * t_strip + SERVED_MIX[1] * t_sweep + SERVED_MIX[2] * t_patch)
     best = max(table, key=lambda r: r["throughput"])
-    print(json.dumps({
+    line = {
         "metric": METRIC, "value": best["throughput"], "unit": "requests/s", "n_gpus": 1,
         "steps": len(rates), "warmup": 1, "ms_per_step": None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -978,7 +1214,10 @@ def run_served(args):
         "plain": {"requests_per_s": plain, "strip_ms": 1000 * t_strip, "sweep_ms": 1000 * t_sweep,
                   "patch_ms": 1000 * t_patch},
         "served_over_plain": best["throughput"] / plain,
-        "server_counters": counters, "clocks": clocks}), flush=True)
+        "server_counters": counters, "clocks": clocks}
+    if embedded:
+        return line
+    print(json.dumps(line), flush=True)
     return 0
 
 
@@ -992,7 +1231,7 @@ UNEVEN_WORKLOAD = ("uneven-size batch: pairs of uint16 patches (0-4095, mean 204
                    "short/2, olap >= 8 x 8; FFT sizes 128..2048 per axis")
 
 
-def run_uneven(args):
+def run_uneven(args, embedded=False):
     import ctypes as C
     import torch
     import alignment_projects_gb300 as aln
@@ -1001,9 +1240,11 @@ def run_uneven(args):
     from alignment_projects_gb300.native import AlnPair, AlnResult, AlnImage
 
     ws, rank, local = dist_env()
+    if embedded:
+        ws, rank = 1, 0
     threads = host_threads()
     torch.cuda.set_device(local)
-    dist = dist_init(ws, "nccl")
+    dist = None if embedded else dist_init(ws, "nccl")
     dev = torch.device("cuda", local)
     L = aln.lib()
     ctx = aln.Context(local)
@@ -1105,17 +1346,7 @@ def run_uneven(args):
                    "kind": "port", "sample": "%d pairs spread over the batch, FP64 C "
                    "restatement of CorrPatches, %.1f s wall on %d threads"
                    % (len(prep), wall, threads)}
-            ok = chk = 0
-            dr = dp = 0.0
-            for k, o in zip(samp, outs):
-                g = out_d[k]
-                dr = max(dr, abs(g.r - o["r"]))
-                if o["status"] == 0 and o["r"] - o["second"] > 1e-3:
-                    chk += 1
-                    ok += (g.peak_x, g.peak_y) == (o["bigx"], o["bigy"])
-                    dp = max(dp, abs(g.dx - o["dx"]), abs(g.dy - o["dy"]))
-            parity = {"pairs": len(outs), "peak_exact": ok, "peak_checked": chk,
-                      "max_abs_dr": dr, "max_abs_dsubpix": dp}
+            parity = corr_parity([out_d[k] for k in samp], outs)
         line = {
             "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -1133,11 +1364,12 @@ def run_uneven(args):
             "truth": {"found": truth, "of": n},
             "host_vs_device_inputs_identical": same,
         }
-        print(json.dumps(line), flush=True)
+        if not embedded:
+            print(json.dumps(line), flush=True)
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
-    return 0
+    return line if embedded else 0
 
 
 def main():

@@ -27,7 +27,21 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "libaln_oracle.so")
 REF_SO = os.path.join(REF_DIR, "libalnref.so")
-REFERENCE_TREE = "/root/reference"
+TREE_RECORD = os.path.join(REF_DIR, "tree.txt")
+
+
+def reference_tree() -> str:
+    """The reference source tree the reference build uses: $ALN_REFERENCE_TREE,
+    else the tree build_ref() last compiled from (recorded beside its
+    outputs), else "" (not available)."""
+    t = os.environ.get("ALN_REFERENCE_TREE", "")
+    if t:
+        return t
+    try:
+        with open(TREE_RECORD) as f:
+            return f.read().strip()
+    except OSError:
+        return ""
 
 RGN_NONE, RGN_MIN, RGN_SECTION, RGN_EXACT, RGN_TABLE = 0, 1, 2, 3, 4
 CNT_NONE, CNT_GT = 0, 1
@@ -100,7 +114,23 @@ class ThmParams(C.Structure):
 
 class ThmRec(C.Structure):
     _fields_ = [("A", C.c_double), ("X", C.c_double), ("Y", C.c_double),
-                ("R", C.c_double), ("T", C.c_double * 6)]
+                ("R", C.c_double), ("T", C.c_double * 6), ("pm", C.c_double)]
+
+
+class ThmMargins(C.Structure):
+    """orc_thm_margins: the decision margins of one search (aln_oracle.h)."""
+    _fields_ = [("eps", C.c_double), ("eps_px", C.c_double), ("mR", C.c_double),
+                ("mpx", C.c_double), ("tolA", C.c_double), ("mpk", C.c_double),
+                ("ndec", C.c_int),
+                ("nties", C.c_int), ("thr_tie", C.c_int)]
+
+
+# tie thresholds of the sweep parity bar: a decision whose relative score
+# margin exceeds SWEEP_EPS (and whose rounded offsets sit farther than
+# SWEEP_EPS_PX from a rounding boundary) is far above the FP32 correlator's
+# error (measured |dR|/R ~1e-7), so the GPU must take it the same way
+SWEEP_EPS = 1e-5
+SWEEP_EPS_PX = 1e-4
 
 
 def _p(a):
@@ -129,12 +159,16 @@ def build(force: bool = False) -> str:
     return ORACLE_SO
 
 
-def build_ref() -> str | None:
-    """Compile the reference's own sources (only where the tree is mounted)."""
-    if not os.path.isdir(REFERENCE_TREE):
+def build_ref(tree: str | None = None) -> str | None:
+    """Compile the reference's own sources from `tree` (default:
+    reference_tree()); None when no tree is given or it is not mounted."""
+    tree = tree or reference_tree()
+    if not tree or not os.path.isdir(os.path.join(tree, "0_GEN")):
         return None
     subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), "-j8",
-                           "REF=" + REFERENCE_TREE], stdout=subprocess.DEVNULL)
+                           "REF=" + tree], stdout=subprocess.DEVNULL)
+    with open(TREE_RECORD, "w") as f:
+        f.write(os.path.abspath(tree) + "\n")
     return REF_SO
 
 
@@ -291,12 +325,18 @@ class Oracle(_Lib):
             P.tdfm[i] = t[i]
         best = ThmRec()
         ncalls = C.c_int(0)
-        err = self.lib.orc_thm_search(_p(pa), _p(va), len(va), _p(pb), _p(vb), len(vb),
-                                      C.c_long(req_area), olap1d, C.byref(P), mode,
-                                      C.c_double(ang0), C.c_double(hfang),
-                                      C.c_double(step), C.byref(best), C.byref(ncalls))
+        M = ThmMargins()
+        M.eps, M.eps_px = SWEEP_EPS, SWEEP_EPS_PX
+        err = self.lib.orc_thm_search_m(_p(pa), _p(va), len(va), _p(pb), _p(vb), len(vb),
+                                        C.c_long(req_area), olap1d, C.byref(P), mode,
+                                        C.c_double(ang0), C.c_double(hfang),
+                                        C.c_double(step), C.byref(best), C.byref(ncalls),
+                                        C.byref(M))
         return {"A": best.A, "X": best.X, "Y": best.Y, "R": best.R, "err": err,
-                "ncalls": ncalls.value}
+                "ncalls": ncalls.value,
+                "margins": {"mR": M.mR, "mpx": M.mpx, "tolA": M.tolA, "mpk": M.mpk,
+                            "ndec": M.ndec,
+                            "nties": M.nties, "thr_tie": bool(M.thr_tie)}}
 
     def thm_finish(self, pa, va, pb, vb, req_area, mode, prior, tptwk=None, olap1d=0,
                    rthresh=0.3, nbmaxht=0.75, pretweak=0, constxy=1, tdfm=None):

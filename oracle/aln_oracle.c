@@ -1074,7 +1074,89 @@ typedef struct {
     double Ta[64];
     double *pts;   /* scratch for rotated points */
     int ncalls;
+    orc_thm_margins *M;   /* decision margins (checker instrumentation), or NULL */
 } thm_state;
+
+#define ORC_UNBOUNDED 1e30
+
+/* ---- decision margins (checker instrumentation, no reference counterpart) */
+
+static void note_tie(thm_state *s, double tol)
+{
+    s->M->nties++;
+    if (tol > s->M->tolA)
+        s->M->tolA = tol;
+}
+
+/* a comparison of two scores x, y; tol = how far the answer's angle can move
+ * if it goes the other way */
+static void note_r(thm_state *s, double x, double y, double tol)
+{
+    if (!s->M)
+        return;
+    s->M->ndec++;
+    if (x == 0.0 && y == 0.0)   /* two calls without a legal lag: exact on any host */
+        return;
+    double m = fabs(x - y) / fmax(1.0, fmax(fabs(x), fabs(y)));
+    if (m < s->M->mR)
+        s->M->mR = m;
+    if (m < s->M->eps)
+        note_tie(s, tol);
+}
+
+/* two records' scores; calls with the same transform are the same
+   computation on any host (bit for bit), so their exact tie is not one */
+static void note_rec(thm_state *s, const orc_thm_rec *a, const orc_thm_rec *b, double tol)
+{
+    if (!s->M)
+        return;
+    if (memcmp(a->T, b->T, sizeof a->T) == 0) {
+        s->M->ndec++;
+        return;
+    }
+    note_r(s, a->R, b->R, tol);
+}
+
+/* an rthresh test of score x; tol as note_r */
+static void note_thr(thm_state *s, double x, double thr, double tol)
+{
+    if (!s->M)
+        return;
+    double m = fabs(x - thr) / fmax(1.0, fabs(x));
+    s->M->ndec++;
+    if (m < s->M->mR)
+        s->M->mR = m;
+    if (m < s->M->eps) {
+        s->M->thr_tie = 1;
+        note_tie(s, tol);
+    }
+}
+
+/* the correlator peak of record C is used (its X, Y steer or are the answer) */
+static void note_pk(thm_state *s, const orc_thm_rec *C, double tol)
+{
+    if (!s->M)
+        return;
+    s->M->ndec++;
+    if (C->pm < s->M->mR)
+        s->M->mR = C->pm;
+    if (C->pm < s->M->eps)
+        note_tie(s, tol);
+}
+
+/* x is rounded half away from zero (the ConstXY line fits) */
+static void note_round(thm_state *s, double x)
+{
+    if (!s->M)
+        return;
+    double a = fabs(x);
+    double m = fabs(a - floor(a) - 0.5);
+    s->M->ndec++;
+    if (m < s->M->mpx)
+        s->M->mpx = m;
+    if (m < s->M->eps_px)
+        note_tie(s, ORC_UNBOUNDED);
+}
 
 static void aff_one(double t[6])
 {
@@ -1146,6 +1228,10 @@ static void thm_rfromangle(thm_state *s, orc_thm_rec *C, double deg, int iaux)
                            s->P.Ry, &o);
     C->X = o.dx;
     C->Y = o.dy;
+    /* the call's own top-two margin (CorrImagesS/R: best vs runner-up key;
+       CorrImagesF picks by FPeak's rules, its margin is not a score gap) */
+    C->pm = (o.status == 0 && o.second > -1e29)
+                ? fabs(C->R - o.second) / fmax(1.0, fabs(C->R)) : ORC_UNBOUNDED;
     s->ncalls++;
 }
 
@@ -1172,6 +1258,7 @@ static double thm_scan_constxy(thm_state *s, orc_thm_rec *best, double center,
     orc_thm_rec *vC = (orc_thm_rec *)malloc(sizeof(orc_thm_rec) * MAXANG);
     int *order = (int *)malloc(sizeof(int) * MAXANG);
     best->X = best->Y = best->A = best->R = 0.0;
+    best->pm = ORC_UNBOUNDED;
     int nC = 0;
     for (double a = center - hlfwid; a <= center + hlfwid && nC < MAXANG; a += step)
         vC[nC++].A = a;
@@ -1184,6 +1271,9 @@ static double thm_scan_constxy(thm_state *s, orc_thm_rec *best, double center,
     const int m = 3, M = 2 * m + 1;
     for (int i = 0; i < nC; ++i) {
         int ic = order[i];
+        /* the ranking decides which candidate is examined next */
+        if (i + 1 < nC)
+            note_r(s, vC[ic].R, vC[order[i + 1]].R, ORC_UNBOUNDED);
         if (ic < m || nC - 1 - ic < m)
             continue;
         double A[7], X[7], Y[7];
@@ -1192,12 +1282,19 @@ static double thm_scan_constxy(thm_state *s, orc_thm_rec *best, double center,
             A[n] = vC[j].A;
             X[n] = round_ref(vC[j].X);
             Y[n] = round_ref(vC[j].Y);
+            note_pk(s, &vC[j], ORC_UNBOUNDED);
+            note_round(s, vC[j].X);
+            note_round(s, vC[j].Y);
             ++n;
         }
         double lc = orc_linefit_r(A, X, M);
+        if (isfinite(lc))
+            note_r(s, fabs(lc), rthresh, ORC_UNBOUNDED);
         if (isfinite(lc) && fabs(lc) < rthresh)
             continue;
         lc = orc_linefit_r(A, Y, M);
+        if (isfinite(lc))
+            note_r(s, fabs(lc), rthresh, ORC_UNBOUNDED);
         if (isfinite(lc) && fabs(lc) < rthresh)
             continue;
         *best = vC[ic];
@@ -1233,6 +1330,10 @@ static double thm_scan_maxr(thm_state *s, orc_thm_rec *best, double center,
     for (int ic = 1; ic < nC; ++ic)
         if (vC[ic].R > best->R)
             *best = vC[ic];
+    /* the maximum against every other candidate (the first maximum wins) */
+    for (int ic = 0; ic < nC; ++ic)
+        if (vC[ic].A != best->A || vC[ic].R != best->R)
+            note_rec(s, best, &vC[ic], fabs(vC[ic].A - best->A));
     free(vC);
     return best->R;
 }
@@ -1270,6 +1371,8 @@ static double thm_ptw_interp(thm_state *s, double *ynew, int sel, double x1, dou
     s->Ta[0] = xnew;
     thm_rfromangle(s, &C, deg, 0);
     *ynew = C.R;
+    if (xnew != x1)   /* else the same call as y1's */
+        note_r(s, *ynew, y1, ORC_UNBOUNDED);
     if (*ynew < y1) {
         xnew = x1;
         *ynew = y1;
@@ -1278,7 +1381,7 @@ static double thm_ptw_interp(thm_state *s, double *ynew, int sel, double x1, dou
 }
 
 /* Pretweaks, CThmScan.cpp:205-323 */
-static int thm_pretweaks(thm_state *s, double bestR, double deg)
+static int thm_pretweaks(thm_state *s, double bestR, double deg, const double *bestT)
 {
     int vused[5] = {0, 0, 0, 0, 0}, anychange = 0;
     const double astep = 0.02;
@@ -1307,11 +1410,22 @@ static int thm_pretweaks(thm_state *s, double bestR, double deg)
                 rbest = vC[ic].R;
                 ibest = ic;
             }
+        for (int ic = 0; ic < nc; ++ic)
+            if (ic != ibest) {
+                if (ibest >= 0)
+                    note_rec(s, &vC[ic], &vC[ibest], ORC_UNBOUNDED);
+                else
+                    note_r(s, vC[ic].R, 0.0, ORC_UNBOUNDED);
+            }
         if (ibest == -1)
             break;
         int bsel = s->Tsel[ibest];
         double ba = s->Ta[ibest];
+        const double ba0 = ba;
         ba = thm_ptw_interp(s, &rbest, bsel, ba, rbest, astep, deg);
+        /* the untweaked transform scores exactly bestR on any host */
+        if (!(ba == ba0 && bestT && memcmp(vC[ibest].T, bestT, 6 * sizeof(double)) == 0))
+            note_r(s, rbest, bestR, ORC_UNBOUNDED);
         if (rbest > bestR) {
             double M[6];
             aff_nu(M, bsel, ba);
@@ -1329,9 +1443,13 @@ static int thm_pretweaks(thm_state *s, double bestR, double deg)
 static double thm_scan_tweaks(thm_state *s, orc_thm_rec *best, double center,
                               double hlfwid, double step)
 {
-    if (thm_scan_sel(s, best, center, hlfwid, step, 1) < s->P.rthresh) {
+    double r0 = thm_scan_sel(s, best, center, hlfwid, step, 1);
+    if (s->P.pretweak)
+        note_thr(s, r0, s->P.rthresh, ORC_UNBOUNDED);
+    if (r0 < s->P.rthresh) {
         if (s->P.pretweak) {
-            if (thm_pretweaks(s, best->R, (best->R > 0.0 ? best->A : center)))
+            if (thm_pretweaks(s, best->R, (best->R > 0.0 ? best->A : center),
+                              best->R > 0.0 ? best->T : NULL))
                 thm_scan_sel(s, best, center, hlfwid, step, 1);
         }
     }
@@ -1347,6 +1465,8 @@ static double thm_peak_hunt(thm_state *s, orc_thm_rec *best, double hlfwid)
     while (R - L > 0.0001) {
         double a;
         thm_rfromangle(s, &C, a = (L + M) / 2.0, -1);
+        /* either branch keeps the answer inside [L, R] */
+        note_r(s, C.R, best->R, R - L);
         if (C.R >= best->R) {
             R = M;
             *best = C;
@@ -1354,6 +1474,7 @@ static double thm_peak_hunt(thm_state *s, orc_thm_rec *best, double hlfwid)
         } else
             L = a;
         thm_rfromangle(s, &C, a = (M + R) / 2.0, -1);
+        note_r(s, C.R, best->R, R - L);
         if (C.R >= best->R) {
             L = M;
             *best = C;
@@ -1361,6 +1482,7 @@ static double thm_peak_hunt(thm_state *s, orc_thm_rec *best, double hlfwid)
         } else
             R = a;
     }
+    note_r(s, B0.R, best->R, fabs(B0.A - best->A));
     if (B0.R > best->R)
         *best = B0;
     return best->R;
@@ -1372,8 +1494,24 @@ int orc_thm_search(const double *xya, const double *va, int na,
                    int mode, double ang0, double hfang, double step,
                    orc_thm_rec *best, int *ncalls)
 {
+    return orc_thm_search_m(xya, va, na, xyb, vb, nb, reqArea, olap1D, P, mode, ang0, hfang,
+                            step, best, ncalls, NULL);
+}
+
+int orc_thm_search_m(const double *xya, const double *va, int na,
+                     const double *xyb, const double *vb, int nb,
+                     long reqArea, int olap1D, const orc_thm_params *P,
+                     int mode, double ang0, double hfang, double step,
+                     orc_thm_rec *best, int *ncalls, orc_thm_margins *M)
+{
     thm_state s;
     memset(&s, 0, sizeof s);
+    s.M = M;
+    if (M) {
+        M->mR = M->mpx = M->mpk = ORC_UNBOUNDED;
+        M->tolA = 0.0;
+        M->ndec = M->nties = M->thr_tie = 0;
+    }
     s.xya = xya;
     s.va = va;
     s.na = na;
@@ -1387,21 +1525,45 @@ int orc_thm_search(const double *xya, const double *va, int na,
     s.pts = (double *)malloc(sizeof(double) * 2 * (size_t)(na > 0 ? na : 1));
     int err = 0;
     best->X = best->Y = best->A = best->R = -999.0;   /* CThmScan::Initialize */
+    best->pm = ORC_UNBOUNDED;
     switch (mode) {
-    case 0:
-        if (thm_scan_tweaks(&s, best, ang0, hfang, step) < P->rthresh ||
-            thm_scan_sel(&s, best, best->A, step * 2.0, step * 0.05, 0) < P->rthresh ||
-            thm_peak_hunt(&s, best, step * 0.05 * 1.5) < P->rthresh)
+    case 0: {
+        /* the short-circuit chain of DenovoBestAngle; a tie on one of the
+           first two tests changes which stages run */
+        double r = thm_scan_tweaks(&s, best, ang0, hfang, step);
+        note_thr(&s, r, P->rthresh, ORC_UNBOUNDED);
+        if (r < P->rthresh) {
             err = 1; /* errLowRDenov */
+            break;
+        }
+        r = thm_scan_sel(&s, best, best->A, step * 2.0, step * 0.05, 0);
+        note_thr(&s, r, P->rthresh, ORC_UNBOUNDED);
+        if (r < P->rthresh) {
+            err = 1;
+            break;
+        }
+        r = thm_peak_hunt(&s, best, step * 0.05 * 1.5);
+        note_thr(&s, r, P->rthresh, 0.0);
+        if (r < P->rthresh)
+            err = 1;
         break;
+    }
     case 1:
         thm_rfromangle(&s, best, ang0, -1);
         break;
-    case 2:
-        if (thm_scan_tweaks(&s, best, ang0, hfang, 0.1) < P->rthresh ||
-            thm_peak_hunt(&s, best, 0.1 * 1.5) < P->rthresh)
+    case 2: {
+        double r = thm_scan_tweaks(&s, best, ang0, hfang, 0.1);
+        note_thr(&s, r, P->rthresh, ORC_UNBOUNDED);
+        if (r < P->rthresh) {
             err = 2; /* errLowRPrior */
+            break;
+        }
+        r = thm_peak_hunt(&s, best, 0.1 * 1.5);
+        note_thr(&s, r, P->rthresh, 0.0);
+        if (r < P->rthresh)
+            err = 2;
         break;
+    }
     case 3:
         thm_scan_sel(&s, best, ang0, hfang, step, 0);
         thm_peak_hunt(&s, best, step * 0.05 * 1.5);
@@ -1410,6 +1572,12 @@ int orc_thm_search(const double *xya, const double *va, int na,
         s.P.constxy = 0;
         thm_scan_sel(&s, best, ang0, hfang, step, 1);
         break;
+    }
+    /* the answer's own correlator peak: its X, Y are reported */
+    if (best->R > -999.0) {
+        note_pk(&s, best, ORC_UNBOUNDED);
+        if (M)
+            M->mpk = best->pm;
     }
     free(s.pts);
     if (ncalls)
@@ -1452,7 +1620,7 @@ int orc_thm_finish(const double *xya, const double *va, int na,
     s.P.Oy = (int)best->Y;
     if (mode == 5) {
         s.P.Rx = s.P.Ry = 40;
-        thm_pretweaks(&s, best->R, best->A);
+        thm_pretweaks(&s, best->R, best->A, NULL);
         thm_rfromangle(&s, best, best->A, -1);
     } else {
         orc_thm_rec b0 = *best;

@@ -106,7 +106,32 @@ typedef struct orc_thm_params {
 typedef struct orc_thm_rec {
     double A, X, Y, R;
     double T[6];
+    double pm;            /* checker field (not in the reference's ThmRec): the
+                             correlator call's own top-two score margin,
+                             relative to max(1, |score|); 1e30 if no peak */
 } orc_thm_rec;
+
+/* Decision margins of one search (checker instrumentation; the reference
+ * has no counterpart).  Every comparison that steers the search -- the
+ * ConstXY ranking prefix down to the accepted angle, the LineFit |r| >= 0.7
+ * tests, the X/Y roundings those fits see, the correlator peaks whose X, Y
+ * are used, MaxR's maximum, PeakHunt's bracket tests, the Pretweaks tests
+ * and the rthresh tests -- is noted with its margin.  A GPU search whose
+ * own arithmetic differs from the oracle's by less than `eps` (relative, on
+ * scores) and `eps_px` (on the rounded offsets) takes every decision whose
+ * margin exceeds those the same way, so it must land on the identical
+ * angle when nties == 0.  Otherwise the angle may move by at most tolA
+ * (1e30: unbounded -- a flipped ranking or threshold can send the search
+ * anywhere), and the err code may differ iff thr_tie. */
+typedef struct orc_thm_margins {
+    double eps, eps_px;   /* inputs: tie thresholds */
+    double mR;            /* smallest relative score margin noted */
+    double mpx;           /* smallest distance (px) of a rounded X/Y from .5 */
+    double tolA;          /* angle bound if every tie flipped (0 if none) */
+    double mpk;           /* the answer's own correlator top-two margin */
+    int ndec, nties;      /* decisions noted, decisions below the thresholds */
+    int thr_tie;          /* an rthresh test was a tie: err may differ */
+} orc_thm_margins;
 
 /* mode: 0 DenovoBestAngle(ang0, hfang, step), 1 RFromAngle(ang0),
  * 2 UsePriorAngles(ang0, hfang), 3 AngleScanSel(ConstXY/MaxR by params,
@@ -117,6 +142,14 @@ int orc_thm_search(const double *xya, const double *va, int na,
                    long reqArea, int olap1D, const orc_thm_params *P,
                    int mode, double ang0, double hfang, double step,
                    orc_thm_rec *best, int *ncalls);
+
+/* orc_thm_search with the decision margins of the run (M may be NULL;
+ * M->eps and M->eps_px are read, the rest written). */
+int orc_thm_search_m(const double *xya, const double *va, int na,
+                     const double *xyb, const double *vb, int nb,
+                     long reqArea, int olap1D, const orc_thm_params *P,
+                     int mode, double ang0, double hfang, double step,
+                     orc_thm_rec *best, int *ncalls, orc_thm_margins *M);
 
 /* PostTweaks (mode 5) / FinishAtFullRes (mode 6) from a prior best
  * (A, X, Y, R) and pretweak transform (NULL: identity).  Mirrors refwrap's

@@ -251,7 +251,11 @@ def save(name, d):
 
 
 def main():
-    O.build_ref()
+    # the reference source tree: argv[1], else $ALN_REFERENCE_TREE / the tree
+    # of the last reference build
+    tree = sys.argv[1] if len(sys.argv) > 1 else None
+    if O.build_ref(tree) is None:
+        sys.exit("usage: make_golden.py <reference source tree>")
     ref = O.Ref()
     save("corr_patches", corr_patches_cases(ref))
     save("corr_images", corr_images_cases(ref))

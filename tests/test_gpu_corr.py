@@ -177,6 +177,22 @@ def test_uneven_u16(ctx, orc, seed):
     assert_parity(g, o, f"uneven seed {seed}")
 
 
+@pytest.mark.parametrize("seed", range(70, 76))
+def test_uneven_u16_large(ctx, orc, seed):
+    """The top of the uneven batch's size range: long sides 700-1024 px,
+    i.e. 2048-point axes on the reference's FFTSize grid."""
+    import oracle
+    from alignment_projects_gb300 import synth
+    p = synth.uneven_pair(seed, smin=700, smax=1024)
+    assert max(p.a.shape) >= 700
+    lg_o = oracle.legal(oracle.RGN_MIN, 8, 8, 0)
+    g = ctx.corr_patches(p.a, p.b, p.ox, p.oy, p.radius, aln_legal(lg_o))
+    o = _oracle_pair(orc, p, lg_o)
+    assert o["nx"] == 2048 or o["ny"] == 2048, (o["nx"], o["ny"])
+    assert_parity(g, o, f"uneven large seed {seed}")
+    assert (g["peak_x"], g["peak_y"]) == p.truth
+
+
 def _disc_case(seed):
     rng = np.random.default_rng(seed)
     w, h = int(rng.integers(24, 200)), int(rng.integers(24, 200))

@@ -96,16 +96,16 @@ def test_reference_caller_links_against_shim(shim):
     compiled from its sources where they lie, links against the shim in place
     of Correlation.o."""
     import oracle
-    src = os.path.join(oracle.REFERENCE_TREE, "Retired_Proj", "4_TestNormCorr",
+    src = os.path.join(oracle.reference_tree(), "Retired_Proj", "4_TestNormCorr",
                        "testnormcorr.cpp")
     timer = os.path.join(os.path.dirname(oracle.REF_SO), "Timer.o")
     if not (os.path.exists(src) and oracle.ref_available() and os.path.exists(timer)):
         pytest.skip("the reference's sources are not mounted here")
-    gen = os.path.join(oracle.REFERENCE_TREE, "0_GEN")
+    gen = os.path.join(oracle.reference_tree(), "0_GEN")
     with tempfile.TemporaryDirectory() as d:
         exe = os.path.join(d, "testnormcorr")
         subprocess.check_call(["g++", "-O1", "-w", "-DTIXML_USE_STL", "-I" + gen,
-                               "-I" + os.path.join(oracle.REFERENCE_TREE, "0_UTL"),
+                               "-I" + os.path.join(oracle.reference_tree(), "0_UTL"),
                                "-I" + os.path.join(ROOT, "oracle", "ref"),
                                "-o", exe, src, timer, "-L" + os.path.dirname(shim),
                                "-laln_corr_shim", "-laln_corr", "-lpthread",
@@ -115,10 +115,10 @@ def test_reference_caller_links_against_shim(shim):
 
 def _reference_tree():
     import oracle
-    if not (os.path.isdir(os.path.join(oracle.REFERENCE_TREE, "0_GEN")) and
+    if not (os.path.isdir(os.path.join(oracle.reference_tree(), "0_GEN")) and
             oracle.ref_available()):
         pytest.skip("the reference's sources are not mounted here")
-    return oracle.REFERENCE_TREE
+    return oracle.reference_tree()
 
 
 def test_thmscan_layout_matches_reference(tmp_path):
