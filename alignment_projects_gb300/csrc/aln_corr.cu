@@ -3044,6 +3044,20 @@ extern "C" int aln_corr_patches_noalloc(const aln_image *a, const aln_image *b, 
     CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64)
         return set_err(nullptr, ALN_ERR_ARG, "noalloc: device %d out of range", dev);
+    // both images must live on the current device: a pointer into another
+    // GPU's memory would be read over the peer link without any error
+    for (const aln_image *im : {a, b}) {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, im->data) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(nullptr, ALN_ERR_ARG, "noalloc: image pointer is not device memory");
+        }
+        if ((at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) ||
+            at.device != dev)
+            return set_err(nullptr, ALN_ERR_ARG,
+                           "noalloc: image memory is on device %d, the current device is %d",
+                           at.device, dev);
+    }
     cudaStream_t st = (cudaStream_t)stream;
     char *base = nullptr;
     if (int rc = noalloc_setup(dev, st, &base))

@@ -427,9 +427,15 @@ int aln_decimate_batch(aln_ctx *ctx, int n, const aln_image *in,
  * montage strip pair up to 256 x 2048 with a disc.
  *
  * Inputs: a and b must be device pointers on the calling thread's current
- * device (on_device = 1).  Output: *out in host memory.  The call runs on
- * `stream` (a cudaStream_t, NULL for the default stream) and returns after
- * the result is copied back.
+ * device (on_device = 1; memory of another device is rejected with
+ * ALN_ERR_ARG).  Output: *out in host memory.  The call runs on `stream` (a
+ * cudaStream_t, NULL for the default stream) and is synchronous: it returns
+ * after the result is copied back.
+ *
+ * Its kernels are the library's general-size FFT kernels on the caller's
+ * frame (wide pairs are not transposed), so it agrees with aln_corr_patches
+ * to FP32 rounding, not bit for bit: the same integer peak wherever the
+ * top-two margin of r exceeds 1e-3, r within 1e-4, dx and dy within 0.01 px.
  *
  * The first call on each device performs a one-time set-up there (looks up
  * the scratch array's device address, fills the FFT twiddle table in it,
