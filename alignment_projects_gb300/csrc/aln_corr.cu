@@ -3145,4 +3145,6 @@ extern "C" int aln_corr_patches_noalloc(const aln_image *a, const aln_image *b, 
 }
 
 #include "aln_sweep.cuh"
+#include "aln_approx.cuh"
+#include "aln_mesh.cuh"
 #include "aln_server.cuh"

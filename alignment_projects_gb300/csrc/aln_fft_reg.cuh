@@ -24,9 +24,13 @@ __device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
 __host__ __device__ constexpr int padded(int n) { return n + (n >> 4); }
 
 // float2 per team in the row kernels: the padded row plus two bins, rounded
-// up to an even count so that every team's region starts on 16 bytes (the
-// row pass stages its input with 16-byte stores)
-__host__ __device__ constexpr int row_pitch(int L) { return (padded(L) + 3) & ~1; }
+// up to an odd count.  The row kernels move data between the teams' rows
+// with one bin per thread and the teams (rows) fastest, G consecutive
+// threads reading (or writing) bin k of G rows at k + g * pitch: an odd
+// pitch puts those on G distinct 8-byte banks (an even one had two threads
+// on every bank).  Regions then start on 8 bytes only: the row pass stages
+// its input bytes from the region's first 16-byte boundary.
+__host__ __device__ constexpr int row_pitch(int L) { return (padded(L) + 2) | 1; }
 
 // exp(DIR * 2 pi i k / 16) for k = 0..7 (DIR = -1 forward)
 template <int K16, int DIR>
@@ -86,6 +90,22 @@ struct DFT<1, DIR> {
 // threads and >= 4 threads per team down to N = 32).
 __host__ __device__ constexpr int fft_radix(int N) { return N >= 512 ? 16 : (N >= 8 ? 8 : N); }
 
+// Barrier of one team of T threads (team g of the CTA, teams of T
+// consecutive threads): a named barrier per team when the team spans whole
+// warps (ids 1.. ; 0 is __syncthreads'), the warp's own barrier when teams
+// are smaller than a warp (all teams of a warp run the same code path).
+// Teams that share no shared-memory data then run apart: one team's wait
+// for its loads does not hold the others at the next exchange.
+template <int T>
+__device__ __forceinline__ void team_sync(int team)
+{
+    static_assert(T < 32 || T % 32 == 0, "teams are whole warps or within one warp");
+    if constexpr (T >= 32)
+        asm volatile("bar.sync %0, %1;" ::"r"(team + 1), "r"(T) : "memory");
+    else
+        __syncwarp();
+}
+
 template <int N, int DIR, int RAD = fft_radix(N)>
 struct RegFFT {
     static constexpr int R = RAD;
@@ -95,9 +115,30 @@ struct RegFFT {
     static constexpr int SMEM = padded(N);             // float2 per team
 
     // v: this thread's R points (x[t + r*T]); sm: the team's exchange buffer.
-    // All threads of the CTA must call this together (it uses __syncthreads).
+    // All threads of the CTA must call this together (it uses __syncthreads);
+    // run_team(..., team) synchronises team `team` alone (team_sync), for
+    // kernels whose teams share no shared-memory data around the call.
     __device__ static void run(float2 (&v)[R], float2 *sm, int t,
                                const float2 *__restrict__ tw)
+    {
+        run_impl<false>(v, sm, t, tw, 0);
+    }
+    __device__ static void run_team(float2 (&v)[R], float2 *sm, int t,
+                                    const float2 *__restrict__ tw, int team)
+    {
+        run_impl<true>(v, sm, t, tw, team);
+    }
+    template <bool TEAM>
+    __device__ static __forceinline__ void sync(int team)
+    {
+        if constexpr (TEAM)
+            team_sync<T>(team);
+        else
+            __syncthreads();
+    }
+    template <bool TEAM>
+    __device__ static void run_impl(float2 (&v)[R], float2 *sm, int t,
+                                    const float2 *__restrict__ tw, int team)
     {
         int Ns = 1;
         if constexpr (R2 > 1) {
@@ -115,7 +156,7 @@ struct RegFFT {
                     v[q + s * m] = u[s];
                 (void)j;
             }
-            __syncthreads();
+            sync<TEAM>(team);
 #pragma unroll
             for (int q = 0; q < m; ++q) {
                 const int j = t + q * T;
@@ -123,7 +164,7 @@ struct RegFFT {
                 for (int s = 0; s < R2; ++s)
                     sm[padi(j * R2 + s)] = v[q + s * m];
             }
-            __syncthreads();
+            sync<TEAM>(team);
 #pragma unroll
             for (int r = 0; r < R; ++r)
                 v[r] = sm[padi(t + r * T)];
@@ -145,11 +186,11 @@ struct RegFFT {
             DFT<R, DIR>::run(v);
             if (p + 1 < P) {
                 const int base = (t - k) * R + k;
-                __syncthreads();
+                sync<TEAM>(team);
 #pragma unroll
                 for (int r = 0; r < R; ++r)
                     sm[padi(base + r * Ns)] = v[r];
-                __syncthreads();
+                sync<TEAM>(team);
 #pragma unroll
                 for (int r = 0; r < R; ++r)
                     v[r] = sm[padi(t + r * T)];

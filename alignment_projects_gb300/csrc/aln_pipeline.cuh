@@ -445,7 +445,7 @@ k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int
     if (y0 >= h)
         return;
     const int y = y0 + team;
-    constexpr int PITCH = row_pitch(L);   // even: 16-byte aligned team regions
+    constexpr int PITCH = row_pitch(L);   // odd: conflict-free transposed reads
     float2 *sm = smem + team * PITCH;
     const void *img = p.img[i];
     const long long st = p.stride[i];
@@ -457,7 +457,9 @@ k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int
         // of the row never leaves the row's allocation page).
         const int es = dt == ALN_U8 ? 1 : 2;
         const int mu = (int)p.mu[i];
-        unsigned char *sb = (unsigned char *)sm;
+        // the region's first 16-byte boundary (at most 8 bytes in): the row's
+        // <= 4L + 30 staged bytes end well inside the 8 * PITCH of the region
+        unsigned char *sb = (unsigned char *)(((uintptr_t)sm + 15) & ~(uintptr_t)15);
         int off = 0;
         if (y < h) {
             const unsigned char *base = (const unsigned char *)img + (long long)y * st * es;
@@ -468,7 +470,7 @@ k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int
             for (int k = t; k < nvec; k += T)
                 ((uint4 *)sb)[k] = src[k];
         }
-        __syncthreads();
+        team_sync<T>(team);   // each team reads back its own row only
         const unsigned char *rb8 = sb + off;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -499,7 +501,7 @@ k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int
             v[r] = z;
         }
     }
-    F::run(v, sm, t, tw);
+    F::run_team(v, sm, t, tw, team);
     // split the half-length transform into the N/2+1 bins of the real row
     __syncthreads();
 #pragma unroll
@@ -589,7 +591,7 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
                 const int y = t + r * T;
                 vb[r] = y < hb ? Tb[y] : make_float2(0.f, 0.f);
             }
-            FF::run(vb, sm, t, tw);
+            FF::run_team(vb, sm, t, tw, team);
         }
 #pragma unroll
         for (int r = 0; r < R; ++r)
@@ -604,7 +606,7 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
             va[r] = y < ha ? Ta[y] : make_float2(0.f, 0.f);
         }
     }
-    FF::run(va, sm, t, tw);
+    FF::run_team(va, sm, t, tw, team);
 #pragma unroll
     for (int r = 0; r < R; ++r)
         va[r] = cmulc(sb[r * T + t], va[r]);   // X2 * conj(X1)
@@ -634,7 +636,7 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
     const int Wy = p.yhi - p.ylo + 1;
     const int nnegy = p.h[0] - 1;
     if (want_r) {
-        FI::run(va, sm, t, tw);
+        FI::run_team(va, sm, t, tw, team);
         if (live && is_p2i) {   // every storage row, in storage order
             float2 *Q = p.Q + (long long)kx * NY;
 #pragma unroll
@@ -662,7 +664,7 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
             }
             va[r] = v;
         }
-        FI::run(va, sm, t, tw);
+        FI::run_team(va, sm, t, tw, team);
         if (live) {
             float2 *Q = (want_r ? p.Q2 : p.Q) + (long long)kx * Wy;
 #pragma unroll
@@ -734,7 +736,7 @@ k2_corrseg(PairDev *pairs, const float2 *__restrict__ tw)
             const int j = t + r * T, y = y0 + j;
             v[r] = (j < B && y < ha) ? Ta[y] : make_float2(0.f, 0.f);
         }
-        FF::run(v, sm, t, tw);
+        FF::run_team(v, sm, t, tw, team);
 #pragma unroll
         for (int r = 0; r < R; ++r)
             park[r * T + t] = v[r];
@@ -743,7 +745,7 @@ k2_corrseg(PairDev *pairs, const float2 *__restrict__ tw)
             const int j = t + r * T, y = y0 + ylo + j;
             v[r] = (j < lb && y >= 0 && y < hb) ? Tb[y] : make_float2(0.f, 0.f);
         }
-        FF::run(v, sm, t, tw);
+        FF::run_team(v, sm, t, tw, team);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const float2 q = cmulc(v[r], park[r * T + t]);   // X2 * conj(X1)
@@ -754,7 +756,7 @@ k2_corrseg(PairDev *pairs, const float2 *__restrict__ tw)
 #pragma unroll
     for (int r = 0; r < R; ++r)
         v[r] = acc[r * T + t];
-    FI::run(v, sm, t, tw);
+    FI::run_team(v, sm, t, tw, team);
     if (live) {
         float2 *Q = p.Q + (long long)kx * Wy;
 #pragma unroll

@@ -80,6 +80,55 @@ class AlnThmResult(C.Structure):
                 ("T", C.c_double * 6), ("err", C.c_int), ("ncalls", C.c_int)]
 
 
+class AlnTilePair(C.Structure):
+    _fields_ = [("a", AlnImage), ("b", AlnImage), ("tabx", C.c_double), ("taby", C.c_double)]
+
+
+class AlnApproxParams(C.Structure):
+    _fields_ = [("xyconf", C.c_double), ("olap1d", C.c_int), ("olap2d", C.c_longlong),
+                ("thmdec", C.c_int), ("mode_prior", C.c_int), ("ang0", C.c_double),
+                ("hfangdn", C.c_double), ("hfangpr", C.c_double), ("rthresh", C.c_double),
+                ("nbmaxht", C.c_double), ("pretweak", C.c_int), ("tweaks", C.c_int),
+                ("limxy", C.c_int)]
+
+
+class AlnApproxResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("err", C.c_int), ("A", C.c_double), ("X", C.c_double),
+                ("Y", C.c_double), ("R", C.c_double), ("T", C.c_double * 6),
+                ("sweep", C.c_double * 4), ("crop", C.c_int * 4), ("crop_w", C.c_int),
+                ("crop_h", C.c_int)]
+
+
+class AlnMeshJob(C.Structure):
+    _fields_ = [("nc", C.c_int), ("ac", C.c_void_p), ("nm", C.c_int), ("k", C.c_int),
+                ("am_idx", C.c_void_p), ("am_w", C.c_void_p), ("av", C.c_void_p),
+                ("bimg", C.c_void_p), ("w", C.c_int), ("h", C.c_int),
+                ("ini_thresh", C.c_double), ("fin_thresh", C.c_double), ("on_device", C.c_int)]
+
+
+class AlnMeshResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("corr", C.c_double), ("corr0", C.c_double),
+                ("evals", C.c_int)]
+
+
+def mesh_job(ac, am_idx, am_w, av, bimg, ini_thresh=0.0, fin_thresh=0.0):
+    """An aln_mesh_job over host arrays (kept alive on the struct): ac nc x 2,
+    am_idx / am_w nm x k (indices ascending per row, -1 unused), av nm,
+    bimg h x w.  ac is copied; the optimised points land in job._ac."""
+    acs = np.ascontiguousarray(ac, np.float64).reshape(-1, 2).copy()
+    idx = np.ascontiguousarray(am_idx, np.int32)
+    wts = np.ascontiguousarray(am_w, np.float64)
+    avs = np.ascontiguousarray(av, np.float64)
+    bim = np.ascontiguousarray(bimg, np.float64)
+    assert idx.shape == wts.shape and idx.ndim == 2 and len(avs) == idx.shape[0]
+    J = AlnMeshJob(len(acs), acs.ctypes.data, idx.shape[0], idx.shape[1], idx.ctypes.data,
+                   wts.ctypes.data, avs.ctypes.data, bim.ctypes.data, bim.shape[1], bim.shape[0],
+                   ini_thresh, fin_thresh, 0)
+    J._ac = acs
+    J._keep = (idx, wts, avs, bim)
+    return J
+
+
 def thumbs_from_points(pa, va, pb, vb, req_area, olap1d=0):
     """Point lists with integer coordinates (a ThmRec) -> AlnThumbs.  A
     becomes a grid with a presence mask; B a raster over its bounding box."""
@@ -191,6 +240,16 @@ def lib():
                                             C.POINTER(C.c_int), C.POINTER(C.c_int),
                                             C.POINTER(C.c_int)]
         L.aln_ctx_set_segmenting.argtypes = [C.c_void_p, C.c_int]
+        L.aln_approx_match_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnTilePair),
+                                             C.POINTER(AlnApproxParams),
+                                             C.POINTER(AlnApproxResult)]
+        L.aln_improve_control_pts_batch.argtypes = [C.c_void_p, C.c_int,
+                                                    C.POINTER(AlnMeshJob),
+                                                    C.POINTER(AlnMeshResult)]
+        L.aln_grad_desc_step.argtypes = [C.c_void_p, C.POINTER(AlnMeshJob), C.c_void_p,
+                                         C.c_void_p, C.POINTER(C.c_double)]
+        L.aln_corr_vectors.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.POINTER(C.c_double), C.POINTER(C.c_int)]
         L.aln_server_create.argtypes = [C.POINTER(AlnServerParams), C.POINTER(C.c_void_p)]
         L.aln_server_destroy.argtypes = [C.c_void_p]
         L.aln_server_submit.argtypes = [C.c_void_p, C.POINTER(AlnRequest),
@@ -436,6 +495,62 @@ class Context:
             tw.ctypes.data if tw is not None else None, out, tout.ctypes.data))
         return [{"A": o.A, "X": o.X, "Y": o.Y, "R": o.R, "err": o.err, "ncalls": o.ncalls,
                  "T": list(o.T), "tptwk": tout[k].tolist()} for k, o in enumerate(out)]
+
+    def approx_match_batch(self, pairs, **params) -> list:
+        """ApproximateMatch for [(a, b, (tabx, taby))] tile pairs (numpy arrays
+        or CUDA tensors of equal size and type); params as
+        aln_approx_params (defaults: 1_DMesh/ApproximateMatch.cpp's with
+        XYCONF 0.75, OLAP2D 40000, THMDEC 4, a denovo sweep of +-10 deg)."""
+        d = dict(xyconf=0.75, olap1d=0, olap2d=40000, thmdec=4, mode_prior=0, ang0=0.0,
+                 hfangdn=10.0, hfangpr=1.0, rthresh=0.3, nbmaxht=0.75, pretweak=0, tweaks=0,
+                 limxy=0)
+        d.update(params)
+        P = AlnApproxParams(**d)
+        n = len(pairs)
+        arr = (AlnTilePair * n)()
+        keep = []
+        for k, (a, b, tab) in enumerate(pairs):
+            ia, ib = image(a), image(b)
+            keep += [ia, ib]
+            arr[k].a, arr[k].b = ia, ib
+            arr[k].tabx, arr[k].taby = tab
+        res = (AlnApproxResult * n)()
+        self._check(self._L.aln_approx_match_batch(self.h, n, arr, C.byref(P), res))
+        return [{"status": r.status, "err": r.err, "A": r.A, "X": r.X, "Y": r.Y, "R": r.R,
+                 "T": list(r.T), "sweep": list(r.sweep),
+                 "crop": list(r.crop) + [r.crop_w, r.crop_h]} for r in res]
+
+    def improve_control_pts_batch(self, jobs) -> list:
+        """ImproveControlPts for a list of mesh_job()s at once.  Returns per
+        job dict(corr, corr0, evals, ac) (ac: the optimised nc x 2 points)."""
+        jobs = list(jobs)
+        n = len(jobs)
+        arr = (AlnMeshJob * n)()
+        for k, J in enumerate(jobs):
+            arr[k] = J
+        res = (AlnMeshResult * n)()
+        self._check(self._L.aln_improve_control_pts_batch(self.h, n, arr, res))
+        return [{"corr": r.corr, "corr0": r.corr0, "evals": r.evals, "ac": J._ac.copy()}
+                for r, J in zip(res, jobs)]
+
+    def grad_desc_step(self, job):
+        """GradDescStep at job's control points: (bnew normalised, dRdc nc x
+        2, CorrVectors(av, bnew))."""
+        bnew = np.zeros(job.nm, np.float64)
+        d = np.zeros((job.nc, 2), np.float64)
+        c = C.c_double(0.0)
+        self._check(self._L.aln_grad_desc_step(self.h, C.byref(job), bnew.ctypes.data,
+                                               d.ctypes.data, C.byref(c)))
+        return bnew, d, c.value
+
+    def corr_vectors(self, a, b):
+        """CorrVectors(a, b): (correlation, count of products >= 1e-8)."""
+        a = np.ascontiguousarray(a, np.float64)
+        b = np.ascontiguousarray(b, np.float64)
+        out, nnz = C.c_double(0.0), C.c_int(0)
+        self._check(self._L.aln_corr_vectors(self.h, a.ctypes.data, b.ctypes.data, len(a),
+                                             C.byref(out), C.byref(nnz)))
+        return out.value, nnz.value
 
     def decimate(self, images, lbin, masks=None, normalize=True) -> list:
         """MakeThumbs' DecimateVector + Normalize of 2-D arrays (point lists

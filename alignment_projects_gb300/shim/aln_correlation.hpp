@@ -60,6 +60,17 @@ double CorrPatchToImage(double &dx, double &dy, const std::vector<Point> &ip1,
                         const std::vector<double> &iv1, const std::vector<double> &i2, int Ox,
                         int Oy, int radius, bool bFilter);
 
+// GradDescStep / CorrVectors / ImproveControlPts (0_GEN/Correlation.cpp:1403-1721)
+void GradDescStep(std::vector<double> &bnew, std::vector<Point> &dRdc,
+                  const std::vector<Point> &ac, const std::vector<std::vector<double> > &am,
+                  const std::vector<double> &av, const std::vector<double> &bimg, int w, int h);
+double CorrVectors(FILE *flog, const std::vector<double> &a, const std::vector<double> &b,
+                   int *nnz = NULL);
+double ImproveControlPts(std::vector<Point> &ac, const std::vector<std::vector<double> > &am,
+                         const std::vector<double> &av, const std::vector<double> &bimg, int w,
+                         int h, FILE *flog, const char *describe, double iniThresh,
+                         double finThresh);
+
 // CorrImagesF / CorrImagesR / CorrImagesS (0_GEN/Correlation.cpp:3066-3290)
 double CorrImagesF(FILE *flog, int verbose, double &dx, double &dy,
                    const std::vector<Point> &ip1, const std::vector<double> &iv1,

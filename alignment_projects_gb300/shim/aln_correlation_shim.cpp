@@ -259,3 +259,137 @@ double CorrImagesS(FILE *flog, int verbose, double &dx, double &dy,
     return corr_images(ALN_CORR_S, flog, verbose, dx, dy, ip1, iv1, ip2, iv2, LegalRgn, arglr,
                        LegalCnt, arglc, mincor, nbmaxht, Ox, Oy, Rx, Ry, fft2);
 }
+
+// ---------------------------------------------------------------------------
+// mesh optimizer: the dense multiplier rows compressed to their nonzero
+// entries (ascending control point), then the GPU's aln_improve_control_pts
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct MeshArgs {
+    std::vector<double> ac;
+    std::vector<int> idx;
+    std::vector<double> wts;
+    aln_mesh_job job;
+};
+
+bool mesh_args(MeshArgs &M, const std::vector<Point> &ac,
+               const std::vector<std::vector<double> > &am, const std::vector<double> &av,
+               const std::vector<double> &bimg, int w, int h, FILE *flog)
+{
+    const int nc = (int)ac.size(), nm = (int)am.size();
+    int k = 1;
+    for (const auto &row : am) {
+        int c = 0;
+        for (double v : row)
+            c += v != 0.0;
+        if (c > k)
+            k = c;
+    }
+    if (nc > ALN_MESH_MAX_NC || k > ALN_MESH_MAX_K || (int)av.size() != nm) {
+        fprintf(flog, "GPU mesh: %d control points / %d multipliers per point unsupported\n",
+                nc, k);
+        return false;
+    }
+    M.ac.resize(2 * (size_t)nc);
+    for (int j = 0; j < nc; ++j) {
+        M.ac[2 * j] = ac[j].x;
+        M.ac[2 * j + 1] = ac[j].y;
+    }
+    M.idx.assign((size_t)nm * k, -1);
+    M.wts.assign((size_t)nm * k, 0.0);
+    for (int i = 0; i < nm; ++i) {
+        int s = 0;
+        for (int j = 0; j < (int)am[i].size() && j < nc; ++j)
+            if (am[i][j] != 0.0) {
+                M.idx[(size_t)i * k + s] = j;
+                M.wts[(size_t)i * k + s] = am[i][j];
+                ++s;
+            }
+    }
+    memset(&M.job, 0, sizeof M.job);
+    M.job.nc = nc;
+    M.job.ac = M.ac.data();
+    M.job.nm = nm;
+    M.job.k = k;
+    M.job.am_idx = M.idx.data();
+    M.job.am_w = M.wts.data();
+    M.job.av = av.data();
+    M.job.bimg = bimg.data();
+    M.job.w = w;
+    M.job.h = h;
+    return true;
+}
+
+}   // namespace
+
+void GradDescStep(std::vector<double> &bnew, std::vector<Point> &dRdc,
+                  const std::vector<Point> &ac, const std::vector<std::vector<double> > &am,
+                  const std::vector<double> &av, const std::vector<double> &bimg, int w, int h)
+{
+    MeshArgs M;
+    const int nc = (int)ac.size();
+    bnew.assign(am.size(), 0.0);
+    dRdc.assign(nc, Point(0.0, 0.0));
+    if (!mesh_args(M, ac, am, av, bimg, w, h, stderr))
+        return;
+    std::vector<double> d(2 * (size_t)nc);
+    if (aln_grad_desc_step(ctx(), &M.job, bnew.data(), d.data(), nullptr) < 0) {
+        fprintf(stderr, "GPU mesh: %s\n", aln_last_error(ctx()));
+        return;
+    }
+    for (int j = 0; j < nc; ++j)
+        dRdc[j] = Point(d[2 * j], d[2 * j + 1]);
+}
+
+double CorrVectors(FILE *flog, const std::vector<double> &a, const std::vector<double> &b,
+                   int *nnz)
+{
+    if (!flog)
+        flog = stdout;
+    if (a.size() != b.size()) {
+        fprintf(flog, "CorrVectors: Sizes differ! %d %ld\n", (int)a.size(), (long)b.size());
+        return 0.0;   // the reference exits here; the library never does
+    }
+    double r = 0.0;
+    if (aln_corr_vectors(ctx(), a.data(), b.data(), (int)a.size(), &r, nnz) < 0) {
+        fprintf(flog, "GPU CorrVectors: %s\n", aln_last_error(ctx()));
+        return 0.0;
+    }
+    return r;
+}
+
+double ImproveControlPts(std::vector<Point> &ac, const std::vector<std::vector<double> > &am,
+                         const std::vector<double> &av, const std::vector<double> &bimg, int w,
+                         int h, FILE *flog, const char *describe, double iniThresh,
+                         double finThresh)
+{
+    MeshArgs M;
+    if (!mesh_args(M, ac, am, av, bimg, w, h, flog))
+        return 0.0;
+    M.job.ini_thresh = iniThresh;
+    M.job.fin_thresh = finThresh;
+    aln_mesh_result r;
+    if (aln_improve_control_pts_batch(ctx(), 1, &M.job, &r) < 0) {
+        fprintf(flog, "GPU mesh: %s\n", aln_last_error(ctx()));
+        return 0.0;
+    }
+    // the reference's report lines (Correlation.cpp:1631-1720)
+    fprintf(flog, "STAT: ImproveCpt: Initial %s correlation %f (%ld pixels).\n", describe,
+            r.corr0, (long)av.size());
+    if (r.corr0 < iniThresh) {
+        fprintf(flog, "FAIL: ImproveCpt: Correlation %f less than %f at start.\n", r.corr0,
+                iniThresh);
+        return 0.0;
+    }
+    if (finThresh < 0) {
+        fprintf(flog, "STAT: ImproveCpt: Skipping optimizer; final corr %f\n", r.corr);
+        return r.corr;
+    }
+    for (size_t j = 0; j < ac.size(); ++j)
+        ac[j] = Point(M.ac[2 * j], M.ac[2 * j + 1]);
+    fprintf(flog, "STAT: ImproveCpt: Final %s correlation %f, (threshold %f).\n", describe,
+            r.corr, finThresh);
+    return r.corr;
+}

@@ -398,3 +398,97 @@ def uneven_batch_torch(seed: int, n: int, device, smin=64, smax=1024):
         out.append(dict(a=a16.to(torch.int16).contiguous(), b=b16.to(torch.int16).contiguous(),
                         truth=(-tx, -ty), ox=0, oy=0, radius=max(1, short // 2)))
     return out
+
+
+# ----------------------------------------------------------------------------
+# mesh-optimizer cases (GradDescStep / ImproveControlPts)
+# ----------------------------------------------------------------------------
+
+def mesh_case(seed: int, box=(96, 80), cells=(2, 2), kind: str = "tri", field=200,
+              warp=1.5, offset=(3.0, -2.0), noise=0.05):
+    """A region-to-region mesh problem.  Region A is the integer points of a
+    box; control points sit on a (cx+1) x (cy+1) lattice over the box, and
+    each point's multipliers are the barycentric weights of its lattice
+    triangle ("tri": 3 per point, cells split along the rising diagonal) or
+    the bilinear weights of its cell ("quad": 4 per point).  B is a smooth
+    synthetic field; A's values are B sampled at the point moved by a smooth
+    warp (an offset plus up to `warp` px of bilinear deformation) with noise,
+    then normalised to mean 0 / sd 1.  The control points start at the
+    lattice moved by the offset alone (the optimiser has the warp to find).
+
+    Returns dict(ac, am_idx, am_w, av, bimg, truth) -- am in compressed rows
+    (indices ascending, -1 unused), ac / truth nc x 2 in B's frame."""
+    rng = np.random.default_rng(seed)
+    f = field_np(seed * 13 + 1, field, field)
+    f = (f - f.mean()) / f.std()
+    bw, bh = box
+    x0 = (field - bw) // 2
+    y0 = (field - bh) // 2
+    gx, gy = cells
+    lx = np.linspace(x0, x0 + bw - 1, gx + 1)
+    ly = np.linspace(y0, y0 + bh - 1, gy + 1)
+    cx, cy = np.meshgrid(lx, ly)
+    ctl = np.stack([cx.ravel(), cy.ravel()], 1)            # j = iy * (gx + 1) + ix
+    dwarp = rng.uniform(-warp, warp, (len(ctl), 2))
+    truth = ctl + np.asarray(offset) + dwarp
+    ys, xs = np.mgrid[y0:y0 + bh, x0:x0 + bw]
+    px, py = xs.ravel().astype(np.float64), ys.ravel().astype(np.float64)
+    ix = np.minimum(((px - x0) / (bw - 1) * gx).astype(int), gx - 1)
+    iy = np.minimum(((py - y0) / (bh - 1) * gy).astype(int), gy - 1)
+    u = (px - lx[ix]) / (lx[ix + 1] - lx[ix])
+    v = (py - ly[iy]) / (ly[iy + 1] - ly[iy])
+    j00 = iy * (gx + 1) + ix
+    j10, j01, j11 = j00 + 1, j00 + gx + 1, j00 + gx + 2
+    if kind == "quad":
+        idx = np.stack([j00, j10, j01, j11], 1)
+        wts = np.stack([(1 - u) * (1 - v), u * (1 - v), (1 - u) * v, u * v], 1)
+    else:
+        lower = u + v <= 1.0
+        # lower triangle (00, 10, 01), upper (10, 01, 11): ascending indices
+        idx = np.where(lower[:, None], np.stack([j00, j10, j01], 1),
+                       np.stack([j10, j01, j11], 1))
+        wts = np.where(lower[:, None], np.stack([1 - u - v, u, v], 1),
+                       np.stack([1 - v, 1 - u, u + v - 1], 1))
+    # true position of each point in B
+    tx = (wts * truth[idx, 0]).sum(1)
+    ty = (wts * truth[idx, 1]).sum(1)
+    av = _bilinear(f, tx, ty) + rng.normal(0.0, noise, len(tx))
+    av = (av - av.mean()) / av.std(ddof=1)
+    ac = ctl + np.asarray(offset)
+    return dict(ac=ac, am_idx=idx.astype(np.int32), am_w=wts, av=av, bimg=f, truth=truth)
+
+
+# ----------------------------------------------------------------------------
+# ApproximateMatch tile pairs
+# ----------------------------------------------------------------------------
+
+def approx_tile_pair(seed: int, tile: int = 512, max_deg=4.0, shift=(90.0, 30.0), jitter=6.0,
+                     noise=6.0):
+    """Two tile x tile uint8 tiles of one synthetic field, overlapping by most
+    of their area: pixel p of A shows field point p + pad; pixel x of B
+    shows field point R(theta)(x - c) + c + s + pad (c the tile centre, s the
+    shift), with gain in [0.9, 1.1] and noise.  So A's pixel p sits in B at
+    R(-theta)(p - c - s) + c: the true a -> b transform.  Tab (what the
+    pipeline predicts) is its translation at the tile centre, -s, off by up
+    to `jitter` px per axis.  Returns dict(a, b, tab, theta, truth T[6])."""
+    rng = np.random.default_rng(seed)
+    theta = float(rng.uniform(-max_deg, max_deg))
+    s = np.asarray(shift, np.float64) * rng.choice([-1.0, 1.0], 2)
+    gain = float(rng.uniform(0.9, 1.1))
+    pad = int(tile * 0.3) + int(abs(s).max()) + 8
+    size = tile + 2 * pad
+    f = field_np(seed * 11 + 7, size, size)
+    a = f[pad:pad + tile, pad:pad + tile]
+    yy, xx = np.mgrid[0:tile, 0:tile].astype(np.float64)
+    c_, s_ = math.cos(math.radians(theta)), math.sin(math.radians(theta))
+    cx = cy = tile / 2.0
+    X = c_ * (xx - cx) - s_ * (yy - cy) + cx + s[0] + pad
+    Y = s_ * (xx - cx) + c_ * (yy - cy) + cy + s[1] + pad
+    b = gain * _bilinear(f, X, Y) + rng.normal(0.0, noise, (tile, tile))
+    # a -> b: x = R(-theta)(p - c - s) + c
+    ci, si = c_, -s_
+    t0 = -(ci * (cx + s[0]) - si * (cy + s[1])) + cx
+    t1 = -(si * (cx + s[0]) + ci * (cy + s[1])) + cy
+    truth = [ci, -si, t0, si, ci, t1]
+    tab = (float(-s[0] + rng.uniform(-jitter, jitter)), float(-s[1] + rng.uniform(-jitter, jitter)))
+    return dict(a=to_u8(a), b=to_u8(b), tab=tab, theta=theta, truth=truth)

@@ -406,6 +406,105 @@ int aln_decimate_batch(aln_ctx *ctx, int n, const aln_image *in,
                        const unsigned char *const *mask, int lbin, int normalize,
                        double *const *out_vals, unsigned char *const *out_mask, double *out_sd);
 
+/* ---- ApproximateMatch ---------------------------------------------------
+ * 1_DMesh/ApproximateMatch.cpp:115-194 for many tile pairs: CThmUtil's Crop
+ * (1_DMesh/CThmUtil.cpp:385-426: the overlap boxes BoxesFromShifts gives for
+ * XYCONF * Tab's translation, or the whole tiles), MakeThumbs (:470-523),
+ * the sweep (:607-633) of a CThmScan set up as ApproximateMatch.cpp:147-154
+ * does, and Finish (:889-971: PostTweaks, FinishAtFullRes,
+ * IsectToImageCoords, the LIMXY test).  The tiles' connected regions are the
+ * whole tiles, px.scl = 1 and Tdfm = identity. */
+typedef struct aln_tile_pair {
+    aln_image a, b;          /* two tiles of equal size and pixel type */
+    double tabx, taby;       /* Tab: the translation of a into b's frame (px) */
+} aln_tile_pair;
+
+typedef struct aln_approx_params {
+    double xyconf;           /* XYCONF: crop to the overlap Tab predicts (0: whole tiles) */
+    int olap1d;              /* OLAP1D */
+    long long olap2d;        /* OLAP2D */
+    int thmdec;              /* THMDEC (1..255) */
+    int mode_prior;          /* 1: UsePriorAngles(ang0, hfangpr) (MODE 'C');
+                                0: DenovoBestAngle(ang0, hfangdn, 0.5) */
+    double ang0, hfangdn, hfangpr;
+    double rthresh, nbmaxht; /* RTRSH, NBMXHT */
+    int pretweak, tweaks;    /* PRETWEAK (sweep), TWEAKS (PostTweaks) */
+    int limxy;               /* LIMXY (0: no test) */
+} aln_approx_params;
+
+typedef struct aln_approx_result {
+    int status;              /* 0 a guess; 1 crop too small; 2 thumbnails too small
+                                or flat; 3 the sweep failed (err); 4 LIMXY reject */
+    int err;                 /* CThmScan err */
+    double A, X, Y, R;       /* the final record, X / Y in tile coordinates */
+    double T[6];             /* the guess (TAffine t[0..5]) */
+    double sweep[4];         /* A, X, Y, R after the sweep (thumbnail units) */
+    int crop[4];             /* crop origins: a's (x, y), b's (x, y) */
+    int crop_w, crop_h;
+} aln_approx_result;
+
+int aln_approx_match_batch(aln_ctx *ctx, int n, const aln_tile_pair *pairs,
+                           const aln_approx_params *params, aln_approx_result *out);
+
+/* ---- mesh optimizer ---------------------------------------------------
+ * GradDescStep, CorrVectors and ImproveControlPts of 0_GEN/Correlation.cpp
+ * (declared Correlation.h:127-152), which 1_DMesh/ImproveMesh.cpp:503 and
+ * 1_DMesh/InSectionOverlap.cpp:303 call after the FFT match to deform a
+ * triangle (or box) mesh of control points for the best correlation.
+ *
+ * The reference's multipliers am are nm dense rows of nc doubles, all zero
+ * but the three or four of the point's triangle or box.  Here each row is
+ * compressed to k slots: am_idx[i*k + s] the control point (ascending
+ * within the row, -1 for an unused slot) and am_w[i*k + s] its multiplier.
+ * Dropping the zero terms leaves every per-point sum as the reference
+ * computes it; the sums over points run in a fixed blocked order on the GPU,
+ * so the results equal the reference's to FP64 rounding of those sums. */
+#define ALN_MESH_MAX_NC 128   /* control points per job */
+#define ALN_MESH_MAX_K 16     /* multiplier slots per point */
+
+typedef struct aln_mesh_job {
+    int nc;                   /* control points, 1..ALN_MESH_MAX_NC */
+    double *ac;               /* nc x 2 (x, y) in B's frame, host: start in,
+                                 optimised points out (ImproveControlPts' ac) */
+    int nm, k;                /* points of region A; slots per point */
+    const int *am_idx;        /* nm x k */
+    const double *am_w;       /* nm x k */
+    const double *av;         /* nm values of A, normalised (mean 0, sd 1) */
+    const double *bimg;       /* w x h raster of B, row-major (w >= 2, h >= 2) */
+    int w, h;
+    double ini_thresh, fin_thresh;   /* ImproveControlPts' iniThresh, finThresh */
+    int on_device;            /* 1: am_idx, am_w, av and bimg are device
+                                 pointers on the context's device */
+} aln_mesh_job;
+
+typedef struct aln_mesh_result {
+    int status;               /* ALN_OK */
+    double corr;              /* ImproveControlPts' return value: the final
+                                 correlation, 0 when the start was below
+                                 ini_thresh, the start when fin_thresh < 0 */
+    double corr0;             /* the starting correlation */
+    int evals;                /* gradient evaluations after the first */
+} aln_mesh_result;
+
+/* ImproveControlPts (0_GEN/Correlation.cpp:1605-1721) for n meshes at once:
+ * the gradient evaluations of all live jobs share each launch; every job
+ * keeps the reference's step rule (10 px halving to 0.05, three small
+ * improvements in a row end it).  jobs[i].ac is updated in place. */
+int aln_improve_control_pts_batch(aln_ctx *ctx, int n, const aln_mesh_job *jobs,
+                                  aln_mesh_result *out);
+
+/* GradDescStep (0_GEN/Correlation.cpp:1403-1478) at job->ac: bnew (nm,
+ * NormalizeNonZeros applied) and dRdc (nc x 2) into host buffers; either
+ * may be NULL.  *corr (may be NULL) receives CorrVectors(av, bnew). */
+int aln_grad_desc_step(aln_ctx *ctx, const aln_mesh_job *job, double *bnew, double *drdc,
+                       double *corr);
+
+/* CorrVectors (0_GEN/Correlation.cpp:1490-1530) of two host vectors of n
+ * doubles: *out the correlation, *nnz (may be NULL) the count of products
+ * not below 1e-8 in magnitude. */
+int aln_corr_vectors(aln_ctx *ctx, const double *a, const double *b, int n, double *out,
+                     int *nnz);
+
 /* ---- allocation-free CorrPatches: no counterpart in the reference ---- */
 
 /* Size of the device scratch array behind aln_corr_patches_noalloc. */

@@ -195,8 +195,63 @@ class _Lib:
         self.lib = C.CDLL(path)
 
 
-class Oracle(_Lib):
+def mesh_arrays(am_idx, am_w, ac):
+    """Compressed multiplier rows (nm x k indices, -1 unused, and weights)
+    and control points (nc x 2) as contiguous arrays."""
+    idx = np.ascontiguousarray(am_idx, np.int32)
+    wts = np.ascontiguousarray(am_w, np.float64)
+    assert idx.shape == wts.shape and idx.ndim == 2
+    return idx, wts, np.ascontiguousarray(ac, np.float64).reshape(-1, 2).copy()
+
+
+class _Mesh:
+    """GradDescStep / CorrVectors / ImproveControlPts
+    (0_GEN/Correlation.cpp:1403-1721) through the prefix's entry points."""
+
+    _pfx = ""
+
+    def _mesh_types(self):
+        for fn in ("corr_vectors", "improve_control_pts"):
+            getattr(self.lib, self._pfx + fn).restype = C.c_double
+
+    def grad_desc_step(self, ac, am_idx, am_w, av, bimg):
+        idx, wts, ac = mesh_arrays(am_idx, am_w, ac)
+        av = np.ascontiguousarray(av, np.float64)
+        bimg = np.ascontiguousarray(bimg, np.float64)
+        nm, k = idx.shape
+        bnew = np.zeros(nm)
+        d = np.zeros((len(ac), 2))
+        getattr(self.lib, self._pfx + "grad_desc_step")(
+            _p(bnew), _p(d), _p(ac), len(ac), _p(idx), _p(wts), k, nm, _p(av), _p(bimg),
+            bimg.shape[1], bimg.shape[0])
+        return bnew, d
+
+    def corr_vectors(self, a, b):
+        a = np.ascontiguousarray(a, np.float64)
+        b = np.ascontiguousarray(b, np.float64)
+        nnz = C.c_int(0)
+        r = getattr(self.lib, self._pfx + "corr_vectors")(_p(a), _p(b), len(a), C.byref(nnz))
+        return r, nnz.value
+
+    def improve_control_pts(self, ac, am_idx, am_w, av, bimg, ini_thresh, fin_thresh):
+        """Returns (corr, optimised control points[, evaluations])."""
+        idx, wts, ac = mesh_arrays(am_idx, am_w, ac)
+        av = np.ascontiguousarray(av, np.float64)
+        bimg = np.ascontiguousarray(bimg, np.float64)
+        nm, k = idx.shape
+        args = [_p(ac), len(ac), _p(idx), _p(wts), k, nm, _p(av), _p(bimg), bimg.shape[1],
+                bimg.shape[0], C.c_double(ini_thresh), C.c_double(fin_thresh)]
+        if self._pfx == "orc_":
+            it = C.c_int(0)
+            r = self.lib.orc_improve_control_pts(*args, C.byref(it))
+            return r, ac, it.value
+        return self.lib.ref_improve_control_pts(*args), ac
+
+
+class Oracle(_Lib, _Mesh):
     """The FP64 C restatement (aln_oracle.c)."""
+
+    _pfx = "orc_"
 
     def __init__(self, path: str | None = None):
         super().__init__(path or build())
@@ -205,6 +260,7 @@ class Oracle(_Lib):
             getattr(L, fn).restype = C.c_double
         L.orc_normalize.restype = C.c_double
         L.orc_linefit_r.restype = C.c_double
+        self._mesh_types()
 
     def corr_patches(self, p1, v1, p2, v2, ox=0, oy=0, radius=4096, lg=None,
                      want_rslt=False):
@@ -364,14 +420,48 @@ class Oracle(_Lib):
                 "ncalls": ncalls.value, "tptwk": tout.tolist()}
 
 
-class Ref(_Lib):
+APPROX_STATUS = {0: "ok", 1: "crop", 2: "thumbs", 3: "sweep", 4: "limxy"}
+
+
+def approx_defaults(**kw):
+    """ApproximateMatch settings (1_DMesh/ApproximateMatch.cpp:120-154 with
+    matchparams-style values) as a dict the Ref and the library take."""
+    d = dict(xyconf=0.75, olap1d=0, olap2d=40000, thmdec=4, mode_prior=0, ang0=0.0,
+             hfangdn=10.0, hfangpr=1.0, rthresh=0.3, nbmaxht=0.75, pretweak=0, tweaks=0,
+             limxy=0)
+    d.update(kw)
+    return d
+
+
+class Ref(_Lib, _Mesh):
     """The reference's own code (compiled from its sources; x86 host only)."""
+
+    _pfx = "ref_"
 
     def __init__(self, path: str | None = None):
         super().__init__(path or REF_SO)
         L = self.lib
         for fn in ("ref_corr_patches", "ref_corr_images", "ref_corr_patch_to_image"):
             getattr(L, fn).restype = C.c_double
+        self._mesh_types()
+
+    def approx_match(self, a, b, tab, **params):
+        """The reference's ApproximateMatch sequence on two whole tiles
+        (refwrap's ref_approx_match).  Returns a dict with status, A, X, Y,
+        R, T, err, sweep (A, X, Y, R), crop (aO, bO, w, h)."""
+        p = approx_defaults(**params)
+        a = np.ascontiguousarray(a, np.float64)
+        b = np.ascontiguousarray(b, np.float64)
+        out = np.zeros(21)
+        st = self.lib.ref_approx_match(
+            _p(a), _p(b), a.shape[1], a.shape[0], C.c_double(tab[0]), C.c_double(tab[1]),
+            C.c_double(p["xyconf"]), p["olap1d"], C.c_long(p["olap2d"]), p["thmdec"],
+            p["mode_prior"], C.c_double(p["ang0"]), C.c_double(p["hfangdn"]),
+            C.c_double(p["hfangpr"]), C.c_double(p["rthresh"]), C.c_double(p["nbmaxht"]),
+            p["pretweak"], p["tweaks"], p["limxy"], _p(out))
+        return {"status": st, "A": out[0], "X": out[1], "Y": out[2], "R": out[3],
+                "T": out[4:10].tolist(), "err": int(out[10]), "sweep": out[11:15].tolist(),
+                "crop": [int(v) for v in out[15:21]]}
 
     def corr_patches(self, p1, v1, p2, v2, ox=0, oy=0, radius=4096, lg=None):
         p1, p2 = _pts(p1), _pts(p2)

@@ -1638,3 +1638,139 @@ int orc_thm_finish(const double *xya, const double *va, int na,
         *ncalls = s.ncalls;
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* Mesh optimizer, 0_GEN/Correlation.cpp:1403-1721                     */
+/* ------------------------------------------------------------------ */
+
+/* NormalizeNonZeros with MeanStd::Stats (sample sd), Maths.cpp:111-124,247-268 */
+static void normalize_nonzeros(double *v, int n)
+{
+    double sum = 0.0, sum2 = 0.0, avg, sd = 0.0;
+    int m = 0;
+    for (int i = 0; i < n; ++i)
+        if (v[i]) {
+            sum += v[i];
+            sum2 += v[i] * v[i];
+            ++m;
+        }
+    avg = sum;
+    if (m > 1) {
+        avg /= m;
+        sd = sqrt(fmax(sum2 - m * avg * avg, 0.0) / (m - 1.0));
+    }
+    for (int i = 0; i < n; ++i)
+        if (v[i])
+            v[i] = (v[i] - avg) / sd;
+}
+
+void orc_grad_desc_step(double *bnew, double *dRdc, const double *ac, int nc,
+                        const int *am_idx, const double *am_w, int k, int nm,
+                        const double *av, const double *bimg, int w, int h)
+{
+    for (int j = 0; j < 2 * nc; ++j)
+        dRdc[j] = 0.0;
+    for (int i = 0; i < nm; ++i) {
+        const int *ix = am_idx + (size_t)i * k;
+        const double *aw = am_w + (size_t)i * k;
+        double x = 0.0, y = 0.0;
+        for (int s = 0; s < k; ++s)
+            if (ix[s] >= 0) {
+                x += aw[s] * ac[2 * ix[s]];
+                y += aw[s] * ac[2 * ix[s] + 1];
+            }
+        if (x < 0.0 || x >= w - 1 || y < 0.0 || y >= h - 1) {
+            bnew[i] = 0.0;
+            continue;
+        }
+        int xl = (int)x, xr = xl + 1, yl = (int)y, yu = yl + 1;
+        double alpha = x - xl, beta = y - yl;
+        double ll = bimg[(size_t)w * yl + xl];
+        double ul = bimg[(size_t)w * yu + xl];
+        double ur = bimg[(size_t)w * yu + xr];
+        double lr = bimg[(size_t)w * yl + xr];
+        double t = lr - ll, u = ul - ll, v = ll - lr - ul + ur;
+        bnew[i] = ll + alpha * t + beta * u + alpha * beta * v;
+        double dbdx = t + beta * v, dbdy = u + alpha * v;
+        dbdx *= av[i];
+        dbdy *= av[i];
+        for (int s = 0; s < k; ++s)
+            if (ix[s] >= 0) {
+                dRdc[2 * ix[s]] += aw[s] * dbdx;
+                dRdc[2 * ix[s] + 1] += aw[s] * dbdy;
+            }
+    }
+    normalize_nonzeros(bnew, nm);
+}
+
+double orc_corr_vectors(const double *a, const double *b, int n, int *nnz)
+{
+    double sum2 = 0.0;
+    int nz = 0, N = n;
+    for (int i = 0; i < n; ++i) {
+        double prod = a[i] * b[i];
+        sum2 += prod;
+        if (fabs(prod) < 1.0E-8)
+            ++nz;
+    }
+    if (!isfinite(sum2)) {
+        nz = N;
+        sum2 = 0.0;
+    }
+    N -= nz;
+    if (nnz)
+        *nnz = N;
+    return N ? sum2 / N : 0.0;
+}
+
+double orc_improve_control_pts(double *ac, int nc, const int *am_idx, const double *am_w,
+                               int k, int nm, const double *av, const double *bimg,
+                               int w, int h, double ini_thresh, double fin_thresh,
+                               int *iters)
+{
+    double *bnew = (double *)malloc(sizeof(double) * (size_t)(nm > 0 ? nm : 1));
+    double *dRdc = (double *)malloc(sizeof(double) * 2 * (size_t)nc);
+    double *dnew = (double *)malloc(sizeof(double) * 2 * (size_t)nc);
+    double *anew = (double *)malloc(sizeof(double) * 2 * (size_t)nc);
+    int inarow = 0, it = 0;
+    orc_grad_desc_step(bnew, dRdc, ac, nc, am_idx, am_w, k, nm, av, bimg, w, h);
+    double corr = orc_corr_vectors(av, bnew, nm, NULL), corr_last = corr;
+    if (corr < ini_thresh)
+        corr = 0.0;
+    else if (fin_thresh >= 0) {
+        for (double step = 10.0; step > 0.05;) {
+            double S = 0.0;
+            for (int i = 0; i < nc; ++i)
+                S += dRdc[2 * i] * dRdc[2 * i] + dRdc[2 * i + 1] * dRdc[2 * i + 1];
+            if (!S)
+                break;   /* all derivatives zero */
+            S = step / sqrt(S);
+            for (int i = 0; i < nc; ++i) {
+                anew[2 * i] = ac[2 * i] + S * dRdc[2 * i];
+                anew[2 * i + 1] = ac[2 * i + 1] + S * dRdc[2 * i + 1];
+            }
+            orc_grad_desc_step(bnew, dnew, anew, nc, am_idx, am_w, k, nm, av, bimg, w, h);
+            double c_new = orc_corr_vectors(av, bnew, nm, NULL);
+            ++it;
+            if (c_new > corr) {
+                memcpy(ac, anew, sizeof(double) * 2 * (size_t)nc);
+                memcpy(dRdc, dnew, sizeof(double) * 2 * (size_t)nc);
+                corr_last = corr;
+                corr = c_new;
+            } else
+                step /= 2.0;
+            if (step <= 2.0 && corr - corr_last < 0.0001) {
+                if (++inarow >= 3)
+                    break;
+            } else
+                inarow = 0;
+        }
+    }
+    free(bnew);
+    free(dRdc);
+    free(dnew);
+    free(anew);
+    if (iters)
+        *iters = it;
+    return corr;
+}

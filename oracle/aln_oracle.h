@@ -160,6 +160,32 @@ int orc_thm_finish(const double *xya, const double *va, int na,
                    const double *prior, const double *tptwk6, orc_thm_rec *best,
                    double *tptwk_out, int *ncalls);
 
+/* ---- mesh optimizer ------------------------------------------------- */
+
+/* The control-point multipliers am (nm rows of nc, mostly zero in the
+ * reference's dense form) are passed compressed: row i's k slots
+ * am_idx[i*k + s] / am_w[i*k + s] hold its nonzero multipliers in increasing
+ * control-point order, unused slots have index -1.  Skipping the zero terms
+ * leaves every sum of the reference's dense loops unchanged, so the results
+ * are the reference's bit for bit. */
+
+/* GradDescStep, 0_GEN/Correlation.cpp:1403-1478 (with NormalizeNonZeros,
+ * Maths.cpp:247-268): bnew[nm], dRdc[2*nc] = (x, y) per control point. */
+void orc_grad_desc_step(double *bnew, double *dRdc, const double *ac, int nc,
+                        const int *am_idx, const double *am_w, int k, int nm,
+                        const double *av, const double *bimg, int w, int h);
+
+/* CorrVectors, 0_GEN/Correlation.cpp:1490-1530 (nnz may be NULL) */
+double orc_corr_vectors(const double *a, const double *b, int n, int *nnz);
+
+/* ImproveControlPts, 0_GEN/Correlation.cpp:1605-1721: ac[2*nc] in/out;
+ * returns the correlation; *iters = GradDescStep evaluations after the
+ * first (may be NULL). */
+double orc_improve_control_pts(double *ac, int nc, const int *am_idx, const double *am_w,
+                               int k, int nm, const double *av, const double *bimg,
+                               int w, int h, double ini_thresh, double fin_thresh,
+                               int *iters);
+
 #ifdef __cplusplus
 }
 #endif

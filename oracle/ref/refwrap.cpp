@@ -13,11 +13,18 @@
  *   Convolve          0_GEN/Correlation.cpp:371-457
  *   CThmScan          0_GEN/CThmScan.cpp (configured as 1_DMesh/ApproximateMatch.cpp:147-154)
  *   DecimateVector / Normalize  0_GEN/Maths.cpp:1315-1364, 192-212
+ *   GradDescStep / CorrVectors / ImproveControlPts  0_GEN/Correlation.cpp:1403-1721
+ *   BoxesFromShifts / BBoxFromPoints  0_GEN/Geometry.cpp:78-176
+ * ref_approx_match chains them as 1_DMesh/ApproximateMatch.cpp does; the
+ * few lines of 1_DMesh/CThmUtil.cpp it needs (that file is not compiled
+ * here) are restated beside it.
  */
 #include "Correlation.h"
 #include "CThmScan.h"
 #include "Maths.h"
 #include "TAffine.h"
+#include "Geometry.h"
+#include <math.h>
 
 #include "../../include/aln_corr.h"
 
@@ -297,6 +304,227 @@ int ref_thm_finish(int na, const double *xya, const double *va,
     for (int i = 0; i < 6; ++i)
         out[4 + i] = T.t[i];
     return S.GetErr();
+}
+
+
+/* The reference's dense multiplier rows from the compressed form
+ * (row i: slots am_idx[i*k + s] / am_w[i*k + s], index -1 unused). */
+static void dense_am(vector<vector<double> > &am, int nm, int nc, int k,
+                     const int *am_idx, const double *am_w)
+{
+    am.assign(nm, vector<double>(nc, 0.0));
+    for (int i = 0; i < nm; ++i)
+        for (int s = 0; s < k; ++s)
+            if (am_idx[(size_t)i * k + s] >= 0)
+                am[i][am_idx[(size_t)i * k + s]] = am_w[(size_t)i * k + s];
+}
+
+void ref_grad_desc_step(double *bnew, double *dRdc, const double *ac, int nc,
+                        const int *am_idx, const double *am_w, int k, int nm,
+                        const double *av, const double *bimg, int w, int h)
+{
+    vector<vector<double> > am;
+    dense_am(am, nm, nc, k, am_idx, am_w);
+    vector<Point> c(nc), d;
+    for (int j = 0; j < nc; ++j)
+        c[j] = Point(ac[2 * j], ac[2 * j + 1]);
+    vector<double> a(av, av + nm), b(bimg, bimg + (size_t)w * h), bn;
+    GradDescStep(bn, d, c, am, a, b, w, h);
+    for (int i = 0; i < nm; ++i)
+        bnew[i] = bn[i];
+    for (int j = 0; j < nc; ++j) {
+        dRdc[2 * j] = d[j].x;
+        dRdc[2 * j + 1] = d[j].y;
+    }
+}
+
+double ref_corr_vectors(const double *a, const double *b, int n, int *nnz)
+{
+    vector<double> va(a, a + n), vb(b, b + n);
+    return CorrVectors(quiet_log(), va, vb, nnz);
+}
+
+double ref_improve_control_pts(double *ac, int nc, const int *am_idx, const double *am_w,
+                               int k, int nm, const double *av, const double *bimg, int w,
+                               int h, double ini_thresh, double fin_thresh)
+{
+    vector<vector<double> > am;
+    dense_am(am, nm, nc, k, am_idx, am_w);
+    vector<Point> c(nc);
+    for (int j = 0; j < nc; ++j)
+        c[j] = Point(ac[2 * j], ac[2 * j + 1]);
+    vector<double> a(av, av + nm), b(bimg, bimg + (size_t)w * h);
+    double r = ImproveControlPts(c, am, a, b, w, h, quiet_log(), "golden", ini_thresh,
+                                 fin_thresh);
+    for (int j = 0; j < nc; ++j) {
+        ac[2 * j] = c[j].x;
+        ac[2 * j + 1] = c[j].y;
+    }
+    return r;
+}
+
+
+/* CThmUtil's SubI (1_DMesh/CThmUtil.h): points relative to their bbox. */
+struct SubIRec {
+    vector<double> v;
+    vector<Point> p;
+    Point O;
+    int w, h;
+};
+
+/* SubI_ThesePoints, 1_DMesh/CThmUtil.cpp:163-189 (values of a w-wide raster) */
+static void subi_these(SubIRec &S, const double *v, int w, const vector<Point> &p)
+{
+    IBox B;
+    BBoxFromPoints(B, p);
+    S.v.resize(p.size());
+    S.p.resize(p.size());
+    for (size_t i = 0; i < p.size(); ++i) {
+        S.v[i] = v[int(p[i].x) + w * int(p[i].y)];
+        S.p[i].x = p[i].x - B.L;
+        S.p[i].y = p[i].y - B.B;
+    }
+    S.O = Point(B.L, B.B);
+    S.w = B.R - B.L + 1;
+    S.h = B.T - B.B + 1;
+}
+
+/* MakeThumbs, 1_DMesh/CThmUtil.cpp:470-523 */
+static bool make_thumbs(ThmRec &thm, const SubIRec &a, const SubIRec &b, int dec, long olap2d,
+                        int olap1d)
+{
+    thm.av = a.v;
+    thm.bv = b.v;
+    thm.ap = a.p;
+    thm.bp = b.p;
+    thm.ftc.clear();
+    thm.reqArea = olap2d;
+    thm.olap1D = olap1d;
+    thm.scl = dec;
+    if (dec > 1) {
+        DecimateVector(thm.ap, thm.av, a.w, a.h, dec);
+        DecimateVector(thm.bp, thm.bv, b.w, b.h, dec);
+        thm.reqArea /= dec * dec;
+        thm.olap1D /= dec;
+    }
+    if ((long)thm.ap.size() < thm.reqArea)
+        return false;
+    if (!Normalize(thm.av) || !Normalize(thm.bv))
+        return false;
+    return true;
+}
+
+/*
+ * ApproximateMatch (1_DMesh/ApproximateMatch.cpp:115-194) for one pair of
+ * w x h tiles whose connected regions are the whole tiles, px.scl = 1,
+ * Tdfm = identity, MODE 'C' (mode_prior = 1: UsePriorAngles from ang0 with
+ * HFANGPR) or a denovo sweep (mode_prior = 0: DenovoBestAngle(ang0, HFANGDN,
+ * 0.5)); Tab = the translation (tabx, taby) of a into b.  Crop with XYCONF
+ * (CThmUtil.cpp:385-426), MakeThumbs(THMDEC), the sweep, Finish
+ * (CThmUtil.cpp:889-971: PostTweaks when TWEAKS, X, Y scaled back,
+ * MakeThumbs(1), FinishAtFullRes, IsectToImageCoords, Check_LIMXY).
+ * Returns 0 ok, 1 crop too small, 2 thumbnails too small or flat, 3 sweep
+ * failed, 4 LIMXY rejection.  out[0..3] A, X, Y, R; out[4..9] T;
+ * out[10] err; out[11..14] the sweep's A, X, Y, R; out[15..18] the crop
+ * origins aO, bO; out[19..20] the crop size.
+ */
+int ref_approx_match(const double *a, const double *b, int w, int h, double tabx,
+                     double taby, double xyconf, int olap1d, long olap2d, int thmdec,
+                     int mode_prior, double ang0, double hfangdn, double hfangpr,
+                     double rthresh, double nbmaxht, int pretweak, int tweaks, int limxy,
+                     double *out)
+{
+    FILE *flog = quiet_log();
+    for (int i = 0; i < 21; ++i)
+        out[i] = 0.0;
+    vector<Point> all;
+    all.reserve((size_t)w * h);
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x)
+            all.push_back(Point(x, y));
+    SubIRec oa, ob;
+    bool whole = xyconf == 0.0;
+    IBox Ba, Bb;
+    if (!whole) {
+        const int dx = int(xyconf * tabx), dy = int(xyconf * taby);
+        BoxesFromShifts(Ba, Bb, w, h, w, h, dx, dy);
+        const int ow = Ba.R - Ba.L + 1, oh = Ba.T - Ba.B + 1;
+        const int min1d = olap1d > 8 ? olap1d : 8;
+        whole = ow < min1d || oh < min1d;
+    }
+    if (whole) {
+        subi_these(oa, a, w, all);
+        subi_these(ob, b, w, all);
+    } else {
+        const IBox *Bx[2] = {&Ba, &Bb};
+        SubIRec *S[2] = {&oa, &ob};
+        const double *V[2] = {a, b};
+        for (int q = 0; q < 2; ++q) {
+            vector<Point> sel;
+            for (const Point &P : all)
+                if (P.x >= Bx[q]->L && P.x <= Bx[q]->R && P.y >= Bx[q]->B && P.y <= Bx[q]->T)
+                    sel.push_back(P);
+            if ((long)sel.size() <= olap2d)
+                return 1;
+            subi_these(*S[q], V[q], w, sel);
+        }
+    }
+    out[15] = oa.O.x;
+    out[16] = oa.O.y;
+    out[17] = ob.O.x;
+    out[18] = ob.O.y;
+    out[19] = oa.w;
+    out[20] = oa.h;
+    ThmRec thm;
+    if (!make_thumbs(thm, oa, ob, thmdec, olap2d, olap1d))
+        return 2;
+    CThmScan S;
+    CorRec best;
+    S.Initialize(flog, best);
+    S.SetTdfm(TAffine());
+    S.SetRThresh(rthresh);
+    S.SetNbMaxHt(nbmaxht);
+    S.SetSweepConstXY(true);
+    S.SetSweepPretweak(pretweak);
+    S.SetUseCorrR(true);
+    S.SetDisc(0, 0, -1, -1);
+    const bool ok = mode_prior ? S.UsePriorAngles(best, 1, ang0, hfangpr, thm)
+                               : S.DenovoBestAngle(best, ang0, hfangdn, 0.5, thm, true);
+    out[11] = best.A;
+    out[12] = best.X;
+    out[13] = best.Y;
+    out[14] = best.R;
+    out[10] = S.GetErr();
+    if (!ok)
+        return 3;
+    if (tweaks)
+        S.PostTweaks(best, thm);
+    best.X *= thm.scl;
+    best.Y *= thm.scl;
+    if (!make_thumbs(thm, oa, ob, 1, olap2d, olap1d))
+        return 2;
+    S.FinishAtFullRes(best, thm);
+    // IsectToImageCoords, CThmUtil.cpp:657-668
+    Point aO = oa.O;
+    best.T.Apply_R_Part(aO);
+    best.X += ob.O.x - aO.x;
+    best.Y += ob.O.y - aO.y;
+    best.T.SetXY(best.X, best.Y);
+    out[0] = best.A;
+    out[1] = best.X;
+    out[2] = best.Y;
+    out[3] = best.R;
+    for (int i = 0; i < 6; ++i)
+        out[4 + i] = best.T.t[i];
+    out[10] = S.GetErr();
+    // Check_LIMXY, CThmUtil.cpp:817-845
+    TAffine Tab(1.0, 0.0, tabx, 0.0, 1.0, taby), I;
+    I.InverseOf(Tab);
+    I = I * best.T;
+    const double err = sqrt(I.t[2] * I.t[2] + I.t[5] * I.t[5]);
+    if (limxy && err > limxy)
+        return 4;
+    return 0;
 }
 
 } /* extern "C" */

@@ -241,6 +241,55 @@ def decimate_cases(ref):
     return {"dec8": dict(pa=A, va=VA, w=256, h=256, lbin=8, xy=xy, v=v)}
 
 
+def mesh_cases(ref):
+    """GradDescStep / ImproveControlPts (0_GEN/Correlation.cpp:1403-1721):
+    triangle and bilinear multipliers, several lattices, and the early exits
+    (initial correlation below iniThresh; finThresh < 0 skips the search)."""
+    out = {}
+    specs = [("tri22", 1, "tri", (2, 2), 0.2, 0.5), ("quad21", 2, "quad", (2, 1), 0.2, 0.5),
+             ("tri33", 3, "tri", (3, 3), 0.2, 0.5), ("quad33", 4, "quad", (3, 3), 0.2, 0.5),
+             ("lowini", 5, "tri", (2, 2), 0.999, 0.5), ("skip", 6, "quad", (2, 2), 0.2, -1.0)]
+    for name, seed, kind, cells, ini, fin in specs:
+        c = synth.mesh_case(seed, box=(72, 60), cells=cells, kind=kind, field=140)
+        bnew, d = ref.grad_desc_step(c["ac"], c["am_idx"], c["am_w"], c["av"], c["bimg"])
+        cv, nnz = ref.corr_vectors(c["av"], bnew)
+        r, ac = ref.improve_control_pts(c["ac"], c["am_idx"], c["am_w"], c["av"], c["bimg"],
+                                        ini, fin)
+        out["mesh_" + name] = dict(ac0=c["ac"], am_idx=c["am_idx"], am_w=c["am_w"], av=c["av"],
+                                   bimg=c["bimg"], ini=ini, fin=fin, bnew0=bnew, drdc0=d,
+                                   corr0=cv, nnz0=nnz, corr=r, ac=ac)
+    return out
+
+
+def approx_cases(ref):
+    """ApproximateMatch's chain (1_DMesh/ApproximateMatch.cpp:115-194) through
+    the reference's own functions: crop, thumbnails, denovo and prior
+    sweeps, PostTweaks, FinishAtFullRes, the coordinate change, and the
+    early exits (crop too small, LIMXY)."""
+    out = {}
+    specs = [("denovo", 1, {}, None), ("tweaks", 2, dict(tweaks=1), None),
+             ("prior", 3, dict(mode_prior=1, hfangpr=2.0), "theta"),
+             ("whole", 4, dict(xyconf=0.0, olap2d=20000), None),
+             ("nocrop", 5, dict(olap2d=200000), None), ("limxy", 6, dict(limxy=1), None)]
+    for name, seed, kw, ang in specs:
+        c = synth.approx_tile_pair(seed, tile=384, shift=(70.0, 24.0))
+        if ang:
+            kw = dict(kw, ang0=round(-c["theta"] * 2) / 2)   # a prior near the truth
+        prm = O.approx_defaults(olap2d=kw.pop("olap2d", 20000), **kw)
+        r = ref.approx_match(c["a"], c["b"], c["tab"], **prm)
+        out["approx_" + name] = dict(a=c["a"], b=c["b"], tab=np.array(c["tab"]),
+                                     truth=np.array(c["truth"]),
+                                     params=np.array([prm[k] for k in APPROX_KEYS], np.float64),
+                                     status=r["status"], A=r["A"], X=r["X"], Y=r["Y"], R=r["R"],
+                                     T=np.array(r["T"]), err=r["err"], sweep=np.array(r["sweep"]),
+                                     crop=np.array(r["crop"]))
+    return out
+
+
+APPROX_KEYS = ("xyconf", "olap1d", "olap2d", "thmdec", "mode_prior", "ang0", "hfangdn",
+               "hfangpr", "rthresh", "nbmaxht", "pretweak", "tweaks", "limxy")
+
+
 def save(name, d):
     flat = {}
     for case, fields in d.items():
@@ -266,6 +315,8 @@ def main():
     save("thm_finish", thm_finish_cases(ref))
     save("thm_scan_f", thm_f_cases(ref))
     save("decimate", decimate_cases(ref))
+    save("mesh", mesh_cases(ref))
+    save("approx", approx_cases(ref))
 
 
 if __name__ == "__main__":

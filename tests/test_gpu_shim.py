@@ -155,3 +155,46 @@ def test_cpp_thmscan_callbacks_and_table(tmp_path):
     mid = vals[2]
     assert abs(mid[1] - table["R"]) <= 1e-4 and abs(mid[2] - table["X"]) <= 1e-3 and \
         abs(mid[3] - table["Y"]) <= 1e-3
+
+
+def test_cpp_mesh_optimizer_through_shim(tmp_path):
+    """GradDescStep / CorrVectors / ImproveControlPts called with the
+    reference's dense multiplier rows through the C++ drop-in: the reference's
+    golden numbers (the GPU sums in blocks: 1e-9 on correlations, 1e-6 px)."""
+    import struct
+    from alignment_projects_gb300 import build as b
+    shim = b.build_shim()
+    exe = os.path.join(str(tmp_path), "mesh_check")
+    here = os.path.dirname(os.path.abspath(__file__))
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-o", exe,
+                           os.path.join(here, "cpp", "mesh_check.cpp"),
+                           "-I" + os.path.join(here, "..", "alignment_projects_gb300", "shim"),
+                           "-L" + os.path.dirname(shim), "-laln_corr_shim", "-laln_corr",
+                           "-Wl,-rpath," + os.path.dirname(shim)])
+    cases = load_golden("mesh")
+    names = sorted(cases)
+    blob = b""
+    for n in names:
+        d = cases[n]
+        nc, nm = len(d["ac0"]), len(d["av"])
+        h, w = d["bimg"].shape
+        dense = np.zeros((nm, nc))
+        rows = np.repeat(np.arange(nm), d["am_idx"].shape[1])
+        idx = d["am_idx"].ravel()
+        keep = idx >= 0
+        dense[rows[keep], idx[keep]] = d["am_w"].ravel()[keep]
+        blob += struct.pack("<4i2d", nc, nm, w, h, float(d["ini"]), float(d["fin"]))
+        blob += np.ascontiguousarray(d["ac0"], np.float64).tobytes() + dense.tobytes()
+        blob += np.ascontiguousarray(d["av"]).tobytes() + np.ascontiguousarray(d["bimg"]).tobytes()
+    path = os.path.join(str(tmp_path), "mesh.bin")
+    with open(path, "wb") as f:
+        f.write(blob)
+    out = subprocess.run([exe, path], check=True, capture_output=True, text=True).stdout
+    lines = out.strip().splitlines()
+    assert len(lines) == len(names)
+    for n, ln in zip(names, lines):
+        d = cases[n]
+        v = [float(x) for x in ln.split()]
+        assert abs(v[0] - float(d["corr0"])) <= 1e-9, n
+        assert abs(v[1] - float(d["corr"])) <= 1e-9, n
+        assert np.abs(np.array(v[2:]).reshape(-1, 2) - d["ac"]).max() <= 1e-6, n

@@ -160,3 +160,19 @@ def test_decimate_against_reference_build(lbin, masked):
     assert np.array_equal(vo, vr)
     if lbin == 16:   # a full 16 x 16 bin is dropped
         assert len(xr) < (-(-w // 16)) * (-(-h // 16))
+
+
+@pytest.mark.parametrize("case", sorted(load_golden("mesh")))
+def test_mesh_optimizer_golden(orc, case):
+    """GradDescStep, CorrVectors and ImproveControlPts: the restatement is the
+    reference's bit for bit (same sums in the same order)."""
+    d = load_golden("mesh")[case]
+    bnew, drdc = orc.grad_desc_step(d["ac0"], d["am_idx"], d["am_w"], d["av"], d["bimg"])
+    assert np.array_equal(bnew, d["bnew0"])
+    assert np.array_equal(drdc, d["drdc0"])
+    cv, nnz = orc.corr_vectors(d["av"], bnew)
+    assert cv == float(d["corr0"]) and nnz == int(d["nnz0"])
+    r, ac, it = orc.improve_control_pts(d["ac0"], d["am_idx"], d["am_w"], d["av"], d["bimg"],
+                                        float(d["ini"]), float(d["fin"]))
+    assert r == float(d["corr"])
+    assert np.array_equal(ac, d["ac"])

@@ -28,6 +28,9 @@ EXPECTED = {
                    "PFbiiPvESC_SE_SC_ddiiiiRS2_ISt7complexIdESaISG_EE",
     "CorrImagesS": "_Z11CorrImagesSP8_IO_FILEiRdS1_RKSt6vectorI5PointSaIS3_EERKS2_IdSaIdEES7_SB_"
                    "PFbiiPvESC_SE_SC_ddiiiiRS2_ISt7complexIdESaISG_EE",
+    "GradDescStep": "_Z12GradDescStepRSt6vectorIdSaIdEERS_I5PointSaIS3_EERKS5_RKS_IS1_SaIS1_EERKS1_SE_ii",
+    "CorrVectors": "_Z11CorrVectorsP8_IO_FILERKSt6vectorIdSaIdEES5_Pi",
+    "ImproveControlPts": "_Z17ImproveControlPtsRSt6vectorI5PointSaIS0_EERKS_IS_IdSaIdEESaIS5_EERKS5_SB_iiP8_IO_FILEPKcdd",
 }
 
 
