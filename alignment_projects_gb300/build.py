@@ -1,6 +1,7 @@
 """Compile the GB300 library (libaln_corr.so) in-tree with nvcc for sm_103a."""
 from __future__ import annotations
 
+import hashlib
 import os
 import subprocess
 import sys
@@ -13,7 +14,8 @@ LIB = os.path.join(LIBDIR, "libaln_corr.so")
 
 SOURCES = ["aln_corr.cu"]
 HEADERS = ["aln_fft.cuh", "aln_fft_reg.cuh", "aln_corr_kernels.cuh", "aln_pipeline.cuh",
-           "aln_sweep.cuh", "aln_server.cuh", "aln_mesh.cuh", "aln_approx.cuh"]
+           "aln_sweep.cuh", "aln_server.cuh", "aln_mesh.cuh", "aln_approx.cuh",
+           "aln_tune.cuh", "aln_points.cuh"]
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-O3", "-lineinfo", "-std=c++17",
@@ -68,7 +70,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     os.makedirs(LIBDIR, exist_ok=True)
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [_nvcc()] + NVCC_FLAGS + ["-shared", "-o", tmp] + srcs + ["-lcudart"]
+    # the build id names the autotuner's choice file: a new build measures anew
+    h = hashlib.sha1()
+    for d in deps:
+        with open(d, "rb") as f:
+            h.update(f.read())
+    cmd = ([_nvcc()] + NVCC_FLAGS + ['-DALN_BUILD_ID="%s"' % h.hexdigest()[:12],
+                                     "-shared", "-o", tmp] + srcs + ["-lcudart", "-ldl"])
     if verbose:
         print(" ".join(cmd), file=sys.stderr)
     subprocess.check_call(cmd)

@@ -39,8 +39,11 @@
 #include "../../include/aln_corr.h"
 
 #include <cuda_runtime.h>
+#include <ctype.h>
 #include <math.h>
 #include <stdarg.h>
+#include <stdlib.h>
+#include <sys/stat.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -1031,6 +1034,11 @@ struct aln_ctx {
     int seg_ns;                                  // CorrPatches column segments:
                                                  // 0 cost model, -1 off, > 0 forced length
     int sms;                                     // SM count (0: not queried yet)
+    char *pts_buf[2];                            // aln_points_image rasters, per slot
+    size_t pts_cap[2];
+    int tune_on;                                 // measured segment choices (aln_tune.cuh)
+    int tuning;                                  // inside a timing run
+    long long tune_classes;                      // classes this context measured
 };
 
 static cudaEvent_t ev_get(aln_ctx *c)
@@ -1196,6 +1204,16 @@ extern "C" int aln_ctx_create(int device, aln_ctx **out)
     ctx->sweep_serial = 0;
     ctx->chunks = 0;
     ctx->h2d_copies = 0;
+    ctx->seg_ns = 0;
+    ctx->sms = 0;
+    {
+        const char *t = getenv("ALN_TUNE");
+        ctx->tune_on = !(t && t[0] == '0');
+    }
+    ctx->tuning = 0;
+    ctx->tune_classes = 0;
+    ctx->pts_buf[0] = ctx->pts_buf[1] = nullptr;
+    ctx->pts_cap[0] = ctx->pts_cap[1] = 0;
     if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&ctx->cstream, cudaStreamNonBlocking)) != cudaSuccess) {
         set_err(nullptr, ALN_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
@@ -1256,6 +1274,9 @@ extern "C" void aln_ctx_destroy(aln_ctx *ctx)
     for (auto &f : ctx->spec_free)
         cudaFree(f.second);
     cudaFree(ctx->dsel);
+    for (int q = 0; q < 2; ++q)
+        if (ctx->pts_buf[q])
+            cudaFree(ctx->pts_buf[q]);
     if (ctx->hres)
         cudaFreeHost(ctx->hres);
     for (int q = 0; q < 2; ++q) {
@@ -1484,6 +1505,8 @@ static void need_rows(const PairDev &d, int img, int lo[2], int hi[2])
     }
 }
 
+#include "aln_tune.cuh"
+
 static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_transpose = false,
                      const ImgSpec *spec = nullptr, bool allow_segment = false)
 {
@@ -1655,6 +1678,8 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
             };
             double best = 0.85 * cost(d.Ny, 3);
             int bns = 0, bseg = 0;
+            std::vector<int> valid;   // segment lengths this pair can take
+            auto nseg_of = [&](int ns) { return (d.h[0] + (ns - Wy + 1) - 1) / (ns - Wy + 1); };
             for (int ns = 64; ns <= 2048 && ns < d.Ny; ns *= 2) {
                 if (pol > 0 && ns != pol)
                     continue;
@@ -1663,14 +1688,37 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
                 // storage row): that must stay >= 0 for the window's rows
                 if (B < 1 || ns <= -d.ylo)
                     continue;
-                const int nseg = (d.h[0] + B - 1) / B;
+                const int nseg = nseg_of(ns);
                 if (nseg > 64)
                     continue;
+                valid.push_back(ns);
                 const double c = cost(ns, 2 * nseg + 1);
                 if (pol > 0 || c < best) {
                     best = c;
                     bns = ns;
                     bseg = nseg;
+                }
+            }
+            // the measured choice of the pair's class (aln_tune.cuh): the
+            // candidates are the cost model's pick, then one transform per
+            // column, then the other valid lengths
+            if (pol == 0 && !valid.empty()) {
+                std::vector<int> cand{bns};
+                if (bns)
+                    cand.push_back(0);
+                for (int ns : valid)
+                    if (ns != bns)
+                        cand.push_back(ns);
+                int t = -1;
+                if (ctx && ctx->tune_on && !ctx->tuning)
+                    t = tuned_segment(ctx, P, d, Wy, cand);
+                else if (!ctx)
+                    t = recorded_segment(d, Wy);
+                if (t == 0) {
+                    bns = 0;
+                } else if (t > 0 && std::find(valid.begin(), valid.end(), t) != valid.end()) {
+                    bns = t;
+                    bseg = nseg_of(t);
                 }
             }
             if (bns) {
@@ -2919,6 +2967,7 @@ extern "C" long long aln_ctx_counter(aln_ctx *ctx, int which)
     case 5: return (long long)ctx->spec_bytes;
     case 6: return ctx->chunks;
     case 7: return ctx->h2d_copies;
+    case 8: return ctx->tune_classes;
     default: return -1;
     }
 }
@@ -2928,6 +2977,14 @@ extern "C" int aln_ctx_set_segmenting(aln_ctx *ctx, int ns)
     if (!ctx || ns < -1 || (ns > 0 && (ns < 64 || ns > 2048 || (ns & (ns - 1)))))
         return ctx ? set_err(ctx, ALN_ERR_ARG, "segment length %d", ns) : ALN_ERR_ARG;
     ctx->seg_ns = ns;
+    return ALN_OK;
+}
+
+extern "C" int aln_ctx_set_tuning(aln_ctx *ctx, int on)
+{
+    if (!ctx)
+        return ALN_ERR_ARG;
+    ctx->tune_on = on ? 1 : 0;
     return ALN_OK;
 }
 
@@ -3145,6 +3202,7 @@ extern "C" int aln_corr_patches_noalloc(const aln_image *a, const aln_image *b, 
 }
 
 #include "aln_sweep.cuh"
+#include "aln_points.cuh"
 #include "aln_approx.cuh"
 #include "aln_mesh.cuh"
 #include "aln_server.cuh"

@@ -240,9 +240,13 @@ def lib():
                                             C.POINTER(C.c_int), C.POINTER(C.c_int),
                                             C.POINTER(C.c_int)]
         L.aln_ctx_set_segmenting.argtypes = [C.c_void_p, C.c_int]
+        L.aln_ctx_set_tuning.argtypes = [C.c_void_p, C.c_int]
         L.aln_approx_match_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnTilePair),
                                              C.POINTER(AlnApproxParams),
                                              C.POINTER(AlnApproxResult)]
+        L.aln_points_image.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                       C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.POINTER(AlnImage), C.c_void_p]
         L.aln_improve_control_pts_batch.argtypes = [C.c_void_p, C.c_int,
                                                     C.POINTER(AlnMeshJob),
                                                     C.POINTER(AlnMeshResult)]
@@ -358,12 +362,19 @@ class Context:
                 "spec_fills": self._L.aln_ctx_counter(self.h, 4),
                 "spec_bytes": self._L.aln_ctx_counter(self.h, 5),
                 "chunks": self._L.aln_ctx_counter(self.h, 6),
-                "h2d_copies": self._L.aln_ctx_counter(self.h, 7)}
+                "h2d_copies": self._L.aln_ctx_counter(self.h, 7),
+                "tune_classes": self._L.aln_ctx_counter(self.h, 8)}
 
     def set_segmenting(self, ns: int):
-        """CorrPatches column segments: 0 cost model, -1 off, or a forced
-        segment transform length (power of two, 64..2048)."""
+        """CorrPatches column segments: 0 the class's measured plan (or the
+        cost model with tuning off), -1 off, or a forced segment transform
+        length (power of two, 64..2048)."""
         self._check(self._L.aln_ctx_set_segmenting(self.h, ns))
+
+    def set_tuning(self, on: bool):
+        """Measured column plans per pair class (the autotuner) or the fixed
+        cost model."""
+        self._check(self._L.aln_ctx_set_tuning(self.h, int(bool(on))))
 
     def set_spectrum_cache(self, nbytes: int):
         self._check(self._L.aln_ctx_set_spectrum_cache(self.h, nbytes))
@@ -519,6 +530,18 @@ class Context:
         return [{"status": r.status, "err": r.err, "A": r.A, "X": r.X, "Y": r.Y, "R": r.R,
                  "T": list(r.T), "sweep": list(r.sweep),
                  "crop": list(r.crop) + [r.crop_w, r.crop_h]} for r in res]
+
+    def points_image(self, xy, v, xmin, ymin, w, h, slot=0):
+        """ImageFromValuesAndPoints / DistributePixel on the device: returns
+        (h x w FP64 raster copy, the aln_image of the device raster)."""
+        xy = np.ascontiguousarray(xy, np.float64).reshape(-1, 2)
+        v = np.ascontiguousarray(v, np.float64)
+        out = np.zeros((h, w), np.float64)
+        im = AlnImage()
+        self._check(self._L.aln_points_image(self.h, slot, len(v), xy.ctypes.data,
+                                             v.ctypes.data, xmin, ymin, w, h, C.byref(im),
+                                             out.ctypes.data))
+        return out, im
 
     def improve_control_pts_batch(self, jobs) -> list:
         """ImproveControlPts for a list of mesh_job()s at once.  Returns per

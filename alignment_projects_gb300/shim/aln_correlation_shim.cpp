@@ -3,8 +3,9 @@
 //
 // What the shim does on the host is the boundary's format work only: point
 // lists become bounding-box rasters (BBoxFromPoints, 0_GEN/Geometry.cpp:
-// 78-106; ImageFromValuesAndPoints / DistributePixel, Geometry.cpp:661-685,
-// Maths.h:236-276), EvalType callbacks become typed legality descriptors,
+// 78-106; integer points are placed, fractional clouds go to the device's
+// DistributePixel splat, aln_points_image), EvalType callbacks become typed
+// legality descriptors,
 // the reference's fft2 / ftc cache vectors become spectrum-cache keys.  Every
 // correlation runs on the GPU; there is no CPU fallback: if the GPU library
 // fails, the call logs the error to flog and returns 0.0, the reference's
@@ -27,6 +28,7 @@ using aln_shim::ctx;
 using aln_shim::IBoxD;
 using aln_shim::bbox;
 using aln_shim::raster;
+using aln_shim::image_of_points;
 using aln_shim::image_of;
 using aln_shim::key_of;
 
@@ -134,11 +136,13 @@ double CorrPatches(FILE *flog, int verbose, double &dx, double &dy,
     if (ip1.empty() || ip2.empty())
         return 0.0;
     const IBoxD B1 = bbox(ip1), B2 = bbox(ip2);
-    const std::vector<double> r1 = raster(ip1, iv1, B1), r2 = raster(ip2, iv2, B2);
+    std::vector<double> r1, r2;
     aln_pair P;
     memset(&P, 0, sizeof P);
-    P.a = image_of(r1, B1);
-    P.b = image_of(r2, B2);
+    if (!image_of_points(ip1, iv1, B1, 0, r1, P.a) || !image_of_points(ip2, iv2, B2, 1, r2, P.b)) {
+        fprintf(flog, "CorrPatches (GPU): %s\n", aln_last_error(ctx()));
+        return 0.0;
+    }
     P.ox = Ox;
     P.oy = Oy;
     P.radius = radius;
@@ -193,11 +197,13 @@ double corr_images(int kind, FILE *flog, int verbose, double &dx, double &dy,
     if (ip1.empty() || ip2.empty())
         return 0.0;
     const IBoxD B1 = bbox(ip1), B2 = bbox(ip2);
-    const std::vector<double> r1 = raster(ip1, iv1, B1), r2 = raster(ip2, iv2, B2);
+    std::vector<double> r1, r2;
     aln_image_job J;
     memset(&J, 0, sizeof J);
-    J.a = image_of(r1, B1);
-    J.b = image_of(r2, B2);
+    if (!image_of_points(ip1, iv1, B1, 0, r1, J.a) || !image_of_points(ip2, iv2, B2, 1, r2, J.b)) {
+        fprintf(flog, "CorrImages (GPU): %s\n", aln_last_error(ctx()));
+        return 0.0;
+    }
     J.kind = kind;
     J.mincor = mincor;
     J.nbmaxht = nbmaxht;

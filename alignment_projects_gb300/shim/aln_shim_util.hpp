@@ -1,9 +1,9 @@
 // aln_shim_util.hpp -- host helpers shared by the C++ drop-ins
 // (aln_correlation_shim.cpp, aln_thmscan_shim.cpp): the per-thread GPU
 // context, point lists -> bounding-box rasters (BBoxFromPoints,
-// 0_GEN/Geometry.cpp:78-106; ImageFromValuesAndPoints / DistributePixel,
-// Geometry.cpp:661-685, Maths.h:236-276) and the fft2 / ftc cache vectors ->
-// spectrum-cache keys.
+// 0_GEN/Geometry.cpp:78-106; integer points placed on the host, fractional
+// clouds splatted on the device by aln_points_image) and the fft2 / ftc
+// cache vectors -> spectrum-cache keys.
 #pragma once
 
 #include <math.h>
@@ -93,6 +93,35 @@ inline aln_image image_of(const std::vector<double> &I, const IBoxD &B)
     im.y0 = B.B;
     im.on_device = 0;
     return im;
+}
+
+// A point list's raster as an aln_image.  Integer points are placed on the
+// host (each value lands on its own pixel; that is a copy, duplicates add);
+// a cloud with fractional points is splatted on the device with
+// DistributePixel's bilinear weights (aln_points_image, context slot
+// `slot`, valid until the next call with that slot).
+template <class P>
+inline bool image_of_points(const std::vector<P> &p, const std::vector<double> &v,
+                            const IBoxD &B, int slot, std::vector<double> &host, aln_image &im)
+{
+    bool integral = true;
+    for (const P &q : p)
+        if (q.x != floor(q.x) || q.y != floor(q.y)) {
+            integral = false;
+            break;
+        }
+    if (integral) {
+        host = raster(p, v, B);
+        im = image_of(host, B);
+        return true;
+    }
+    std::vector<double> xy(2 * p.size());
+    for (size_t k = 0; k < p.size(); ++k) {
+        xy[2 * k] = p[k].x;
+        xy[2 * k + 1] = p[k].y;
+    }
+    return aln_points_image(ctx(), slot, (int)p.size(), xy.data(), v.data(), B.L, B.B,
+                            B.R - B.L + 1, B.T - B.B + 1, &im, nullptr) == ALN_OK;
 }
 
 // fft2 / ftc: the reference reuses image 2's spectrum while the vector keeps

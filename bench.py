@@ -1293,6 +1293,22 @@ def run_uneven(args, embedded=False):
     prof = ctx.profile()
     cnt = ctx.counters()
     value = ws * n * args.steps / (ms / 1000.0)
+    # the same batch on the fixed cost model's plans (autotuner off)
+    ctx_fixed = aln.Context(local)
+    ctx_fixed.set_tuning(False)
+    out_f = (AlnResult * n)()
+    if L.aln_corr_patches_batch(ctx_fixed.h, n, arr_d, out_f) < 0:
+        raise RuntimeError(L.aln_last_error(ctx_fixed.h).decode())
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        L.aln_corr_patches_batch(ctx_fixed.h, n, arr_d, out_f)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_fixed = e0.elapsed_time(e1)
+    ctx_fixed.close()
+    fixed_same_peaks = sum(1 for k in range(n) if (out_f[k].peak_x, out_f[k].peak_y) ==
+                           (out_d[k].peak_x, out_d[k].peak_y))
     # end to end: the patches in one pinned buffer, pair after pair
     nbytes = sum(2 * (p["a"].numel() + p["b"].numel()) for p in batch)
     pinned = torch.empty(nbytes // 2, dtype=torch.int16, pin_memory=True)
@@ -1358,6 +1374,11 @@ def run_uneven(args, embedded=False):
                     "h2d_bytes_per_step": (cnt2["h2d_bytes"]) // args.steps,
                     "d2h_bytes_per_step": (cnt2["d2h_bytes"]) // args.steps},
             "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": cnt["launches"],
+            "autotuner": {"tuned_pairs_per_s": value,
+                          "fixed_plan_pairs_per_s": n * args.steps / (ms_fixed / 1000.0),
+                          "tuned_over_fixed": ms_fixed / ms,
+                          "classes_timed": ctx.counters()["tune_classes"],
+                          "same_peaks": fixed_same_peaks, "of": n},
             "chunks_per_step": cnt["chunks"] / args.steps,
             "kernels_ms": {k: round(v[1], 3) for k, v in sorted(prof.items())},
             "parity": parity,

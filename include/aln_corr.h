@@ -138,8 +138,23 @@ int aln_ctx_profile(aln_ctx *ctx, int cap, const char **names, long long *launch
  * bytes, 3 = spectrum-cache hits, 4 = spectrum-cache fills (counted since
  * the last aln_ctx_profile_reset), 5 = device bytes the cache holds,
  * 6 = batch chunks run, 7 = host-to-device staging transfers issued (both
- * since the last reset). */
+ * since the last reset), 8 = pair classes this context timed for the
+ * autotuner. */
 long long aln_ctx_counter(aln_ctx *ctx, int which);
+
+/* Autotuner (no reference counterpart; replaces the reference's fixed
+ * transform-size rule, 0_GEN/Correlation.cpp:333-359, for CorrPatches'
+ * column plan): with tuning on (the default; environment ALN_TUNE=0 turns
+ * it off for new contexts), the first CorrPatches pair of a new class --
+ * (Nx/2, Ny, window height and a's height rounded up to powers of two, a's
+ * pixel size) -- times every valid column plan (one Ny-point transform per
+ * column, or segments of each valid length NS) on synthetic device pairs of
+ * its geometry with CUDA events, and the fastest becomes the class's plan.
+ * Choices are kept per process and in <library dir>/tune/<GPU name>-<build
+ * id>.txt (or $ALN_TUNE_DIR), which later processes read; an entry never
+ * changes once made, so a pair's numbers do not depend on its batch.  Off:
+ * the fixed cost model N (log2 N + 4) per transform. */
+int aln_ctx_set_tuning(aln_ctx *ctx, int on);
 
 /* Spectrum cache: the device-resident form of the reference's fft2 / ftc
  * cache arguments (CorrPatches' `vector<CD> &fft2`, 0_GEN/Correlation.cpp:
@@ -405,6 +420,19 @@ int aln_thm_call_batch(aln_ctx *ctx, int npairs, const aln_thumbs *thumbs,
 int aln_decimate_batch(aln_ctx *ctx, int n, const aln_image *in,
                        const unsigned char *const *mask, int lbin, int normalize,
                        double *const *out_vals, unsigned char *const *out_mask, double *out_sd);
+
+/* ImageFromValuesAndPoints with DistributePixel (0_GEN/Geometry.cpp:661-685,
+ * 0_GEN/Maths.h:236-276) on the device: n points xy[2i], xy[2i+1] with
+ * values v[i] (host) painted into a w x h raster whose corner is (xmin,
+ * ymin), bilinear weights for fractional points, duplicates adding.  The
+ * raster stays in the context's device memory (slot 0 or 1, reused by the
+ * next call with that slot) and *out describes it (FP64, on_device = 1,
+ * x0 = xmin, y0 = ymin), ready for the correlators; host_copy (may be NULL)
+ * receives a copy (w x h doubles).  Per-pixel sums are exact 64-bit fixed
+ * point at the finest scale the largest |v| allows, so the raster does not
+ * depend on the order the points land in. */
+int aln_points_image(aln_ctx *ctx, int slot, int n, const double *xy, const double *v,
+                     int xmin, int ymin, int w, int h, aln_image *out, double *host_copy);
 
 /* ---- ApproximateMatch ---------------------------------------------------
  * 1_DMesh/ApproximateMatch.cpp:115-194 for many tile pairs: CThmUtil's Crop

@@ -357,6 +357,14 @@ class Oracle(_Lib, _Mesh):
                               int(prenorm))
         return dst
 
+    def image_from_points(self, pts, vals, xmin, ymin, w, h):
+        """ImageFromValuesAndPoints + DistributePixel (h x w FP64 raster)."""
+        xy = _pts(pts)
+        v = np.ascontiguousarray(vals, np.float64)
+        img = np.zeros((h, w), np.float64)
+        self.lib.orc_image_from_points(_p(img), w, h, _p(v), _p(xy), len(v), xmin, ymin)
+        return img
+
     def decimate_normalize(self, pts, vals, w, h, lbin, normalize=True):
         xy = _pts(pts).copy()
         v = np.ascontiguousarray(vals, np.float64).copy()
