@@ -3202,6 +3202,7 @@ extern "C" int aln_corr_patches_noalloc(const aln_image *a, const aln_image *b, 
 }
 
 #include "aln_sweep.cuh"
+#include "aln_thmpair.cuh"
 #include "aln_points.cuh"
 #include "aln_approx.cuh"
 #include "aln_mesh.cuh"

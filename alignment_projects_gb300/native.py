@@ -99,6 +99,36 @@ class AlnApproxResult(C.Structure):
                 ("crop_h", C.c_int)]
 
 
+class AlnThmPair(C.Structure):
+    _fields_ = [("atl", C.c_int), ("acr", C.c_int), ("btl", C.c_int), ("bcr", C.c_int),
+                ("err", C.c_int), ("A", C.c_double), ("R", C.c_double), ("T", C.c_double * 6)]
+
+
+def thmpair_write(dir_, alr, blr, recs):
+    """Append ThmPair entries (dicts atl, acr, btl, bcr, err, A, R, T) to
+    <dir>/ThmPair_<alr>^<blr>.txt (0_GEN/PipeFiles.cpp's format)."""
+    n = len(recs)
+    arr = (AlnThmPair * n)()
+    for k, r in enumerate(recs):
+        arr[k] = AlnThmPair(r["atl"], r["acr"], r["btl"], r["bcr"], r.get("err", 0), r["A"],
+                            r["R"], (C.c_double * 6)(*r["T"]))
+    rc = lib().aln_thmpair_write(dir_.encode(), alr, blr, n, arr)
+    if rc < 0:
+        raise AlnError(rc, lib().aln_last_error(None).decode())
+
+
+def thmpair_read(dir_, alr, blr) -> list:
+    """The table's entries as dicts (ReadAllThmPair)."""
+    L = lib()
+    n = L.aln_thmpair_read(dir_.encode(), alr, blr, 0, None)
+    if n < 0:
+        raise AlnError(n, L.aln_last_error(None).decode())
+    arr = (AlnThmPair * max(n, 1))()
+    L.aln_thmpair_read(dir_.encode(), alr, blr, n, arr)
+    return [{"atl": r.atl, "acr": r.acr, "btl": r.btl, "bcr": r.bcr, "err": r.err, "A": r.A,
+             "R": r.R, "T": list(r.T)} for r in arr[:n]]
+
+
 class AlnMeshJob(C.Structure):
     _fields_ = [("nc", C.c_int), ("ac", C.c_void_p), ("nm", C.c_int), ("k", C.c_int),
                 ("am_idx", C.c_void_p), ("am_w", C.c_void_p), ("av", C.c_void_p),
@@ -247,6 +277,10 @@ def lib():
         L.aln_points_image.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                        C.c_int, C.c_int, C.c_int, C.c_int,
                                        C.POINTER(AlnImage), C.c_void_p]
+        L.aln_thmpair_write.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int,
+                                        C.POINTER(AlnThmPair)]
+        L.aln_thmpair_read.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int,
+                                       C.POINTER(AlnThmPair)]
         L.aln_improve_control_pts_batch.argtypes = [C.c_void_p, C.c_int,
                                                     C.POINTER(AlnMeshJob),
                                                     C.POINTER(AlnMeshResult)]

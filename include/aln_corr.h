@@ -474,6 +474,27 @@ typedef struct aln_approx_result {
 int aln_approx_match_batch(aln_ctx *ctx, int n, const aln_tile_pair *pairs,
                            const aln_approx_params *params, aln_approx_result *out);
 
+/* ThmPair table entry (0_GEN/PipeFiles.h:146-152): a tile pair's match. */
+typedef struct aln_thmpair {
+    int atl, acr, btl, bcr;  /* tile ids and connected-region ids of a and b */
+    int err;                 /* CThmScan err */
+    double A, R;             /* angle (deg) and correlation */
+    double T[6];             /* the a -> b transform (TAffine t[0..5]) */
+} aln_thmpair;
+
+/* Appends n entries to <dir>/ThmPair_<alr>^<blr>.txt (dir NULL or "": the
+ * working directory), writing WriteThmPairHdr's header line first when the
+ * table is new, each entry in WriteThmPair's format
+ * (0_GEN/PipeFiles.cpp:1282-1360); entries with a negative tile id are
+ * skipped, as there.  Appends from several processes are serialised with a
+ * file lock. */
+int aln_thmpair_write(const char *dir, int alr, int blr, int n, const aln_thmpair *recs);
+
+/* Reads the table's entries (ReadAllThmPair, 0_GEN/PipeFiles.cpp:1216-1280):
+ * returns how many there are (entries beyond cap are counted, not stored),
+ * or a negative status. */
+int aln_thmpair_read(const char *dir, int alr, int blr, int cap, aln_thmpair *out);
+
 /* ---- mesh optimizer ---------------------------------------------------
  * GradDescStep, CorrVectors and ImproveControlPts of 0_GEN/Correlation.cpp
  * (declared Correlation.h:127-152), which 1_DMesh/ImproveMesh.cpp:503 and
