@@ -1214,8 +1214,13 @@ extern "C" int aln_ctx_create(int device, aln_ctx **out)
     ctx->tune_classes = 0;
     ctx->pts_buf[0] = ctx->pts_buf[1] = nullptr;
     ctx->pts_cap[0] = ctx->pts_cap[1] = 0;
+    // the copy stream at the device's highest priority: its staging blocks
+    // are scheduled ahead of the compute kernels' waiting blocks
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
     if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaStreamCreateWithFlags(&ctx->cstream, cudaStreamNonBlocking)) != cudaSuccess) {
+        (e = cudaStreamCreateWithPriority(&ctx->cstream, cudaStreamNonBlocking, prio_hi)) !=
+            cudaSuccess) {
         set_err(nullptr, ALN_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
         delete ctx;
         return ALN_ERR_CUDA;
@@ -2282,6 +2287,36 @@ static void assign_staging(std::vector<PairPlan *> &win, char *base)
     }
 }
 
+// Host-to-device staging by the SMs: page-locked host memory is mapped into
+// the device's address space, so a grid of 16-byte loads and stores moves
+// it.  On GB300 this ran at the host link's 208 GB/s where copy-engine
+// transfers of the same page-locked buffers inside this library's batches
+// ran at 70 GB/s; its few small blocks run beside the compute kernels.
+// Both addresses need not be aligned alike: then bytes, else a byte head,
+// 16-byte body and byte tail.
+__global__ void __launch_bounds__(256) k_h2d_stage(char *__restrict__ dst,
+                                                   const char *__restrict__ src, size_t n)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if ((((uintptr_t)dst ^ (uintptr_t)src) & 15) != 0) {
+        for (size_t i = t0; i < n; i += stride)
+            dst[i] = src[i];
+        return;
+    }
+    const size_t mis = (16 - ((uintptr_t)src & 15)) & 15;
+    const size_t head = mis < n ? mis : n;
+    for (size_t i = t0; i < head; i += stride)
+        dst[i] = src[i];
+    const size_t nv = (n - head) / 16;
+    const uint4 *__restrict__ s4 = (const uint4 *)(src + head);
+    uint4 *__restrict__ d4 = (uint4 *)(dst + head);
+    for (size_t i = t0; i < nv; i += stride)
+        d4[i] = s4[i];
+    for (size_t i = head + nv * 16 + t0; i < n; i += stride)
+        dst[i] = src[i];
+}
+
 static int stage_window(aln_ctx *ctx, std::vector<PairPlan *> &win, int wp)
 {
     CK(cudaStreamWaitEvent(ctx->cstream, ctx->ev_wdone[wp], 0));
@@ -2289,15 +2324,38 @@ static int stage_window(aln_ctx *ctx, std::vector<PairPlan *> &win, int wp)
     const char *run_src = nullptr, *run_end = nullptr;
     char *run_dst = nullptr;
     auto flush = [&]() -> int {
-        // one transfer per run, in pieces of at most 64 MiB
-        for (const char *q = run_src; q && q < run_end;) {
-            const size_t b = std::min((size_t)(run_end - q), (size_t)64 << 20);
-            CK(cudaMemcpyAsync(run_dst + (q - run_src), q, b, cudaMemcpyHostToDevice,
-                               ctx->cstream));
-            ctx->h2d_bytes += (long long)b;
-            ctx->h2d_copies++;
-            q += b;
+        if (!run_src || run_end <= run_src) {
+            run_src = run_end = nullptr;
+            return ALN_OK;
         }
+        const size_t b = (size_t)(run_end - run_src);
+        // page-locked runs by the SMs (k_h2d_stage), pageable ones by the
+        // copy engine (it stages them through its own pinned buffers)
+        // (the run's first and last bytes both page-locked and mapped at the
+        // same offset: one allocation, or contiguous ones mapped alike)
+        cudaPointerAttributes at, at2;
+        const bool locked = cudaPointerGetAttributes(&at, run_src) == cudaSuccess &&
+                            at.type == cudaMemoryTypeHost && at.devicePointer &&
+                            cudaPointerGetAttributes(&at2, run_end - 1) == cudaSuccess &&
+                            at2.type == cudaMemoryTypeHost &&
+                            (const char *)at2.devicePointer - (const char *)at.devicePointer ==
+                                (ptrdiff_t)(b - 1);
+        cudaGetLastError();
+        if (locked) {
+            if (!ctx->sms) {
+                cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->device);
+                ctx->sms = std::max(ctx->sms, 1);
+            }
+            // the run through its device alias (the same address under UVA)
+            k_h2d_stage<<<2 * ctx->sms, 256, 0, ctx->cstream>>>(
+                run_dst, (const char *)at.devicePointer, b);
+            CK(cudaGetLastError());
+            ctx->launches++;
+        } else {
+            CK(cudaMemcpyAsync(run_dst, run_src, b, cudaMemcpyHostToDevice, ctx->cstream));
+        }
+        ctx->h2d_bytes += (long long)b;
+        ctx->h2d_copies++;
         run_src = run_end = nullptr;
         run_dst = nullptr;
         return ALN_OK;
@@ -2364,18 +2422,23 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
             return rc;
     }
     // Windows: runs of consecutive jobs (submission order) whose host inputs
-    // fit one staging buffer.  A window's host images are copied in one go
-    // on the copy stream -- adjacent host images with one transfer -- while
-    // the previous window computes.  Inside a window, jobs are grouped by FFT
-    // size and job kind (submission order kept) and split into chunks
-    // bounded by the workspace budget.  Device-resident inputs need no
-    // staging: then the whole batch is one window.  The staging cap is 4x
-    // the workspace budget (16 GiB by default), so batches of a few GB are
-    // one window: on GB300 the host-to-device copies ran at 55-70 GB/s while
-    // kernels ran beside them and at 210 GB/s alone, so for the montage batch
-    // (3.96 GB of strips) copying first and computing after took 60 ms per
-    // 4096 pairs against 98 ms with 512 MB windows overlapped.
-    const size_t win_cap = std::max((size_t)64 << 20, ctx->ws_budget * 4);
+    // fit one staging buffer.  A window's host images are copied on the copy
+    // stream -- adjacent host images with one transfer, by the SMs when they
+    // are page-locked -- while the previous window computes.  Inside a
+    // window, jobs are grouped by FFT size and job kind (submission order
+    // kept) and split into chunks bounded by the workspace budget.
+    // Device-resident inputs need no staging: then the whole batch is one
+    // window.  Host batches of at least 512 MB are cut into about four
+    // windows (at least 128 MB each), so only the first window's copy is not
+    // hidden behind computation: at the host link's ~210 GB/s a window's
+    // copy takes half the time of its kernels for the montage strips.
+    size_t host_bytes = 0;
+    for (const auto &pl : plans)
+        if (pl.d.status == 0)
+            host_bytes += pl.in_bytes[0] + pl.in_bytes[1];
+    const size_t win_cap = host_bytes >= ((size_t)512 << 20)
+                               ? std::max((size_t)128 << 20, (host_bytes + 3) / 4)
+                               : std::max((size_t)64 << 20, ctx->ws_budget * 4);
     std::vector<std::vector<PairPlan *>> windows(1);
     {
         size_t sb = 0;
@@ -3202,6 +3265,7 @@ extern "C" int aln_corr_patches_noalloc(const aln_image *a, const aln_image *b, 
 }
 
 #include "aln_sweep.cuh"
+#include "aln_ingest.cuh"
 #include "aln_thmpair.cuh"
 #include "aln_points.cuh"
 #include "aln_approx.cuh"

@@ -281,6 +281,10 @@ def lib():
                                         C.POINTER(AlnThmPair)]
         L.aln_thmpair_read.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int,
                                        C.POINTER(AlnThmPair)]
+        L.aln_pixpair_dims.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                       C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.aln_pixpair_condition.argtypes = [C.c_void_p, C.POINTER(AlnImage), C.c_int, C.c_int,
+                                            C.c_int, C.c_int, C.c_void_p, C.c_void_p]
         L.aln_improve_control_pts_batch.argtypes = [C.c_void_p, C.c_int,
                                                     C.POINTER(AlnMeshJob),
                                                     C.POINTER(AlnMeshResult)]
@@ -576,6 +580,21 @@ class Context:
                                              v.ctypes.data, xmin, ymin, w, h, C.byref(im),
                                              out.ctypes.data))
         return out, im
+
+    def pixpair_condition(self, tile, order=2, r1=0, r2=0, max1dpix=0):
+        """PixPair::Load's conditioning of one tile: (vfy, aln, scl) -- the
+        flattened image and the matcher's image at the working size."""
+        ws, hs, scl = C.c_int(), C.c_int(), C.c_int()
+        h, w = tile.shape
+        if self._L.aln_pixpair_dims(w, h, max1dpix, C.byref(ws), C.byref(hs),
+                                    C.byref(scl)) != ALN_OK:
+            raise AlnError(ALN_ERR_ARG, "tile size not a multiple of the scale")
+        vfy = np.zeros((hs.value, ws.value), np.float64)
+        aln_ = np.zeros((hs.value, ws.value), np.float64)
+        im = image(tile)
+        self._check(self._L.aln_pixpair_condition(self.h, C.byref(im), order, r1, r2, max1dpix,
+                                                  vfy.ctypes.data, aln_.ctypes.data))
+        return vfy, aln_, scl.value
 
     def improve_control_pts_batch(self, jobs) -> list:
         """ImproveControlPts for a list of mesh_job()s at once.  Returns per

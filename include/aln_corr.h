@@ -474,6 +474,22 @@ typedef struct aln_approx_result {
 int aln_approx_match_batch(aln_ctx *ctx, int n, const aln_tile_pair *pairs,
                            const aln_approx_params *params, aln_approx_result *out);
 
+/* ---- tile conditioning (PixPair::Load, 0_GEN/CPixPair.cpp:209-494) ------
+ * aln_pixpair_dims: the working size PixPair::Load downsamples a w x h tile
+ * to (halving while a side exceeds max1dpix; max1dpix <= 0: no
+ * downsampling); ALN_NO_PEAK when w, h are not multiples of the scale (the
+ * reference's "Dimensions not multiple of scale" failure).
+ * aln_pixpair_condition: one uint8 tile (Raster8FromAny's) through LegPolyFlatten of
+ * the given order (0_GEN/Maths.cpp:1006-1085) and Normalize, then, when
+ * r2 > 0, the DoG band-pass of radii r1 < r2 (MakeDoGKernel + Convolve +
+ * Normalize), then the box downsampling.  vfy (may be NULL) receives the
+ * flattened image at the working size (PixPair's avs_vfy), aln the image the
+ * matcher correlates (avs_aln: DoG'd when r2 > 0); both ws x hs doubles on
+ * the host. */
+int aln_pixpair_dims(int w, int h, int max1dpix, int *ws, int *hs, int *scl);
+int aln_pixpair_condition(aln_ctx *ctx, const aln_image *tile, int order, int r1, int r2,
+                          int max1dpix, double *vfy, double *aln);
+
 /* ThmPair table entry (0_GEN/PipeFiles.h:146-152): a tile pair's match. */
 typedef struct aln_thmpair {
     int atl, acr, btl, bcr;  /* tile ids and connected-region ids of a and b */

@@ -453,6 +453,19 @@ class Ref(_Lib, _Mesh):
             getattr(L, fn).restype = C.c_double
         self._mesh_types()
 
+    def pixpair_condition(self, tile, order=2, r1=0, r2=0, max1dpix=0):
+        """PixPair::Load's conditioning of a uint8 tile through the
+        reference's functions (refwrap's ref_pixpair_condition)."""
+        t = np.ascontiguousarray(tile, np.uint8)
+        h, w = t.shape
+        ws, hs, scl = w, h, 1
+        while max1dpix > 0 and (ws > max1dpix or hs > max1dpix):
+            ws, hs, scl = ws // 2, hs // 2, scl * 2
+        vfy = np.zeros((hs, ws))
+        aln = np.zeros((hs, ws))
+        self.lib.ref_pixpair_condition(_p(t), w, h, order, r1, r2, ws, hs, scl, _p(vfy), _p(aln))
+        return vfy, aln, scl
+
     def approx_match(self, a, b, tab, **params):
         """The reference's ApproximateMatch sequence on two whole tiles
         (refwrap's ref_approx_match).  Returns a dict with status, A, X, Y,

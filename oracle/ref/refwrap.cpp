@@ -15,6 +15,7 @@
  *   DecimateVector / Normalize  0_GEN/Maths.cpp:1315-1364, 192-212
  *   GradDescStep / CorrVectors / ImproveControlPts  0_GEN/Correlation.cpp:1403-1721
  *   BoxesFromShifts / BBoxFromPoints  0_GEN/Geometry.cpp:78-176
+ *   LegPolyFlatten / Normalize  0_GEN/Maths.cpp:1006-1085, 192-212
  * ref_approx_match chains them as 1_DMesh/ApproximateMatch.cpp does; the
  * few lines of 1_DMesh/CThmUtil.cpp it needs (that file is not compiled
  * here) are restated beside it.
@@ -524,6 +525,57 @@ int ref_approx_match(const double *a, const double *b, int w, int h, double tabx
     const double err = sqrt(I.t[2] * I.t[2] + I.t[5] * I.t[5]);
     if (limxy && err > limxy)
         return 4;
+    return 0;
+}
+
+
+/*
+ * PixPair::Load's conditioning of one uint8 tile (0_GEN/CPixPair.cpp:
+ * 209-494): the reference's LegPolyFlatten, Convolve and Normalize; its
+ * static MakeDoGKernel (:38-83) and the PixPair::Downsample member (:90-110)
+ * restated here (CPixPair.cpp is not compiled).  vfy / aln: ws x hs outputs
+ * (the caller sizes them with the same halving rule).  Returns 0.
+ */
+int ref_pixpair_condition(const unsigned char *ras, int w, int h, int order, int r1, int r2,
+                          int ws, int hs, int scl, double *vfy, double *aln)
+{
+    vector<double> avf, flt;
+    LegPolyFlatten(avf, ras, w, h, order);
+    const vector<double> *al = &avf;
+    if (r2 > 0) {
+        const int d = 3 * r2, D = 2 * d + 1;
+        double s1 = 0.0, s2 = 0.0;
+        for (int y = -d; y <= d; ++y)
+            for (int x = -d; x <= d; ++x) {
+                double R = x * x + y * y;
+                s1 += exp(-(R / (2 * r1 * r1)));
+                s2 += exp(-(R / (2 * r2 * r2)));
+            }
+        vector<double> DoG(D * D);
+        for (int y = -d; y <= d; ++y)
+            for (int x = -d; x <= d; ++x) {
+                double R = x * x + y * y;
+                double v1 = exp(-(R / (2 * r1 * r1)));
+                double v2 = exp(-(R / (2 * r2 * r2)));
+                DoG[x + d + D * (y + d)] = v1 / s1 - v2 / s2;
+            }
+        vector<CD> kfft;
+        Convolve(flt, avf, w, h, &DoG[0], D, D, true, true, kfft, quiet_log());
+        Normalize(flt);
+        al = &flt;
+    }
+    const int n = scl * scl;
+    const vector<double> *src[2] = {&avf, al};
+    double *dst[2] = {vfy, aln};
+    for (int q = 0; q < 2; ++q)
+        for (int iy = 0; iy < hs; ++iy)
+            for (int ix = 0; ix < ws; ++ix) {
+                double sum = 0.0;
+                for (int dy = 0; dy < scl; ++dy)
+                    for (int dx = 0; dx < scl; ++dx)
+                        sum += (*src[q])[ix * scl + dx + w * (iy * scl + dy)];
+                dst[q][ix + ws * iy] = sum / n;
+            }
     return 0;
 }
 

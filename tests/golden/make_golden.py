@@ -290,6 +290,24 @@ APPROX_KEYS = ("xyconf", "olap1d", "olap2d", "thmdec", "mode_prior", "ang0", "hf
                "hfangpr", "rthresh", "nbmaxht", "pretweak", "tweaks", "limxy")
 
 
+def pixpair_cases(ref):
+    """PixPair::Load's tile conditioning (0_GEN/CPixPair.cpp:209-494):
+    Legendre flattening of orders 0-6, the DoG band-pass, downsampling."""
+    out = {}
+    for name, seed, order, r1, r2, mx, shape in [("o2", 1, 2, 0, 0, 0, (160, 224)),
+                                                 ("o2dog", 2, 2, 3, 6, 0, (160, 224)),
+                                                 ("o0down", 3, 0, 0, 0, 100, (192, 256)),
+                                                 ("o6dogdown", 4, 6, 2, 4, 64, (192, 256))]:
+        f = synth.field_np(seed * 17 + 3, *shape)
+        yy, xx = np.mgrid[0:shape[0], 0:shape[1]]
+        f = f + 25.0 * (xx / shape[1]) - 15.0 * (yy / shape[0]) ** 2   # a shading to flatten
+        t = synth.to_u8(f)
+        vfy, aln, scl = ref.pixpair_condition(t, order, r1, r2, mx)
+        out["pixpair_" + name] = dict(tile=t, order=order, r1=r1, r2=r2, max1dpix=mx, scl=scl,
+                                      vfy=vfy, aln=aln)
+    return out
+
+
 def save(name, d):
     flat = {}
     for case, fields in d.items():
@@ -317,6 +335,7 @@ def main():
     save("decimate", decimate_cases(ref))
     save("mesh", mesh_cases(ref))
     save("approx", approx_cases(ref))
+    save("pixpair", pixpair_cases(ref))
 
 
 if __name__ == "__main__":
