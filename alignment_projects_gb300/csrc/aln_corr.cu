@@ -2294,6 +2294,7 @@ static void assign_staging(std::vector<PairPlan *> &win, char *base)
 // ran at 70 GB/s; its few small blocks run beside the compute kernels.
 // Both addresses need not be aligned alike: then bytes, else a byte head,
 // 16-byte body and byte tail.
+#define H2D_UNROLL 4
 __global__ void __launch_bounds__(256) k_h2d_stage(char *__restrict__ dst,
                                                    const char *__restrict__ src, size_t n)
 {
@@ -2311,10 +2312,23 @@ __global__ void __launch_bounds__(256) k_h2d_stage(char *__restrict__ dst,
     const size_t nv = (n - head) / 16;
     const uint4 *__restrict__ s4 = (const uint4 *)(src + head);
     uint4 *__restrict__ d4 = (uint4 *)(dst + head);
-    for (size_t i = t0; i < nv; i += stride)
+    // H2D_UNROLL loads in flight per thread before their stores: few blocks
+    // keep the host link busy, leaving the SMs' issue slots to the kernels
+    // that run beside the staging
+    size_t i = t0;
+    for (; i + (H2D_UNROLL - 1) * stride < nv; i += H2D_UNROLL * stride) {
+        uint4 v[H2D_UNROLL];
+#pragma unroll
+        for (int u = 0; u < H2D_UNROLL; ++u)
+            v[u] = s4[i + u * stride];
+#pragma unroll
+        for (int u = 0; u < H2D_UNROLL; ++u)
+            d4[i + u * stride] = v[u];
+    }
+    for (; i < nv; i += stride)
         d4[i] = s4[i];
-    for (size_t i = head + nv * 16 + t0; i < n; i += stride)
-        dst[i] = src[i];
+    for (size_t j = head + nv * 16 + t0; j < n; j += stride)
+        dst[j] = src[j];
 }
 
 static int stage_window(aln_ctx *ctx, std::vector<PairPlan *> &win, int wp)
@@ -2347,7 +2361,7 @@ static int stage_window(aln_ctx *ctx, std::vector<PairPlan *> &win, int wp)
                 ctx->sms = std::max(ctx->sms, 1);
             }
             // the run through its device alias (the same address under UVA)
-            k_h2d_stage<<<2 * ctx->sms, 256, 0, ctx->cstream>>>(
+            k_h2d_stage<<<std::max(1, ctx->sms / 4), 256, 0, ctx->cstream>>>(
                 run_dst, (const char *)at.devicePointer, b);
             CK(cudaGetLastError());
             ctx->launches++;

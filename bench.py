@@ -517,6 +517,8 @@ def run_gpu(args):
     prof_e2e = ctx.profile()
     ctx.set_profiling(False)
     e2e_value = ws * n * args.steps / (ms_e2e / 1000.0)
+    stage_ms = prof_e2e.get("h2d_staging", (0, 0.0))[1] / args.steps
+    staging_gbs = strip_bytes / (stage_ms / 1000.0) / 1e9 if stage_ms > 0 else None
 
     # the host link alone: one pinned-to-device copy of the step's strips
     # (bounds e2e when the copies cannot hide behind the kernels)
@@ -582,7 +584,10 @@ def run_gpu(args):
             samp = [(host_bufs[k][0].numpy(), host_bufs[k][1].numpy())
                     for k in range(min(n, max(args.cpu_sample, args.parity_sample)))]
             cpu_pps, per, outs, wall = cpu_pairs_per_s(samp, threads)
+            per_ms = sorted(1000.0 * x for x in per)
             cpu = {"value": cpu_pps, "unit": "pairs/s", "cores": threads, "kind": "port",
+                   "p50_ms_per_pair": per_ms[len(per_ms) // 2],
+                   "p99_ms_per_pair": per_ms[min(len(per_ms) - 1, int(0.99 * len(per_ms)))],
                    "sample": "%d of the batch's pairs, FP64 C restatement of CorrPatches, "
                              "%.1f s wall on %d threads" % (len(samp), wall, threads)}
             ok = tot = 0
@@ -615,8 +620,13 @@ def run_gpu(args):
             "e2e": {"value": e2e_value, "unit": "pairs/s",
                     "h2d_bytes_per_step": cnt["h2d_bytes"] // args.steps,
                     "d2h_bytes_per_step": cnt["d2h_bytes"] // args.steps,
-                    "h2d_link_gbs": h2d_gbs, "h2d_link_gbs_4_streams": h2d_gbs4,
-                    "copy_bound_pairs_per_s": n / (strip_bytes / (h2d_gbs * 1e9))},
+                    "staging_gbs": staging_gbs,
+                    "staging_note": "the library's host-to-device staging (SM copies of the "
+                                    "page-locked strips, overlapped with the previous "
+                                    "window's kernels), CUDA events on its copy stream",
+                    "copy_bound_pairs_per_s": (n / (strip_bytes / (staging_gbs * 1e9))
+                                               if staging_gbs else None),
+                    "torch_copy_gbs": h2d_gbs, "torch_copy_gbs_4_streams": h2d_gbs4},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic,
