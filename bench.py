@@ -1316,6 +1316,7 @@ def run_uneven(args, embedded=False):
     e1.record()
     torch.cuda.synchronize()
     ms_fixed = e0.elapsed_time(e1)
+    chunks_fixed = ctx_fixed.counters()["chunks"] / (args.steps + 1)
     ctx_fixed.close()
     fixed_same_peaks = sum(1 for k in range(n) if (out_f[k].peak_x, out_f[k].peak_y) ==
                            (out_d[k].peak_x, out_d[k].peak_y))
@@ -1388,6 +1389,8 @@ def run_uneven(args, embedded=False):
                           "fixed_plan_pairs_per_s": n * args.steps / (ms_fixed / 1000.0),
                           "tuned_over_fixed": ms_fixed / ms,
                           "classes_timed": ctx.counters()["tune_classes"],
+                          "chunks_per_step_tuned": cnt["chunks"] / args.steps,
+                          "chunks_per_step_fixed": chunks_fixed,
                           "same_peaks": fixed_same_peaks, "of": n},
             "chunks_per_step": cnt["chunks"] / args.steps,
             "kernels_ms": {k: round(v[1], 3) for k, v in sorted(prof.items())},
