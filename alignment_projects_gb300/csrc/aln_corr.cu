@@ -49,6 +49,7 @@
 
 #include <algorithm>
 #include <map>
+#include <set>
 #include <mutex>
 #include <string>
 #include <tuple>
@@ -1021,10 +1022,11 @@ struct aln_ctx {
     std::vector<std::string> prof_names;  // stable storage for returned names
     // spectrum cache (device-resident X2 per keyed image b)
     std::map<SpecKey, SpecEntry> spec;
+    std::set<std::pair<unsigned long long, SpecKey>> spec_lru;   // (tick, key) of every entry
     std::multimap<size_t, float2 *> spec_free;   // evicted buffers by size
     size_t spec_bytes, spec_cap;                 // all buffers held / limit
     unsigned long long spec_tick;
-    long long spec_hits, spec_fills;
+    long long spec_hits, spec_fills, spec_evictions;
     int *dsel;                                   // cache-fill job lists (whole batch)
     size_t dsel_cap;
     int *dsel_cur;                               // the current chunk's list
@@ -1037,6 +1039,7 @@ struct aln_ctx {
     char *pts_buf[2];                            // aln_points_image rasters, per slot
     size_t pts_cap[2];
     int tune_on;                                 // measured segment choices (aln_tune.cuh)
+    int split_on;                                // CorrPatches rows of 3 * 2^k, 5 * 2^k points
     int tuning;                                  // inside a timing run
     long long tune_classes;                      // classes this context measured
 };
@@ -1197,7 +1200,7 @@ extern "C" int aln_ctx_create(int device, aln_ctx **out)
     ctx->spec_bytes = 0;
     ctx->spec_cap = (size_t)8 << 30;
     ctx->spec_tick = 0;
-    ctx->spec_hits = ctx->spec_fills = 0;
+    ctx->spec_hits = ctx->spec_fills = ctx->spec_evictions = 0;
     ctx->dsel = nullptr;
     ctx->dsel_cap = 0;
     ctx->dsel_cur = nullptr;
@@ -1210,6 +1213,7 @@ extern "C" int aln_ctx_create(int device, aln_ctx **out)
         const char *t = getenv("ALN_TUNE");
         ctx->tune_on = !(t && t[0] == '0');
     }
+    ctx->split_on = 1;
     ctx->tuning = 0;
     ctx->tune_classes = 0;
     ctx->pts_buf[0] = ctx->pts_buf[1] = nullptr;
@@ -1241,14 +1245,17 @@ extern "C" int aln_ctx_create(int device, aln_ctx **out)
         delete ctx;
         return ALN_ERR_CUDA;
     }
-    // twiddle table tw[N + m] = exp(-2 pi i m / N), N = 1..ALN_MAX_N
-    std::vector<float2> h(2 * ALN_MAX_N);
+    // twiddle tables tw[base + N + m] = exp(-2 pi i m / N): every power of
+    // two N <= ALN_MAX_N (base 0), then N = 3 * 2^k and N = 5 * 2^k
+    // (tw_base(N), aln_fft_reg.cuh)
+    std::vector<float2> h(TW_TOTAL, make_float2(0.f, 0.f));
     h[0] = make_float2(1.f, 0.f);
-    for (int N = 1; N <= ALN_MAX_N; N <<= 1)
-        for (int m = 0; m < N; ++m) {
-            const double a = -2.0 * M_PI * (double)m / (double)N;
-            h[N + m] = make_float2((float)cos(a), (float)sin(a));
-        }
+    for (int n1 : {1, 3, 5})
+        for (int N = n1; N <= ALN_MAX_N; N <<= 1)
+            for (int m = 0; m < N; ++m) {
+                const double a = -2.0 * M_PI * (double)m / (double)N;
+                h[tw_base(N) + N + m] = make_float2((float)cos(a), (float)sin(a));
+            }
     if ((e = cudaMalloc(&ctx->tw, sizeof(float2) * h.size())) != cudaSuccess ||
         (e = cudaMemcpy(ctx->tw, h.data(), sizeof(float2) * h.size(),
                         cudaMemcpyHostToDevice)) != cudaSuccess) {
@@ -1310,6 +1317,27 @@ static int ceil_pow2(int n)
 }
 
 extern "C" int aln_fft_size(int n1, int n2) { return ceil_pow2(n1 + n2 - 1); }
+
+// CorrPatches row half-lengths L = 3 * 2^k and 5 * 2^k (grids Nx = 2L of
+// 160-3072 points) the row kernels are built for, ascending
+#define ALN_CASES_LMIX(X) X(80) X(96) X(160) X(192) X(320) X(384) X(640) X(768) X(1280) X(1536)
+
+// The CorrPatches grid length for `need` points: the smallest power of two
+// >= need, or with split lengths on the smallest 2L >= need of
+// ALN_CASES_LMIX when that is shorter.  The FFT's work per row and the
+// number of column transforms both scale with the length, and the row
+// transform's cost per point barely depends on the split (a radix-3 or
+// radix-5 step in registers), so the shortest grid is the fastest.
+static int patches_len(int need, bool split)
+{
+    int best = std::max(2, ceil_pow2(need));
+    if (split) {
+#define X(v) if (2 * (v) >= need && 2 * (v) < best) best = 2 * (v); else
+        ALN_CASES_LMIX(X) {}
+#undef X
+    }
+    return best;
+}
 
 extern "C" int aln_fft_size_sqr(int w1, int h1, int w2, int h2)
 {
@@ -1411,9 +1439,42 @@ struct PairPlan {
     char *staged[2];             // device staging of host inputs (set per window)
 };
 
+// Cache entry bookkeeping: the map and the (tick, key) LRU index together.
+static void spec_touch(aln_ctx *ctx, std::map<SpecKey, SpecEntry>::iterator it)
+{
+    ctx->spec_lru.erase(std::make_pair(it->second.tick, it->first));
+    it->second.tick = ctx->spec_tick;
+    ctx->spec_lru.insert(std::make_pair(it->second.tick, it->first));
+}
+static void spec_insert(aln_ctx *ctx, const SpecKey &K, const SpecEntry &e)
+{
+    ctx->spec[K] = e;
+    ctx->spec_lru.insert(std::make_pair(e.tick, K));
+}
+static std::map<SpecKey, SpecEntry>::iterator
+spec_erase(aln_ctx *ctx, std::map<SpecKey, SpecEntry>::iterator it)
+{
+    ctx->spec_lru.erase(std::make_pair(it->second.tick, it->first));
+    return ctx->spec.erase(it);
+}
+
+// Whether `bytes` more of device memory leave the workspace budget plus
+// 2 GiB free (the cache grows into free HBM, never into what the batches
+// need next).
+static bool spec_room(aln_ctx *ctx, size_t bytes)
+{
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return fr >= bytes + ctx->ws_budget + ((size_t)2 << 30);
+}
+
 // A device buffer for a new cache entry of `bytes`, evicting entries not used
-// by the current chunk (least recently used first).  Buffers are reused on
-// the context's stream, so a kernel still reading an evicted entry finishes
+// by the current chunk (least recently used first) while the cache is at its
+// cap or the device is short of free memory.  Buffers are reused on the
+// context's stream, so a kernel still reading an evicted entry finishes
 // before the buffer is filled again.  Returns NULL when nothing fits.
 static float2 *spec_alloc(aln_ctx *ctx, size_t bytes)
 {
@@ -1423,7 +1484,7 @@ static float2 *spec_alloc(aln_ctx *ctx, size_t bytes)
         ctx->spec_free.erase(f);
         return b;
     }
-    while (ctx->spec_bytes + bytes > ctx->spec_cap) {
+    while (ctx->spec_bytes + bytes > ctx->spec_cap || !spec_room(ctx, bytes)) {
         if (!ctx->spec_free.empty()) {
             auto g = std::prev(ctx->spec_free.end());
             cudaFree(g->second);   // waits for the device: rare
@@ -1431,16 +1492,13 @@ static float2 *spec_alloc(aln_ctx *ctx, size_t bytes)
             ctx->spec_free.erase(g);
             continue;
         }
-        auto lru = ctx->spec.end();
-        for (auto it = ctx->spec.begin(); it != ctx->spec.end(); ++it)
-            if (it->second.tick < ctx->spec_tick &&
-                (lru == ctx->spec.end() || it->second.tick < lru->second.tick))
-                lru = it;
-        if (lru == ctx->spec.end())
-            return nullptr;
+        if (ctx->spec_lru.empty() || ctx->spec_lru.begin()->first >= ctx->spec_tick)
+            return nullptr;   // every entry is in use by the current chunk
+        auto lru = ctx->spec.find(ctx->spec_lru.begin()->second);
         float2 *b = lru->second.X2;
         const size_t lb = lru->second.bytes;
-        ctx->spec.erase(lru);
+        spec_erase(ctx, lru);
+        ctx->spec_evictions++;
         if (lb == bytes)
             return b;
         ctx->spec_free.insert(std::make_pair(lb, b));
@@ -1461,7 +1519,7 @@ static void spec_drop(aln_ctx *ctx, int ns, unsigned long long k0, unsigned long
         if (std::get<0>(it->first) == ns && std::get<1>(it->first) >= k0 &&
             std::get<1>(it->first) <= k1) {
             ctx->spec_free.insert(std::make_pair(it->second.bytes, it->second.X2));
-            it = ctx->spec.erase(it);
+            it = spec_erase(ctx, it);
         } else {
             ++it;
         }
@@ -1512,8 +1570,12 @@ static void need_rows(const PairDev &d, int img, int lo[2], int hi[2])
 
 #include "aln_tune.cuh"
 
+// allow_split: the caller runs the register pipeline (batch path), whose row
+// kernels take the split lengths of ALN_CASES_LMIX; the allocation-free
+// entry point's kernels take powers of two only.
 static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_transpose = false,
-                     const ImgSpec *spec = nullptr, bool allow_segment = false)
+                     const ImgSpec *spec = nullptr, bool allow_segment = false,
+                     bool allow_split = false)
 {
     if (spec)
         allow_transpose = false;   // the R image keeps the caller's orientation
@@ -1661,15 +1723,21 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
         // also holds both images unfolded (Nx >= w0, w1).  The plain product
         // makes the values at those lags the same sums as on the reference's
         // grid (the whitened S product of CorrImagesS is not grid-invariant).
-        const int nx = std::max(2, ceil_pow2(std::max(
-                                       std::max(d.w[0], d.w[1]),
-                                       std::max(d.w[1] - 1 - d.xlo, d.xhi + d.w[0] - 1) + 1)));
+        // The row axis may take a split length (3 * 2^k or 5 * 2^k points,
+        // patches_len); columns stay powers of two (segments or one
+        // transform).  The sums at the disc's lags are the same on any
+        // alias-free grid.
         const int ny = std::max(2, ceil_pow2(std::max(
                                        std::max(d.h[0], d.h[1]),
                                        std::max(d.h[1] - 1 - d.ylo, d.yhi + d.h[0] - 1) + 1)));
-        d.Nx = std::min(d.Nx, nx);
         d.Ny = std::min(d.Ny, ny);
-        d.logNx = ilog2(d.Nx);
+        // (columns of >= 8 points: the register pipeline's range)
+        const bool split = allow_split && (ctx ? ctx->split_on != 0 : true) && d.Ny >= 8;
+        const int nx = patches_len(std::max(std::max(d.w[0], d.w[1]),
+                                            std::max(d.w[1] - 1 - d.xlo, d.xhi + d.w[0] - 1) + 1),
+                                   split);
+        d.Nx = std::min(d.Nx, nx);
+        d.logNx = odd_part(d.Nx) == 1 ? ilog2(d.Nx) : 0;   // the split lengths have none
         d.logNy = ilog2(d.Ny);
         // Segmented columns (k2_corrseg) where they take fewer FFT
         // point-passes: 2 nseg + 1 transforms of NS points against 3 of Ny
@@ -1785,7 +1853,7 @@ extern "C" int aln_corr_patches_grid(const aln_pair *P, int *nx, int *ny, int *n
     if (!P || !nx || !ny || !nseg || !transposed)
         return ALN_ERR_ARG;
     PairPlan pl;
-    if (int rc = plan_pair(nullptr, *P, pl, true, nullptr, P->b_key == 0))
+    if (int rc = plan_pair(nullptr, *P, pl, true, nullptr, P->b_key == 0, true))
         return rc;
     const bool empty = pl.d.status == ALN_NO_PEAK;
     *nx = empty ? 0 : pl.d.Nx;
@@ -1882,7 +1950,7 @@ static int cols_per_cta(int Ny) { return std::max(1, std::min(16, 4096 / Ny)); }
 template <int LL>
 static void launch_rowfft2(aln_ctx *ctx, int n, int maxh)
 {
-    constexpr int T = LL / rowfft_radix(LL);
+    constexpr int T = RowFFT<LL>::T;
     const int thr = rowfft_threads(T), G = thr / T;
     const size_t sm = (size_t)G * row_pitch(LL) * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_rowfft<LL>, sm);
@@ -1894,7 +1962,7 @@ static void launch_rowfft2(aln_ctx *ctx, int n, int maxh)
 template <int LL>
 static void launch_fill_rows(aln_ctx *ctx, int nsel, int maxh)
 {
-    constexpr int T = LL / rowfft_radix(LL);
+    constexpr int T = RowFFT<LL>::T;
     const int thr = rowfft_threads(T), G = thr / T;
     const size_t sm = (size_t)G * row_pitch(LL) * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_rowfft<LL>, sm);
@@ -1979,7 +2047,7 @@ static void launch_corrseg(aln_ctx *ctx, int n, int L)
 template <int LL>
 static void launch_lagrow2(aln_ctx *ctx, int n, int maxWy)
 {
-    constexpr int T = RegFFT<LL, +1>::T;
+    constexpr int T = FFTOf<LL, +1>::T;
     const int thr = std::max(256, T), G = thr / T;
     const size_t sm = (size_t)G * row_pitch(LL) * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_lagrow<LL>, sm);
@@ -2021,6 +2089,7 @@ static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int
     switch (L) {
 #define X(v) case v: launch_rowfft2<v>(ctx, n, maxh); break;
         ALN_CASES_L(X)
+        ALN_CASES_LMIX(X)
 #undef X
     default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
     }
@@ -2041,6 +2110,7 @@ static int launch_fft_pipeline(aln_ctx *ctx, int L, int Ny, int n, int maxh, int
         switch (L) {
 #define X(v) case v: launch_lagrow2<v>(ctx, n, maxWy); break;
             ALN_CASES_L(X)
+            ALN_CASES_LMIX(X)
 #undef X
         default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
         }
@@ -2103,14 +2173,14 @@ static void prep_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, int off, ch
                             corrcol_radix_of(pl.d.Ny, pl.d.mode == JOB_PATCHES ? 1 : 0));
             auto it = ctx->spec.find(K);
             if (it != ctx->spec.end()) {
-                it->second.tick = ctx->spec_tick;
+                spec_touch(ctx, it);
                 pl.d.b_cached = 1;
                 pl.d.X2 = it->second.X2;
                 ctx->spec_hits++;
             } else {
                 const size_t bytes = al256((size_t)(pl.d.Nx / 2 + 1) * pl.d.Ny * sizeof(float2));
                 if (float2 *buf = spec_alloc(ctx, bytes)) {
-                    ctx->spec[K] = SpecEntry{buf, bytes, ctx->spec_tick};
+                    spec_insert(ctx, K, SpecEntry{buf, bytes, ctx->spec_tick});
                     pl.d.b_cached = 1;
                     pl.d.X2 = buf;
                     fills.push_back(k);
@@ -2182,6 +2252,7 @@ static int launch_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, const Chun
         switch (L) {
 #define X(v) case v: launch_fill_rows<v>(ctx, cl.nfill, cl.fill_maxh); break;
             ALN_CASES_L(X)
+            ALN_CASES_LMIX(X)
 #undef X
         default: return set_err(ctx, ALN_ERR_UNSUPPORTED, "row length %d", L);
         }
@@ -2432,7 +2503,7 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
         plans[k].key = keys ? keys[k].key : pairs[k].b_key;
         const ImgSpec *sp = (specs && specs[k].kind != 0) ? &specs[k] : nullptr;
         if (int rc = plan_pair(ctx, pairs[k], plans[k], sp == nullptr, sp,
-                               sp == nullptr && plans[k].key == 0))
+                               sp == nullptr && plans[k].key == 0, sp == nullptr))
             return rc;
     }
     // Windows: runs of consecutive jobs (submission order) whose host inputs
@@ -3001,7 +3072,7 @@ extern "C" void aln_ctx_profile_reset(aln_ctx *ctx)
     ctx->prof_acc.clear();
     ctx->launches = 0;
     ctx->h2d_bytes = ctx->d2h_bytes = 0;
-    ctx->spec_hits = ctx->spec_fills = 0;
+    ctx->spec_hits = ctx->spec_fills = ctx->spec_evictions = 0;
     ctx->chunks = 0;
     ctx->h2d_copies = 0;
 }
@@ -3045,6 +3116,7 @@ extern "C" long long aln_ctx_counter(aln_ctx *ctx, int which)
     case 6: return ctx->chunks;
     case 7: return ctx->h2d_copies;
     case 8: return ctx->tune_classes;
+    case 9: return ctx->spec_evictions;
     default: return -1;
     }
 }
@@ -3065,6 +3137,14 @@ extern "C" int aln_ctx_set_tuning(aln_ctx *ctx, int on)
     return ALN_OK;
 }
 
+extern "C" int aln_ctx_set_split_grids(aln_ctx *ctx, int on)
+{
+    if (!ctx)
+        return ALN_ERR_ARG;
+    ctx->split_on = on ? 1 : 0;
+    return ALN_OK;
+}
+
 extern "C" int aln_ctx_set_spectrum_cache(aln_ctx *ctx, size_t bytes)
 {
     if (!ctx)
@@ -3081,14 +3161,11 @@ extern "C" int aln_ctx_set_spectrum_cache(aln_ctx *ctx, size_t bytes)
             ctx->spec_free.erase(g);
             continue;
         }
-        if (ctx->spec.empty())
+        if (ctx->spec_lru.empty())
             break;
-        auto lru = ctx->spec.begin();
-        for (auto it = ctx->spec.begin(); it != ctx->spec.end(); ++it)
-            if (it->second.tick < lru->second.tick)
-                lru = it;
+        auto lru = ctx->spec.find(ctx->spec_lru.begin()->second);
         ctx->spec_free.insert(std::make_pair(lru->second.bytes, lru->second.X2));
-        ctx->spec.erase(lru);
+        spec_erase(ctx, lru);
     }
     return ALN_OK;
 }

@@ -6,7 +6,11 @@
 // radix-2 splits with exact constants), preceded by twiddles from the device
 // table tw[N' + m] = exp(-2 pi i m / N'); between passes the team exchanges
 // data once through a padded shared-memory buffer (index i -> i + i/16,
-// which keeps the strided Stockham writes free of bank conflicts).  When N
+// which keeps the strided Stockham writes of radix 16 free of bank
+// conflicts; at radix 8 the writes cost 1.17-1.25x the conflict-free count
+// of 8-byte wavefronts, and an XOR swizzle that removed that ran slower in
+// the 512-point column kernel: its per-access address arithmetic took
+// registers and spilled).  When N
 // is not a power of R the first pass has a smaller radix R2 = N / R^P and
 // each thread runs R/R2 of its butterflies.  After the last pass thread t
 // holds X[t + r*T]: the same layout as the input, so a forward transform, a
@@ -113,8 +117,11 @@ struct RegFFT {
     static constexpr int P = ilog2c(N) / ilog2c(R);    // full radix-R passes
     static constexpr int R2 = N / ipowc(R, P);         // first-pass radix (1: none)
     static constexpr int SMEM = padded(N);             // float2 per team
+    static constexpr int V = R;                        // points per thread
+    // register slot q of thread t holds point t + q T, in and out
+    __device__ __forceinline__ static int in_idx(int t, int q) { return t + q * T; }
+    __device__ __forceinline__ static int out_idx(int t, int q) { return t + q * T; }
 
-    // v: this thread's R points (x[t + r*T]); sm: the team's exchange buffer.
     // All threads of the CTA must call this together (it uses __syncthreads);
     // run_team(..., team) synchronises team `team` alone (team_sync), for
     // kernels whose teams share no shared-memory data around the call.
@@ -199,3 +206,190 @@ struct RegFFT {
         }
     }
 };
+
+// ---------------------------------------------------------------------------
+// Lengths N = N1 * 2^k (N1 = 3 or 5)
+// ---------------------------------------------------------------------------
+
+// odd factor of n (n > 0)
+__host__ __device__ constexpr int odd_part(int n) { return (n & 1) ? n : odd_part(n / 2); }
+
+// Twiddles of the lengths N1 * 2^k sit after the power-of-two table, in
+// the same scheme: tw[base(N1) + N + m] = exp(-2 pi i m / N) for every
+// N = N1 * 2^k <= ALN_MAX_N.  Each table spans 2 * (its largest N).
+constexpr int TW_POW2_SIZE = 2 * ALN_MAX_N;
+constexpr int TW3_BASE = TW_POW2_SIZE;
+constexpr int TW3_SIZE = 3 * ALN_MAX_N / 2;   // largest N = 3 * ALN_MAX_N / 4
+constexpr int TW5_BASE = TW3_BASE + TW3_SIZE;
+constexpr int TW5_SIZE = 5 * ALN_MAX_N / 4;   // largest N = 5 * ALN_MAX_N / 8
+constexpr int TW_TOTAL = TW5_BASE + TW5_SIZE;
+
+__host__ __device__ constexpr int tw_base(int N)
+{
+    return odd_part(N) == 1 ? 0 : odd_part(N) == 3 ? TW3_BASE : TW5_BASE;
+}
+
+// exp(DIR * 2 pi i m / N), 0 <= m < N, N a power of two or N1 * 2^k
+template <int N, int DIR>
+__device__ __forceinline__ float2 twn(const float2 *__restrict__ tw, int m)
+{
+    static_assert(odd_part(N) == 1 || odd_part(N) == 3 || odd_part(N) == 5, "length");
+    float2 w = __ldg(&tw[tw_base(N) + N + m]);
+    if (DIR > 0)
+        w.y = -w.y;
+    return w;
+}
+
+// In-place N1-point DFT, natural order (N1 = 3, 5), sign DIR.  The constants
+// are cos and sin of 2 pi / 3, 2 pi / 5 and 4 pi / 5.
+template <int N1, int DIR>
+struct DFTOdd;
+
+template <int DIR>
+struct DFTOdd<3, DIR> {
+    __device__ __forceinline__ static void run(float2 *x)
+    {
+        constexpr float S = DIR * 0.86602540378443865f;   // DIR * sin(2 pi / 3)
+        const float2 a = cadd(x[1], x[2]), b = csub(x[1], x[2]);
+        const float2 m = make_float2(x[0].x - 0.5f * a.x, x[0].y - 0.5f * a.y);
+        const float2 ib = make_float2(-S * b.y, S * b.x);   // i * DIR * sin * b
+        x[0] = cadd(x[0], a);
+        x[1] = cadd(m, ib);
+        x[2] = csub(m, ib);
+    }
+};
+
+template <int DIR>
+struct DFTOdd<5, DIR> {
+    __device__ __forceinline__ static void run(float2 *x)
+    {
+        constexpr float C1 = 0.30901699437494742f;          // cos(2 pi / 5)
+        constexpr float C2 = -0.80901699437494742f;         // cos(4 pi / 5)
+        constexpr float S1 = DIR * 0.95105651629515357f;    // DIR * sin(2 pi / 5)
+        constexpr float S2 = DIR * 0.58778525229247313f;    // DIR * sin(4 pi / 5)
+        const float2 a1 = cadd(x[1], x[4]), b1 = csub(x[1], x[4]);
+        const float2 a2 = cadd(x[2], x[3]), b2 = csub(x[2], x[3]);
+        const float2 m1 = make_float2(x[0].x + C1 * a1.x + C2 * a2.x,
+                                      x[0].y + C1 * a1.y + C2 * a2.y);
+        const float2 m2 = make_float2(x[0].x + C2 * a1.x + C1 * a2.x,
+                                      x[0].y + C2 * a1.y + C1 * a2.y);
+        // i * (S1 b1 + S2 b2) and i * (S2 b1 - S1 b2)
+        const float2 j1 = make_float2(-(S1 * b1.y + S2 * b2.y), S1 * b1.x + S2 * b2.x);
+        const float2 j2 = make_float2(-(S2 * b1.y - S1 * b2.y), S2 * b1.x - S1 * b2.x);
+        x[0] = make_float2(x[0].x + a1.x + a2.x, x[0].y + a1.y + a2.y);
+        x[1] = cadd(m1, j1);
+        x[4] = csub(m1, j1);
+        x[2] = cadd(m2, j2);
+        x[3] = csub(m2, j2);
+    }
+};
+
+// Radix of the power-of-two sub-transforms.  N1 = 3: 8 up to 64 points,
+// else 4 (12 points per thread: at radix 8, 24 points per thread, the row
+// kernel spilled 180-850 bytes from 128-point sub-transforms up); N1 = 5: 4
+// (20 points per thread).
+__host__ __device__ constexpr int mix_radix(int N1, int N2)
+{
+    return N2 < 4 ? N2 : N1 == 3 && N2 <= 64 ? (fft_radix(N2) < 8 ? fft_radix(N2) : 8) : 4;
+}
+
+// FFT of length N = N1 * N2 (N2 a power of two) by one Cooley-Tukey split:
+// N1 sub-transforms of N2 points (RegFFT, one after another through the
+// same exchange buffer), twiddles W_N^(n1 k2) and an N1-point DFT per k2 in
+// registers -- no exchange beyond the sub-transforms' own.  A team of
+// T = N2 / R threads holds V = N1 R points per thread, slot q = n1 R + r:
+//   DIF false (decimation in time):  in  x[n1 + N1 (t + r T)],
+//                                    out X[(t + r T) + N2 n1];
+//   DIF true (decimation in frequency): the two layouts swapped.
+// A forward DIT transform, a pointwise product and an inverse DIF transform
+// therefore chain with no exchange, as the power-of-two RegFFT's do.
+template <int N1, int N2, int DIR, bool DIF, int RAD = mix_radix(N1, N2)>
+struct MixFFT {
+    using Sub = RegFFT<N2, DIR, RAD>;
+    static constexpr int R = Sub::R;
+    static constexpr int T = Sub::T;
+    static constexpr int V = N1 * R;
+    static constexpr int N = N1 * N2;
+    static constexpr int SMEM = Sub::SMEM;
+
+    __device__ __forceinline__ static int in_idx(int t, int q)
+    {
+        const int a = q / R, j = t + (q - a * R) * T;
+        return DIF ? j + N2 * a : a + N1 * j;
+    }
+    __device__ __forceinline__ static int out_idx(int t, int q)
+    {
+        const int a = q / R, j = t + (q - a * R) * T;
+        return DIF ? a + N1 * j : j + N2 * a;
+    }
+    __device__ static void run(float2 (&v)[V], float2 *sm, int t, const float2 *__restrict__ tw)
+    {
+        run_impl<false>(v, sm, t, tw, 0);
+    }
+    __device__ static void run_team(float2 (&v)[V], float2 *sm, int t,
+                                    const float2 *__restrict__ tw, int team)
+    {
+        run_impl<true>(v, sm, t, tw, team);
+    }
+    template <bool TEAM>
+    __device__ static __forceinline__ void subs(float2 (&v)[V], float2 *sm, int t,
+                                                const float2 *__restrict__ tw, int team)
+    {
+#pragma unroll
+        for (int a = 0; a < N1; ++a) {
+            float2 u[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                u[r] = v[a * R + r];
+            Sub::template run_impl<TEAM>(u, sm, t, tw, team);
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                v[a * R + r] = u[r];
+        }
+    }
+    template <bool TEAM>
+    __device__ static void run_impl(float2 (&v)[V], float2 *sm, int t,
+                                    const float2 *__restrict__ tw, int team)
+    {
+        if constexpr (!DIF)
+            subs<TEAM>(v, sm, t, tw, team);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int j = t + r * T;
+            float2 z[N1];
+#pragma unroll
+            for (int a = 0; a < N1; ++a)
+                z[a] = v[a * R + r];
+            if constexpr (!DIF) {
+#pragma unroll
+                for (int a = 1; a < N1; ++a)
+                    z[a] = cmul(z[a], twn<N, DIR>(tw, a * j));
+                DFTOdd<N1, DIR>::run(z);
+            } else {
+                DFTOdd<N1, DIR>::run(z);
+#pragma unroll
+                for (int a = 1; a < N1; ++a)
+                    z[a] = cmul(z[a], twn<N, DIR>(tw, a * j));
+            }
+#pragma unroll
+            for (int a = 0; a < N1; ++a)
+                v[a * R + r] = z[a];
+        }
+        if constexpr (DIF)
+            subs<TEAM>(v, sm, t, tw, team);
+    }
+};
+
+// The register FFT of length N (a power of two, or N1 * 2^k with N1 = 3, 5):
+// RegFFT at radix PRAD, or MixFFT in the DIT (DIF = false) or DIF layout.
+template <bool POW2, int N, int DIR, bool DIF, int PRAD>
+struct FFTSel {
+    using type = RegFFT<N, DIR, PRAD>;
+};
+template <int N, int DIR, bool DIF, int PRAD>
+struct FFTSel<false, N, DIR, DIF, PRAD> {
+    using type = MixFFT<odd_part(N), N / odd_part(N), DIR, DIF>;
+};
+template <int N, int DIR, bool DIF = false, int PRAD = fft_radix(N)>
+using FFTOf = typename FFTSel<odd_part(N) == 1, N, DIR, DIF, PRAD>::type;
+

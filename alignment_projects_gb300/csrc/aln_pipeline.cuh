@@ -35,12 +35,14 @@ __device__ __forceinline__ void two_sum_acc(float &s, float &e, float x)
 
 // Column prefix sums of v, v^2 and (v != 0) at the rows the lag window needs
 // (IntegrateImage's sums, 0_GEN/Correlation.cpp:49-105, restricted to the
-// rows IntegralTable will read).  grid (ceil(w/32), 2*npairs), block
-// (32, SAT_WARPS): each CTA owns 32 columns of one image; warp ty owns rows
-// [ty*segh, (ty+1)*segh) and walks them once, storing its local column
-// prefix at the needed rows.  The warps' exclusive offsets per column go to
-// segoff[ty][c]; k2_sat2w adds them.  Exact int64 for 8/16-bit pixels, FP64
-// otherwise.  Also writes the column totals (mean shift).
+// rows IntegralTable will read).  The count table is written for every job
+// (zeros without a count rule): skipping its stores changed this walk's
+// code and made it 1.7x slower on the montage strips.  grid (ceil(w/32),
+// 2*npairs), block (32, SAT_WARPS): each CTA owns 32 columns of one image;
+// warp ty owns rows [ty*segh, (ty+1)*segh) and walks them once, storing its
+// local column prefix at the needed rows.  The warps' exclusive offsets per
+// column go to segoff[ty][c]; k2_sat2w adds them.  Exact int64 for 8/16-bit
+// pixels, FP64 otherwise.  Also writes the column totals (mean shift).
 #define SAT_WARPS 16
 
 // Accumulator of a warp's segment-local sums: 32-bit for uint8 pixels (a
@@ -311,6 +313,8 @@ __device__ __forceinline__ void sat2_row_any(const PairDev &p, int i, int slot, 
     TA *__restrict__ rS = S + (long long)slot * w;
     TA *__restrict__ rQ = Q + (long long)slot * w;
     int *__restrict__ rN = p.satN[i] + (long long)slot * w;
+    // the count table only where a count rule reads it (uniform per job)
+    const bool want_n = p.cnt_kind == ALN_CNT_GT;
     TA cs = 0, cq = 0;
     int cn = 0;
     for (int c0 = 0; c0 < w; c0 += 32) {
@@ -323,25 +327,29 @@ __device__ __forceinline__ void sat2_row_any(const PairDev &p, int i, int slot, 
                 vs = rS[c] + oS[c];
                 vq = rQ[c] + oQ[c];
             }
-            vn = rN[c] + oN[c];
+            if (want_n)
+                vn = rN[c] + oN[c];
         }
         if (SQ) {
             vs = warp_incl_scan(vs, lane) + cs;
             vq = warp_incl_scan(vq, lane) + cq;
         }
-        vn = warp_incl_scan(vn, lane) + cn;
+        if (want_n)
+            vn = warp_incl_scan(vn, lane) + cn;
         if (ok) {
             if (SQ) {
                 rS[c] = vs;
                 rQ[c] = vq;
             }
-            rN[c] = vn;
+            if (want_n)
+                rN[c] = vn;
         }
         if (SQ) {
             cs = __shfl_sync(0xffffffff, vs, 31);
             cq = __shfl_sync(0xffffffff, vq, 31);
         }
-        cn = __shfl_sync(0xffffffff, vn, 31);
+        if (want_n)
+            cn = __shfl_sync(0xffffffff, vn, 31);
     }
 }
 
@@ -421,17 +429,29 @@ __host__ __device__ constexpr int rowfft_threads(int T) { return T * 4 > 512 ? 5
 // register FFT's default below.
 __host__ __device__ constexpr int rowfft_radix(int L) { return L >= 128 ? 16 : fft_radix(L); }
 
-// Each team of L / rowfft_radix(L) threads transforms one row.  G =
-// blockDim.x / T rows per CTA; smem: G * row_pitch(L) float2 per CTA.
-// Occupancy: 5 CTAs per SM up to 256-point rows (48 registers, no spills),
-// 64 registers per thread above.
+// The row transform of half-length L: the power-of-two RegFFT at
+// rowfft_radix(L), or for L = 3 * 2^k, 5 * 2^k (CorrPatches grids) the
+// MixFFT split.
 template <int L>
-__global__ void __launch_bounds__(rowfft_threads(L / rowfft_radix(L)),
-                                  L <= 256 ? 5 : 1024 / rowfft_threads(L / rowfft_radix(L)))
+using RowFFT = FFTOf<L, -1, false, rowfft_radix(L)>;
+
+// CTAs per SM the row kernel is compiled for: 5 up to 256-point
+// power-of-two rows (48 registers, no spills), 64 registers per thread for
+// longer rows and for the split lengths (12-24 points per thread).
+template <int L>
+__host__ __device__ constexpr int rowfft_minb()
+{
+    return odd_part(L) == 1 && L <= 256 ? 5 : 1024 / rowfft_threads(RowFFT<L>::T);
+}
+
+// Each team of T threads (RowFFT<L>::T) transforms one row.  G =
+// blockDim.x / T rows per CTA; smem: G * row_pitch(L) float2 per CTA.
+template <int L>
+__global__ void __launch_bounds__(rowfft_threads(RowFFT<L>::T), rowfft_minb<L>())
 k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int *sel)
 {
-    using F = RegFFT<L, -1, rowfft_radix(L)>;
-    constexpr int R = F::R, T = F::T;
+    using F = RowFFT<L>;
+    constexpr int V = F::V, T = F::T;
     constexpr int G = rowfft_threads(T) / T;
     extern __shared__ float2 smem[];
     // sel: the jobs of this launch are pairs[sel[z]] (spectrum-cache fills)
@@ -449,7 +469,7 @@ k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int
     float2 *sm = smem + team * PITCH;
     const void *img = p.img[i];
     const long long st = p.stride[i];
-    float2 v[R];
+    float2 v[V];
     if (dt == ALN_U8 || dt == ALN_U16) {
         // integer pixels, integer shift: exact before the conversion.  The
         // row is staged in shared memory with 16-byte loads from its
@@ -473,8 +493,8 @@ k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int
         team_sync<T>(team);   // each team reads back its own row only
         const unsigned char *rb8 = sb + off;
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int n = t + r * T;
+        for (int q = 0; q < V; ++q) {
+            const int n = F::in_idx(t, q);
             float2 z = make_float2(0.f, 0.f);
             if (y < h) {
                 const int xa = 2 * n, xb = 2 * n + 1;
@@ -483,13 +503,13 @@ k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int
                 if (xb < w)
                     z.y = (float)((es == 1 ? (int)rb8[xb] : (int)((const uint16_t *)rb8)[xb]) - mu);
             }
-            v[r] = z;
+            v[q] = z;
         }
     } else {
         const double mu = p.mu[i];
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int n = t + r * T;
+        for (int q = 0; q < V; ++q) {
+            const int n = F::in_idx(t, q);
             float2 z = make_float2(0.f, 0.f);
             if (y < h) {
                 const int xa = 2 * n, xb = 2 * n + 1;
@@ -498,32 +518,43 @@ k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int
                 if (xb < w)
                     z.y = (float)(load_px(img, dt, y * st + xb) - mu);
             }
-            v[r] = z;
+            v[q] = z;
         }
     }
     F::run_team(v, sm, t, tw, team);
     // split the half-length transform into the N/2+1 bins of the real row
     __syncthreads();
 #pragma unroll
-    for (int r = 0; r < R; ++r)
-        sm[padi(t + r * T)] = v[r];
+    for (int q = 0; q < V; ++q)
+        sm[padi(F::out_idx(t, q))] = v[q];
     __syncthreads();
     float2 *T_ = p.T[i];
     const int Ts = p.Ts[i];
     const int rows = min(G, h - y0);
-    // bins for (kx, row) with row fastest: coalesced [kx][y] stores
-    for (int e = threadIdx.x; e < (L + 1) * G; e += blockDim.x) {
+    // bins for (kx, row) with row fastest: coalesced [kx][y] stores.  Bin kx
+    // needs Z[kx] and conj(Z[L - kx]) (indices mod L), bin L - kx the same
+    // two values swapped: one item makes both (kx = 0..L/2; L is even).
+    for (int e = threadIdx.x; e < (L / 2 + 1) * G; e += blockDim.x) {
         const int kx = e / G, rr = e - kx * G;
         if (rr >= rows)
             continue;
         const float2 *Z = smem + rr * PITCH;
-        const float2 a = Z[padi(kx & (L - 1))];
-        const float2 b = cconj(Z[padi((L - kx) & (L - 1))]);
-        const float2 ev = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
-        const float2 dd = make_float2(0.5f * (a.x - b.x), 0.5f * (a.y - b.y));
-        const float2 o = make_float2(dd.y, -dd.x);
-        const float2 wv = __ldg(&tw[2 * L + kx]);
-        T_[(long long)kx * Ts + y0 + rr] = cadd(ev, cmul(o, wv));
+        const float2 A = Z[padi(kx)];
+        const float2 B = Z[padi(kx == 0 ? 0 : L - kx)];
+        float2 *dst = T_ + y0 + rr;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int k = h ? L - kx : kx;
+            if (h && k == kx)
+                break;   // kx = L/2: one bin
+            const float2 a = h ? B : A;
+            const float2 b = cconj(h ? A : B);
+            const float2 ev = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
+            const float2 dd = make_float2(0.5f * (a.x - b.x), 0.5f * (a.y - b.y));
+            const float2 o = make_float2(dd.y, -dd.x);
+            const float2 wv = twn<2 * L, -1>(tw, k);
+            dst[(long long)k * Ts] = cadd(ev, cmul(o, wv));
+        }
     }
 }
 
@@ -862,8 +893,8 @@ __device__ __forceinline__ void load_lag_rows(float2 *base, int stride,
 template <int L>
 __global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
 {
-    using F = RegFFT<L, +1>;
-    constexpr int R = F::R, T = F::T;
+    using F = FFTOf<L, +1>;   // RegFFT, or MixFFT for L = 3 * 2^k, 5 * 2^k
+    constexpr int V = F::V, T = F::T;
     constexpr int PITCH = row_pitch(L);   // holds L+1 bins, then 2L reals
     extern __shared__ float2 smem[];
     __shared__ double red_r[32];
@@ -885,10 +916,10 @@ __global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
     // spectrum bins of the CTA's lag rows
     load_lag_rows<L, T>(smem, PITCH, p.Q, Wy, j0);
     __syncthreads();
-    float2 v[R];
+    float2 v[V];
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const int k = t + r * T;
+    for (int q = 0; q < V; ++q) {
+        const int k = F::in_idx(t, q);
         float2 a = sm[padi(k)];
         float2 b = cconj(sm[padi(L - k)]);
         if (k == 0) {
@@ -897,22 +928,24 @@ __global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
         }
         const float2 e = cadd(a, b);
         const float2 dd = csub(a, b);
-        float2 wv = __ldg(&tw[2 * L + k]);
-        wv.y = -wv.y;   // W^{-k}
+        const float2 wv = twn<2 * L, +1>(tw, k);   // W^{-k}
         const float2 o = cmul(dd, wv);
-        v[r] = make_float2(e.x - o.y, e.y + o.x);
+        v[q] = make_float2(e.x - o.y, e.y + o.x);
     }
-    F::run(v, sm, t, tw);
+    // the teams' rows are their own from here on: team barriers only
+    F::run_team(v, sm, t, tw, team);
     __syncthreads();
     float *C = (float *)sm;   // 2L reals, unpadded
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const int n = t + r * T;
-        C[2 * n] = v[r].x;
-        C[2 * n + 1] = v[r].y;
+    for (int q = 0; q < V; ++q) {
+        const int n = F::out_idx(t, q);
+        C[2 * n] = v[q].x;
+        C[2 * n + 1] = v[q].y;
     }
     __syncthreads();
-    const float invf = 1.0f / ((float)Nx * (float)Ny);   // a power of two: exact
+    // 1 / (Nx Ny): exact for power-of-two grids; on the split lengths one
+    // more FP32 rounding, below the transform's own error
+    const float invf = 1.0f / ((float)Nx * (float)Ny);
     double br = -1.0e30;
     long long bk = 0x7fffffffffffffffLL;
     if (live) {
@@ -1026,7 +1059,7 @@ __global__ void __launch_bounds__(256, SONLY ? 3 : 2) k2_lagimg(PairDev *pairs, 
             const float2 o = cmul(dd, wv);
             v[r] = make_float2(e.x - o.y, e.y + o.x);
         }
-        F::run(v, reg, t, tw);
+        F::run_team(v, reg, t, tw, team);   // the team's own row
         __syncthreads();
         float *C = (float *)reg;
 #pragma unroll
@@ -1477,7 +1510,7 @@ __global__ void k2_lagp2i(PairDev *pairs, const float2 *__restrict__ tw)
         const float2 o = cmul(dd, wv);
         v[r] = make_float2(e.x - o.y, e.y + o.x);
     }
-    F::run(v, sm, t, tw);
+    F::run_team(v, sm, t, tw, team);   // the team's own row
     double br = -1.0e30;
     long long bk = 0x7fffffffffffffffLL;
     if (live) {

@@ -340,10 +340,14 @@ extern "C" long long aln_server_counter(aln_server *S, int which)
     case 1: return S->n_fin;
     case 2: return S->n_batches;
     case 3: return (long long)S->q.size();
-    case 4: {
+    case 4:
+    case 5:
+    case 6:
+    case 7: {
         long long h = 0;
         for (aln_ctx *c : S->ctxs)
-            h += c->spec_hits;
+            h += which == 4 ? c->spec_hits : which == 5 ? c->spec_fills
+                 : which == 6 ? c->spec_evictions : (long long)c->spec_bytes;
         return h;
     }
     default: return -1;

@@ -8,10 +8,12 @@
 // register FFT radix, shared-memory passes, how many columns a batch
 // brings), not on a formula.  So the first time a pair of a new class
 // appears, the tuner times every valid choice on synthetic device pairs of
-// that exact geometry (CUDA events around whole batches of them), keeps the
-// fastest (when it beats the cost model's pick by more than 10 %), and
-// records it in a file named for the GPU and the library
-// build, which later processes read back.
+// that exact geometry (CUDA events around whole batches of them) and
+// records in a file named for the GPU and the library build (which later
+// processes read back) either the fastest choice, when it beats the cost
+// model's pick by more than 10 %, or "cost model" (-1).  With "cost model"
+// every pair of the class keeps its own cost-model plan: the class spans a
+// range of heights, and the representative's pick is not the others'.
 //
 // Class: (Nx / 2, the unsegmented Ny, the window height Wy rounded up to a
 // power of two, a's height rounded up to a power of two, a's pixel size).
@@ -43,7 +45,7 @@ struct TuneKey {
 };
 
 static std::mutex g_tune_lock;
-static std::map<TuneKey, int> g_tune;           // -> 0 unsegmented, NS > 0
+static std::map<TuneKey, int> g_tune;           // -> -1 cost model, 0 unsegmented, NS > 0
 static bool g_tune_loaded[64];
 static std::string g_tune_path[64];
 
@@ -93,7 +95,7 @@ static void tune_load(int dev)
         int ns = -1;
         if (sscanf(line.c_str(), "%d %d %d %d %d %d", &k.L, &k.nyf, &k.wyb, &k.h0b, &k.es,
                    &ns) == 6 &&
-            ns >= 0)
+            ns >= -1)
             g_tune[k] = ns;
     }
 }
@@ -141,7 +143,8 @@ static int tune_images(aln_ctx *ctx, const aln_pair &P, void **buf, aln_pair &S)
 
 // The class's measured choice for a pair planned as d (caller-frame pair P),
 // whose valid segment lengths are cand (the cost model's pick first, 0 =
-// unsegmented).  Returns the choice, or -1 when it cannot be measured.
+// unsegmented).  Returns the choice, or -1 for the cost model's plan (the
+// class entry says so, or the class cannot be measured).
 static int tuned_segment(aln_ctx *ctx, const aln_pair &P, const PairDev &d, int Wy,
                          const std::vector<int> &cand)
 {
@@ -203,18 +206,16 @@ static int tuned_segment(aln_ctx *ctx, const aln_pair &P, const PairDev &d, int 
     cudaFree(buf);
     cudaGetLastError();
     ctx->tune_classes++;
-    // the fastest; the cost model's pick unless another beats it by > 10 %
-    // (a class that leaves the common plan splits the batch's chunks: on the
-    // uneven batch, overriding at 3 % made the whole batch 2.7 % slower)
+    // the fastest, where it beats the cost model's pick by > 10 % (a class
+    // that leaves the common plan splits the batch's chunks); else the cost
+    // model, pair by pair
     size_t best = 0;
     for (size_t c = 1; c < cand.size(); ++c)
         if (ms[c] < ms[best])
             best = c;
-    if (ms[best] > 0.90f * ms[0])
-        best = 0;
     if (ms[best] >= 1e29f)
         return -1;
-    const int choice = cand[best];
+    const int choice = ms[best] > 0.90f * ms[0] ? -1 : cand[best];
     g_tune[key] = choice;
     if (FILE *f = fopen(g_tune_path[dev].c_str(), "a")) {
         fprintf(f, "%d %d %d %d %d %d ", key.L, key.nyf, key.wyb, key.h0b, key.es, choice);

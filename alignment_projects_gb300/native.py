@@ -271,6 +271,7 @@ def lib():
                                             C.POINTER(C.c_int)]
         L.aln_ctx_set_segmenting.argtypes = [C.c_void_p, C.c_int]
         L.aln_ctx_set_tuning.argtypes = [C.c_void_p, C.c_int]
+        L.aln_ctx_set_split_grids.argtypes = [C.c_void_p, C.c_int]
         L.aln_approx_match_batch.argtypes = [C.c_void_p, C.c_int, C.POINTER(AlnTilePair),
                                              C.POINTER(AlnApproxParams),
                                              C.POINTER(AlnApproxResult)]
@@ -401,7 +402,8 @@ class Context:
                 "spec_bytes": self._L.aln_ctx_counter(self.h, 5),
                 "chunks": self._L.aln_ctx_counter(self.h, 6),
                 "h2d_copies": self._L.aln_ctx_counter(self.h, 7),
-                "tune_classes": self._L.aln_ctx_counter(self.h, 8)}
+                "tune_classes": self._L.aln_ctx_counter(self.h, 8),
+                "spec_evictions": self._L.aln_ctx_counter(self.h, 9)}
 
     def set_segmenting(self, ns: int):
         """CorrPatches column segments: 0 the class's measured plan (or the
@@ -413,6 +415,11 @@ class Context:
         """Measured column plans per pair class (the autotuner) or the fixed
         cost model."""
         self._check(self._L.aln_ctx_set_tuning(self.h, int(bool(on))))
+
+    def set_split_grids(self, on: bool):
+        """CorrPatches rows of 3 * 2^k and 5 * 2^k points where shorter than
+        the power of two (default on), or powers of two only."""
+        self._check(self._L.aln_ctx_set_split_grids(self.h, int(bool(on))))
 
     def set_spectrum_cache(self, nbytes: int):
         self._check(self._L.aln_ctx_set_spectrum_cache(self.h, nbytes))
@@ -865,4 +872,5 @@ class Server:
     def counters(self) -> dict:
         c = self._L.aln_server_counter
         return {"submitted": c(self.h, 0), "finished": c(self.h, 1), "batches": c(self.h, 2),
-                "waiting": c(self.h, 3), "spec_hits": c(self.h, 4)}
+                "waiting": c(self.h, 3), "spec_hits": c(self.h, 4), "spec_fills": c(self.h, 5),
+                "spec_evictions": c(self.h, 6), "spec_bytes": c(self.h, 7)}

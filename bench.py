@@ -78,6 +78,13 @@ def parse():
     ap.add_argument("--served-requests", type=int, default=2000)
     ap.add_argument("--served-strips", type=int, default=512)
     ap.add_argument("--served-groups", type=int, default=32)
+    ap.add_argument("--served-tiles", type=int, default=0,
+                    help="served at tile scale: sweep tiles B keyed by this many distinct tile "
+                         "ids (patch tiles by half as many), each reused by 6 neighbours in a "
+                         "sliding window of active tiles; spectrum caches bounded by free HBM "
+                         "(0: the pooled default, every group keyed once)")
+    ap.add_argument("--served-window", type=int, default=32,
+                    help="tiles whose neighbour requests are in flight at once (--served-tiles)")
     ap.add_argument("--uneven-pairs", type=int, default=20000)
     ap.add_argument("--c1-pairs", type=int, default=64)
     return ap.parse_args()
@@ -1089,6 +1096,98 @@ def served_requests(pools, n, seed):
     return reqs, cls, keep
 
 
+class TileWalk:
+    """Tile ids 0..n-1 in a random order, `window` of them active at a time;
+    each draw takes a random active tile, which retires after `uses` draws
+    (its 6 neighbours) and lets the next id in."""
+
+    def __init__(self, n, window, uses, seed):
+        self.rng = np.random.default_rng(seed)
+        self.order = self.rng.permutation(n)
+        self.next = 0
+        self.uses = uses
+        self.active = []
+        while len(self.active) < window and self.next < n:
+            self.active.append([int(self.order[self.next]), 0])
+            self.next += 1
+
+    def draw(self):
+        """(tile id, neighbour index), or None when every tile is used up."""
+        if not self.active:
+            return None
+        k = int(self.rng.integers(len(self.active)))
+        tile, used = self.active[k]
+        self.active[k][1] += 1
+        if self.active[k][1] >= self.uses:
+            if self.next < len(self.order):
+                self.active[k] = [int(self.order[self.next]), 0]
+                self.next += 1
+            else:
+                self.active.pop(k)
+        return tile, used
+
+
+def served_tile_requests(pools, n_tiles, window, seed):
+    """The tile-scale stream: the 70/20/10 mix until every one of n_tiles
+    sweep tiles (keys 10^7 + id) has served its 6 neighbours; patch tiles
+    (keys 2 * 10^7 + id) walk n_tiles / 2 ids at their own pace.  Pixels come
+    from the pools (tile id modulo the pool), so distinct keys hold equal
+    pixels -- the cache's promise runs one way only: equal keys, equal
+    images."""
+    import ctypes as C
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300.native import AlnRequest, AlnThumbs, _thm_params
+    strips, thumbs, patches = pools
+    rng = np.random.default_rng(seed)
+    sweeps = TileWalk(n_tiles, window, 6, seed + 1)
+    pw = TileWalk(max(1, n_tiles // 2), window, 6, seed + 2)
+    lg_s = aln.legal(aln.RGN_SECTION, 1500, 1500, 30000)
+    lg_p = aln.legal(aln.RGN_MIN, 32, 32, 0)
+    thm = _thm_params()
+    reqs, cls, keep = [], [], [lg_s, lg_p]
+    n_groups = len(thumbs) // 6
+    ci = 0
+    while True:
+        c = int(rng.choice(3, p=SERVED_MIX))
+        r = AlnRequest()
+        if c == 0:
+            a, b, ox, oy, rad = strips[ci % len(strips)]
+            ci += 1
+            r.kind = aln.REQ_PATCHES
+            r.pair.a, r.pair.b = aln.image(a), aln.image(b)
+            r.pair.ox, r.pair.oy, r.pair.radius = ox, oy, rad
+            r.pair.legal = lg_s
+        elif c == 1:
+            d = sweeps.draw()
+            if d is None:
+                break
+            tile, j = d
+            src = thumbs[(tile % n_groups) * 6 + j]
+            T = AlnThumbs()
+            C.memmove(C.addressof(T), C.addressof(src), C.sizeof(AlnThumbs))
+            T.b_key = 10_000_000 + tile
+            keep.append(T)
+            r.kind = aln.REQ_SWEEP
+            r.thumbs = T
+            r.thm = thm
+            r.thm_mode, r.ang0, r.hfang, r.step = aln.THM_DENOVO, 0.0, 10.0, 0.5
+        else:
+            d = pw.draw()
+            if d is None:
+                pw = TileWalk(max(1, n_tiles // 2), window, 6, seed + 3 + len(reqs))
+                d = pw.draw()
+            tile, j = d
+            a, b, _ = patches[(tile % n_groups) * 6 + j]
+            r.kind = aln.REQ_PATCHES
+            r.pair.a, r.pair.b = aln.image(a), aln.image(b)
+            r.pair.radius = 4096
+            r.pair.legal = lg_p
+            r.pair.b_key = 20_000_000 + tile
+        reqs.append(r)
+        cls.append(c)
+    return reqs, np.array(cls), keep
+
+
 def served_run(srv, reqs, rate, seed):
     """Submit reqs at Poisson times of `rate` per second; collect every reply.
     Returns (wall seconds first submit -> last reply, replies by index)."""
@@ -1158,7 +1257,9 @@ def run_served(args, embedded=False):
     dev = torch.device("cuda", local)
     pools = served_pools(5, dev, args.served_strips, args.served_groups)
     torch.cuda.synchronize()
-    srv = aln.Server(local, workers=2)
+    tiles = getattr(args, "served_tiles", 0) if not embedded else 0
+    # tile scale: each worker's spectrum cache bounded by free HBM alone
+    srv = aln.Server(local, workers=2, cache_bytes=(1 << 64) - 1 if tiles else 0)
     rates = [float(r) for r in args.served_rates.split(",")]
     # warm-up: every class through the server
     reqs, cls, keep = served_requests(pools, 200, 11)
@@ -1167,14 +1268,29 @@ def run_served(args, embedded=False):
     clk.start()
     table = []
     for k, rate in enumerate(rates):
-        reqs, cls, keep = served_requests(pools, args.served_requests, 100 + k)
+        if tiles:
+            reqs, cls, keep = served_tile_requests(pools, tiles, args.served_window, 100 + k)
+        else:
+            reqs, cls, keep = served_requests(pools, args.served_requests, 100 + k)
+        c0 = srv.counters()
+        free0 = torch.cuda.mem_get_info(local)[0]
         wall, done = served_run(srv, reqs, rate, 200 + k)
+        c1 = srv.counters()
         lat = np.array([done[i][1] for i in range(len(reqs))])
         bad = sum(1 for i in range(len(reqs)) if done[i][0] < 0)
         row = {"offered_rate": rate, "requests": len(reqs), "throughput": len(reqs) / wall,
                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                "mean_batch": float(np.mean([done[i][3] for i in range(len(reqs))])),
-               "errors": bad}
+               "errors": bad,
+               "spec_hits": c1["spec_hits"] - c0["spec_hits"],
+               "spec_fills": c1["spec_fills"] - c0["spec_fills"],
+               "spec_evictions": c1["spec_evictions"] - c0["spec_evictions"],
+               "cache_gb_after": c1["spec_bytes"] / 1e9,
+               "free_hbm_gb_before": free0 / 1e9,
+               "free_hbm_gb_after": torch.cuda.mem_get_info(local)[0] / 1e9}
+        if tiles:
+            row["distinct_sweep_keys"] = int(tiles)
+            row["distinct_patch_keys"] = int(max(1, tiles // 2))
         for c, name in enumerate(("strips", "sweeps", "patches")):
             m = cls == c
             if m.any():
@@ -1217,7 +1333,14 @@ def run_served(args, embedded=False):
         "steps": len(rates), "warmup": 1, "ms_per_step": None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": SERVED_WORKLOAD, "requests_per_rate": args.served_requests,
-                   "rates": rates, "note": "one step = one offered rate; value = best throughput"},
+                   "rates": rates, "note": "one step = one offered rate; value = best throughput",
+                   "tiles": tiles or None,
+                   "tile_note": ("sweep tiles B keyed by %d distinct ids, patch tiles by %d, each "
+                                 "reused by 6 neighbours (a sliding window of %d active tiles); "
+                                 "caches bounded by free HBM" % (tiles, max(1, tiles // 2),
+                                                                 args.served_window)
+                                 if tiles else "pooled: %d sweep and %d patch keys"
+                                 % (args.served_groups, args.served_groups))},
         "e2e": {"value": best["throughput"], "unit": "requests/s",
                 "note": "host inputs through the server API: value is end to end"},
         "rates": table,
@@ -1303,19 +1426,27 @@ def run_uneven(args, embedded=False):
     prof = ctx.profile()
     cnt = ctx.counters()
     value = ws * n * args.steps / (ms / 1000.0)
-    # the same batch on the fixed cost model's plans (autotuner off)
+    # the same batch on the fixed cost model's plans (autotuner off), and
+    # the tuned plans again, both without the per-launch profiling events of
+    # the timed region above (about 1200 launches per step here)
     ctx_fixed = aln.Context(local)
     ctx_fixed.set_tuning(False)
     out_f = (AlnResult * n)()
     if L.aln_corr_patches_batch(ctx_fixed.h, n, arr_d, out_f) < 0:
         raise RuntimeError(L.aln_last_error(ctx_fixed.h).decode())
-    torch.cuda.synchronize()
-    e0.record()
-    for _ in range(args.steps):
-        L.aln_corr_patches_batch(ctx_fixed.h, n, arr_d, out_f)
-    e1.record()
-    torch.cuda.synchronize()
-    ms_fixed = e0.elapsed_time(e1)
+    ctx.set_profiling(False)
+
+    def timed(c, out):
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            L.aln_corr_patches_batch(c.h, n, arr_d, out)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    ms_fixed = timed(ctx_fixed, out_f)
+    ms_tuned = timed(ctx, out_d)
     chunks_fixed = ctx_fixed.counters()["chunks"] / (args.steps + 1)
     ctx_fixed.close()
     fixed_same_peaks = sum(1 for k in range(n) if (out_f[k].peak_x, out_f[k].peak_y) ==
@@ -1385,9 +1516,10 @@ def run_uneven(args, embedded=False):
                     "h2d_bytes_per_step": (cnt2["h2d_bytes"]) // args.steps,
                     "d2h_bytes_per_step": (cnt2["d2h_bytes"]) // args.steps},
             "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": cnt["launches"],
-            "autotuner": {"tuned_pairs_per_s": value,
+            "autotuner": {"tuned_pairs_per_s": n * args.steps / (ms_tuned / 1000.0),
                           "fixed_plan_pairs_per_s": n * args.steps / (ms_fixed / 1000.0),
-                          "tuned_over_fixed": ms_fixed / ms,
+                          "tuned_over_fixed": ms_fixed / ms_tuned,
+                          "note": "both timed without per-launch profiling events",
                           "classes_timed": ctx.counters()["tune_classes"],
                           "chunks_per_step_tuned": cnt["chunks"] / args.steps,
                           "chunks_per_step_fixed": chunks_fixed,

@@ -139,7 +139,7 @@ int aln_ctx_profile(aln_ctx *ctx, int cap, const char **names, long long *launch
  * the last aln_ctx_profile_reset), 5 = device bytes the cache holds,
  * 6 = batch chunks run, 7 = host-to-device staging transfers issued (both
  * since the last reset), 8 = pair classes this context timed for the
- * autotuner. */
+ * autotuner, 9 = spectrum-cache entries evicted (since the last reset). */
 long long aln_ctx_counter(aln_ctx *ctx, int which);
 
 /* Autotuner (no reference counterpart; replaces the reference's fixed
@@ -149,12 +149,26 @@ long long aln_ctx_counter(aln_ctx *ctx, int which);
  * (Nx/2, Ny, window height and a's height rounded up to powers of two, a's
  * pixel size) -- times every valid column plan (one Ny-point transform per
  * column, or segments of each valid length NS) on synthetic device pairs of
- * its geometry with CUDA events, and the fastest becomes the class's plan.
+ * its geometry with CUDA events.  A plan that beats the cost model's pick by
+ * more than 10 % becomes the class's plan; otherwise the class is marked
+ * "cost model" and each of its pairs keeps its own cost-model plan.
  * Choices are kept per process and in <library dir>/tune/<GPU name>-<build
  * id>.txt (or $ALN_TUNE_DIR), which later processes read; an entry never
  * changes once made, so a pair's numbers do not depend on its batch.  Off:
  * the fixed cost model N (log2 N + 4) per transform. */
 int aln_ctx_set_tuning(aln_ctx *ctx, int on);
+
+/* CorrPatches transform rows of 3 * 2^k and 5 * 2^k points (on by
+ * default).  Replaces the reference's power-of-two size rule (FFTSize,
+ * 0_GEN/Correlation.cpp:333-359) on the row axis of the batched path: a
+ * pair's grid is the shortest alias-free length for its disc among powers
+ * of two and 2L for L in {80, 96, 160, 192, 320, 384, 640, 768, 1280,
+ * 1536}.  The correlation sums at the disc's lags are the same on every
+ * alias-free grid, so r, the peak and the sub-pixel offsets agree with the
+ * power-of-two plan within FP32 rounding.  Off: powers of two only.
+ * CorrImages jobs always keep the reference's power-of-two grids (the
+ * whitened S product depends on the grid). */
+int aln_ctx_set_split_grids(aln_ctx *ctx, int on);
 
 /* Spectrum cache: the device-resident form of the reference's fft2 / ftc
  * cache arguments (CorrPatches' `vector<CD> &fft2`, 0_GEN/Correlation.cpp:
@@ -169,7 +183,10 @@ int aln_ctx_set_tuning(aln_ctx *ctx, int on);
  * aln_ctx_set_segmenting(ctx, -1); a segmented uncached job agrees within
  * FP32 rounding).
  * `bytes` bounds the device memory the cache holds (default 8 GiB; 0 turns
- * it off and releases it); least recently used entries are evicted. */
+ * it off and releases it; SIZE_MAX: bounded by free device memory alone).
+ * The cache also never grows into the last (workspace limit + 2 GiB) of
+ * free device memory.  Least recently used entries are evicted first
+ * (entries the running chunk reads are kept). */
 int aln_ctx_set_spectrum_cache(aln_ctx *ctx, size_t bytes);
 
 /* CorrPatches column segmenting for this context: 0 = the cost model
@@ -641,7 +658,8 @@ typedef struct aln_server_params {
     size_t mem_budget;    /* device bytes for request workspaces, all workers
                              together (0: half of the free device memory, at most 16 GiB) */
     int max_batch;        /* requests per batch (0: 4096) */
-    size_t cache_bytes;   /* spectrum cache per worker (0: 2 GiB) */
+    size_t cache_bytes;   /* spectrum cache per worker (0: 2 GiB; SIZE_MAX: bounded
+                             by free device memory, aln_ctx_set_spectrum_cache) */
 } aln_server_params;
 
 enum { ALN_REQ_PATCHES = 0, ALN_REQ_IMAGES = 1, ALN_REQ_SWEEP = 2 };
@@ -681,7 +699,8 @@ int aln_server_wait(aln_server *s, unsigned long long ticket, int timeout_ms, al
 int aln_server_collect(aln_server *s, int cap, int timeout_ms, unsigned long long *tickets,
                        aln_reply *out);
 /* which: 0 requests submitted, 1 finished, 2 batches run, 3 waiting now,
- * 4 spectrum-cache hits (all workers). */
+ * 4 spectrum-cache hits, 5 fills, 6 evictions, 7 device bytes the caches
+ * hold (4-7 summed over the workers). */
 long long aln_server_counter(aln_server *s, int which);
 const char *aln_server_last_error(aln_server *s);
 

@@ -82,15 +82,18 @@ def _pair(w0, h0, w1, h1, ox, oy, radius, buf):
 
 
 def test_corr_patches_grid_keeps_disc_lags_alias_free():
-    """The CorrPatches transform grid: a power of two, no larger than the
-    reference's FFTSize grid, holding both images, and leaving every lag of
-    the disc window free of wrap-around (x + m N outside the linear support
-    [-(w0-1), w1-1] for m != 0).  Host planning only."""
+    """The CorrPatches transform grid: the shortest alias-free length -- a
+    power of two, or on the row axis a split length 2L (L = 3 * 2^k,
+    5 * 2^k) -- no larger than the reference's FFTSize grid, holding both
+    images, and leaving every lag of the disc window free of wrap-around
+    (x + m N outside the linear support [-(w0-1), w1-1] for m != 0).  Host
+    planning only."""
     import numpy as np
     import alignment_projects_gb300 as aln
     buf = np.zeros(4096 * 4096, np.uint8)
     rng = np.random.default_rng(5)
-    shrunk = segmented = 0
+    shrunk = segmented = split = 0
+    split_lens = {2 * L for L in (80, 96, 160, 192, 320, 384, 640, 768, 1280, 1536)}
     cases = [(256, 2048, 256, 2048, 0, 0, 64), (200, 2048, 200, 2048, 0, 0, 64),
              (512, 512, 512, 512, 0, 0, 4096), (300, 120, 280, 100, 0, 0, 30),
              (64, 64, 64, 64, 40, -40, 10), (1, 1, 1, 1, 0, 0, 5)]
@@ -115,10 +118,17 @@ def test_corr_patches_grid_keeps_disc_lags_alias_free():
             assert ny & (ny - 1) == 0 and ny < aln.lib().aln_fft_size(h0, h1)
             assert seg_len + wy - 1 <= ny and nseg * seg_len >= h0
             segmented += 1
+        # the row length: the shortest alias-free one of the powers of two
+        # and the split lengths
+        need = max(max(w0, w1), max(w1 - 1 - xlo, xhi + w0 - 1) + 1)
+        cands = [c for c in split_lens | {max(2, 1 << (need - 1).bit_length())} if c >= need]
+        assert nx == min(min(cands), max(2, aln.lib().aln_fft_size(w0, w1))), (nx, need)
+        split += nx in split_lens
         for n, a0, a1, lo, hi in ((nx, w0, w1, xlo, xhi),) + (
                 () if nseg else ((ny, h0, h1, ylo, yhi),)):
             ref = aln.lib().aln_fft_size(a0, a1)
-            assert n & (n - 1) == 0 and n <= max(2, ref), (n, ref)
+            assert (n & (n - 1) == 0 or (n is nx and n in split_lens)) and n <= max(2, ref), \
+                (n, ref)
             assert n >= max(a0, a1)
             for m in (-2, -1, 1, 2):
                 for d in (lo, hi):
@@ -126,5 +136,6 @@ def test_corr_patches_grid_keeps_disc_lags_alias_free():
             shrunk += n < ref
     assert shrunk > 50   # many discs allow a smaller grid
     assert segmented > 10
+    assert split > 50    # and many a split row length
     # the montage strips (W x 2048, disc radius 64) are segmented
     assert aln.corr_patches_grid(_pair(200, 2048, 200, 2048, 0, 0, 64, buf))[2] > 0

@@ -281,6 +281,77 @@ def test_disc_grids_shrink_and_batch(ctx):
         assert g == single
 
 
+@pytest.fixture(scope="module")
+def ctx_pow2():
+    """A context with power-of-two transform grids only."""
+    import alignment_projects_gb300 as aln
+    c = aln.Context(0)
+    c.set_split_grids(False)
+    yield c
+    c.close()
+
+
+def _grid_of(job):
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300.native import AlnPair
+    P = AlnPair()
+    P.a, P.b = aln.image(job["a"]), aln.image(job["b"])
+    P.ox, P.oy, P.radius = job["ox"], job["oy"], job["radius"]
+    return aln.corr_patches_grid(P)
+
+
+SPLIT_NX = (160, 192, 320, 384, 640, 768, 1280, 1536, 2560, 3072)
+
+
+@pytest.mark.parametrize("nx", SPLIT_NX)
+def test_split_row_lengths_match_power_of_two(ctx, ctx_pow2, nx):
+    """Rows of 3 * 2^k and 5 * 2^k points: a uint8 pair that needs exactly nx
+    row points (width nx - 24, disc radius 24) is planned onto that split
+    length and gives the power-of-two plan's numbers -- the same peak (the
+    true offset), r within 1e-4, the sub-pixel offsets within 0.01 px."""
+    import alignment_projects_gb300 as aln
+    from alignment_projects_gb300 import synth
+    rad, m = 24, 16
+    w = nx - rad
+    h = w + 16                     # taller than wide: rows stay the x axis
+    rng = np.random.default_rng(nx)
+    tx, ty = (int(v) for v in rng.integers(-12, 13, 2))
+    f = synth.field_np(nx, h + 2 * m, w + 2 * m)
+    a = synth.to_u8(f[m:m + h, m:m + w] + rng.normal(0.0, 8.0, (h, w)))
+    b = synth.to_u8(f[m + ty:m + ty + h, m + tx:m + tx + w] + rng.normal(0.0, 8.0, (h, w)))
+    job = dict(a=a, b=b, ox=0, oy=0, radius=rad, legal=aln.legal(aln.RGN_MIN, 32, 32, 0))
+    gx, _, _, tr = _grid_of(job)
+    assert (gx, tr) == (nx, 0), (gx, tr)
+    g = ctx.corr_patches_batch([job])[0]
+    ref = ctx_pow2.corr_patches_batch([job])[0]
+    assert g["status"] == ref["status"] == aln.ALN_OK
+    assert (g["peak_x"], g["peak_y"]) == (ref["peak_x"], ref["peak_y"]) == (-tx, -ty), (g, ref)
+    assert abs(g["r"] - ref["r"]) <= R_TOL, (g, ref)
+    assert abs(g["dx"] - ref["dx"]) <= PX_TOL and abs(g["dy"] - ref["dy"]) <= PX_TOL, (g, ref)
+
+
+@pytest.mark.parametrize("W", [170, 250, 300])
+def test_split_montage_strips_against_oracle(ctx, orc, W):
+    """Montage strips whose rows need W + 64 points: 256 (a power of two),
+    320 (5 * 64) and 384 (3 * 128) -- held to the oracle's bar, alone and in
+    one batch with the other widths."""
+    import oracle
+    from alignment_projects_gb300 import synth
+    lg_o = oracle.legal(oracle.RGN_SECTION, 1500, 1500, 30000)
+    ps = [synth.montage_pair(900 + W + k, wmin=w, wmax=w)
+          for k, w in enumerate((W, 170, 250, 300))]
+    jobs = [dict(a=p.a, b=p.b, ox=p.ox, oy=p.oy, radius=p.radius, legal=aln_legal(lg_o))
+            for p in ps]
+    want_nx = {170: 256, 250: 320, 300: 384}[W]
+    assert _grid_of(jobs[0])[0] == want_nx
+    batch = ctx.corr_patches_batch(jobs)
+    g = ctx.corr_patches(jobs[0]["a"], jobs[0]["b"], 0, 0, 64, jobs[0]["legal"])
+    assert g == batch[0]
+    assert_parity(g, _oracle_pair(orc, ps[0], lg_o), f"split strip W={W}")
+    if not ps[0].decoy:
+        assert (g["peak_x"], g["peak_y"]) == ps[0].truth
+
+
 @pytest.mark.parametrize("ns", [-1, 0, 256, 512, 1024, 2048])
 def test_segmented_columns(ctx, orc, ns):
     """CorrPatches with the column axis cut into segments of every forced

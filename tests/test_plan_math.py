@@ -99,6 +99,39 @@ def test_plan_equals_linear_correlation(seed):
                 (seed, dx, dy, nx, ny, nseg)
 
 
+SPLIT_L = (80, 96, 160, 192, 320, 384, 640, 768, 1280, 1536)
+
+
+def _shortest_len(need):
+    pow2 = max(2, 1 << (need - 1).bit_length())
+    return min([pow2] + [2 * L for L in SPLIT_L if 2 * L >= need])
+
+
+@pytest.mark.parametrize("W", [170, 193, 250, 256, 257, 300, 307])
+def test_split_row_lengths_for_montage_strips(W):
+    """Montage strips (W x 600 here, disc radius 64 at 0): the row axis
+    takes the shortest alias-free length among powers of two and the split
+    lengths 2L (L = 3 * 2^k, 5 * 2^k) -- W + 64 points are needed -- and
+    that grid still gives the linear correlation at the disc's lags."""
+    import alignment_projects_gb300 as aln
+    keep = []
+    h = 600
+    nx, ny, nseg, tr = aln.corr_patches_grid(_pair(W, h, W, h, 0, 0, 64, keep))
+    assert not tr
+    assert nx == _shortest_len(W + 64), (W, nx)
+    rng = np.random.default_rng(W)
+    a = rng.standard_normal((h, W))
+    b = rng.standard_normal((h, W))
+    xlo, xhi, ylo, yhi = _window(W, h, W, h, 0, 0, 64)
+    got = _plan_corr(a, b, nx, ny, nseg, ylo, yhi)
+    for dy in (ylo, -17, 0, 5, yhi):
+        for dx in (xlo, -63, -1, 0, 1, 40, xhi):
+            if dx * dx + dy * dy > 64 * 64:
+                continue
+            want = _direct(a, b, dx, dy)
+            assert abs(got[dy - ylo, dx % nx] - want) <= 1e-9 * max(1.0, abs(want)), (W, dx, dy)
+
+
 def test_some_plans_are_segmented():
     import alignment_projects_gb300 as aln
     keep = []
