@@ -1950,9 +1950,9 @@ static int cols_per_cta(int Ny) { return std::max(1, std::min(16, 4096 / Ny)); }
 template <int LL>
 static void launch_rowfft2(aln_ctx *ctx, int n, int maxh)
 {
-    constexpr int T = RowFFT<LL>::T;
+    constexpr int T = rowfft_T<LL>();
     const int thr = rowfft_threads(T), G = thr / T;
-    const size_t sm = (size_t)G * row_pitch(LL) * sizeof(float2);
+    const size_t sm = ((size_t)G * rowfft_pitch<LL>() + 16) * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_rowfft<LL>, sm);
     LAUNCH(ctx, "k2_rowfft", k2_rowfft<LL>, dim3((maxh + G - 1) / G, 2, n), thr, sm,
            ctx->dpairs, ctx->tw, -1, (const int *)nullptr);
@@ -1962,9 +1962,9 @@ static void launch_rowfft2(aln_ctx *ctx, int n, int maxh)
 template <int LL>
 static void launch_fill_rows(aln_ctx *ctx, int nsel, int maxh)
 {
-    constexpr int T = RowFFT<LL>::T;
+    constexpr int T = rowfft_T<LL>();
     const int thr = rowfft_threads(T), G = thr / T;
-    const size_t sm = (size_t)G * row_pitch(LL) * sizeof(float2);
+    const size_t sm = ((size_t)G * rowfft_pitch<LL>() + 16) * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_rowfft<LL>, sm);
     LAUNCH(ctx, "k2_rowfft", k2_rowfft<LL>, dim3((maxh + G - 1) / G, 1, nsel), thr, sm,
            ctx->dpairs, ctx->tw, 1, (const int *)ctx->dsel_cur);
@@ -2048,7 +2048,7 @@ template <int LL>
 static void launch_lagrow2(aln_ctx *ctx, int n, int maxWy)
 {
     constexpr int T = FFTOf<LL, +1>::T;
-    const int thr = std::max(256, T), G = thr / T;
+    constexpr int thr = lagrow_threads(T), G = thr / T;
     const size_t sm = (size_t)G * row_pitch(LL) * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_lagrow<LL>, sm);
     LAUNCH(ctx, "k2_lagrow", k2_lagrow<LL>, dim3((maxWy + G - 1) / G, n), thr, sm,

@@ -110,13 +110,18 @@ __device__ __forceinline__ void team_sync(int team)
         __syncwarp();
 }
 
-template <int N, int DIR, int RAD = fft_radix(N)>
+// PADK: exchange-buffer padding i -> i + (i >> PADK): 4 (one slot per 16)
+// by default; 3 for kernels whose teams of <= 8 threads share a half-warp
+// with a neighbour team placed 8 bank pairs away (the row pass), where it
+// keeps both teams' strided writes on distinct banks.
+template <int N, int DIR, int RAD = fft_radix(N), int PADK = 4>
 struct RegFFT {
     static constexpr int R = RAD;
     static constexpr int T = N / R;                    // threads per transform
     static constexpr int P = ilog2c(N) / ilog2c(R);    // full radix-R passes
     static constexpr int R2 = N / ipowc(R, P);         // first-pass radix (1: none)
-    static constexpr int SMEM = padded(N);             // float2 per team
+    static constexpr int SMEM = N + (N >> PADK);       // float2 per team
+    __device__ __forceinline__ static int pad(int i) { return i + (i >> PADK); }
     static constexpr int V = R;                        // points per thread
     // register slot q of thread t holds point t + q T, in and out
     __device__ __forceinline__ static int in_idx(int t, int q) { return t + q * T; }
@@ -169,12 +174,12 @@ struct RegFFT {
                 const int j = t + q * T;
 #pragma unroll
                 for (int s = 0; s < R2; ++s)
-                    sm[padi(j * R2 + s)] = v[q + s * m];
+                    sm[pad(j * R2 + s)] = v[q + s * m];
             }
             sync<TEAM>(team);
 #pragma unroll
             for (int r = 0; r < R; ++r)
-                v[r] = sm[padi(t + r * T)];
+                v[r] = sm[pad(t + r * T)];
             Ns = R2;
         }
 #pragma unroll
@@ -196,11 +201,11 @@ struct RegFFT {
                 sync<TEAM>(team);
 #pragma unroll
                 for (int r = 0; r < R; ++r)
-                    sm[padi(base + r * Ns)] = v[r];
+                    sm[pad(base + r * Ns)] = v[r];
                 sync<TEAM>(team);
 #pragma unroll
                 for (int r = 0; r < R; ++r)
-                    v[r] = sm[padi(t + r * T)];
+                    v[r] = sm[pad(t + r * T)];
             }
             Ns *= R;
         }
@@ -303,9 +308,9 @@ __host__ __device__ constexpr int mix_radix(int N1, int N2)
 //   DIF true (decimation in frequency): the two layouts swapped.
 // A forward DIT transform, a pointwise product and an inverse DIF transform
 // therefore chain with no exchange, as the power-of-two RegFFT's do.
-template <int N1, int N2, int DIR, bool DIF, int RAD = mix_radix(N1, N2)>
+template <int N1, int N2, int DIR, bool DIF, int RAD = mix_radix(N1, N2), int PADK = 4>
 struct MixFFT {
-    using Sub = RegFFT<N2, DIR, RAD>;
+    using Sub = RegFFT<N2, DIR, RAD, PADK>;
     static constexpr int R = Sub::R;
     static constexpr int T = Sub::T;
     static constexpr int V = N1 * R;
@@ -381,15 +386,23 @@ struct MixFFT {
 };
 
 // The register FFT of length N (a power of two, or N1 * 2^k with N1 = 3, 5):
-// RegFFT at radix PRAD, or MixFFT in the DIT (DIF = false) or DIF layout.
-template <bool POW2, int N, int DIR, bool DIF, int PRAD>
+// RegFFT at radix PRAD, or MixFFT in the DIT (DIF = false) or DIF layout;
+// PADK: the exchange padding (RegFFT).
+template <bool POW2, int N, int DIR, bool DIF, int PRAD, int PADK>
 struct FFTSel {
-    using type = RegFFT<N, DIR, PRAD>;
+    using type = RegFFT<N, DIR, PRAD, PADK>;
 };
-template <int N, int DIR, bool DIF, int PRAD>
-struct FFTSel<false, N, DIR, DIF, PRAD> {
-    using type = MixFFT<odd_part(N), N / odd_part(N), DIR, DIF>;
+template <int N, int DIR, bool DIF, int PRAD, int PADK>
+struct FFTSel<false, N, DIR, DIF, PRAD, PADK> {
+    using type = MixFFT<odd_part(N), N / odd_part(N), DIR, DIF,
+                        mix_radix(odd_part(N), N / odd_part(N)), PADK>;
 };
-template <int N, int DIR, bool DIF = false, int PRAD = fft_radix(N)>
-using FFTOf = typename FFTSel<odd_part(N) == 1, N, DIR, DIF, PRAD>::type;
+template <int N, int DIR, bool DIF = false, int PRAD = fft_radix(N), int PADK = 4>
+using FFTOf = typename FFTSel<odd_part(N) == 1, N, DIR, DIF, PRAD, PADK>::type;
 
+// Team size of FFTOf<N, ., ., PRAD> without instantiating it.
+__host__ __device__ constexpr int fft_team(int N, int PRAD)
+{
+    return odd_part(N) == 1 ? N / PRAD
+                            : (N / odd_part(N)) / mix_radix(odd_part(N), N / odd_part(N));
+}

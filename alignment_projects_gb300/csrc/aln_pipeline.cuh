@@ -429,11 +429,46 @@ __host__ __device__ constexpr int rowfft_threads(int T) { return T * 4 > 512 ? 5
 // register FFT's default below.
 __host__ __device__ constexpr int rowfft_radix(int L) { return L >= 128 ? 16 : fft_radix(L); }
 
+// Shared-memory layout of the row kernel.  Each team owns one row's region:
+// the row's staged bytes, then the transform's exchange buffer, then the
+// row's L bins (plain index), reused in that order.  Teams of T <= 8
+// threads share a half-warp with 16 / T - 1 neighbours: region starts are
+// shifted (by under 16 float2) so that the teams of a half-warp sit T bank
+// pairs apart -- their consecutive and odd-strided accesses then fall on
+// distinct banks -- and so that any 16 consecutive regions start on
+// distinct bank pairs (the epilogue reads one bin of 16 rows at a time).
+// The split lengths take the transform in decimation-in-frequency order (a
+// team's threads read consecutive pixel pairs), and teams of <= 8 threads
+// pad the exchange buffer by one slot per 8.  (Modelled on 8-byte
+// half-warp wavefronts: the odd-pitch layout with padding per 16 cost
+// 1.75-4x the conflict-free count on the 160- and 192-point rows.)
+template <int L>
+__host__ __device__ constexpr int rowfft_T() { return fft_team(L, rowfft_radix(L)); }
+template <int L>
+__host__ __device__ constexpr int rowfft_padk() { return rowfft_T<L>() <= 8 ? 3 : 4; }
+
 // The row transform of half-length L: the power-of-two RegFFT at
 // rowfft_radix(L), or for L = 3 * 2^k, 5 * 2^k (CorrPatches grids) the
 // MixFFT split.
 template <int L>
-using RowFFT = FFTOf<L, -1, false, rowfft_radix(L)>;
+using RowFFT = FFTOf<L, -1, true, rowfft_radix(L), rowfft_padk<L>()>;
+
+// float2 per team region: the bins, the exchange buffer and the staged
+// bytes (<= 4L + 38 with the 16-byte alignment) all fit, plus the shift.
+template <int L>
+__host__ __device__ constexpr int rowfft_pitch()
+{
+    constexpr int a = L + 1, b = RowFFT<L>::SMEM, c = (4 * L + 38 + 7) / 8;
+    return (a > b ? (a > c ? a : c) : (b > c ? b : c)) + 15;
+}
+// start of team g's region (float2); a CTA needs G * pitch + 16 float2
+template <int L>
+__host__ __device__ constexpr int rowfft_base(int g)
+{
+    constexpr int T = rowfft_T<L>(), P = rowfft_pitch<L>();
+    const int want = T < 16 ? ((g % (16 / T)) * T + g / (16 / T)) % 16 : g % 16;
+    return g * P + ((want - g * P) % 16 + 16) % 16;
+}
 
 // CTAs per SM the row kernel is compiled for: 5 up to 256-point
 // power-of-two rows (48 registers, no spills), 64 registers per thread for
@@ -441,13 +476,13 @@ using RowFFT = FFTOf<L, -1, false, rowfft_radix(L)>;
 template <int L>
 __host__ __device__ constexpr int rowfft_minb()
 {
-    return odd_part(L) == 1 && L <= 256 ? 5 : 1024 / rowfft_threads(RowFFT<L>::T);
+    return odd_part(L) == 1 && L <= 256 ? 5 : 1024 / rowfft_threads(rowfft_T<L>());
 }
 
-// Each team of T threads (RowFFT<L>::T) transforms one row.  G =
-// blockDim.x / T rows per CTA; smem: G * row_pitch(L) float2 per CTA.
+// Each team of T threads (rowfft_T<L>()) transforms one row.  G =
+// blockDim.x / T rows per CTA.
 template <int L>
-__global__ void __launch_bounds__(rowfft_threads(RowFFT<L>::T), rowfft_minb<L>())
+__global__ void __launch_bounds__(rowfft_threads(rowfft_T<L>()), rowfft_minb<L>())
 k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int *sel)
 {
     using F = RowFFT<L>;
@@ -465,8 +500,7 @@ k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int
     if (y0 >= h)
         return;
     const int y = y0 + team;
-    constexpr int PITCH = row_pitch(L);   // odd: conflict-free transposed reads
-    float2 *sm = smem + team * PITCH;
+    float2 *sm = smem + rowfft_base<L>(team);
     const void *img = p.img[i];
     const long long st = p.stride[i];
     float2 v[V];
@@ -478,7 +512,7 @@ k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int
         const int es = dt == ALN_U8 ? 1 : 2;
         const int mu = (int)p.mu[i];
         // the region's first 16-byte boundary (at most 8 bytes in): the row's
-        // <= 4L + 30 staged bytes end well inside the 8 * PITCH of the region
+        // <= 4L + 30 staged bytes end inside the region (rowfft_pitch)
         unsigned char *sb = (unsigned char *)(((uintptr_t)sm + 15) & ~(uintptr_t)15);
         int off = 0;
         if (y < h) {
@@ -526,7 +560,7 @@ k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < V; ++q)
-        sm[padi(F::out_idx(t, q))] = v[q];
+        sm[F::out_idx(t, q)] = v[q];
     __syncthreads();
     float2 *T_ = p.T[i];
     const int Ts = p.Ts[i];
@@ -538,9 +572,9 @@ k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int
         const int kx = e / G, rr = e - kx * G;
         if (rr >= rows)
             continue;
-        const float2 *Z = smem + rr * PITCH;
-        const float2 A = Z[padi(kx)];
-        const float2 B = Z[padi(kx == 0 ? 0 : L - kx)];
+        const float2 *Z = smem + rowfft_base<L>(rr);
+        const float2 A = Z[kx];
+        const float2 B = Z[kx == 0 ? 0 : L - kx];
         float2 *dst = T_ + y0 + rr;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -864,11 +898,11 @@ __device__ __forceinline__ const PairDev &stage_job(const PairDev *pairs, int j,
 // (team g at base + g * stride), loaded by the whole CTA so that a warp's
 // loads cover whole 8-row segments of Q (G consecutive j per kx); four loads
 // per thread are in flight before their stores.
-template <int L, int T>
+// G: rows per CTA (blockDim.x / T).
+template <int L, int T, int G = (T >= 256 ? T : 256) / T>
 __device__ __forceinline__ void load_lag_rows(float2 *base, int stride,
                                               const float2 *__restrict__ Q, int Wy, int j0)
 {
-    constexpr int G = (T >= 256 ? T : 256) / T;
     constexpr int TOT = (L + 1) * G;
     const int nt = blockDim.x;
     for (int e0 = threadIdx.x; e0 < TOT; e0 += 4 * nt) {
@@ -890,8 +924,18 @@ __device__ __forceinline__ void load_lag_rows(float2 *base, int stride,
     }
 }
 
+// Threads per CTA of k2_lagrow: eight lag rows per CTA for teams smaller
+// than a warp (the split lengths' 8-thread teams would otherwise take 32 rows
+// per CTA, and a 129-row disc window 160 team-rows), at least one whole warp
+// (the row reduction shuffles over full warps), 256 threads for larger teams.
+__host__ __device__ constexpr int lagrow_threads(int T)
+{
+    return T < 32 ? (8 * T < 32 ? 32 : 8 * T) : (T >= 256 ? T : 256);
+}
+
 template <int L>
-__global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
+__global__ void __launch_bounds__(lagrow_threads(FFTOf<L, +1>::T))
+k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
 {
     using F = FFTOf<L, +1>;   // RegFFT, or MixFFT for L = 3 * 2^k, 5 * 2^k
     constexpr int V = F::V, T = F::T;
@@ -914,7 +958,7 @@ __global__ void k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
     float2 *sm = smem + team * PITCH;
     const int Nx = p.Nx, Ny = p.Ny;
     // spectrum bins of the CTA's lag rows
-    load_lag_rows<L, T>(smem, PITCH, p.Q, Wy, j0);
+    load_lag_rows<L, T, lagrow_threads(T) / T>(smem, PITCH, p.Q, Wy, j0);
     __syncthreads();
     float2 v[V];
 #pragma unroll
