@@ -2037,9 +2037,9 @@ static void launch_corrseg(aln_ctx *ctx, int n, int L)
     int G = GMAX;
     while (G > 1 && (long long)((L + 1 + G - 1) / G) * n < 2LL * ctx->sms)
         G /= 2;
-    const size_t sm = (size_t)G * (padded(NS) + 2 * NS) * sizeof(float2);
-    smem_attr(ctx->device, (const void *)k2_corrseg<NS>,
-              (size_t)GMAX * (padded(NS) + 2 * NS) * sizeof(float2));
+    constexpr int per_team = padded(NS) + (corrseg_regs<NS>() ? 0 : 2 * NS);   // float2
+    const size_t sm = (size_t)G * per_team * sizeof(float2);
+    smem_attr(ctx->device, (const void *)k2_corrseg<NS>, (size_t)GMAX * per_team * sizeof(float2));
     LAUNCH(ctx, "k2_corrseg", k2_corrseg<NS>, dim3((L + 1 + G - 1) / G, n), G * T, sm,
            ctx->dpairs, ctx->tw);
 }

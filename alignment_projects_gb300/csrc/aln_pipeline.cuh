@@ -39,15 +39,85 @@ __device__ __forceinline__ void two_sum_acc(float &s, float &e, float x)
 // (zeros without a count rule): skipping its stores changed this walk's
 // code and made it 1.7x slower on the montage strips.  grid (ceil(w/32),
 // 2*npairs), block (32, SAT_WARPS): each CTA owns 32 columns of one image;
-// warp ty owns rows [ty*segh, (ty+1)*segh) and walks them once, storing its
+// warp ty owns the rows of segment ty (sat_seg_start) and walks them once, storing its
 // local column prefix at the needed rows.  The warps' exclusive offsets per
 // column go to segoff[ty][c]; k2_sat2w adds them.  Exact int64 for 8/16-bit
 // pixels, FP64 otherwise.  Also writes the column totals (mean shift).
 #define SAT_WARPS 16
 
+// Row segments of the column walk, balanced by work: a row costs 1, a row
+// the lag window needs (stored) costs 1 + sat_need_cost, and segment g holds
+// the rows whose cost position falls in [g, g + 1) * total / SAT_WARPS.  The
+// needed rows sit at both ends of the image, so for uint8 pixels equal row
+// counts left the first and last warps of a CTA twice as long as the rest,
+// which waited at the CTA barrier (stall "barrier" 8.0 per issue on the
+// montage strips; weight 2: k3_sat 4.19 -> 3.83 ms per step).  Wider pixels
+// sum in 64 bits, so a stored row costs relatively less: weight 2 made the
+// uint16 uneven batch's k3_sat 20 % slower, and they keep equal row counts.
+// k3_sat and k2_sat2w compute the same map.  A segment spans at most
+// 3 h / 16 rows (cost <= 3 h).
+__device__ __forceinline__ int sat_need_cost(const PairDev &p, int i)
+{
+    return p.dt[i] == ALN_U8 ? 2 : 0;
+}
+
+__device__ __forceinline__ int sat_cost(const PairDev &p, int i, int y)
+{
+    const int k = sat_need_cost(p, i);
+    int c = y;
+    const int lo0 = p.need_lo[i][0], hi0 = p.need_hi[i][0];
+    const int lo1 = p.need_lo[i][1], hi1 = p.need_hi[i][1];
+    if (hi0 >= lo0)
+        c += k * min(max(y - lo0, 0), hi0 - lo0 + 1);
+    if (hi1 >= lo1)
+        c += k * min(max(y - lo1, 0), hi1 - lo1 + 1);
+    return c;
+}
+
+// segment of row y (0 <= y < h)
+__device__ __forceinline__ int sat_seg_of(const PairDev &p, int i, int y)
+{
+    const long long total = sat_cost(p, i, p.h[i]);
+    return (int)((long long)sat_cost(p, i, y) * SAT_WARPS / max(total, 1LL));
+}
+
+// first row of segment g (g = SAT_WARPS: h): the least y with
+// cost(y) * SAT_WARPS >= g * total.  need_rows() makes the two needed
+// intervals disjoint and ordered (or the second empty), so cost is linear
+// with slope 1 before, between and after them and 1 + k inside them, and
+// the least y with cost(y) >= C follows piece by piece.  (A binary search
+// here -- some 14 dependent steps per warp -- cost the uneven batch's small
+// images a fifth of their walk.)
+__device__ __forceinline__ int sat_seg_start(const PairDev &p, int i, int g)
+{
+    const int h = p.h[i], k = sat_need_cost(p, i);
+    const long long total = sat_cost(p, i, h);
+    const int C = (int)(((long long)g * total + SAT_WARPS - 1) / SAT_WARPS);
+    int y;
+    if (k == 0) {
+        y = C;
+    } else {
+        const int lo0 = p.need_lo[i][0], lo1 = p.need_lo[i][1];
+        const int len0 = max(0, p.need_hi[i][0] - lo0 + 1);
+        const int len1 = max(0, p.need_hi[i][1] - lo1 + 1);
+        const int k1 = k + 1;
+        if (len0 == 0 || C <= lo0)
+            y = C;   // (len0 == 0: no needed row at all)
+        else if (C <= lo0 + k1 * len0)
+            y = lo0 + (C - lo0 + k) / k1;
+        else if (len1 == 0 || C <= lo1 + k * len0)
+            y = C - k * len0;
+        else if (C <= lo1 + k * len0 + k1 * len1)
+            y = lo1 + (C - lo1 - k * len0 + k) / k1;
+        else
+            y = C - k * (len0 + len1);
+    }
+    return min(max(y, 0), h);
+}
+
 // Accumulator of a warp's segment-local sums: 32-bit for uint8 pixels (a
-// segment is at most 512 rows -- h <= 8192 -- so the sums of v and v^2 stay
-// below 2^26), the table type otherwise.
+// segment is at most 1536 rows -- h <= 8192 -- so the sums of v and v^2 stay
+// below 2^27), the table type otherwise.
 template <typename TA, typename PIX>
 struct SatAcc {
     typedef TA type;
@@ -61,12 +131,11 @@ template <typename TA, typename PIX, bool SQ = true>
 __device__ __forceinline__ void sat_cols(const PairDev &p, int i, TA *shS, TA *shQ, int *shN)
 {
     typedef typename SatAcc<TA, PIX>::type AC;
-    const int w = p.w[i], h = p.h[i];
+    const int w = p.w[i];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int c = blockIdx.x * 32 + tx;
     const bool cok = c < w;
-    const int segh = (h + SAT_WARPS - 1) / SAT_WARPS;
-    const int y0 = min(h, ty * segh), y1 = min(h, y0 + segh);
+    const int y0 = sat_seg_start(p, i, ty), y1 = sat_seg_start(p, i, ty + 1);
     const PIX *img = (const PIX *)p.img[i];
     const long long st = p.stride[i];
     const int lo0 = p.need_lo[i][0], hi0 = p.need_hi[i][0];
@@ -306,7 +375,7 @@ __device__ __forceinline__ void sat2_row_any(const PairDev &p, int i, int slot, 
                                              TA *Q, int lane)
 {
     const int w = p.w[i];
-    const int seg = y / ((p.h[i] + SAT_WARPS - 1) / SAT_WARPS);
+    const int seg = sat_seg_of(p, i, y);
     const TA *__restrict__ oS = (const TA *)p.segS[i] + (long long)seg * w;
     const TA *__restrict__ oQ = (const TA *)p.segQ[i] + (long long)seg * w;
     const int *__restrict__ oN = p.segN[i] + (long long)seg * w;
@@ -363,7 +432,7 @@ __device__ __forceinline__ void sat2_row_counts(const PairDev &p, int i, int slo
 {
     constexpr int K = 8;
     const int w = p.w[i];
-    const int seg = y / ((p.h[i] + SAT_WARPS - 1) / SAT_WARPS);
+    const int seg = sat_seg_of(p, i, y);
     const int *__restrict__ oN = p.segN[i] + (long long)seg * w;
     int *__restrict__ rN = p.satN[i] + (long long)slot * w;
     int cn = 0;
@@ -752,21 +821,34 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
 // correlation on NS points the linear one at e in [0, Wy).  The segments'
 // spectral products are summed (one accumulator per column) and inverted
 // once: 2 nseg + 1 transforms of NS points instead of 3 of Ny.  Each thread
-// keeps its accumulator and parked a-spectrum points in its own shared-memory
-// slots (no exchange).  Output: Q[kx][e], as k2_corrcol; the column
-// transform length the lag kernel normalises by is NS (p.Ny).
+// keeps its accumulator and parked a-spectrum points to itself, in
+// registers or its own shared-memory slots (corrseg_regs; no exchange).
+// Output: Q[kx][e], as k2_corrcol; the column transform length the lag
+// kernel normalises by is NS (p.Ny).
 // Per-thread radix of the segment transforms.  Measured on the montage
-// strips (6 segments of 512 points): radix 8 at 3 CTAs per SM ran 25%
-// faster than radix 16 at 2 (spills, low occupancy); at 1024 and 2048 points
-// radix 16 stays ahead.
+// strips (6 segments of 512 points, accumulator then in shared memory):
+// radix 8 at 3 CTAs per SM ran 25% faster than radix 16 at 2 (spills, low
+// occupancy); at 1024 and 2048 points radix 16 stays ahead.
 template <int NS>
 __host__ __device__ constexpr int corrseg_radix()
 {
     return NS == 512 ? 8 : fft_radix(NS);
 }
 
+// Where a thread keeps its parked a-spectrum points and the column's
+// accumulated product: registers at radix <= 8 (each thread owns the same R
+// points throughout; a third fewer shared-memory wavefronts than parking
+// them in shared memory, 2 CTAs per SM at 128 registers instead of 3 at 80:
+// k2_corrseg<512> 10.18 -> 9.84 ms per montage step), shared memory at
+// radix 16 (32 more points per thread spilled 260-280 bytes).
 template <int NS>
-__global__ void __launch_bounds__(256, corrseg_radix<NS>() >= 16 ? 2 : 3)
+__host__ __device__ constexpr bool corrseg_regs()
+{
+    return corrseg_radix<NS>() <= 8;
+}
+
+template <int NS>
+__global__ void __launch_bounds__(256, 2)
 k2_corrseg(PairDev *pairs, const float2 *__restrict__ tw)
 {
     using FF = RegFFT<NS, -1, corrseg_radix<NS>()>;
@@ -785,8 +867,10 @@ k2_corrseg(PairDev *pairs, const float2 *__restrict__ tw)
     const bool live = kx < L1;
     const int kxc = live ? kx : L1 - 1;   // idle teams compute a copy, store nothing
     float2 *sm = smem + team * FF::SMEM;
-    float2 *park = smem + G * FF::SMEM + team * (2 * NS);
-    float2 *acc = park + NS;
+    constexpr bool REGS = corrseg_regs<NS>();
+    float2 parkr[REGS ? R : 1], accr[REGS ? R : 1];
+    float2 *park = REGS ? nullptr : smem + G * FF::SMEM + team * (2 * NS);
+    float2 *acc = REGS ? nullptr : park + NS;
     const float2 *Ta = p.T[0] + (long long)kxc * p.Ts[0];
     const float2 *Tb = p.T[1] + (long long)kxc * p.Ts[1];
     const int ha = p.h[0], hb = p.h[1];
@@ -803,8 +887,12 @@ k2_corrseg(PairDev *pairs, const float2 *__restrict__ tw)
         }
         FF::run_team(v, sm, t, tw, team);
 #pragma unroll
-        for (int r = 0; r < R; ++r)
-            park[r * T + t] = v[r];
+        for (int r = 0; r < R; ++r) {
+            if constexpr (REGS)
+                parkr[r] = v[r];
+            else
+                park[r * T + t] = v[r];
+        }
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const int j = t + r * T, y = y0 + ylo + j;
@@ -813,14 +901,23 @@ k2_corrseg(PairDev *pairs, const float2 *__restrict__ tw)
         FF::run_team(v, sm, t, tw, team);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            const float2 q = cmulc(v[r], park[r * T + t]);   // X2 * conj(X1)
-            acc[r * T + t] = s == 0 ? q : cadd(acc[r * T + t], q);
+            if constexpr (REGS) {
+                const float2 q = cmulc(v[r], parkr[r]);   // X2 * conj(X1)
+                accr[r] = s == 0 ? q : cadd(accr[r], q);
+            } else {
+                const float2 q = cmulc(v[r], park[r * T + t]);
+                acc[r * T + t] = s == 0 ? q : cadd(acc[r * T + t], q);
+            }
         }
     }
     float2 v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r)
-        v[r] = acc[r * T + t];
+    for (int r = 0; r < R; ++r) {
+        if constexpr (REGS)
+            v[r] = accr[r];
+        else
+            v[r] = acc[r * T + t];
+    }
     FI::run_team(v, sm, t, tw, team);
     if (live) {
         float2 *Q = p.Q + (long long)kx * Wy;
