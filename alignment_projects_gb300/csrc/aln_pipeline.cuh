@@ -995,30 +995,32 @@ __device__ __forceinline__ const PairDev &stage_job(const PairDev *pairs, int j,
 // (team g at base + g * stride), loaded by the whole CTA so that a warp's
 // loads cover whole 8-row segments of Q (G consecutive j per kx); four loads
 // per thread are in flight before their stores.
-// G: rows per CTA (blockDim.x / T).
+// G: rows per CTA (blockDim.x / T).  The copies are asynchronous
+// (cp.async, 8 bytes each, global -> shared without registers), so every
+// element a thread moves is in flight at once; the loads through registers
+// this replaces kept four per thread in flight, and the lag kernels waited on
+// them (long-scoreboard stalls, k2_lagimg 33 % warps active).  The caller's
+// __syncthreads after the call publishes the rows to the CTA.
+__device__ __forceinline__ void cp_async8(void *dst_shared, const void *src_global)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_shared);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src_global) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 template <int L, int T, int G = (T >= 256 ? T : 256) / T>
 __device__ __forceinline__ void load_lag_rows(float2 *base, int stride,
                                               const float2 *__restrict__ Q, int Wy, int j0)
 {
     constexpr int TOT = (L + 1) * G;
-    const int nt = blockDim.x;
-    for (int e0 = threadIdx.x; e0 < TOT; e0 += 4 * nt) {
-        float2 v[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = e0 + q * nt;
-            const int kx = e / G, g = e - kx * G;
-            v[q] = e < TOT ? __ldg(&Q[(long long)kx * Wy + min(j0 + g, Wy - 1)])
-                           : make_float2(0.f, 0.f);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = e0 + q * nt;
-            const int kx = e / G, g = e - kx * G;
-            if (e < TOT)
-                base[g * stride + padi(kx)] = v[q];
-        }
+    for (int e = threadIdx.x; e < TOT; e += blockDim.x) {
+        const int kx = e / G, g = e - kx * G;
+        cp_async8(&base[g * stride + padi(kx)], &Q[(long long)kx * Wy + min(j0 + g, Wy - 1)]);
     }
+    cp_async_wait_all();
 }
 
 // Threads per CTA of k2_lagrow: eight lag rows per CTA for teams smaller
