@@ -50,7 +50,9 @@
 #include <algorithm>
 #include <map>
 #include <set>
+#include <atomic>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -1041,6 +1043,7 @@ struct aln_ctx {
     int tune_on;                                 // measured segment choices (aln_tune.cuh)
     int split_on;                                // CorrPatches rows of 3 * 2^k, 5 * 2^k points
     int tuning;                                  // inside a timing run
+    int tune_defer;                              // parallel planning: unknown classes wait
     long long tune_classes;                      // classes this context measured
 };
 
@@ -1120,12 +1123,20 @@ static void prof_collect(aln_ctx *c)
 // query, the allocation-free entry point): one message per host thread
 static thread_local char g_create_err[512];
 
+// (a context's message under a lock: batch planning runs on several host
+// threads)
+static std::mutex g_err_lock;
 static int set_err(aln_ctx *c, int code, const char *fmt, ...)
 {
     char *buf = c ? c->err : g_create_err;
     va_list ap;
     va_start(ap, fmt);
-    vsnprintf(buf, 512, fmt, ap);
+    if (c) {
+        std::lock_guard<std::mutex> g(g_err_lock);
+        vsnprintf(buf, 512, fmt, ap);
+    } else {
+        vsnprintf(buf, 512, fmt, ap);
+    }
     va_end(ap);
     return code;
 }
@@ -1215,6 +1226,7 @@ extern "C" int aln_ctx_create(int device, aln_ctx **out)
     }
     ctx->split_on = 1;
     ctx->tuning = 0;
+    ctx->tune_defer = 0;
     ctx->tune_classes = 0;
     ctx->pts_buf[0] = ctx->pts_buf[1] = nullptr;
     ctx->pts_cap[0] = ctx->pts_cap[1] = 0;
@@ -1437,6 +1449,7 @@ struct PairPlan {
     int key_ns;                  // spectrum-cache key of image b (0: none)
     unsigned long long key;
     char *staged[2];             // device staging of host inputs (set per window)
+    int tune_deferred;           // planned while its autotuner class was unknown
 };
 
 // Cache entry bookkeeping: the map and the (tick, key) LRU index together.
@@ -1787,6 +1800,10 @@ static int plan_pair(aln_ctx *ctx, const aln_pair &P, PairPlan &pl, bool allow_t
                     t = tuned_segment(ctx, P, d, Wy, cand);
                 else if (!ctx)
                     t = recorded_segment(d, Wy);
+                if (t == -2) {   // class not measured yet; planned again after
+                    pl.tune_deferred = 1;
+                    t = -1;
+                }
                 if (t == 0) {
                     bns = 0;
                 } else if (t > 0 && std::find(valid.begin(), valid.end(), t) != valid.end()) {
@@ -2234,7 +2251,9 @@ static int launch_chunk(aln_ctx *ctx, std::vector<PairPlan *> &chunk, const Chun
                                cudaMemcpyHostToDevice, st));
     if (cl.sw > 0)
         LAUNCH(ctx, "k_transpose", k_transpose,
-               dim3(cl.t8 ? (cl.sw + 127) / 128 : (cl.sw + 31) / 32, (cl.sh + 31) / 32, 2 * n),
+               dim3(cl.t8 ? (cl.sw + 128 * TR_TILES - 1) / (128 * TR_TILES)
+                          : (cl.sw + 32 * TR_TILES - 1) / (32 * TR_TILES),
+                    (cl.sh + 31) / 32, 2 * n),
                dim3(32, 8), 0, ctx->dpairs);
     const int mode = cl.mode;
     if (mode != JOB_P2I) {
@@ -2489,6 +2508,16 @@ struct JobKey {
     unsigned long long key;
 };
 
+// Host threads for planning a batch of n pairs: one per 256 pairs, at most
+// 16 and the machine's hardware threads; 1 below 512 pairs.
+static int plan_threads(int n)
+{
+    if (n < 512)
+        return 1;
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    return std::max(1, std::min({16, hw, n / 256}));
+}
+
 static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const ImgSpec *specs,
                       aln_result *out, const JobKey *keys = nullptr)
 {
@@ -2496,15 +2525,54 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
         return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
     CK(cudaSetDevice(ctx->device));
     std::vector<PairPlan> plans(npairs);
-    for (int k = 0; k < npairs; ++k) {
+    auto plan_one = [&](int k) {
         plans[k].src = &pairs[k];
         plans[k].index = k;
         plans[k].key_ns = keys ? keys[k].ns : 0;
         plans[k].key = keys ? keys[k].key : pairs[k].b_key;
+        plans[k].tune_deferred = 0;
         const ImgSpec *sp = (specs && specs[k].kind != 0) ? &specs[k] : nullptr;
-        if (int rc = plan_pair(ctx, pairs[k], plans[k], sp == nullptr, sp,
-                               sp == nullptr && plans[k].key == 0, sp == nullptr))
+        return plan_pair(ctx, pairs[k], plans[k], sp == nullptr, sp,
+                         sp == nullptr && plans[k].key == 0, sp == nullptr);
+    };
+    // Plans are independent per pair, and a large batch's planning (a few
+    // microseconds per pair, while the device waits) runs on host threads.
+    // A pair of an autotuner class not measured yet is planned again on this
+    // thread afterwards: measuring runs timing batches on this context.
+    const int nthr = plan_threads(npairs);
+    if (nthr > 1) {
+        ctx->tune_defer = 1;
+        std::atomic<int> next(0), first_err(0);
+        auto work = [&]() {
+            for (;;) {
+                const int k0 = next.fetch_add(64);
+                if (k0 >= npairs || first_err.load(std::memory_order_relaxed))
+                    return;
+                for (int k = k0; k < std::min(npairs, k0 + 64); ++k)
+                    if (int rc = plan_one(k)) {
+                        int z = 0;
+                        first_err.compare_exchange_strong(z, rc);
+                        return;
+                    }
+            }
+        };
+        std::vector<std::thread> pool;
+        for (int q = 1; q < nthr; ++q)
+            pool.emplace_back(work);
+        work();
+        for (auto &th : pool)
+            th.join();
+        ctx->tune_defer = 0;
+        if (int rc = first_err.load())
             return rc;
+        for (int k = 0; k < npairs; ++k)
+            if (plans[k].tune_deferred)
+                if (int rc = plan_one(k))
+                    return rc;
+    } else {
+        for (int k = 0; k < npairs; ++k)
+            if (int rc = plan_one(k))
+                return rc;
     }
     // Windows: runs of consecutive jobs (submission order) whose host inputs
     // fit one staging buffer.  A window's host images are copied on the copy
@@ -2516,7 +2584,9 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
     // window.  Host batches of at least 512 MB are cut into about four
     // windows (at least 128 MB each), so only the first window's copy is not
     // hidden behind computation: at the host link's ~210 GB/s a window's
-    // copy takes half the time of its kernels for the montage strips.
+    // copy takes half the time of its kernels for the montage strips.  (Eight
+    // and sixteen windows measured slower end to end on the montage batch:
+    // 96.9k and 85.9k pairs/s against 98.8k with four.)
     size_t host_bytes = 0;
     for (const auto &pl : plans)
         if (pl.d.status == 0)

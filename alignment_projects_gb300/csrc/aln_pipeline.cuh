@@ -269,10 +269,14 @@ __device__ __forceinline__ void store_bits(char *p, int es, long long idx, unsig
     }
 }
 
-// grid (ceil(max caller w / 32), ceil(max caller h / 32), 2*npairs), block (32, 8):
-// frame pixel (xf, yf) = caller pixel (yf, xf).  uint8 images use 32 x 128
-// tiles (blockIdx.x counts 128 columns; a launch whose transposed images are
-// all uint8 has grid x = ceil(max caller w / 128)).
+// grid (ceil(max caller w / (32 TR_TILES)), ceil(max caller h / 32),
+// 2*npairs), block (32, 8): frame pixel (xf, yf) = caller pixel (yf, xf).
+// uint8 images use 32 x 128 tiles (blockIdx.x then counts 128 TR_TILES
+// columns; a launch whose transposed images are all uint8 has grid x =
+// ceil(max caller w / (128 TR_TILES))).  Each CTA moves TR_TILES tiles side
+// by side: a 4 KB tile per CTA left the montage strips' transposes bound by
+// block scheduling (hundreds of thousands of CTAs per step).
+#define TR_TILES 4
 __global__ void k_transpose(PairDev *pairs)
 {
     __shared__ unsigned long long tile[32][33];
@@ -281,71 +285,80 @@ __global__ void k_transpose(PairDev *pairs)
     if (p.status != 0 || !p.transposed)
         return;
     const int sw = p.h[i], sh = p.w[i];   // caller's width and height
-    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    const int y0 = blockIdx.y * 32;
     if (y0 >= sh)
         return;
     const int es = p.dt[i] == ALN_U8 ? 1 : p.dt[i] == ALN_U16 ? 2 : p.dt[i] == ALN_F32 ? 4 : 8;
     const char *src = (const char *)p.src_img[i];
     const long long sst = p.src_stride[i];
     if (es == 1) {
-        // uint8: a 32 x 128 tile per CTA (blockIdx.x counts 128-column tiles)
+        // uint8: 32 x 128 tiles
         unsigned char(*t8)[132] = (unsigned char(*)[132])tile;
-        const int xb0 = blockIdx.x * 128;
-        if (xb0 >= sw)
-            return;
-        // 4-byte loads where the caller's rows allow them (4-byte aligned
-        // base and stride, the whole word inside the row)
-        const bool vec = (((uintptr_t)src | (uintptr_t)sst) & 3) == 0;
-        for (int rr = threadIdx.y; rr < 32; rr += 8) {
-            const int yy = y0 + rr;
-            const int xq = xb0 + 4 * threadIdx.x;
-            if (vec && yy < sh && xq + 3 < sw) {
-                *(unsigned int *)&t8[rr][4 * threadIdx.x] =
-                    *(const unsigned int *)(src + yy * sst + xq);
-                continue;
-            }
-            for (int m = 0; m < 4; ++m) {
-                const int x = xq + m;
-                t8[rr][4 * threadIdx.x + m] =
-                    (yy < sh && x < sw) ? (unsigned char)src[yy * sst + x] : 0;
-            }
-        }
-        __syncthreads();
         unsigned char *dst = (unsigned char *)p.img[i];
         const long long dstr = p.stride[i];
         const int tid = threadIdx.y * 32 + threadIdx.x;
-        for (int e = tid; e < 128 * 8; e += 256) {
-            const int j = e >> 3, wq = e & 7;
-            const int xs = xb0 + j, ys = y0 + 4 * wq;
-            if (xs >= sw || ys >= sh)
-                continue;
-            if (ys + 3 < sh && (dstr & 3) == 0) {
-                const unsigned int word = (unsigned int)t8[4 * wq][j] |
-                                          ((unsigned int)t8[4 * wq + 1][j] << 8) |
-                                          ((unsigned int)t8[4 * wq + 2][j] << 16) |
-                                          ((unsigned int)t8[4 * wq + 3][j] << 24);
-                *(unsigned int *)(dst + xs * dstr + ys) = word;
-            } else {
-                for (int m = 0; m < 4 && ys + m < sh; ++m)
-                    dst[xs * dstr + ys + m] = t8[4 * wq + m][j];
+        // 4-byte loads where the caller's rows allow them (4-byte aligned
+        // base and stride, the whole word inside the row)
+        const bool vec = (((uintptr_t)src | (uintptr_t)sst) & 3) == 0;
+        for (int kt = 0; kt < TR_TILES; ++kt) {
+            const int xb0 = (blockIdx.x * TR_TILES + kt) * 128;
+            if (xb0 >= sw)
+                break;   // uniform over the CTA
+            if (kt > 0)
+                __syncthreads();   // the previous tile's reads are done
+            for (int rr = threadIdx.y; rr < 32; rr += 8) {
+                const int yy = y0 + rr;
+                const int xq = xb0 + 4 * threadIdx.x;
+                if (vec && yy < sh && xq + 3 < sw) {
+                    *(unsigned int *)&t8[rr][4 * threadIdx.x] =
+                        *(const unsigned int *)(src + yy * sst + xq);
+                    continue;
+                }
+                for (int m = 0; m < 4; ++m) {
+                    const int x = xq + m;
+                    t8[rr][4 * threadIdx.x + m] =
+                        (yy < sh && x < sw) ? (unsigned char)src[yy * sst + x] : 0;
+                }
+            }
+            __syncthreads();
+            for (int e = tid; e < 128 * 8; e += 256) {
+                const int j = e >> 3, wq = e & 7;
+                const int xs = xb0 + j, ys = y0 + 4 * wq;
+                if (xs >= sw || ys >= sh)
+                    continue;
+                if (ys + 3 < sh && (dstr & 3) == 0) {
+                    const unsigned int word = (unsigned int)t8[4 * wq][j] |
+                                              ((unsigned int)t8[4 * wq + 1][j] << 8) |
+                                              ((unsigned int)t8[4 * wq + 2][j] << 16) |
+                                              ((unsigned int)t8[4 * wq + 3][j] << 24);
+                    *(unsigned int *)(dst + xs * dstr + ys) = word;
+                } else {
+                    for (int m = 0; m < 4 && ys + m < sh; ++m)
+                        dst[xs * dstr + ys + m] = t8[4 * wq + m][j];
+                }
             }
         }
         return;
     }
-    if (x0 >= sw)
-        return;
-    for (int yy = threadIdx.y; yy < 32; yy += 8) {
-        const int y = y0 + yy, x = x0 + threadIdx.x;
-        if (y < sh && x < sw)
-            tile[yy][threadIdx.x] = load_bits(src, es, y * sst + x);
-    }
-    __syncthreads();
     char *dst = (char *)p.img[i];
     const long long dstr = p.stride[i];
-    for (int xx = threadIdx.y; xx < 32; xx += 8) {
-        const int x = x0 + xx, y = y0 + threadIdx.x;
-        if (x < sw && y < sh)
-            store_bits(dst, es, x * dstr + y, tile[threadIdx.x][xx]);
+    for (int kt = 0; kt < TR_TILES; ++kt) {
+        const int x0 = (blockIdx.x * TR_TILES + kt) * 32;
+        if (x0 >= sw)
+            break;   // uniform over the CTA
+        if (kt > 0)
+            __syncthreads();
+        for (int yy = threadIdx.y; yy < 32; yy += 8) {
+            const int y = y0 + yy, x = x0 + threadIdx.x;
+            if (y < sh && x < sw)
+                tile[yy][threadIdx.x] = load_bits(src, es, y * sst + x);
+        }
+        __syncthreads();
+        for (int xx = threadIdx.y; xx < 32; xx += 8) {
+            const int x = x0 + xx, y = y0 + threadIdx.x;
+            if (x < sw && y < sh)
+                store_bits(dst, es, x * dstr + y, tile[threadIdx.x][xx]);
+        }
     }
 }
 

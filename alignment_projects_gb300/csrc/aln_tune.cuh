@@ -144,7 +144,8 @@ static int tune_images(aln_ctx *ctx, const aln_pair &P, void **buf, aln_pair &S)
 // The class's measured choice for a pair planned as d (caller-frame pair P),
 // whose valid segment lengths are cand (the cost model's pick first, 0 =
 // unsegmented).  Returns the choice, or -1 for the cost model's plan (the
-// class entry says so, or the class cannot be measured).
+// class entry says so, or the class cannot be measured), or -2 for a class
+// not measured yet while the context plans on several threads.
 static int tuned_segment(aln_ctx *ctx, const aln_pair &P, const PairDev &d, int Wy,
                          const std::vector<int> &cand)
 {
@@ -158,6 +159,8 @@ static int tuned_segment(aln_ctx *ctx, const aln_pair &P, const PairDev &d, int 
     auto it = g_tune.find(key);
     if (it != g_tune.end())
         return it->second;
+    if (ctx->tune_defer)
+        return -2;   // parallel planning: the caller plans this pair again
     // time each choice on a batch of copies of a synthetic pair like P
     void *buf = nullptr;
     aln_pair S;

@@ -77,3 +77,20 @@ def test_fixed_and_tuned_plans_agree():
     for f, t in zip(fixed, tuned):
         assert (f["peak_x"], f["peak_y"]) == (t["peak_x"], t["peak_y"])
         assert abs(f["r"] - t["r"]) <= 1e-4
+
+
+def test_parallel_planning_equals_single_pairs():
+    """A batch large enough to plan on host threads (640 pairs, above the
+    512-pair threshold) gives each pair the numbers it gets alone, bit for
+    bit; classes the autotuner had not measured are planned again on the
+    calling thread after the parallel pass (measuring runs GPU batches)."""
+    import alignment_projects_gb300 as aln
+    jobs, _ = _pairs(range(2000, 2640), 64, 400)
+    c = aln.Context(0)
+    c.set_tuning(True)
+    got = c.corr_patches_batch(jobs)
+    for k in range(0, len(jobs), 37):
+        j = jobs[k]
+        alone = c.corr_patches(j["a"], j["b"], j["ox"], j["oy"], j["radius"], j["legal"])
+        assert alone == got[k], (k, alone, got[k])
+    c.close()
