@@ -51,6 +51,7 @@
 #include <map>
 #include <set>
 #include <atomic>
+#include <chrono>
 #include <mutex>
 #include <thread>
 #include <string>
@@ -1029,7 +1030,9 @@ struct aln_ctx {
     size_t spec_bytes, spec_cap;                 // all buffers held / limit
     unsigned long long spec_tick;
     long long spec_hits, spec_fills, spec_evictions;
+    long long host_plan_us, host_prep_us;        // batch host time: planning, chunk preparation
     int *dsel;                                   // cache-fill job lists (whole batch)
+    int *hsel;                                   // their page-locked host copy
     size_t dsel_cap;
     int *dsel_cur;                               // the current chunk's list
     unsigned long long sweep_serial;             // key namespace of each sweep call
@@ -1212,7 +1215,9 @@ extern "C" int aln_ctx_create(int device, aln_ctx **out)
     ctx->spec_cap = (size_t)8 << 30;
     ctx->spec_tick = 0;
     ctx->spec_hits = ctx->spec_fills = ctx->spec_evictions = 0;
+    ctx->host_plan_us = ctx->host_prep_us = 0;
     ctx->dsel = nullptr;
+    ctx->hsel = nullptr;
     ctx->dsel_cap = 0;
     ctx->dsel_cur = nullptr;
     ctx->sweep_serial = 0;
@@ -1298,6 +1303,8 @@ extern "C" void aln_ctx_destroy(aln_ctx *ctx)
     for (auto &f : ctx->spec_free)
         cudaFree(f.second);
     cudaFree(ctx->dsel);
+    if (ctx->hsel)
+        cudaFreeHost(ctx->hsel);
     for (int q = 0; q < 2; ++q)
         if (ctx->pts_buf[q])
             cudaFree(ctx->pts_buf[q]);
@@ -2524,6 +2531,7 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
     if (!ctx || npairs < 0 || (npairs && (!pairs || !out)))
         return ctx ? set_err(ctx, ALN_ERR_ARG, "bad arguments") : ALN_ERR_ARG;
     CK(cudaSetDevice(ctx->device));
+    const auto t_plan0 = std::chrono::steady_clock::now();
     std::vector<PairPlan> plans(npairs);
     auto plan_one = [&](int k) {
         plans[k].src = &pairs[k];
@@ -2574,6 +2582,10 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
             if (int rc = plan_one(k))
                 return rc;
     }
+    if (!ctx->tuning)
+        ctx->host_plan_us += std::chrono::duration_cast<std::chrono::microseconds>(
+                                 std::chrono::steady_clock::now() - t_plan0)
+                                 .count();
     // Windows: runs of consecutive jobs (submission order) whose host inputs
     // fit one staging buffer.  A window's host images are copied on the copy
     // stream -- adjacent host images with one transfer, by the SMs when they
@@ -2658,42 +2670,33 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
         return rc;
     if (int rc = ensure_hres(ctx, (size_t)std::max(npairs, 1)))
         return rc;
-    // host side of every chunk first: staging addresses, workspaces, cache
-    // keys, one job table and one fill list for the whole batch
+    // Staging addresses of every window first; then each chunk's host side
+    // (workspaces, cache keys, its job-table slice) just before its launch,
+    // so the host prepares chunk c + 1 while the device runs chunk c.  The
+    // fill list holds at most one entry per job: sized for the whole batch.
+    for (size_t w = 0; w < windows.size(); ++w)
+        assign_staging(windows[w], ctx->ws + (w & 1) * max_stage);
+    cudaStream_t st = ctx->stream;
+    if ((size_t)npairs > ctx->dsel_cap) {
+        CK(cudaStreamSynchronize(st));
+        cudaFree(ctx->dsel);
+        if (ctx->hsel)
+            cudaFreeHost(ctx->hsel);
+        ctx->dsel = nullptr;
+        ctx->hsel = nullptr;
+        ctx->dsel_cap = 0;
+        const size_t cap = std::max<size_t>((size_t)npairs, 4096);
+        CK(cudaMalloc(&ctx->dsel, cap * sizeof(int)));
+        CK(cudaHostAlloc((void **)&ctx->hsel, cap * sizeof(int), cudaHostAllocDefault));
+        ctx->dsel_cap = cap;
+    }
     std::vector<std::vector<PairPlan *> *> order;
     std::vector<ChunkLaunch> cls;
     std::vector<int> fills;
     int off = 0;
-    for (size_t w = 0; w < windows.size(); ++w) {
-        assign_staging(windows[w], ctx->ws + (w & 1) * max_stage);
-        for (auto &chunk : wchunks[w]) {
-            ChunkLaunch cl;
-            prep_chunk(ctx, chunk, off, ctx->ws + nstage * max_stage, ctx->htab + off, fills,
-                       cl);
-            cls.push_back(cl);
-            order.push_back(&chunk);
-            off += cl.n;
-        }
-    }
-    if (fills.size() > ctx->dsel_cap) {
-        CK(cudaStreamSynchronize(ctx->stream));
-        cudaFree(ctx->dsel);
-        ctx->dsel = nullptr;
-        ctx->dsel_cap = 0;
-        const size_t cap = std::max<size_t>(fills.size(), 4096);
-        CK(cudaMalloc(&ctx->dsel, cap * sizeof(int)));
-        ctx->dsel_cap = cap;
-    }
-    cudaStream_t st = ctx->stream;
-    if (off > 0)
-        CK(cudaMemcpyAsync(ctx->dpairs_base, ctx->htab, (size_t)off * sizeof(PairDev),
-                           cudaMemcpyHostToDevice, st));
-    if (!fills.empty())
-        CK(cudaMemcpyAsync(ctx->dsel, fills.data(), fills.size() * sizeof(int),
-                           cudaMemcpyHostToDevice, st));
+    long long prep_us = 0;
     // two-stage pipeline: window w+1's copies are queued before window w's
     // kernels, on the copy stream; the kernels wait for their window only
-    size_t ci = 0;
     for (size_t w = 0; w <= windows.size(); ++w) {
         if (w < windows.size()) {
             if (int rc = stage_window(ctx, windows[w], (int)(w & 1))) {
@@ -2707,8 +2710,26 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
         const size_t cw = w - 1;   // the window computed now
         const int wp = (int)(cw & 1);
         CK(cudaStreamWaitEvent(st, ctx->ev_copy[wp], 0));
-        for (size_t q = 0; q < wchunks[cw].size(); ++q, ++ci) {
-            if (int rc = launch_chunk(ctx, *order[ci], cls[ci])) {
+        for (auto &chunk : wchunks[cw]) {
+            const auto t0 = std::chrono::steady_clock::now();
+            ChunkLaunch cl;
+            prep_chunk(ctx, chunk, off, ctx->ws + nstage * max_stage, ctx->htab + off, fills,
+                       cl);
+            prep_us += std::chrono::duration_cast<std::chrono::microseconds>(
+                           std::chrono::steady_clock::now() - t0)
+                           .count();
+            CK(cudaMemcpyAsync(ctx->dpairs_base + off, ctx->htab + off,
+                               (size_t)cl.n * sizeof(PairDev), cudaMemcpyHostToDevice, st));
+            if (cl.nfill) {   // through page-locked memory: no stream sync on the host
+                memcpy(ctx->hsel + cl.fill_off, fills.data() + cl.fill_off,
+                       (size_t)cl.nfill * sizeof(int));
+                CK(cudaMemcpyAsync(ctx->dsel + cl.fill_off, ctx->hsel + cl.fill_off,
+                                   (size_t)cl.nfill * sizeof(int), cudaMemcpyHostToDevice, st));
+            }
+            cls.push_back(cl);
+            order.push_back(&chunk);
+            off += cl.n;
+            if (int rc = launch_chunk(ctx, chunk, cl)) {
                 cudaStreamSynchronize(ctx->cstream);
                 cudaStreamSynchronize(st);
                 return rc;
@@ -2716,6 +2737,8 @@ static int batch_impl(aln_ctx *ctx, int npairs, const aln_pair *pairs, const Img
         }
         CK(cudaEventRecord(ctx->ev_wdone[wp], st));
     }
+    if (!ctx->tuning)
+        ctx->host_prep_us += prep_us;
     if (off > 0) {
         CK(cudaMemcpyAsync(ctx->hres, ctx->dres_base, (size_t)off * sizeof(ResultDev),
                            cudaMemcpyDeviceToHost, st));
@@ -3143,6 +3166,7 @@ extern "C" void aln_ctx_profile_reset(aln_ctx *ctx)
     ctx->launches = 0;
     ctx->h2d_bytes = ctx->d2h_bytes = 0;
     ctx->spec_hits = ctx->spec_fills = ctx->spec_evictions = 0;
+    ctx->host_plan_us = ctx->host_prep_us = 0;
     ctx->chunks = 0;
     ctx->h2d_copies = 0;
 }
@@ -3187,6 +3211,8 @@ extern "C" long long aln_ctx_counter(aln_ctx *ctx, int which)
     case 7: return ctx->h2d_copies;
     case 8: return ctx->tune_classes;
     case 9: return ctx->spec_evictions;
+    case 10: return ctx->host_plan_us;
+    case 11: return ctx->host_prep_us;
     default: return -1;
     }
 }

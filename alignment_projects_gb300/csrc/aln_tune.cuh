@@ -154,11 +154,20 @@ static int tuned_segment(aln_ctx *ctx, const aln_pair &P, const PairDev &d, int 
         return -1;
     const TuneKey key{dev, d.Nx / 2, d.Ny, tune_pow2(Wy), tune_pow2(d.h[0]),
                       (int)dtype_size(d.dt[0])};
+    // Entries never change once made, so each planning thread keeps the
+    // ones it has seen and takes the lock only for a class new to it (with
+    // 16 threads planning, one lock per pair cost the uneven batch 3 %).
+    static thread_local std::map<TuneKey, int> seen;
+    auto sit = seen.find(key);
+    if (sit != seen.end())
+        return sit->second;
     std::lock_guard<std::mutex> g(g_tune_lock);
     tune_load(dev);
     auto it = g_tune.find(key);
-    if (it != g_tune.end())
+    if (it != g_tune.end()) {
+        seen[key] = it->second;
         return it->second;
+    }
     if (ctx->tune_defer)
         return -2;   // parallel planning: the caller plans this pair again
     // time each choice on a batch of copies of a synthetic pair like P
@@ -220,6 +229,7 @@ static int tuned_segment(aln_ctx *ctx, const aln_pair &P, const PairDev &d, int 
         return -1;
     const int choice = ms[best] > 0.90f * ms[0] ? -1 : cand[best];
     g_tune[key] = choice;
+    seen[key] = choice;
     if (FILE *f = fopen(g_tune_path[dev].c_str(), "a")) {
         fprintf(f, "%d %d %d %d %d %d ", key.L, key.nyf, key.wyb, key.h0b, key.es, choice);
         for (size_t c = 0; c < cand.size(); ++c)

@@ -403,7 +403,9 @@ class Context:
                 "chunks": self._L.aln_ctx_counter(self.h, 6),
                 "h2d_copies": self._L.aln_ctx_counter(self.h, 7),
                 "tune_classes": self._L.aln_ctx_counter(self.h, 8),
-                "spec_evictions": self._L.aln_ctx_counter(self.h, 9)}
+                "spec_evictions": self._L.aln_ctx_counter(self.h, 9),
+                "host_plan_us": self._L.aln_ctx_counter(self.h, 10),
+                "host_prep_us": self._L.aln_ctx_counter(self.h, 11)}
 
     def set_segmenting(self, ns: int):
         """CorrPatches column segments: 0 the class's measured plan (or the

@@ -444,7 +444,8 @@ def run_gpu(args):
     ms_dev = e0.elapsed_time(e1)
     clocks = clk.stop()
     prof = ctx.profile()
-    launches = ctx.counters()["launches"]
+    cdev = ctx.counters()
+    launches = cdev["launches"]
     ctx.set_profiling(False)
     ms_dev = max_over_ranks(dist, ms_dev, dev)
     value = ws * n * args.steps / (ms_dev / 1000.0)
@@ -658,6 +659,11 @@ def run_gpu(args):
             "kernels_ms": {k: round(v[1], 3) for k, v in sorted(ours.items())},
             "kernels_ms_e2e": {k: round(v[1], 3) for k, v in sorted(prof_e2e.items())},
             "e2e_host_wall_ms_per_step": 1000.0 * t_host / args.steps,
+            "host_ms_per_step": {"plan": cdev["host_plan_us"] / 1000.0 / args.steps,
+                                 "chunk_prep": cdev["host_prep_us"] / 1000.0 / args.steps,
+                                 "note": "device-resident timed region; planning precedes the "
+                                         "first launch, chunk preparation overlaps the previous "
+                                         "chunk's kernels"},
             "chunks_per_step": cnt["chunks"] / args.steps,
             "h2d_copies_per_step": cnt["h2d_copies"] / args.steps,
             "plain": {"pairs_per_s": plain_pps, "p50_ms": lat_ms[len(lat_ms) // 2],

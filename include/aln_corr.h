@@ -139,7 +139,9 @@ int aln_ctx_profile(aln_ctx *ctx, int cap, const char **names, long long *launch
  * the last aln_ctx_profile_reset), 5 = device bytes the cache holds,
  * 6 = batch chunks run, 7 = host-to-device staging transfers issued (both
  * since the last reset), 8 = pair classes this context timed for the
- * autotuner, 9 = spectrum-cache entries evicted (since the last reset). */
+ * autotuner, 9 = spectrum-cache entries evicted, 10 = host microseconds
+ * spent planning batches, 11 = host microseconds preparing their chunks
+ * (9-11 since the last reset). */
 long long aln_ctx_counter(aln_ctx *ctx, int which);
 
 /* Autotuner (no reference counterpart; replaces the reference's fixed
