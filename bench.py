@@ -699,7 +699,7 @@ def run_gpu(args):
 # ---------------------------------------------------------------------------
 
 def c1_plain(args, local):
-    """BASELINE config 1: 512^2 uint8 pairs (FFT 1024^2, full lag window,
+    """The plain-pair workload: 512^2 uint8 pairs (FFT 1024^2, full lag window,
     olap >= 32 x 32) through the plain one-pair-per-call path (host and
     device inputs) and as one batch; parity and the CPU port on the host
     cores for the same pairs."""
