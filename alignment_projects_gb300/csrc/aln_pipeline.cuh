@@ -644,32 +644,36 @@ k2_rowfft(PairDev *pairs, const float2 *__restrict__ tw, int only_img, const int
     for (int q = 0; q < V; ++q)
         sm[F::out_idx(t, q)] = v[q];
     __syncthreads();
-    float2 *T_ = p.T[i];
-    const int Ts = p.Ts[i];
-    const int rows = min(G, h - y0);
     // bins for (kx, row) with row fastest: coalesced [kx][y] stores.  Bin kx
     // needs Z[kx] and conj(Z[L - kx]) (indices mod L), bin L - kx the same
-    // two values swapped: one item makes both (kx = 0..L/2; L is even).
-    for (int e = threadIdx.x; e < (L / 2 + 1) * G; e += blockDim.x) {
-        const int kx = e / G, rr = e - kx * G;
-        if (rr >= rows)
-            continue;
-        const float2 *Z = smem + rowfft_base<L>(rr);
+    // two values swapped: one item makes both (kx = 0..L/2; L is even).  The
+    // CTA has G * T threads, so thread x always takes row x % G and bins
+    // kx = x / G + m T: its row's region and store pointers are set once.
+    constexpr int THR = G * T;
+    const int rr = threadIdx.x % G;
+    if (rr >= min(G, h - y0))
+        return;
+    const float2 *Z = smem + rowfft_base<L>(rr);
+    const long long Ts = p.Ts[i];
+    const int kx0 = threadIdx.x / G;
+    float2 *lo = p.T[i] + y0 + rr + kx0 * Ts;          // bin kx
+    float2 *hi = p.T[i] + y0 + rr + (L - kx0) * Ts;    // bin L - kx
+    const float2 *twk = tw + tw_base(2 * L) + 2 * L;   // exp(-2 pi i k / 2L) at twk[k]
+    for (int kx = kx0; kx <= L / 2; kx += THR / G, lo += (THR / G) * Ts, hi -= (THR / G) * Ts) {
         const float2 A = Z[kx];
         const float2 B = Z[kx == 0 ? 0 : L - kx];
-        float2 *dst = T_ + y0 + rr;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int k = h ? L - kx : kx;
-            if (h && k == kx)
+        for (int hh = 0; hh < 2; ++hh) {
+            const int k = hh ? L - kx : kx;
+            if (hh && k == kx)
                 break;   // kx = L/2: one bin
-            const float2 a = h ? B : A;
-            const float2 b = cconj(h ? A : B);
+            const float2 a = hh ? B : A;
+            const float2 b = cconj(hh ? A : B);
             const float2 ev = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
             const float2 dd = make_float2(0.5f * (a.x - b.x), 0.5f * (a.y - b.y));
             const float2 o = make_float2(dd.y, -dd.x);
-            const float2 wv = twn<2 * L, -1>(tw, k);
-            dst[(long long)k * Ts] = cadd(ev, cmul(o, wv));
+            const float2 wv = __ldg(&twk[k]);
+            *(hh ? hi : lo) = cadd(ev, cmul(o, wv));
         }
     }
 }
