@@ -622,8 +622,10 @@ int aln_corr_vectors(aln_ctx *ctx, const double *a, const double *b, int n, doub
  *
  * The first call on each device performs a one-time set-up there (looks up
  * the scratch array's device address, fills the FFT twiddle table in it,
- * enables the large shared-memory kernel configurations); make that first
- * call before any stream capture.  All calls on a device share the one
+ * enables the large shared-memory kernel configurations).  Every call
+ * synchronises its stream and copies through host memory, so no call, the
+ * first or any later one, may be made while a stream of the device is being
+ * captured into a CUDA graph.  All calls on a device share the one
  * scratch array and leave their data in it: calls that overlap on the GPU
  * (several host threads, or several streams) race and must be serialised by
  * the caller.  Every buffer is fully written before it is read, so no
