@@ -16,7 +16,7 @@ SOURCES = ["aln_corr.cu"]
 HEADERS = ["aln_fft.cuh", "aln_fft_reg.cuh", "aln_corr_kernels.cuh", "aln_pipeline.cuh",
            "aln_sweep.cuh", "aln_server.cuh", "aln_mesh.cuh", "aln_approx.cuh",
            "aln_tune.cuh", "aln_points.cuh",
-           "aln_thmpair.cuh", "aln_ingest.cuh"]
+           "aln_thmpair.cuh", "aln_ingest.cuh", "aln_row_layout.cuh"]
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-O3", "-lineinfo", "-std=c++17",

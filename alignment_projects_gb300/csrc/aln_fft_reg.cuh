@@ -111,9 +111,10 @@ __device__ __forceinline__ void team_sync(int team)
 }
 
 // PADK: exchange-buffer padding i -> i + (i >> PADK): 4 (one slot per 16)
-// by default; 3 for kernels whose teams of <= 8 threads share a half-warp
-// with a neighbour team placed 8 bank pairs away (the row pass), where it
-// keeps both teams' strided writes on distinct banks.
+// by default; log2 T (one slot per T points) for the row pass's teams of
+// T = 2, 4, 8 threads, which share a half-warp with neighbour teams placed
+// T bank pairs away: it keeps all the teams' strided writes on distinct
+// banks.
 template <int N, int DIR, int RAD = fft_radix(N), int PADK = 4>
 struct RegFFT {
     static constexpr int R = RAD;

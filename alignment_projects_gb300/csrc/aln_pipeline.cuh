@@ -19,6 +19,7 @@
 #pragma once
 
 #include "aln_fft_reg.cuh"
+#include "aln_row_layout.cuh"
 
 __device__ __forceinline__ bool int_pixels(int dt) { return dt == ALN_U8 || dt == ALN_U16; }
 
@@ -503,63 +504,7 @@ __global__ void k2_sat2w(PairDev *pairs)
 // forward rows
 // ---------------------------------------------------------------------------
 
-// threads per CTA of the row kernels: >= 256, four teams when teams are large
-__host__ __device__ constexpr int rowfft_threads(int T) { return T * 4 > 512 ? 512 : (T * 4 < 256 ? 256 : T * 4); }
-
-// Per-thread radix of the row transforms: 16 from 128 points up (fewer
-// shared-memory exchange passes: the row kernel is bound by them), the
-// register FFT's default below.
-__host__ __device__ constexpr int rowfft_radix(int L) { return L >= 128 ? 16 : fft_radix(L); }
-
-// Shared-memory layout of the row kernel.  Each team owns one row's region:
-// the row's staged bytes, then the transform's exchange buffer, then the
-// row's L bins (plain index), reused in that order.  Teams of T <= 8
-// threads share a half-warp with 16 / T - 1 neighbours: region starts are
-// shifted (by under 16 float2) so that the teams of a half-warp sit T bank
-// pairs apart -- their consecutive and odd-strided accesses then fall on
-// distinct banks -- and so that any 16 consecutive regions start on
-// distinct bank pairs (the epilogue reads one bin of 16 rows at a time).
-// The split lengths take the transform in decimation-in-frequency order (a
-// team's threads read consecutive pixel pairs), and teams of <= 8 threads
-// pad the exchange buffer by one slot per 8.  (Modelled on 8-byte
-// half-warp wavefronts: the odd-pitch layout with padding per 16 cost
-// 1.75-4x the conflict-free count on the 160- and 192-point rows.)
-template <int L>
-__host__ __device__ constexpr int rowfft_T() { return fft_team(L, rowfft_radix(L)); }
-template <int L>
-__host__ __device__ constexpr int rowfft_padk() { return rowfft_T<L>() <= 8 ? 3 : 4; }
-
-// The row transform of half-length L: the power-of-two RegFFT at
-// rowfft_radix(L), or for L = 3 * 2^k, 5 * 2^k (CorrPatches grids) the
-// MixFFT split.
-template <int L>
-using RowFFT = FFTOf<L, -1, true, rowfft_radix(L), rowfft_padk<L>()>;
-
-// float2 per team region: the bins, the exchange buffer and the staged
-// bytes (<= 4L + 38 with the 16-byte alignment) all fit, plus the shift.
-template <int L>
-__host__ __device__ constexpr int rowfft_pitch()
-{
-    constexpr int a = L + 1, b = RowFFT<L>::SMEM, c = (4 * L + 38 + 7) / 8;
-    return (a > b ? (a > c ? a : c) : (b > c ? b : c)) + 15;
-}
-// start of team g's region (float2); a CTA needs G * pitch + 16 float2
-template <int L>
-__host__ __device__ constexpr int rowfft_base(int g)
-{
-    constexpr int T = rowfft_T<L>(), P = rowfft_pitch<L>();
-    const int want = T < 16 ? ((g % (16 / T)) * T + g / (16 / T)) % 16 : g % 16;
-    return g * P + ((want - g * P) % 16 + 16) % 16;
-}
-
-// CTAs per SM the row kernel is compiled for: 5 up to 256-point
-// power-of-two rows (48 registers, no spills), 64 registers per thread for
-// longer rows and for the split lengths (12-24 points per thread).
-template <int L>
-__host__ __device__ constexpr int rowfft_minb()
-{
-    return odd_part(L) == 1 && L <= 256 ? 5 : 1024 / rowfft_threads(rowfft_T<L>());
-}
+// launch shape and shared-memory layout: aln_row_layout.cuh
 
 // Each team of T threads (rowfft_T<L>()) transforms one row.  G =
 // blockDim.x / T rows per CTA.
