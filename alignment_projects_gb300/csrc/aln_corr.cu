@@ -1999,7 +1999,7 @@ static void launch_fill_cols_rad(aln_ctx *ctx, int nsel, int L)
 {
     constexpr int T = NY / RAD;
     const int thr = std::max(256, T), G = thr / T;
-    const size_t sm = (size_t)G * padded(NY) * sizeof(float2);
+    const size_t sm = (size_t)G * RegFFT<NY, -1, RAD>::SMEM * sizeof(float2);   // k2_colspec's FF
     smem_attr(ctx->device, (const void *)k2_colspec<NY, RAD>, sm);
     LAUNCH(ctx, "k2_colspec", (k2_colspec<NY, RAD>), dim3((L + 1 + G - 1) / G, nsel), thr, sm,
            ctx->dpairs, ctx->tw, (const int *)ctx->dsel_cur);
@@ -2028,7 +2028,9 @@ static void launch_corrcol_var(aln_ctx *ctx, int n, int L, int cached)
 {
     constexpr int T = NY / corrcol_radix<NY, VAR>();
     constexpr int thr = corrcol_threads<NY, VAR>(), G = thr / T;
-    const size_t sm = (size_t)G * (padded(NY) + NY) * sizeof(float2);
+    // per team: k2_corrcol's exchange buffer (FF::SMEM) and b's spectrum (NY)
+    const size_t sm =
+        (size_t)G * (RegFFT<NY, -1, corrcol_radix<NY, VAR>()>::SMEM + NY) * sizeof(float2);
     void (*kern)(PairDev *, const float2 *, int) = k2_corrcol<NY, VAR>;
     smem_attr(ctx->device, (const void *)kern, sm);
     LAUNCH(ctx, "k2_corrcol", kern, dim3((L + 1 + G - 1) / G, n), thr, sm, ctx->dpairs, ctx->tw,
@@ -2061,7 +2063,10 @@ static void launch_corrseg(aln_ctx *ctx, int n, int L)
     int G = GMAX;
     while (G > 1 && (long long)((L + 1 + G - 1) / G) * n < 2LL * ctx->sms)
         G /= 2;
-    constexpr int per_team = padded(NS) + (corrseg_regs<NS>() ? 0 : 2 * NS);   // float2
+    // float2 per team: k2_corrseg's exchange buffer (FF::SMEM), then the parked
+    // spectrum and accumulator when they are not held in registers
+    constexpr int per_team =
+        RegFFT<NS, -1, corrseg_radix<NS>()>::SMEM + (corrseg_regs<NS>() ? 0 : 2 * NS);
     const size_t sm = (size_t)G * per_team * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_corrseg<NS>, (size_t)GMAX * per_team * sizeof(float2));
     LAUNCH(ctx, "k2_corrseg", k2_corrseg<NS>, dim3((L + 1 + G - 1) / G, n), G * T, sm,

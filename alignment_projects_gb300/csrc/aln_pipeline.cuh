@@ -657,6 +657,7 @@ k2_corrcol(PairDev *pairs, const float2 *__restrict__ tw, int use_cached_b)
     constexpr bool PLAIN = VAR == 1, SONLY = VAR == 2;
     using FF = RegFFT<NY, -1, corrcol_radix<NY, VAR>()>;
     using FI = RegFFT<NY, +1, corrcol_radix<NY, VAR>()>;
+    static_assert(FI::SMEM <= FF::SMEM, "the inverse runs in the forward transform's buffer");
     constexpr int R = FF::R, T = FF::T;
     extern __shared__ float2 smem[];
     PairDev &p = pairs[blockIdx.y];
@@ -815,6 +816,7 @@ k2_corrseg(PairDev *pairs, const float2 *__restrict__ tw)
 {
     using FF = RegFFT<NS, -1, corrseg_radix<NS>()>;
     using FI = RegFFT<NS, +1, corrseg_radix<NS>()>;
+    static_assert(FI::SMEM <= FF::SMEM, "the inverse runs in the forward transform's buffer");
     constexpr int R = FF::R, T = FF::T;
     extern __shared__ float2 smem[];
     const PairDev &p = pairs[blockIdx.y];
@@ -999,6 +1001,7 @@ __global__ void __launch_bounds__(lagrow_threads(FFTOf<L, +1>::T))
 k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
 {
     using F = FFTOf<L, +1>;   // RegFFT, or MixFFT for L = 3 * 2^k, 5 * 2^k
+    static_assert(F::SMEM <= row_pitch(L), "the exchange buffer fits the team's row region");
     constexpr int V = F::V, T = F::T;
     constexpr int PITCH = row_pitch(L);   // holds L+1 bins, then 2L reals
     extern __shared__ float2 smem[];
@@ -1114,6 +1117,7 @@ template <int L, bool SONLY>
 __global__ void __launch_bounds__(256, SONLY ? 3 : 2) k2_lagimg(PairDev *pairs, const float2 *__restrict__ tw)
 {
     using F = RegFFT<L, +1>;
+    static_assert(F::SMEM <= row_pitch(L), "the exchange buffer fits the team's row region");
     constexpr int R = F::R, T = F::T;
     constexpr int PITCH = row_pitch(L);
     extern __shared__ float2 smem[];
@@ -1579,6 +1583,7 @@ template <int L>
 __global__ void k2_lagp2i(PairDev *pairs, const float2 *__restrict__ tw)
 {
     using F = RegFFT<L, +1>;
+    static_assert(F::SMEM <= row_pitch(L), "the exchange buffer fits the team's row region");
     constexpr int R = F::R, T = F::T;
     constexpr int PITCH = row_pitch(L);
     extern __shared__ float2 smem[];
