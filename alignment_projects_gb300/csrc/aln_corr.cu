@@ -2078,7 +2078,7 @@ static void launch_lagrow2(aln_ctx *ctx, int n, int maxWy)
 {
     constexpr int T = FFTOf<LL, +1>::T;
     constexpr int thr = lagrow_threads(T), G = thr / T;
-    const size_t sm = (size_t)G * row_pitch(LL) * sizeof(float2);
+    const size_t sm = (size_t)G * lag_pitch<LL>() * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_lagrow<LL>, sm);
     LAUNCH(ctx, "k2_lagrow", k2_lagrow<LL>, dim3((maxWy + G - 1) / G, n), thr, sm,
            ctx->dpairs, ctx->tw);
@@ -2089,7 +2089,7 @@ static void launch_lagp2i(aln_ctx *ctx, int n, int maxWy)
 {
     constexpr int T = RegFFT<LL, +1>::T;
     const int thr = std::max(256, T), G = thr / T;
-    const size_t sm = (size_t)G * row_pitch(LL) * sizeof(float2);
+    const size_t sm = (size_t)G * lag_pitch<LL>() * sizeof(float2);
     smem_attr(ctx->device, (const void *)k2_lagp2i<LL>, sm);
     LAUNCH(ctx, "k2_lagp2i", k2_lagp2i<LL>, dim3((maxWy + G - 1) / G, n), thr, sm, ctx->dpairs,
            ctx->tw);
@@ -2100,7 +2100,7 @@ static void launch_lagimg2(aln_ctx *ctx, int n, int maxWy, bool both, bool sonly
 {
     constexpr int T = RegFFT<LL, +1>::T;
     const int thr = std::max(256, T), G = thr / T;
-    const size_t sm = (size_t)G * row_pitch(LL) * (both ? 2 : 1) * sizeof(float2);
+    const size_t sm = (size_t)G * lag_pitch<LL>() * (both ? 2 : 1) * sizeof(float2);
     void (*kern)(PairDev *, const float2 *) = sonly ? k2_lagimg<LL, true> : k2_lagimg<LL, false>;
     smem_attr(ctx->device, (const void *)kern, sm);
     LAUNCH(ctx, "k2_lagimg", kern, dim3((maxWy + G - 1) / G, n), thr, sm, ctx->dpairs, ctx->tw);

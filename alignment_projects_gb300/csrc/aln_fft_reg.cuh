@@ -5,12 +5,12 @@
 // Stockham pass is an R-point DFT in registers (radix 2/4/8/16 built from
 // radix-2 splits with exact constants), preceded by twiddles from the device
 // table tw[N' + m] = exp(-2 pi i m / N'); between passes the team exchanges
-// data once through a padded shared-memory buffer (index i -> i + i/16,
-// which keeps the strided Stockham writes of radix 16 free of bank
-// conflicts; at radix 8 the writes cost 1.17-1.25x the conflict-free count
-// of 8-byte wavefronts, and an XOR swizzle that removed that ran slower in
-// the 512-point column kernel: its per-access address arithmetic took
-// registers and spilled).  When N
+// data once through a padded shared-memory buffer, each exchange with its own
+// padding (xpad_shift / xpad_mul below) so that neither its strided writes
+// nor its consecutive reads share a bank pair within a half-warp.  (An XOR
+// swizzle does the same for one layout, and ran slower in the 512-point
+// column kernel: its per-access address arithmetic took registers and
+// spilled.)  When N
 // is not a power of R the first pass has a smaller radix R2 = N / R^P and
 // each thread runs R/R2 of its butterflies.  After the last pass thread t
 // holds X[t + r*T]: the same layout as the input, so a forward transform, a
@@ -27,14 +27,6 @@ __host__ __device__ constexpr int ipowc(int b, int e) { return e == 0 ? 1 : b * 
 __device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
 __host__ __device__ constexpr int padded(int n) { return n + (n >> 4); }
 
-// float2 per team in the row kernels: the padded row plus two bins, rounded
-// up to an odd count.  The row kernels move data between the teams' rows
-// with one bin per thread and the teams (rows) fastest, G consecutive
-// threads reading (or writing) bin k of G rows at k + g * pitch: an odd
-// pitch puts those on G distinct 8-byte banks (an even one had two threads
-// on every bank).  Regions then start on 8 bytes only: the row pass stages
-// its input bytes from the region's first 16-byte boundary.
-__host__ __device__ constexpr int row_pitch(int L) { return (padded(L) + 2) | 1; }
 
 // exp(DIR * 2 pi i k / 16) for k = 0..7 (DIR = -1 forward)
 template <int K16, int DIR>
@@ -110,19 +102,69 @@ __device__ __forceinline__ void team_sync(int team)
         __syncwarp();
 }
 
-// PADK: exchange-buffer padding i -> i + (i >> PADK): 4 (one slot per 16)
-// by default; log2 T (one slot per T points) for the row pass's teams of
-// T = 2, 4, 8 threads, which share a half-warp with neighbour teams placed
-// T bank pairs away: it keeps all the teams' strided writes on distinct
-// banks.
+// Exchange padding.  The exchange after a pass whose butterflies are ns
+// points apart (ns = 1 after the first pass) has each half-warp write
+// groups of ns consecutive slots, ns R apart, and read 16 consecutive slots.
+// Slot i sits at buffer index i + c (i >> b):
+//   radix 8, teams of T >= 16 threads (a half-warp inside one team) and
+//     1 < ns < 16: b = max(4, log2(ns R)), c = ns: each write group lands ns
+//     bank pairs after the previous one, so the 16 / ns groups of a
+//     half-warp cover the 16 pairs once (one slot per 16 left these
+//     exchanges at 1.5x the conflict-free count of 8-byte wavefronts);
+//   otherwise b = PADK, c = 1: one slot per 2^PADK points (4 by default,
+//     which at radix 16 already moves each write group ns R / 16 = ns bank
+//     pairs on; log2 T for the row pass's teams of T = 2, 4, 8 threads,
+//     which share a half-warp with neighbour teams placed T bank pairs
+//     away).  The split lengths' radix-4 sub-transforms keep one slot per 16
+//     (1.25-2.5x): the rule above made their row kernels, capped at 64
+//     registers, spill up to 2.6x more.
+// b >= 4 keeps each aligned run of 16 slots on 16 distinct bank pairs (the
+// reads).  The index grows with i, so every exchange is a permutation.
+__host__ __device__ constexpr int xpad_shift(int ns, int R, int T, int PADK)
+{
+    // log2(ns R) for R = 8 and ns = 2, 4, 8 (a select, not a recursion: ns is
+    // a constant only once the pass loop is unrolled)
+    return R == 8 && T >= 16 && ns > 1 && ns < 16 ? (ns == 2 ? 4 : ns == 4 ? 5 : 6) : PADK;
+}
+__host__ __device__ constexpr int xpad_mul(int ns, int R, int T)
+{
+    return R == 8 && T >= 16 && ns > 1 && ns < 16 ? ns : 1;
+}
+__host__ __device__ constexpr int xpad_index(int ns, int R, int T, int PADK, int i)
+{
+    return i + xpad_mul(ns, R, T) * (i >> xpad_shift(ns, R, T, PADK));
+}
+// float2 per team: the largest index of any exchange of an N-point
+// transform at radix R (first pass of radix R2 = N / R^P, then P passes),
+// and never less than N + (N >> PADK)
+__host__ __device__ constexpr int regfft_smem(int N, int R, int PADK)
+{
+    const int T = N / R, P = ilog2c(N) / ilog2c(R), R2 = N / ipowc(R, P);
+    int m = N + (N >> PADK), ns = 1;
+    if (R2 > 1) {
+        const int e = xpad_index(1, R, T, PADK, N - 1) + 1;
+        m = e > m ? e : m;
+        ns = R2;
+    }
+    for (int p = 0; p + 1 < P; ++p, ns *= R) {
+        const int e = xpad_index(ns, R, T, PADK, N - 1) + 1;
+        m = e > m ? e : m;
+    }
+    return m;
+}
+
 template <int N, int DIR, int RAD = fft_radix(N), int PADK = 4>
 struct RegFFT {
     static constexpr int R = RAD;
     static constexpr int T = N / R;                    // threads per transform
     static constexpr int P = ilog2c(N) / ilog2c(R);    // full radix-R passes
     static constexpr int R2 = N / ipowc(R, P);         // first-pass radix (1: none)
-    static constexpr int SMEM = N + (N >> PADK);       // float2 per team
-    __device__ __forceinline__ static int pad(int i) { return i + (i >> PADK); }
+    static constexpr int SMEM = regfft_smem(N, R, PADK);   // float2 per team
+    // buffer index of slot i in the exchange after butterflies ns apart
+    __device__ __forceinline__ static int xpad(int ns, int i)
+    {
+        return xpad_index(ns, R, T, PADK, i);
+    }
     static constexpr int V = R;                        // points per thread
     // register slot q of thread t holds point t + q T, in and out
     __device__ __forceinline__ static int in_idx(int t, int q) { return t + q * T; }
@@ -175,12 +217,12 @@ struct RegFFT {
                 const int j = t + q * T;
 #pragma unroll
                 for (int s = 0; s < R2; ++s)
-                    sm[pad(j * R2 + s)] = v[q + s * m];
+                    sm[xpad(1, j * R2 + s)] = v[q + s * m];
             }
             sync<TEAM>(team);
 #pragma unroll
             for (int r = 0; r < R; ++r)
-                v[r] = sm[pad(t + r * T)];
+                v[r] = sm[xpad(1, t + r * T)];
             Ns = R2;
         }
 #pragma unroll
@@ -202,11 +244,11 @@ struct RegFFT {
                 sync<TEAM>(team);
 #pragma unroll
                 for (int r = 0; r < R; ++r)
-                    sm[pad(base + r * Ns)] = v[r];
+                    sm[xpad(Ns, base + r * Ns)] = v[r];
                 sync<TEAM>(team);
 #pragma unroll
                 for (int r = 0; r < R; ++r)
-                    v[r] = sm[pad(t + r * T)];
+                    v[r] = sm[xpad(Ns, t + r * T)];
             }
             Ns *= R;
         }

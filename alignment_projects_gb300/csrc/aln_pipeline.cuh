@@ -1001,9 +1001,9 @@ __global__ void __launch_bounds__(lagrow_threads(FFTOf<L, +1>::T))
 k2_lagrow(PairDev *pairs, const float2 *__restrict__ tw)
 {
     using F = FFTOf<L, +1>;   // RegFFT, or MixFFT for L = 3 * 2^k, 5 * 2^k
-    static_assert(F::SMEM <= row_pitch(L), "the exchange buffer fits the team's row region");
+    static_assert(F::SMEM <= lag_pitch<L>(), "the exchange buffer fits the team's row region");
     constexpr int V = F::V, T = F::T;
-    constexpr int PITCH = row_pitch(L);   // holds L+1 bins, then 2L reals
+    constexpr int PITCH = lag_pitch<L>();   // holds L+1 bins, then 2L reals
     extern __shared__ float2 smem[];
     __shared__ double red_r[32];
     __shared__ long long red_k[32];
@@ -1117,9 +1117,9 @@ template <int L, bool SONLY>
 __global__ void __launch_bounds__(256, SONLY ? 3 : 2) k2_lagimg(PairDev *pairs, const float2 *__restrict__ tw)
 {
     using F = RegFFT<L, +1>;
-    static_assert(F::SMEM <= row_pitch(L), "the exchange buffer fits the team's row region");
+    static_assert(F::SMEM <= lag_pitch<L>(), "the exchange buffer fits the team's row region");
     constexpr int R = F::R, T = F::T;
-    constexpr int PITCH = row_pitch(L);
+    constexpr int PITCH = lag_pitch<L>();
     extern __shared__ float2 smem[];
     __shared__ double red_r[32], red_s[32], red_s2[32];
     __shared__ long long red_k[32];
@@ -1583,9 +1583,9 @@ template <int L>
 __global__ void k2_lagp2i(PairDev *pairs, const float2 *__restrict__ tw)
 {
     using F = RegFFT<L, +1>;
-    static_assert(F::SMEM <= row_pitch(L), "the exchange buffer fits the team's row region");
+    static_assert(F::SMEM <= lag_pitch<L>(), "the exchange buffer fits the team's row region");
     constexpr int R = F::R, T = F::T;
-    constexpr int PITCH = row_pitch(L);
+    constexpr int PITCH = lag_pitch<L>();
     extern __shared__ float2 smem[];
     __shared__ double red_r[32];
     __shared__ long long red_k[32];

@@ -1,7 +1,8 @@
-// aln_row_layout.cuh -- launch shape and shared-memory layout of the row
-// kernel k2_rowfft (aln_pipeline.cuh): team size, teams per CTA, exchange
-// padding, region pitch and region starts.  Host and device code both use
-// these (the launch sizes its shared memory from rowfft_pitch).
+// aln_row_layout.cuh -- shared-memory layouts of the row kernels
+// (aln_pipeline.cuh): the row pass k2_rowfft (team size, teams per CTA,
+// exchange padding, region pitch and region starts) and the lag kernels'
+// team pitch.  Host and device code both use these (the launches size their
+// shared memory from rowfft_pitch and lag_pitch).
 #pragma once
 
 #include "aln_fft_reg.cuh"
@@ -73,4 +74,17 @@ template <int L>
 __host__ __device__ constexpr int rowfft_minb()
 {
     return odd_part(L) == 1 && L <= 256 ? 5 : 1024 / rowfft_threads(rowfft_T<L>());
+}
+
+// float2 per team in the lag kernels (k2_lagrow, k2_lagimg, k2_lagp2i): the
+// team's L + 1 bins at padi(k) and the inverse transform's exchange buffer
+// (both from the region's start), rounded up to an odd count.  The CTA
+// loads the rows with one bin per thread and the teams (rows) fastest, G
+// consecutive threads writing bin k of G rows at k + g * pitch: an odd pitch
+// puts those on G distinct 8-byte banks (an even one had two threads on
+// every bank).
+template <int L>
+__host__ __device__ constexpr int lag_pitch()
+{
+    return (padded(L) + 2 > FFTOf<L, +1>::SMEM ? padded(L) + 2 : FFTOf<L, +1>::SMEM) | 1;
 }

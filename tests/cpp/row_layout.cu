@@ -1,9 +1,12 @@
-// Prints the row kernel's launch shape and shared-memory layout
+// Prints the row kernels' shared-memory layouts
 // (alignment_projects_gb300/csrc/aln_row_layout.cuh) for every row length
-// the library instantiates, one line per length:
+// the library instantiates, one line per length for the row pass:
 //   L T G padk smem pitch base(0) .. base(G-1)
 // (T threads per team, G teams per CTA, exchange padding i + (i >> padk),
-// exchange buffer float2, region pitch float2, region starts float2).
+// exchange buffer float2, region pitch float2, region starts float2), and
+// one for the lag kernels:
+//   lag L pitch smem
+// (team pitch float2, the inverse transform's exchange buffer float2).
 // Host code only: it runs without a GPU.
 #include <cstdio>
 
@@ -19,6 +22,7 @@ static void show()
     for (int g = 0; g < G; ++g)
         std::printf(" %d", rowfft_base<L>(g));
     std::printf("\n");
+    std::printf("lag %d %d %d\n", L, lag_pitch<L>(), FFTOf<L, +1>::SMEM);
 }
 
 int main()

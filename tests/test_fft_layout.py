@@ -8,7 +8,15 @@ numpy.fft on the CPU.  The restatement follows the kernels' code:
   Stockham passes (twiddle index Ns R + r k, exchange write address
   (t - k) R + k + r Ns, read address t + r T), each exchange a permutation
   of the padded buffer that reads no slot it did not write, and thread t's
-  slot q holding point t + q T before and after;
+  slot q holding point t + q T before and after.  Each exchange's padding
+  (buffer index i + c (i >> b)) and the buffer size come from the library's
+  own constexpr functions: tests/cpp/fft_layout.cu prints them for every
+  radix and padding the library instantiates;
+* the bank model of those paddings (8-byte accesses, a half-warp's 16
+  threads taking one wavefront per distinct address on the busiest of the
+  16 bank pairs): no exchange costs more than with one slot per 2^PADK
+  points, and radix-8 exchanges of teams of 16 threads or more are
+  conflict-free;
 * MixFFT<N1, N2, DIR, DIF>: the N1 sub-transforms, twiddles W_N^(a j) from
   the N1 * 2^k table and the odd DFTs with the kernel's formulas, in both
   layouts (in_idx / out_idx);
@@ -18,8 +26,15 @@ numpy.fft on the CPU.  The restatement follows the kernels' code:
 Twiddles are kept in FP64 here (the device table is the same values rounded
 to FP32), so the comparison is to FP64 rounding: this checks indices and
 signs, not FP32 accuracy, which the GPU parity tests cover."""
+import os
+import shutil
+import subprocess
+
 import numpy as np
 import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(os.path.dirname(HERE), "alignment_projects_gb300", "csrc")
 
 ALN_MAX_N = 1 << 13                       # aln_fft.cuh: ALN_MAX_LOG 13
 TW_POW2_SIZE = 2 * ALN_MAX_N
@@ -76,6 +91,31 @@ def _table():
 TW = _table()
 
 
+def _layout():
+    """(N, R, PADK) -> T, SMEM and the exchanges' (ns, b, c), printed by
+    tests/cpp/fft_layout.cu from aln_fft_reg.cuh's constexpr functions."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        return None
+    import tempfile
+    d = tempfile.mkdtemp(prefix="fft_layout")
+    exe = os.path.join(d, "fft_layout")
+    subprocess.check_call([nvcc, "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a",
+                           "-I" + CSRC, "-o", exe, os.path.join(HERE, "cpp", "fft_layout.cu")])
+    out = {}
+    for ln in subprocess.check_output([exe], text=True).splitlines():
+        f = [int(x) for x in ln.split()]
+        n, r, padk, T, smem = f[:5]
+        ex = [tuple(f[5 + 3 * i:8 + 3 * i]) for i in range((len(f) - 5) // 3)]
+        out[(n, r, padk)] = dict(T=T, smem=smem, ex=ex)
+    shutil.rmtree(d, ignore_errors=True)
+    return out
+
+
+LAYOUT = _layout()
+needs_layout = pytest.mark.skipif(LAYOUT is None, reason="nvcc not found")
+
+
 def test_twiddle_table_layout():
     """Every length's slots are its own, the three tables end where
     TW_TOTAL says, and each table's last length fills its table exactly."""
@@ -118,23 +158,25 @@ def dft_odd(z, n1, sign):
 
 
 class Exchange:
-    """The padded exchange buffer pad(i) = i + (i >> padk): checks that one
-    exchange's writes are distinct and that reads only see written slots."""
+    """The team's exchange buffer of `size` float2; exchange e indexes slot i
+    at i + c_e (i >> b_e).  Checks that one exchange's writes are distinct,
+    inside the buffer, and that its reads only see written slots."""
 
-    def __init__(self, n, padk):
-        self.padk = padk
-        self.size = n + (n >> padk)
+    def __init__(self, n, size, pads):
+        self.size = size
         self.n = n
-
-    def pad(self, i):
-        return i + (i >> self.padk)
+        self.pads = list(pads)
+        self.e = 0
 
     def swap(self, writes, reads):
         """writes: list of (index array, values); reads: list of index arrays."""
+        b, c = self.pads[self.e]
+        self.e += 1
+        pad = lambda i: i + c * (i >> b)
         sm = np.full(self.size, np.nan + 0j)
         seen = np.zeros(self.size, np.int64)
         for idx, val in writes:
-            p = self.pad(idx)
+            p = pad(idx)
             assert p.max() < self.size
             np.add.at(seen, p, 1)
             sm[p] = val
@@ -142,7 +184,7 @@ class Exchange:
         assert seen.sum() == self.n
         out = []
         for idx in reads:
-            p = self.pad(idx)
+            p = pad(idx)
             assert seen[p].all(), "a thread reads a slot nobody wrote"
             out.append(sm[p])
         return np.stack(out, axis=1)
@@ -150,12 +192,14 @@ class Exchange:
 
 def regfft(v, n, sign, r, padk=4):
     """RegFFT<N, DIR, R, PADK>::run_impl over all T threads at once;
-    v[t, q] is thread t's register slot q."""
+    v[t, q] is thread t's register slot q.  Exchange paddings and the buffer
+    size are the library's (LAYOUT)."""
     T = n // r
     P = ilog2(n) // ilog2(r)
     r2 = n // r ** P
     t = np.arange(T)
-    ex = Exchange(n, padk)
+    lay = LAYOUT[(n, r, padk)]
+    ex = Exchange(n, lay["smem"], [(b, c) for _, b, c in lay["ex"]])
     v = v.copy()
     ns = 1
     if r2 > 1:
@@ -168,6 +212,7 @@ def regfft(v, n, sign, r, padk=4):
             j = t + q * T
             for s in range(r2):
                 writes.append((j * r2 + s, v[:, q + s * m]))
+        assert lay["ex"][ex.e][0] == 1
         v = ex.swap(writes, [t + rr * T for rr in range(r)])
         ns = r2
     for p in range(P):
@@ -181,9 +226,11 @@ def regfft(v, n, sign, r, padk=4):
         v = dft(v, r, sign)
         if p + 1 < P:
             base = (t - k) * r + k
+            assert lay["ex"][ex.e][0] == ns
             v = ex.swap([(base + rr * ns, v[:, rr]) for rr in range(r)],
                         [t + rr * T for rr in range(r)])
         ns *= r
+    assert ex.e == len(ex.pads)
     return v
 
 
@@ -242,23 +289,94 @@ def _check(got, want, n):
 POW2 = [1 << k for k in range(1, ilog2(ALN_MAX_N) + 1)]
 
 
+def row_padk(T):
+    """rowfft_padk (aln_row_layout.cuh): one pad slot per T points for teams
+    of 2, 4 and 8 threads, per 16 otherwise."""
+    return 4 if T >= 16 else 3 if T >= 8 else 2 if T >= 4 else 1 if T >= 2 else 4
+
+
+@needs_layout
 @pytest.mark.parametrize("n", POW2)
 @pytest.mark.parametrize("sign", [-1, +1])
 def test_regfft_layout(n, sign):
-    """Every radix a kernel can instantiate for this length (2-16), both
-    exchange paddings: slot q of thread t holds x[t + q T] in, X[t + q T]
-    out."""
+    """Every radix (2-16) and team padding the library instantiates for this
+    length: slot q of thread t holds x[t + q T] in, X[t + q T] out."""
     rng = np.random.default_rng(n * 7 + sign)
     x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
     want = _ref(x, sign)
+    done = 0
     for r in (2, 4, 8, 16):
         if r > n:
             continue
         T = n // r
         idx = np.arange(T)[:, None] + np.arange(r)[None, :] * T
-        for padk in (3, 4):
+        for padk in (1, 2, 3, 4):
+            if (n, r, padk) not in LAYOUT:
+                continue
             got = regfft(x[idx], n, sign, r, padk)
             _check(got, want[idx], n)
+            done += 1
+    assert done
+
+
+def _warp_exchanges(n, r):
+    """Per exchange of RegFFT<n, ., r>: (ns, write index lists, read index
+    lists), one index per thread of the team's first warp."""
+    T = n // r
+    P = ilog2(n) // ilog2(r)
+    r2 = n // r ** P
+    t = np.arange(min(T, 32))
+    out = []
+    ns = 1
+    if r2 > 1:
+        m = r // r2
+        w = [(t + q * T) * r2 + s for q in range(m) for s in range(r2)]
+        out.append((1, w, [t + rr * T for rr in range(r)]))
+        ns = r2
+    for p in range(P):
+        if p + 1 < P:
+            k = t & (ns - 1)
+            w = [(t - k) * r + k + rr * ns for rr in range(r)]
+            out.append((ns, w, [t + rr * T for rr in range(r)]))
+        ns *= r
+    return out
+
+
+def _wavefronts(idx_lists, b, c):
+    """8-byte accesses: per half-warp instruction, the distinct addresses on
+    the busiest of the 16 bank pairs; summed, over the conflict-free count."""
+    tot = ideal = 0
+    for idx in idx_lists:
+        a = idx + c * (idx >> b)
+        for h in range(0, len(a), 16):
+            banks = {}
+            for x in set(int(v) for v in a[h:h + 16]):
+                banks[x % 16] = banks.get(x % 16, 0) + 1
+            tot += max(banks.values())
+            ideal += 1
+    return tot / ideal
+
+
+@needs_layout
+def test_exchange_bank_model():
+    """For teams of 16 threads or more (a half-warp inside one team): no
+    exchange's padding costs more wavefronts than one slot per 2^PADK
+    points, and every radix-8 exchange is conflict-free (one slot per 16
+    left the second exchange at 1.5x)."""
+    checked = 0
+    for (n, r, padk), lay in LAYOUT.items():
+        if lay["T"] < 16 or padk != 4:   # teams of 16+ threads always pad with 4
+            continue
+        exs = _warp_exchanges(n, r)
+        assert [e[0] for e in exs] == [e[0] for e in lay["ex"]], (n, r)
+        for (ns, w, rd), (_, b, c) in zip(exs, lay["ex"]):
+            new = _wavefronts(w + rd, b, c)
+            old = _wavefronts(w + rd, padk, 1)
+            assert new <= old + 1e-12, (n, r, padk, ns, new, old)
+            if r == 8:
+                assert new == 1.0, (n, r, padk, ns, new)
+            checked += 1
+    assert checked
 
 
 def _mix_lengths():
@@ -271,6 +389,7 @@ def _mix_lengths():
     return out
 
 
+@needs_layout
 @pytest.mark.parametrize("n1,n2", _mix_lengths())
 def test_mixfft_layouts(n1, n2):
     """N = 3 * 2^k and 5 * 2^k at the radix mix_radix picks: the DIT layout
@@ -285,11 +404,12 @@ def test_mixfft_layouts(n1, n2):
         for dif in (False, True):
             iin = mix_idx(n1, n2, r, dif, True)
             iout = mix_idx(n1, n2, r, dif, False)
-            got = mixfft(x[iin], n1, n2, sign, dif, r, 3 if n2 // r <= 8 else 4)
+            got = mixfft(x[iin], n1, n2, sign, dif, r, row_padk(n2 // r))
             _check(got, want[iout], n)
 
 
-@pytest.mark.parametrize("n", [80, 96, 160, 192, 320, 384, 640, 768, 1280, 1536, 256, 512])
+@needs_layout
+@pytest.mark.parametrize("n", [80, 96, 160, 192, 320, 384, 640, 768, 1280, 1536, 128, 256, 512])
 def test_row_transform_chains_with_lag_transform(n):
     """The row pass's forward transform (decimation in frequency for split
     lengths) and the lag pass's inverse (decimation in time) meet in one
@@ -303,7 +423,7 @@ def test_row_transform_chains_with_lag_transform(n):
         ri = fft_radix(n)                          # FFTOf<L, +1>
         T = n // rf
         idx = np.arange(T)[:, None] + np.arange(rf)[None, :] * T
-        spec = regfft(x[idx], n, -1, rf)
+        spec = regfft(x[idx], n, -1, rf, row_padk(T))
         # the lag pass gets its input through memory by bin index
         flat = np.empty(n, np.complex128)
         flat[idx] = spec
@@ -314,7 +434,7 @@ def test_row_transform_chains_with_lag_transform(n):
         return
     n2 = n // n1
     r = mix_radix(n1, n2)
-    padk = 3 if n2 // r <= 8 else 4
+    padk = row_padk(n2 // r)
     assert (mix_idx(n1, n2, r, True, False) == mix_idx(n1, n2, r, False, True)).all()
     iin = mix_idx(n1, n2, r, True, True)
     spec = mixfft(x[iin], n1, n2, -1, True, r, padk)

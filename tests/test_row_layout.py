@@ -6,6 +6,8 @@ instantiates.  This test checks it:
 * each team's region holds its staged row bytes (from the region's first
   16-byte boundary), its exchange buffer and its L + 1 bins; regions do not
   overlap and end inside the G * pitch + 16 float2 the launch allocates;
+* the lag kernels' team pitch holds the L + 1 bins at padi(k) and the
+  inverse transform's exchange buffer, and is odd;
 * a bank model of 8-byte shared-memory accesses (a half-warp's 16 threads
   take one wavefront per distinct address on the busiest of the 16 bank
   pairs): the register FFT's exchanges (write and read addresses of
@@ -40,6 +42,10 @@ def layout(tmp_path_factory):
                            "-I" + CSRC, "-o", exe, os.path.join(HERE, "cpp", "row_layout.cu")])
     out = {}
     for ln in subprocess.check_output([exe], text=True).splitlines():
+        if ln.startswith("lag "):
+            L, pitch, smem = (int(x) for x in ln.split()[1:])
+            out.setdefault("lag", {})[L] = dict(pitch=pitch, smem=smem)
+            continue
         f = [int(x) for x in ln.split()]
         L, T, G, padk, smem, pitch = f[:6]
         out[L] = dict(T=T, G=G, padk=padk, smem=smem, pitch=pitch, base=f[6:])
@@ -58,10 +64,20 @@ def _instantiated_lengths():
 
 def test_every_row_length_is_covered(layout):
     assert _instantiated_lengths() <= set(layout)
+    assert _instantiated_lengths() <= set(layout["lag"])
+
+
+def test_lag_pitch(layout):
+    for L, d in layout["lag"].items():
+        padi_last = L + (L >> 4)            # padi(L), the last bin's slot
+        assert d["pitch"] > padi_last + 1 and d["pitch"] >= d["smem"], L
+        assert d["pitch"] % 2 == 1, L
 
 
 def test_regions_hold_their_data_and_stay_apart(layout):
     for L, d in layout.items():
+        if L == "lag":
+            continue
         need = max(L + 1, d["smem"], (4 * L + 30 + 8 + 7) // 8)
         assert d["pitch"] >= need + 15, L
         b = d["base"]
@@ -162,6 +178,8 @@ EXCHANGE_FACTOR = {160: 1.25, 320: 1.75, 384: 4 / 3, 640: 4 / 3, 768: 1.5, 1280:
 
 def test_bank_model(layout):
     for L, d in layout.items():
+        if L == "lag":
+            continue
         ex = _exchange_factor(L, d)
         assert ex <= EXCHANGE_FACTOR.get(L, 1.0) + 1e-9, (L, ex)
         ep = _epilogue_factor(L, d)
