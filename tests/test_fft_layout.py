@@ -91,12 +91,22 @@ def _table():
 TW = _table()
 
 
-def _layout():
+_LAYOUT = {}
+
+
+def layout():
     """(N, R, PADK) -> T, SMEM and the exchanges' (ns, b, c), printed by
-    tests/cpp/fft_layout.cu from aln_fft_reg.cuh's constexpr functions."""
+    tests/cpp/fft_layout.cu from aln_fft_reg.cuh's constexpr functions;
+    built on first use (never at collection), skipped without nvcc."""
+    if not _LAYOUT:
+        _LAYOUT.update(_build_layout())
+    return _LAYOUT
+
+
+def _build_layout():
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
-        return None
+        pytest.skip("nvcc not found")
     import tempfile
     d = tempfile.mkdtemp(prefix="fft_layout")
     exe = os.path.join(d, "fft_layout")
@@ -110,10 +120,6 @@ def _layout():
         out[(n, r, padk)] = dict(T=T, smem=smem, ex=ex)
     shutil.rmtree(d, ignore_errors=True)
     return out
-
-
-LAYOUT = _layout()
-needs_layout = pytest.mark.skipif(LAYOUT is None, reason="nvcc not found")
 
 
 def test_twiddle_table_layout():
@@ -193,12 +199,12 @@ class Exchange:
 def regfft(v, n, sign, r, padk=4):
     """RegFFT<N, DIR, R, PADK>::run_impl over all T threads at once;
     v[t, q] is thread t's register slot q.  Exchange paddings and the buffer
-    size are the library's (LAYOUT)."""
+    size are the library's (layout())."""
     T = n // r
     P = ilog2(n) // ilog2(r)
     r2 = n // r ** P
     t = np.arange(T)
-    lay = LAYOUT[(n, r, padk)]
+    lay = layout()[(n, r, padk)]
     ex = Exchange(n, lay["smem"], [(b, c) for _, b, c in lay["ex"]])
     v = v.copy()
     ns = 1
@@ -295,7 +301,6 @@ def row_padk(T):
     return 4 if T >= 16 else 3 if T >= 8 else 2 if T >= 4 else 1 if T >= 2 else 4
 
 
-@needs_layout
 @pytest.mark.parametrize("n", POW2)
 @pytest.mark.parametrize("sign", [-1, +1])
 def test_regfft_layout(n, sign):
@@ -311,7 +316,7 @@ def test_regfft_layout(n, sign):
         T = n // r
         idx = np.arange(T)[:, None] + np.arange(r)[None, :] * T
         for padk in (1, 2, 3, 4):
-            if (n, r, padk) not in LAYOUT:
+            if (n, r, padk) not in layout():
                 continue
             got = regfft(x[idx], n, sign, r, padk)
             _check(got, want[idx], n)
@@ -357,14 +362,13 @@ def _wavefronts(idx_lists, b, c):
     return tot / ideal
 
 
-@needs_layout
 def test_exchange_bank_model():
     """For teams of 16 threads or more (a half-warp inside one team): no
     exchange's padding costs more wavefronts than one slot per 2^PADK
     points, and every radix-8 exchange is conflict-free (one slot per 16
     left the second exchange at 1.5x)."""
     checked = 0
-    for (n, r, padk), lay in LAYOUT.items():
+    for (n, r, padk), lay in layout().items():
         if lay["T"] < 16 or padk != 4:   # teams of 16+ threads always pad with 4
             continue
         exs = _warp_exchanges(n, r)
@@ -389,7 +393,6 @@ def _mix_lengths():
     return out
 
 
-@needs_layout
 @pytest.mark.parametrize("n1,n2", _mix_lengths())
 def test_mixfft_layouts(n1, n2):
     """N = 3 * 2^k and 5 * 2^k at the radix mix_radix picks: the DIT layout
@@ -408,7 +411,6 @@ def test_mixfft_layouts(n1, n2):
             _check(got, want[iout], n)
 
 
-@needs_layout
 @pytest.mark.parametrize("n", [80, 96, 160, 192, 320, 384, 640, 768, 1280, 1536, 128, 256, 512])
 def test_row_transform_chains_with_lag_transform(n):
     """The row pass's forward transform (decimation in frequency for split
