@@ -205,11 +205,9 @@ struct RegFFT {
                 for (int s = 0; s < R2; ++s)
                     u[s] = v[q + s * m];
                 DFT<R2, DIR>::run(u);
-                const int j = t + q * T;
 #pragma unroll
                 for (int s = 0; s < R2; ++s)
                     v[q + s * m] = u[s];
-                (void)j;
             }
             sync<TEAM>(team);
 #pragma unroll
